@@ -1,0 +1,48 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+PKG = os.path.join(ROOT, "caviar-v2_gb300")
+for p in (PKG, os.path.join(ROOT, "oracle"), ROOT):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+def golden_cases():
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+
+
+def load_golden(name):
+    import numpy as np
+
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    return {k: z[k] for k in z.files}
+
+
+def golden_params(g):
+    """Parameter dict (workloads vocabulary) of a golden case."""
+    nt = int(g["ntypes"])
+    return dict(
+        lo=g["lo"], hi=g["hi"], ntypes=nt, nl_cutoff=float(g["nl_cutoff"]), nl_coef=float(g["nl_coef"]),
+        ghost_cutoff=float(g["ghost_cutoff"]), lj_cutoff=float(g["lj_cutoff"]), eps=g["eps"], sigma=g["sigma"],
+        cutoff_list=g["cutoff_list"] if int(g["cutoff_list_on"]) else None, mass=g["mass"], k_b=float(g["k_b"]),
+        dt=float(g["dt"]), integrator=int(g["integrator"]), lang_temperature=float(g["lang_temperature"]),
+        lang_friction=float(g["lang_friction"]), lang_kb=float(g["lang_kb"]), seed=0, n_r_df=int(g["n_r_df"]),
+        use_cell_list=int(g["use_cell_list"]), pressure_process=int(g["pressure_process"]),
+    )
+
+
+@pytest.fixture(scope="session")
+def oracle_lib():
+    import cav_oracle
+
+    cav_oracle.build()
+    return cav_oracle
