@@ -1,0 +1,648 @@
+// cav_api.cu -- the extern "C" boundary (include/cavgpu.h): context life cycle,
+// uploads/downloads in the reference's host layouts, step orchestration with
+// CUDA graphs, and the parity exports.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "cav_common.cuh"
+
+using namespace cav;
+
+namespace {
+
+constexpr int MAX_GRAPH_STEPS = 1000;  // steps captured per graph, and thermo records per chunk
+
+struct GraphEntry {
+  int S, every, prof;
+  cudaGraphExec_t exec;
+};
+
+}  // namespace
+
+struct cavgpu_ctx {
+  cavgpu_params p{};
+  Dev d{};
+  Box b{};
+  StepConsts sc{};
+  LaunchCfg lc{};
+  ThermoCfg tc{};
+  PairTab tab_h{};
+  cudaStream_t st = nullptr;
+  int n = 0;
+  bool uploaded = false, set_up = false;
+  long long steps_done = 0;
+  long long graph_launches = 0, kernel_launches = 0;
+  int max_nb = 0;
+  std::vector<GraphEntry> graphs;
+  // reference binning (Neighborlist::init, src/neighborlist.cpp:334-342)
+  double cutoff_extra = 0.0, cutoff_inv = 0.0, lo_local[3] = {0, 0, 0};
+  int ref_nb[3] = {0, 0, 0};
+  // profiling
+  bool prof = false;
+  std::vector<cudaEvent_t> ev0, ev1;
+  double prof_ms = 0.0;
+  long long prof_launches = 0;
+  // allocations
+  std::vector<void *> allocs;
+  size_t nbr_bytes = 0;
+};
+
+namespace {
+
+int cuda_rc(cudaError_t e) { return e == cudaSuccess ? CAVGPU_OK : (e == cudaErrorMemoryAllocation ? CAVGPU_E_NOMEM : CAVGPU_E_CUDA); }
+
+#define CK(x)                        \
+  do {                               \
+    int _rc = cuda_rc(x);            \
+    if (_rc) return _rc;             \
+  } while (0)
+#define RK(x)              \
+  do {                     \
+    int _rc = (x);         \
+    if (_rc) return _rc;   \
+  } while (0)
+
+template <class T>
+int dalloc(cavgpu_ctx *c, T **p, size_t count) {
+  void *q = nullptr;
+  cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+  if (e != cudaSuccess) { cudaGetLastError(); return CAVGPU_E_NOMEM; }
+  c->allocs.push_back(q);
+  *p = static_cast<T *>(q);
+  return CAVGPU_OK;
+}
+
+void free_graphs(cavgpu_ctx *c) {
+  for (auto &g : c->graphs) cudaGraphExecDestroy(g.exec);
+  c->graphs.clear();
+}
+
+int kernels_per_step(const cavgpu_ctx *c) { (void)c; return 1 /*drift*/ + 8 /*rebuild*/ + 1 /*force*/; }
+
+// one MD step on the stream (captured or eager).  k = step index inside the chunk.
+int enqueue_step(cavgpu_ctx *c, int k, bool thermo, int ring_slot) {
+  const bool lang = c->p.integrator == CAVGPU_VELOCITY_VERLET_LANGEVIN;
+  RK(launch_drift(c->d, c->b, c->sc, c->lc, k, thermo && lang, c->st));
+  RK(launch_rebuild(c->d, c->b, c->lc, 0, c->st));
+  if (c->prof && k < (int)c->ev0.size()) CK(cudaEventRecord(c->ev0[k], c->st));
+  RK(launch_force(c->d, c->b, c->sc, c->lc, lang ? 2 : 1, thermo, k, c->st));
+  if (c->prof && k < (int)c->ev1.size()) CK(cudaEventRecord(c->ev1[k], c->st));
+  c->kernel_launches += kernels_per_step(c);
+  if (thermo) {
+    const int nb_ke = lang ? drift_grid_blocks(c->lc) : force_grid_blocks(c->lc);
+    RK(launch_thermo_final(c->d, c->tc, nb_ke, force_grid_blocks(c->lc), ring_slot, c->st));
+    c->kernel_launches += 1;
+  }
+  return CAVGPU_OK;
+}
+
+int ensure_events(cavgpu_ctx *c, int S) {
+  while ((int)c->ev0.size() < S) {
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    c->ev0.push_back(a);
+    c->ev1.push_back(b);
+  }
+  return CAVGPU_OK;
+}
+
+int collect_profile(cavgpu_ctx *c, int count) {
+  CK(cudaStreamSynchronize(c->st));
+  for (int k = 0; k < count; ++k) {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c->ev0[k], c->ev1[k]));
+    c->prof_ms += ms;
+    c->prof_launches += 1;
+  }
+  return CAVGPU_OK;
+}
+
+GraphEntry *get_graph(cavgpu_ctx *c, int S, int every, int *rc) {
+  for (auto &g : c->graphs)
+    if (g.S == S && g.every == every && g.prof == (int)c->prof) return &g;
+  *rc = CAVGPU_OK;
+  if (c->prof && (*rc = ensure_events(c, S))) return nullptr;
+  cudaGraph_t graph = nullptr;
+  if ((*rc = cuda_rc(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal)))) return nullptr;
+  const long long kl = c->kernel_launches;
+  int erc = CAVGPU_OK;
+  for (int k = 0; k < S && !erc; ++k) {
+    const bool th = every > 0 && ((k + 1) % every == 0);
+    erc = enqueue_step(c, k, th, th ? (k + 1) / every - 1 : -1);
+  }
+  if (!erc) erc = launch_advance_step(c->d, S, c->st);
+  cudaError_t e = cudaStreamEndCapture(c->st, &graph);
+  c->kernel_launches = kl;  // capture does not launch
+  if (erc || e != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    *rc = erc ? erc : CAVGPU_E_CUDA;
+    return nullptr;
+  }
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) { *rc = CAVGPU_E_CUDA; return nullptr; }
+  c->graphs.push_back({S, every, (int)c->prof, exec});
+  return &c->graphs.back();
+}
+
+int read_flags(cavgpu_ctx *c, int *f) {
+  CK(cudaMemcpyAsync(f, c->d.flags, F_NWORDS * sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return CAVGPU_OK;
+}
+
+int check_status(cavgpu_ctx *c) {
+  int f[F_NWORDS];
+  RK(read_flags(c, f));
+  c->max_nb = std::max(c->max_nb, f[F_MAXNB]);
+  if (f[F_NAN]) return CAVGPU_E_NAN;
+  if (f[F_OVERFLOW]) return CAVGPU_E_NLIST_OVERFLOW;
+  return CAVGPU_OK;
+}
+
+// (re)allocate the neighbour list for `cap` slots per atom
+int alloc_nbr(cavgpu_ctx *c, int cap) {
+  cap = (cap + 31) / 32 * 32;
+  const int A = 32 / c->d.tpa;
+  const size_t rows = (size_t)((c->n + A - 1) / A) * A;
+  const size_t bytes = rows * (size_t)cap * sizeof(uint32_t);
+  if (c->d.nbr) {
+    auto it = std::find(c->allocs.begin(), c->allocs.end(), (void *)c->d.nbr);
+    if (it != c->allocs.end()) c->allocs.erase(it);
+    cudaFree(c->d.nbr);
+    c->d.nbr = nullptr;
+  }
+  void *q = nullptr;
+  if (cudaMalloc(&q, bytes) != cudaSuccess) { cudaGetLastError(); return CAVGPU_E_NOMEM; }
+  c->allocs.push_back(q);
+  c->d.nbr = static_cast<uint32_t *>(q);
+  c->d.cap = cap;
+  c->nbr_bytes = bytes;
+  free_graphs(c);  // graphs hold the old Dev by value
+  return CAVGPU_OK;
+}
+
+// forced list build; grows the capacity until the build fits
+int forced_build(cavgpu_ctx *c) {
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    int zero[F_NWORDS] = {0};
+    int f[F_NWORDS];
+    RK(read_flags(c, f));
+    zero[F_REBUILDS] = f[F_REBUILDS];
+    CK(cudaMemcpyAsync(c->d.flags, zero, sizeof(zero), cudaMemcpyHostToDevice, c->st));
+    RK(launch_rebuild(c->d, c->b, c->lc, 1, c->st));
+    c->kernel_launches += 8;
+    RK(read_flags(c, f));
+    c->max_nb = f[F_MAXNB];
+    if (!f[F_OVERFLOW]) return CAVGPU_OK;
+    RK(alloc_nbr(c, (int)(f[F_OVERFLOW] * 1.25) + 32));
+  }
+  return CAVGPU_E_NLIST_OVERFLOW;
+}
+
+int thermo_now(cavgpu_ctx *c, bool langevin_ke_from_drift) {
+  const int nb_ke = langevin_ke_from_drift ? drift_grid_blocks(c->lc) : force_grid_blocks(c->lc);
+  RK(launch_thermo_final(c->d, c->tc, nb_ke, force_grid_blocks(c->lc), -1, c->st));
+  c->kernel_launches += 1;
+  return CAVGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void cavgpu_default_params(cavgpu_params *p) {
+  std::memset(p, 0, sizeof(*p));
+  for (int a = 0; a < 3; ++a) { p->bc[a] = 1; p->hi[a] = 1.0; }
+  p->ntypes = 1;
+  p->nl_cutoff = 2.5;
+  p->nl_coef = 1.12347;  // Neighborlist::cutoff_extra_coef default (inc/caviar2/neighborlist.hpp:147)
+  p->lj_cutoff = 2.5;
+  for (int k = 0; k < CAVGPU_MAX_TYPES * CAVGPU_MAX_TYPES; ++k) { p->eps[k] = 1.0; p->sigma[k] = 1.0; }
+  for (int t = 0; t < CAVGPU_MAX_TYPES; ++t) p->mass[t] = 1.0;
+  p->k_b = 1.0;
+  p->dt = 0.001;
+  p->lang_kb = 1.0;
+  p->lang_kbt = -1.0;
+  p->n_r_df = 3;
+  p->precision = CAVGPU_FP64;
+}
+
+const char *cavgpu_strerror(int s) {
+  switch (s) {
+    case CAVGPU_OK: return "ok";
+    case CAVGPU_E_ARG: return "invalid argument";
+    case CAVGPU_E_CUDA: return "CUDA error (or no CUDA device)";
+    case CAVGPU_E_NAN: return "NaN acceleration";
+    case CAVGPU_E_NLIST_OVERFLOW: return "neighbour list capacity exceeded";
+    case CAVGPU_E_STATE: return "call out of order";
+    case CAVGPU_E_NOMEM: return "device allocation failed";
+    case CAVGPU_E_RANGE: return "size beyond the stated maximum";
+    default: return "unknown status";
+  }
+}
+
+int cavgpu_create(const cavgpu_params *p, cavgpu_ctx **out) {
+  if (!p || !out) return CAVGPU_E_ARG;
+  *out = nullptr;
+  if (p->ntypes < 1 || p->ntypes > CAVGPU_MAX_TYPES) return CAVGPU_E_ARG;
+  if (p->bc[0] != 1 || p->bc[1] != 1 || p->bc[2] != 1) return CAVGPU_E_ARG;
+  if (!(p->nl_cutoff > 0.0) || !(p->nl_coef >= 1.0) || !(p->lj_cutoff >= 0.0) || !(p->dt >= 0.0)) return CAVGPU_E_ARG;
+  if (p->precision != CAVGPU_FP64 && p->precision != CAVGPU_MIXED) return CAVGPU_E_ARG;
+  if (p->integrator != CAVGPU_VELOCITY_VERLET && p->integrator != CAVGPU_VELOCITY_VERLET_LANGEVIN) return CAVGPU_E_ARG;
+  if (p->n_r_df < 0 || p->n_r_df > 3) return CAVGPU_E_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) { cudaGetLastError(); return CAVGPU_E_CUDA; }
+  cavgpu_ctx *c = new (std::nothrow) cavgpu_ctx();
+  if (!c) return CAVGPU_E_NOMEM;
+  c->p = *p;
+  Box &b = c->b;
+  const double ce = p->nl_cutoff * p->nl_coef;  // Neighborlist::init (src/neighborlist.cpp:317)
+  c->cutoff_extra = ce;
+  for (int a = 0; a < 3; ++a) {
+    b.lo[a] = p->lo[a];
+    b.hi[a] = p->hi[a];
+    b.L[a] = p->hi[a] - p->lo[a];  // Domain::update_after_domain_change (src/domain.cpp:498)
+    if (!(b.L[a] >= 2.0 * ce)) { delete c; return CAVGPU_E_ARG; }  // one image per pair
+    int nc = (int)std::floor(b.L[a] / ce);
+    while (nc > 1 && b.L[a] / nc < ce * (1.0 + 1e-10)) --nc;
+    b.nc[a] = std::max(nc, 1);
+    b.w[a] = b.L[a] / b.nc[a];
+    b.inv_w[a] = 1.0 / b.w[a];
+    b.wf[a] = (float)b.w[a];
+    // Domain::calculate_local_domain with grid index 0 of 1 (src/domain.cpp:320-326)
+    c->lo_local[a] = p->lo[a] + (p->hi[a] - p->lo[a]) * 0 / 1;
+    const double hi_local = p->lo[a] + (p->hi[a] - p->lo[a]) * 1 / 1;
+    c->cutoff_inv = 1.0 / ce;
+    c->ref_nb[a] = (int)std::ceil((hi_local - c->lo_local[a]) * c->cutoff_inv);
+  }
+  b.ncell = b.nc[0] * b.nc[1] * b.nc[2];
+  b.ce2 = ce * ce;
+  b.ce2_lo = (float)(b.ce2 * (1.0 - 2e-4));
+  b.ce2_hi = (float)(b.ce2 * (1.0 + 2e-4));
+  b.thr2 = 0.25 * (ce - p->nl_cutoff) * (ce - p->nl_cutoff);
+  // pair table (force_field::Lj, src/force/lj.cpp:453-484)
+  PairTab &t = c->tab_h;
+  const int nt = p->ntypes;
+  t.nt = nt;
+  for (int a = 0; a < nt; ++a)
+    for (int q = 0; q < nt; ++q) {
+      const int k = a * nt + q;
+      const double rc = p->cutoff_list_on ? p->cutoff_list[k] : p->lj_cutoff;
+      const double rc2 = rc * rc, eps = p->eps[k], sig = p->sigma[k];
+      if (rc < 0.0) { delete c; return CAVGPU_E_ARG; }
+      t.rc2[k] = eps == 0.0 ? -1.0 : rc2;
+      t.sig2[k] = sig * sig;
+      t.eps4[k] = 4.0 * eps;
+      const double sc2 = rc2 > 0 ? sig * sig / rc2 : 0.0, sc6 = sc2 * sc2 * sc2;
+      t.gc[k] = rc2 > 0 ? 4.0 * eps * sc6 * (6.0 - 12.0 * sc6) / rc2 : 0.0;
+      t.uc[k] = 4.0 * eps * (sc6 * sc6 - sc6);
+    }
+  for (int a = 0; a < nt; ++a) {
+    t.mass[a] = p->mass[a];
+    t.minv[a] = p->mass[a] == 0.0 ? 0.0 : 1.0 / p->mass[a];  // Atom_data::add_type_mass (src/atom_data.cpp:368-383)
+  }
+  // integrator constants (src/md_simulator.cpp:394-405)
+  StepConsts &sc = c->sc;
+  sc.dt = p->dt;
+  sc.hdt = 0.5 * p->dt;
+  if (p->integrator == CAVGPU_VELOCITY_VERLET_LANGEVIN) {
+    const double fr = p->lang_friction, dt = p->dt;
+    sc.la = (2.0 - fr * dt) / (2.0 + fr * dt);
+    if (p->lang_kbt > 0) sc.lb = std::sqrt(p->lang_kbt * fr * 0.5 * dt);
+    else if (p->lang_kb > 0 && p->lang_temperature > 0) sc.lb = std::sqrt(p->lang_kb * p->lang_temperature * fr * 0.5 * dt);
+    else { delete c; return CAVGPU_E_ARG; }
+    sc.lc = 2.0 * dt / (2.0 + fr * dt);
+  }
+  sc.seed = p->seed;
+  sc.noise_off = p->noise_off;
+  // launch shape
+  c->lc.precision = p->precision;
+  c->lc.integrator = p->integrator;
+  c->lc.tpa = p->threads_per_atom ? p->threads_per_atom : (p->precision == CAVGPU_MIXED ? 4 : 4);
+  c->lc.block = p->block_size ? p->block_size : 128;
+  if (c->lc.tpa != 1 && c->lc.tpa != 2 && c->lc.tpa != 4 && c->lc.tpa != 8 && c->lc.tpa != 16) { delete c; return CAVGPU_E_ARG; }
+  if (c->lc.block < 32 || c->lc.block > 256 || c->lc.block % 32) { delete c; return CAVGPU_E_ARG; }
+  c->d.tpa = c->lc.tpa;
+  if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) { delete c; return CAVGPU_E_CUDA; }
+  int rc = dalloc(c, &c->d.tab, 1);
+  if (!rc) rc = dalloc(c, &c->d.flags, F_NWORDS);
+  if (!rc) rc = dalloc(c, &c->d.thermo, 8);
+  if (!rc) rc = dalloc(c, &c->d.step_base, 1);
+  if (!rc) rc = dalloc(c, &c->d.thermo_ring, 4 * (size_t)MAX_GRAPH_STEPS);
+  if (!rc) rc = cuda_rc(cudaMemcpyAsync(c->d.tab, &c->tab_h, sizeof(PairTab), cudaMemcpyHostToDevice, c->st));
+  if (!rc) rc = cuda_rc(cudaMemsetAsync(c->d.flags, 0, F_NWORDS * sizeof(int), c->st));
+  if (!rc) rc = cuda_rc(cudaMemsetAsync(c->d.thermo, 0, 8 * sizeof(double), c->st));
+  if (!rc) rc = cuda_rc(cudaMemsetAsync(c->d.step_base, 0, sizeof(long long), c->st));
+  if (!rc) rc = cuda_rc(cudaStreamSynchronize(c->st));
+  if (rc) { cavgpu_destroy(c); return rc; }
+  *out = c;
+  return CAVGPU_OK;
+}
+
+void cavgpu_destroy(cavgpu_ctx *c) {
+  if (!c) return;
+  if (c->st) cudaStreamSynchronize(c->st);
+  free_graphs(c);
+  for (auto e : c->ev0) cudaEventDestroy(e);
+  for (auto e : c->ev1) cudaEventDestroy(e);
+  for (void *q : c->allocs) cudaFree(q);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+}
+
+int cavgpu_upload(cavgpu_ctx *c, int64_t n, const double *pos3, const double *vel3, const uint64_t *type,
+                  const uint64_t *id) {
+  if (!c || n < 1 || !pos3 || !type) return CAVGPU_E_ARG;
+  if (c->uploaded) return CAVGPU_E_STATE;
+  if (n > MAX_ATOMS) return CAVGPU_E_RANGE;
+  const int N = (int)n;
+  std::vector<dbl4> hp(N), hv(N);
+  std::vector<int> ht(N);
+  std::vector<uint32_t> hid(N);
+  std::vector<char> seen(id ? N : 0, 0);
+  double msum = 0.0;
+  for (int i = 0; i < N; ++i) {
+    for (int a = 0; a < 3; ++a) {
+      const double x = pos3[3 * i + a];
+      // Atom_data::position_inside_global_domain (src/atom_data.cpp:548-559)
+      if (!(x >= c->p.lo[a] && x < c->p.hi[a])) return CAVGPU_E_ARG;
+    }
+    if (type[i] >= (uint64_t)c->p.ntypes) return CAVGPU_E_ARG;
+    const uint64_t ii = id ? id[i] : (uint64_t)i;
+    if (ii >= (uint64_t)N || (id && seen[ii]++)) return CAVGPU_E_ARG;  // ids must be a permutation of 0..n-1
+    hp[i] = make_dbl4(pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2], (double)type[i]);
+    hv[i] = vel3 ? make_dbl4(vel3[3 * i], vel3[3 * i + 1], vel3[3 * i + 2], 0.0) : make_dbl4(0, 0, 0, 0);
+    ht[i] = (int)type[i];
+    hid[i] = (uint32_t)ii;
+    msum += c->p.mass[type[i]];
+  }
+  c->n = N;
+  c->sc.n = N;
+  c->lc.n = N;
+  c->tc.n = N;
+  c->tc.n_r_df = c->p.n_r_df;
+  c->tc.k_b = c->p.k_b;
+  // finalize_pressure_mpi_domain volume (src/atom_data/kinetic_energy.cpp:242-243)
+  double vol = 1.0;
+  for (int a = 0; a < 3; ++a) vol *= (c->p.lo[a] + (c->p.hi[a] - c->p.lo[a]) * 1 / 1) - c->lo_local[a];
+  c->tc.volume = vol;
+  c->tc.langevin = c->p.integrator == CAVGPU_VELOCITY_VERLET_LANGEVIN;
+  Dev &d = c->d;
+  const size_t nblk = (size_t)std::max(force_grid_blocks(c->lc), 1);
+  const size_t nblk_d = (size_t)std::max((N + 255) / 256, 1);
+  int rc = CAVGPU_OK;
+  dbl4 **d4[] = {&d.pos, &d.vel, &d.acc, &d.acc_old, &d.pos_ref, &d.t_pos, &d.t_vel, &d.t_acc, &d.t_acc_old};
+  for (auto pp : d4) if (!rc) rc = dalloc(c, pp, N);
+  if (!rc) rc = dalloc(c, &d.rel, N);
+  int **di[] = {&d.type, &d.cell_of, &d.t_type, &d.atom_cell, &d.perm, &d.perm_tmp, &d.nnbr};
+  for (auto pp : di) if (!rc) rc = dalloc(c, pp, N);
+  if (!rc) rc = dalloc(c, &d.id, N);
+  if (!rc) rc = dalloc(c, &d.t_id, N);
+  if (!rc) rc = dalloc(c, &d.cell_count, c->b.ncell);
+  if (!rc) rc = dalloc(c, &d.cell_cursor, c->b.ncell);
+  if (!rc) rc = dalloc(c, &d.cell_start, (size_t)c->b.ncell + 1);
+  if (!rc) rc = dalloc(c, &d.partials_ke, 4 * std::max(nblk, nblk_d));
+  if (!rc) rc = dalloc(c, &d.partials_ev, 2 * nblk);
+  if (!rc) rc = dalloc(c, &d.h3, 3 * (size_t)N);
+  if (!rc) rc = dalloc(c, &d.hi3, 3 * (size_t)N);
+  if (rc) return rc;
+  // initial capacity from the density: 1.4 x the mean count in the cutoff sphere, plus headroom
+  const double rho = N / (c->b.L[0] * c->b.L[1] * c->b.L[2]);
+  const double ce = c->cutoff_extra;
+  int cap = c->p.nbr_capacity > 0 ? c->p.nbr_capacity : (int)(1.4 * rho * 4.18879020479 * ce * ce * ce) + 48;
+  RK(alloc_nbr(c, cap));
+  CK(cudaMemcpyAsync(d.pos, hp.data(), N * sizeof(dbl4), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(d.vel, hv.data(), N * sizeof(dbl4), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemsetAsync(d.acc, 0, N * sizeof(dbl4), c->st));
+  CK(cudaMemsetAsync(d.acc_old, 0, N * sizeof(dbl4), c->st));
+  CK(cudaMemcpyAsync(d.type, ht.data(), N * sizeof(int), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(d.id, hid.data(), N * sizeof(uint32_t), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemsetAsync(d.cell_count, 0, c->b.ncell * sizeof(int), c->st));
+  CK(cudaMemsetAsync(d.cell_cursor, 0, c->b.ncell * sizeof(int), c->st));
+  double th[8] = {0, 0, 0, 0, 0, msum, 0, 0};
+  CK(cudaMemcpyAsync(d.thermo, th, sizeof(th), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->uploaded = true;
+  return CAVGPU_OK;
+}
+
+int cavgpu_setup(cavgpu_ctx *c) {
+  if (!c) return CAVGPU_E_ARG;
+  if (!c->uploaded) return CAVGPU_E_STATE;
+  RK(forced_build(c));
+  RK(launch_force(c->d, c->b, c->sc, c->lc, 0, 1, 0, c->st));
+  c->kernel_launches += 1;
+  RK(thermo_now(c, false));
+  RK(check_status(c));
+  c->set_up = true;
+  return CAVGPU_OK;
+}
+
+int cavgpu_run(cavgpu_ctx *c, int64_t nsteps, int64_t every, double *out4) {
+  if (!c || nsteps < 0 || every < 0 || (every > 0 && !out4)) return CAVGPU_E_ARG;
+  if (!c->set_up) return CAVGPU_E_STATE;
+  if (nsteps == 0) return CAVGPU_OK;
+  const bool lang = c->p.integrator == CAVGPU_VELOCITY_VERLET_LANGEVIN;
+  int S = c->p.steps_per_graph > 0 ? std::min(c->p.steps_per_graph, MAX_GRAPH_STEPS) : 50;
+  if (every > 0) S = (int)std::max<int64_t>(every, (S / every) * every);
+  const int nrec = every > 0 ? (int)(S / every) : 0;
+  int64_t done = 0, rec = 0;
+  int rc = CAVGPU_OK;
+  // whole chunks through the graph
+  while (nsteps - done >= S && nsteps - done > 1) {
+    // keep the last step out of the graph when no thermo recording is asked, so that the
+    // final state always carries a fresh temperature (finalize_temperature runs every step)
+    if (every == 0 && nsteps - done == S) break;
+    GraphEntry *g = get_graph(c, S, (int)every, &rc);
+    if (!g) return rc;
+    CK(cudaGraphLaunch(g->exec, c->st));
+    c->graph_launches += 1;
+    c->kernel_launches += (long long)S * kernels_per_step(c) + 1 + (every > 0 ? nrec : 0);
+    if (c->prof) RK(collect_profile(c, S));
+    RK(check_status(c));
+    if (every > 0) {
+      CK(cudaMemcpyAsync(out4 + 4 * rec, c->d.thermo_ring, 4 * sizeof(double) * nrec, cudaMemcpyDeviceToHost, c->st));
+      CK(cudaStreamSynchronize(c->st));
+      rec += nrec;
+    }
+    done += S;
+    c->steps_done += S;
+  }
+  // remaining steps eagerly
+  while (done < nsteps) {
+    const bool last = done == nsteps - 1;
+    const bool th = (every > 0 && (done + 1) % every == 0) || (every == 0 && last);
+    if (c->prof) RK(ensure_events(c, 1));
+    RK(enqueue_step(c, 0, th, (every > 0 && th) ? 0 : -1));
+    RK(launch_advance_step(c->d, 1, c->st));
+    c->kernel_launches += 1;
+    if (c->prof) RK(collect_profile(c, 1));
+    if (every > 0 && th) {
+      CK(cudaMemcpyAsync(out4 + 4 * rec, c->d.thermo_ring, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+      rec += 1;
+    }
+    ++done;
+    c->steps_done += 1;
+  }
+  RK(check_status(c));
+  (void)lang;
+  return CAVGPU_OK;
+}
+
+int cavgpu_step(cavgpu_ctx *c, int64_t nsteps) { return cavgpu_run(c, nsteps, 0, nullptr); }
+
+int cavgpu_forces(cavgpu_ctx *c, double *virial, double *pe) {
+  if (!c) return CAVGPU_E_ARG;
+  if (!c->set_up) return CAVGPU_E_STATE;
+  RK(forced_build(c));
+  RK(launch_force(c->d, c->b, c->sc, c->lc, 0, 1, 0, c->st));
+  c->kernel_launches += 1;
+  RK(thermo_now(c, false));
+  RK(check_status(c));
+  double th[8];
+  CK(cudaMemcpyAsync(th, c->d.thermo, sizeof(th), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (virial) *virial = th[3];
+  if (pe) *pe = th[4];
+  return CAVGPU_OK;
+}
+
+int cavgpu_thermo(cavgpu_ctx *c, double *out6) {
+  if (!c || !out6) return CAVGPU_E_ARG;
+  if (!c->set_up) return CAVGPU_E_STATE;
+  double th[8];
+  int f[F_NWORDS];
+  CK(cudaMemcpyAsync(th, c->d.thermo, sizeof(th), cudaMemcpyDeviceToHost, c->st));
+  RK(read_flags(c, f));
+  for (int k = 0; k < 5; ++k) out6[k] = th[k];
+  out6[5] = (double)f[F_REBUILDS];
+  return CAVGPU_OK;
+}
+
+int cavgpu_download(cavgpu_ctx *c, double *pos3, double *vel3, double *acc3) {
+  if (!c) return CAVGPU_E_ARG;
+  if (!c->uploaded) return CAVGPU_E_STATE;
+  double *outs[3] = {pos3, vel3, acc3};
+  for (int w = 0; w < 3; ++w) {
+    if (!outs[w]) continue;
+    RK(launch_to_host_order(c->d, c->b, c->n, w, c->st));
+    CK(cudaMemcpyAsync(outs[w], c->d.h3, 3 * sizeof(double) * c->n, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+  }
+  return CAVGPU_OK;
+}
+
+int64_t cavgpu_export_pairs(cavgpu_ctx *c, int32_t *out5, int64_t cap) {
+  if (!c || (cap > 0 && !out5)) return CAVGPU_E_ARG;
+  if (!c->set_up) return CAVGPU_E_STATE;
+  std::vector<int> nn(c->n);
+  if (cudaMemcpyAsync(nn.data(), c->d.nnbr, c->n * sizeof(int), cudaMemcpyDeviceToHost, c->st) != cudaSuccess ||
+      cudaStreamSynchronize(c->st) != cudaSuccess)
+    return CAVGPU_E_CUDA;
+  int64_t total = 0;
+  for (int v : nn) total += v;
+  const int64_t take = std::min(total, cap);
+  if (take <= 0) return total;
+  int32_t *rows = nullptr;
+  unsigned long long *cnt = nullptr;
+  if (cudaMalloc(&rows, (size_t)take * 5 * sizeof(int32_t)) != cudaSuccess) { cudaGetLastError(); return CAVGPU_E_NOMEM; }
+  if (cudaMalloc(&cnt, sizeof(unsigned long long)) != cudaSuccess) { cudaFree(rows); cudaGetLastError(); return CAVGPU_E_NOMEM; }
+  int rc = cuda_rc(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), c->st));
+  if (!rc) rc = launch_export_pairs(c->d, c->b, c->n, c->p.precision == CAVGPU_MIXED ? 1 : 0, rows, cnt, take, c->st);
+  if (!rc) rc = cuda_rc(cudaMemcpyAsync(out5, rows, (size_t)take * 5 * sizeof(int32_t), cudaMemcpyDeviceToHost, c->st));
+  if (!rc) rc = cuda_rc(cudaStreamSynchronize(c->st));
+  cudaFree(rows);
+  cudaFree(cnt);
+  return rc ? rc : total;
+}
+
+int cavgpu_export_bins(cavgpu_ctx *c, int32_t *owned3, int32_t *nbins3) {
+  if (!c) return CAVGPU_E_ARG;
+  if (!c->uploaded) return CAVGPU_E_STATE;
+  if (nbins3) for (int a = 0; a < 3; ++a) nbins3[a] = c->ref_nb[a];
+  if (!owned3) return CAVGPU_OK;
+  RK(launch_to_host_order(c->d, c->b, c->n, 0, c->st));
+  RK(launch_ref_bins(c->d, c->n, c->cutoff_inv, c->ref_nb, c->lo_local, c->st));
+  CK(cudaMemcpyAsync(owned3, c->d.hi3, 3 * sizeof(int32_t) * c->n, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return CAVGPU_OK;
+}
+
+int64_t cavgpu_export_ghosts(cavgpu_ctx *c, double ghost_cutoff, int32_t *src, int32_t *shift3, double *pos3,
+                             int32_t *bins3, int64_t cap) {
+  if (!c || ghost_cutoff < 0.0) return CAVGPU_E_ARG;
+  if (!c->uploaded) return CAVGPU_E_STATE;
+  const int N = c->n;
+  int *counts = nullptr, *starts = nullptr;
+  int32_t *gs = nullptr, *gsh = nullptr, *gb = nullptr;
+  double *gp = nullptr;
+  const int64_t gcap = std::max<int64_t>(cap, 0);
+  int rc = CAVGPU_OK;
+  auto M = [&](void **q, size_t bytes) {
+    if (!rc && cudaMalloc(q, std::max<size_t>(bytes, 16)) != cudaSuccess) { cudaGetLastError(); rc = CAVGPU_E_NOMEM; }
+  };
+  M((void **)&counts, (size_t)N * sizeof(int));
+  M((void **)&starts, ((size_t)N + 1) * sizeof(int));
+  M((void **)&gs, (size_t)gcap * sizeof(int32_t));
+  M((void **)&gsh, (size_t)gcap * 3 * sizeof(int32_t));
+  M((void **)&gp, (size_t)gcap * 3 * sizeof(double));
+  M((void **)&gb, (size_t)gcap * 3 * sizeof(int32_t));
+  int total = 0;
+  if (!rc) rc = launch_to_host_order(c->d, c->b, N, 0, c->st);
+  if (!rc) rc = launch_ghosts(c->d, c->b, N, ghost_cutoff, counts, starts, gs, gsh, gp, gb, gcap, c->cutoff_inv,
+                              c->ref_nb, c->lo_local, c->st);
+  if (!rc) rc = cuda_rc(cudaMemcpyAsync(&total, starts + N, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  if (!rc) rc = cuda_rc(cudaStreamSynchronize(c->st));
+  const int64_t take = std::min<int64_t>(total, gcap);
+  if (!rc && take > 0) {
+    if (src) rc = cuda_rc(cudaMemcpy(src, gs, take * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    if (!rc && shift3) rc = cuda_rc(cudaMemcpy(shift3, gsh, take * 3 * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    if (!rc && pos3) rc = cuda_rc(cudaMemcpy(pos3, gp, take * 3 * sizeof(double), cudaMemcpyDeviceToHost));
+    if (!rc && bins3) rc = cuda_rc(cudaMemcpy(bins3, gb, take * 3 * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  }
+  cudaFree(counts); cudaFree(starts); cudaFree(gs); cudaFree(gsh); cudaFree(gp); cudaFree(gb);
+  return rc ? rc : total;
+}
+
+int cavgpu_stats(cavgpu_ctx *c, int64_t *o) {
+  if (!c || !o) return CAVGPU_E_ARG;
+  int f[F_NWORDS] = {0};
+  if (c->uploaded) RK(read_flags(c, f));
+  o[0] = c->steps_done;
+  o[1] = f[F_REBUILDS];
+  o[2] = std::max(c->max_nb, f[F_MAXNB]);
+  o[3] = c->d.cap;
+  o[4] = c->lc.tpa;
+  o[5] = c->lc.block;
+  o[6] = c->graph_launches;
+  o[7] = c->kernel_launches;
+  return CAVGPU_OK;
+}
+
+void *cavgpu_stream(cavgpu_ctx *c) { return c ? (void *)c->st : nullptr; }
+
+int cavgpu_set_profiling(cavgpu_ctx *c, int32_t on) {
+  if (!c) return CAVGPU_E_ARG;
+  c->prof = on != 0;
+  c->prof_ms = 0.0;
+  c->prof_launches = 0;
+  return CAVGPU_OK;
+}
+
+int cavgpu_read_profile(cavgpu_ctx *c, double *out2) {
+  if (!c || !out2) return CAVGPU_E_ARG;
+  out2[0] = (double)c->prof_launches;
+  out2[1] = c->prof_ms;
+  return CAVGPU_OK;
+}
+
+}  // extern "C"

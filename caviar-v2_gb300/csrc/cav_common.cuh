@@ -1,0 +1,198 @@
+// cav_common.cuh -- device state, constants and small device helpers shared by
+// the sm_103a kernels of the CAVIAR2 MD step.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "cavgpu.h"
+
+namespace cav {
+
+// 32-byte aligned 4-vector of doubles: one 256-bit access per atom
+typedef double4_32a dbl4;
+__host__ __device__ inline dbl4 make_dbl4(double x, double y, double z, double w) {
+  dbl4 r;
+  r.x = x; r.y = y; r.z = z; r.w = w;
+  return r;
+}
+// read-only (non-coherent) 256-bit load of a neighbour's position
+__device__ inline dbl4 ldg_dbl4(const dbl4 *p) {
+  dbl4 r;
+  asm("ld.global.nc.v4.f64 {%0,%1,%2,%3}, [%4];" : "=d"(r.x), "=d"(r.y), "=d"(r.z), "=d"(r.w) : "l"(p));
+  return r;
+}
+
+constexpr int MAXT = CAVGPU_MAX_TYPES;
+// neighbour entry: bits 0..26 = atom slot j, bits 27..31 = image code (0..26)
+constexpr int CODE_SHIFT = 27;
+constexpr uint32_t IDX_MASK = (1u << CODE_SHIFT) - 1u;
+constexpr int64_t MAX_ATOMS = (int64_t)IDX_MASK;  // 134,217,727
+constexpr int CODE_ZERO = 13;                      // (0,0,0)
+
+// device flag words
+enum Flag : int {
+  F_REBUILD = 0,   // list must be rebuilt before the next force (half-skin test fired)
+  F_MAXNB = 1,     // largest neighbour count seen by the last build
+  F_OVERFLOW = 2,  // a build wanted more than `cap` slots
+  F_NAN = 3,       // NaN acceleration seen
+  F_NAN_ATOM = 4,  // host index of one NaN atom
+  F_REBUILDS = 5,  // rebuild count
+  F_NWORDS = 8
+};
+
+// Per type-pair constants of the shifted-force LJ (force_field::Lj,
+// src/force/lj.cpp:470-484).  For r^2 <= rc2:
+//   coef(r) = g(r) - g(rc),  g(r) = eps4 * s6 * (6 - 12 s6) / r^2,  s6 = (sig2/r^2)^3
+//   V(r)    = eps4 (s6^2 - s6) - uc - gc/2 (r^2 - rc2),  gc = g(rc), uc = U(rc)
+// rc2 < 0 marks an eps == 0 pair (skipped, src/force/lj.cpp:471-472).
+struct PairTab {
+  double rc2[MAXT * MAXT], sig2[MAXT * MAXT], eps4[MAXT * MAXT], gc[MAXT * MAXT], uc[MAXT * MAXT];
+  double minv[MAXT], mass[MAXT];
+  int nt;
+};
+
+struct Box {
+  double lo[3], hi[3], L[3];
+  int nc[3];          // search grid cells per axis (cell width >= list cutoff)
+  double w[3], inv_w[3];
+  float wf[3];
+  double ce2;         // cutoff_extra^2, the list predicate r^2 < ce2 (src/neighborlist.cpp:258, :508)
+  float ce2_lo, ce2_hi;  // FP32 pre-screen band around ce2
+  double thr2;        // 0.25 (cutoff_extra - cutoff)^2 (src/neighborlist.cpp:318)
+  int ncell;
+};
+
+struct StepConsts {
+  double dt, hdt, dt2h;       // dt, 0.5*dt, unused
+  double la, lb, lc;          // Langevin a, b, c (src/md_simulator.cpp:398-405)
+  uint64_t seed;
+  int noise_off;
+  int n;
+};
+
+// Device arrays of one system, in cell-sorted slot order.
+struct Dev {
+  dbl4 *pos, *vel, *acc, *acc_old, *pos_ref;
+  float4 *rel;                // position relative to the build cell's origin; w = type bits
+  int *type;
+  uint32_t *id;               // host (insertion) index
+  int *cell_of;               // build cell of each slot
+  // rebuild scratch
+  dbl4 *t_pos, *t_vel, *t_acc, *t_acc_old;
+  int *t_type;
+  uint32_t *t_id;
+  int *atom_cell, *cell_count, *cell_start, *cell_cursor, *perm, *perm_tmp;
+  // neighbour list
+  uint32_t *nbr;
+  int *nnbr;
+  int cap;                    // slots per atom (multiple of 32)
+  int tpa;                    // force-kernel lanes per atom (fixes the list layout)
+  // status, reductions
+  int *flags;
+  double *partials_ke;        // per-block {sum m v^2, sum m v} (4 per block)
+  double *partials_ev;        // per-block {sum -coef r^2, sum V} over both pair orders (2 per block)
+  double *thermo;             // {KE, T, P, virialForce, PE, total mass, -, -}
+  double *thermo_ring;        // recorded thermo points (4 per record)
+  long long *step_base;       // step counter read by the Langevin kernels
+  PairTab *tab;
+  // host-order staging for downloads
+  double *h3;
+  int32_t *hi3;
+};
+
+// ---- neighbour-list layout -------------------------------------------------
+// For a force kernel with `tpa` lanes per atom, a warp serves A = 32/tpa atoms;
+// entry k of atom i sits so that one warp-wide load reads 32 consecutive words.
+__host__ __device__ inline size_t nbr_index(int i, int k, int cap, int tpa) {
+  const int A = 32 / tpa;
+  return (size_t)(i / A) * (size_t)cap * A + (size_t)(k / tpa) * 32 + (size_t)(k % tpa) * A + (i % A);
+}
+
+__host__ __device__ inline int image_code(int sx, int sy, int sz) { return (sx + 1) + 3 * (sy + 1) + 9 * (sz + 1); }
+
+// ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) -----------------------
+__device__ inline void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    if (r) { k0 += W0; k1 += W1; }
+    const uint32_t hi0 = __umulhi(M0, c[0]), lo0 = M0 * c[0];
+    const uint32_t hi1 = __umulhi(M1, c[2]), lo1 = M1 * c[2];
+    const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+    c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+  }
+}
+
+constexpr uint32_t LANG_TAG = 0x4C414E47u;
+
+// Langevin noise of atom `id` at `step`: Box-Muller on one Philox block (FP64).
+__device__ inline void langevin_eta(uint64_t seed, long long step, uint32_t id, double &e0, double &e1, double &e2) {
+  uint32_t c[4] = {(uint32_t)step, (uint32_t)((unsigned long long)step >> 32), id, LANG_TAG};
+  philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+  const double s = 2.3283064365386963e-10;  // 2^-32
+  const double u0 = ((double)c[0] + 0.5) * s, u1 = ((double)c[1] + 0.5) * s;
+  const double u2 = ((double)c[2] + 0.5) * s, u3 = ((double)c[3] + 0.5) * s;
+  const double r0 = sqrt(-2.0 * log(u0)), r1 = sqrt(-2.0 * log(u2));
+  double sn, cs;
+  sincospi(2.0 * u1, &sn, &cs);
+  e0 = r0 * cs;
+  e1 = r0 * sn;
+  e2 = r1 * cospi(2.0 * u3);
+}
+
+// FP32 variant for the mixed-precision form (noise precision is immaterial).
+__device__ inline void langevin_eta_f(uint64_t seed, long long step, uint32_t id, double &e0, double &e1,
+                                      double &e2) {
+  uint32_t c[4] = {(uint32_t)step, (uint32_t)((unsigned long long)step >> 32), id, LANG_TAG};
+  philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+  const float s = 2.3283064365386963e-10f;
+  const float u0 = ((float)c[0] + 0.5f) * s, u1 = ((float)c[1] + 0.5f) * s;
+  const float u2 = ((float)c[2] + 0.5f) * s, u3 = ((float)c[3] + 0.5f) * s;
+  const float r0 = sqrtf(-2.0f * logf(fmaxf(u0, 1e-30f))), r1 = sqrtf(-2.0f * logf(fmaxf(u2, 1e-30f)));
+  float sn, cs;
+  sincospif(2.0f * u1, &sn, &cs);
+  e0 = (double)(r0 * cs);
+  e1 = (double)(r0 * sn);
+  e2 = (double)(r1 * cospif(2.0f * u3));
+}
+
+// ---- host-side launch helpers (defined in cav_kernels.cu) -------------------
+struct LaunchCfg {
+  int precision;   // CAVGPU_FP64 / CAVGPU_MIXED
+  int integrator;  // CAVGPU_VELOCITY_VERLET / ..._LANGEVIN
+  int tpa, block;
+  int n;
+  int pressure;    // n_r_df etc. are in ThermoCfg
+};
+
+struct ThermoCfg {
+  int n_r_df;
+  double k_b, volume;
+  int n;
+  int langevin;  // pressure without the force virial (computed before the force)
+};
+
+// Kernel launchers.  `forced` rebuilds regardless of the device flag; otherwise
+// the rebuild kernels return at once unless the half-skin test set F_REBUILD.
+int drift_grid_blocks(const LaunchCfg &lc);
+int force_grid_blocks(const LaunchCfg &lc);
+int launch_drift(const Dev &d, const Box &b, const StepConsts &sc, const LaunchCfg &lc, int k_in_chunk,
+                 int thermo, cudaStream_t st);
+int launch_rebuild(const Dev &d, const Box &b, const LaunchCfg &lc, int forced, cudaStream_t st);
+// kick: 0 = force only, 1 = VV closing kick, 2 = Langevin closing update.
+// thermo: virial/PE partials (and KE partials unless kick == 2).
+int launch_force(const Dev &d, const Box &b, const StepConsts &sc, const LaunchCfg &lc, int kick, int thermo,
+                 int k_in_chunk, cudaStream_t st);
+int launch_thermo_final(const Dev &d, const ThermoCfg &tc, int nb_ke, int nb_ev, int ring_slot, cudaStream_t st);
+int launch_advance_step(const Dev &d, int nsteps, cudaStream_t st);
+int launch_to_host_order(const Dev &d, const Box &b, int n, int what, cudaStream_t st);
+int launch_export_pairs(const Dev &d, const Box &b, int n, int mode, int32_t *rows, unsigned long long *counter,
+                        int64_t cap, cudaStream_t st);
+int launch_ref_bins(const Dev &d, int n, double cutoff_inv, const int nb[3], const double lo_local[3],
+                    cudaStream_t st);
+int launch_ghosts(const Dev &d, const Box &b, int n, double gc, int *counts, int *starts, int32_t *src,
+                  int32_t *shift3, double *pos3, int32_t *bins3, int64_t cap, double cutoff_inv, const int nb[3],
+                  const double lo_local[3], cudaStream_t st);
+
+}  // namespace cav

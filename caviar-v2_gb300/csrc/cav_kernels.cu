@@ -1,0 +1,562 @@
+// cav_kernels.cu -- sm_103a kernels of the CAVIAR2 MD step (cell binning,
+// Verlet-list build, integrator stages, thermo reductions, parity exports).
+// The pair-force kernels live in cav_force.cu.
+#include "cav_common.cuh"
+
+namespace cav {
+
+#define FULL_MASK 0xffffffffu
+
+static inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// ---------------------------------------------------------------------------
+// block reduction of NV doubles in a fixed order (deterministic)
+// ---------------------------------------------------------------------------
+template <int NV>
+__device__ inline void block_sum_store(double (&v)[NV], double *out /* NV doubles */) {
+  __shared__ double sh[32][NV];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(FULL_MASK, v[k], o);
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) sh[wid][k] = v[k];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < NV; ++k) {
+      double s = 0.0;
+      for (int w = 0; w < nw; ++w) s += sh[w][k];
+      out[k] = s;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// integrator stage 1: drift (velocity Verlet) -- src/md_simulator.cpp:640-656
+//   r(t+dt) = r + v dt + 0.5 a dt^2 ; a_old = a ; NaN check ; half-skin test
+// ---------------------------------------------------------------------------
+__device__ inline void update_rel(const Dev &d, const Box &b, int i, const dbl4 &x) {
+  const int c = d.cell_of[i];
+  const int cx = c % b.nc[0], cy = (c / b.nc[0]) % b.nc[1], cz = c / (b.nc[0] * b.nc[1]);
+  float4 r;
+  r.x = (float)(x.x - (b.lo[0] + cx * b.w[0]));
+  r.y = (float)(x.y - (b.lo[1] + cy * b.w[1]));
+  r.z = (float)(x.z - (b.lo[2] + cz * b.w[2]));
+  r.w = __int_as_float((int)x.w);
+  d.rel[i] = r;
+}
+
+__device__ inline void half_skin_test(const Dev &d, const Box &b, int i, const dbl4 &x) {
+  const dbl4 r = d.pos_ref[i];
+  const double dx = x.x - r.x, dy = x.y - r.y, dz = x.z - r.z;
+  if (dx * dx + dy * dy + dz * dz > b.thr2) d.flags[F_REBUILD] = 1;
+}
+
+__device__ inline void nan_check(const Dev &d, int i, const dbl4 &a) {
+  if (isnan(a.x) || isnan(a.y) || isnan(a.z)) {
+    d.flags[F_NAN] = 1;
+    d.flags[F_NAN_ATOM] = (int)d.id[i];
+  }
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(256) k_drift_vv(Dev d, Box b, StepConsts sc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= sc.n) return;
+  dbl4 x = d.pos[i];
+  const dbl4 v = d.vel[i], a = d.acc[i];
+  nan_check(d, i, a);
+  // pos += vel*dt + ((acc*0.5)*dt)*dt, unfused as in the reference expression
+  x.x = __dadd_rn(x.x, __dadd_rn(__dmul_rn(v.x, sc.dt), __dmul_rn(__dmul_rn(__dmul_rn(a.x, 0.5), sc.dt), sc.dt)));
+  x.y = __dadd_rn(x.y, __dadd_rn(__dmul_rn(v.y, sc.dt), __dmul_rn(__dmul_rn(__dmul_rn(a.y, 0.5), sc.dt), sc.dt)));
+  x.z = __dadd_rn(x.z, __dadd_rn(__dmul_rn(v.z, sc.dt), __dmul_rn(__dmul_rn(__dmul_rn(a.z, 0.5), sc.dt), sc.dt)));
+  d.pos[i] = x;
+  d.acc_old[i] = a;
+  half_skin_test(d, b, i, x);
+  if (MIXED) update_rel(d, b, i, x);
+}
+
+// Langevin first half (src/md_simulator.cpp:748-837):
+//   v += (a*0.5)*dt + eta*b ; [temperature here] ; r += v*c
+template <bool MIXED, bool THERMO>
+__global__ void __launch_bounds__(256) k_lang_a(Dev d, Box b, StepConsts sc, int k_in_chunk) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double part[4] = {0.0, 0.0, 0.0, 0.0};
+  if (i < sc.n) {
+    dbl4 x = d.pos[i], v = d.vel[i];
+    const dbl4 a = d.acc[i];
+    nan_check(d, i, a);
+    double e0 = 0.0, e1 = 0.0, e2 = 0.0;
+    if (!sc.noise_off) {
+      const long long step = *d.step_base + k_in_chunk;
+      if (MIXED) langevin_eta_f(sc.seed, step, d.id[i], e0, e1, e2);
+      else langevin_eta(sc.seed, step, d.id[i], e0, e1, e2);
+    }
+    v.x = __dadd_rn(v.x, __dadd_rn(__dmul_rn(__dmul_rn(a.x, 0.5), sc.dt), __dmul_rn(e0, sc.lb)));
+    v.y = __dadd_rn(v.y, __dadd_rn(__dmul_rn(__dmul_rn(a.y, 0.5), sc.dt), __dmul_rn(e1, sc.lb)));
+    v.z = __dadd_rn(v.z, __dadd_rn(__dmul_rn(__dmul_rn(a.z, 0.5), sc.dt), __dmul_rn(e2, sc.lb)));
+    if (THERMO) {
+      const double m = d.tab->mass[(int)x.w];
+      part[0] = m * (v.x * v.x + v.y * v.y + v.z * v.z);
+      part[1] = m * v.x; part[2] = m * v.y; part[3] = m * v.z;
+    }
+    x.x = __dadd_rn(x.x, __dmul_rn(v.x, sc.lc));
+    x.y = __dadd_rn(x.y, __dmul_rn(v.y, sc.lc));
+    x.z = __dadd_rn(x.z, __dmul_rn(v.z, sc.lc));
+    d.pos[i] = x;
+    d.vel[i] = v;
+    half_skin_test(d, b, i, x);
+    if (MIXED) update_rel(d, b, i, x);
+  }
+  if (THERMO) block_sum_store<4>(part, &d.partials_ke[(size_t)blockIdx.x * 4]);
+}
+
+// ---------------------------------------------------------------------------
+// list rebuild: wrap + bin -> scan -> scatter -> per-cell sort -> gather -> build
+// (Neighborlist::update_cell_list + update_verlet_list_from_cell_list,
+//  src/neighborlist.cpp:422-455, 496-553; Domain::fix_position, src/domain.cpp:443-493)
+// ---------------------------------------------------------------------------
+__device__ inline bool rebuild_off(const Dev &d, int forced) { return !forced && d.flags[F_REBUILD] == 0; }
+
+__global__ void __launch_bounds__(256) k_bin(Dev d, Box b, int n, int forced) {
+  if (rebuild_off(d, forced)) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool act = i < n;
+  int c = 0;
+  if (act) {
+    dbl4 p = d.pos[i];
+    // single-image wrap exactly as Domain::fix_position
+    if (p.x < b.lo[0]) p.x += b.L[0]; else if (p.x > b.hi[0]) p.x -= b.L[0];
+    if (p.y < b.lo[1]) p.y += b.L[1]; else if (p.y > b.hi[1]) p.y -= b.L[1];
+    if (p.z < b.lo[2]) p.z += b.L[2]; else if (p.z > b.hi[2]) p.z -= b.L[2];
+    d.pos[i] = p;
+    int cx = (int)floor((p.x - b.lo[0]) * b.inv_w[0]);
+    int cy = (int)floor((p.y - b.lo[1]) * b.inv_w[1]);
+    int cz = (int)floor((p.z - b.lo[2]) * b.inv_w[2]);
+    cx = min(max(cx, 0), b.nc[0] - 1);
+    cy = min(max(cy, 0), b.nc[1] - 1);
+    cz = min(max(cz, 0), b.nc[2] - 1);
+    c = cx + b.nc[0] * (cy + b.nc[1] * cz);
+    d.atom_cell[i] = c;
+  }
+  if (i == 0) d.flags[F_MAXNB] = 0;
+  // warp-aggregated counting: one atomic per distinct cell in the warp
+  const unsigned m = __ballot_sync(FULL_MASK, act);
+  if (act) {
+    const unsigned peers = __match_any_sync(m, c);
+    if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&d.cell_count[c], __popc(peers));
+  }
+}
+
+// exclusive scan of `count[0..m)` into start[0..m] with one block; zeroes
+// count and (if non-null) cursor for the next use
+__global__ void __launch_bounds__(1024) k_scan(const Dev d, int *count, int *start, int *cursor, int m, int forced) {
+  if (rebuild_off(d, forced)) return;
+  __shared__ int warp_tot[32];
+  const int t = threadIdx.x, nt = blockDim.x;
+  const int per = (m + nt - 1) / nt;
+  const int beg = min(t * per, m), end = min(beg + per, m);
+  int s = 0;
+  for (int k = beg; k < end; ++k) s += count[k];
+  // block exclusive scan of s
+  const int lane = t & 31, wid = t >> 5;
+  int inc = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(FULL_MASK, inc, o);
+    if (lane >= o) inc += y;
+  }
+  if (lane == 31) warp_tot[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    int wv = lane < (nt >> 5) ? warp_tot[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(FULL_MASK, wv, o);
+      if (lane >= o) wv += y;
+    }
+    warp_tot[lane] = wv;
+  }
+  __syncthreads();
+  int run = inc - s + (wid ? warp_tot[wid - 1] : 0);
+  for (int k = beg; k < end; ++k) {
+    start[k] = run;
+    run += count[k];
+    count[k] = 0;
+    if (cursor) cursor[k] = 0;
+  }
+  if (t == nt - 1) start[m] = run;
+}
+
+__global__ void __launch_bounds__(256) k_scatter(Dev d, int n, int forced) {
+  if (rebuild_off(d, forced)) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int c = d.atom_cell[i];
+  d.perm_tmp[d.cell_start[c] + atomicAdd(&d.cell_cursor[c], 1)] = i;
+}
+
+// one warp per cell: order the cell's atoms by host index (deterministic lists)
+__global__ void __launch_bounds__(256) k_cell_sort(Dev d, int ncell, int forced) {
+  if (rebuild_off(d, forced)) return;
+  const int cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (cell >= ncell) return;
+  const int s = d.cell_start[cell], e = d.cell_start[cell + 1], n = e - s;
+  for (int a = lane; a < n; a += 32) {
+    const int ia = d.perm_tmp[s + a];
+    const uint32_t ida = d.id[ia];
+    int rank = 0;
+    for (int q = 0; q < n; ++q) rank += d.id[d.perm_tmp[s + q]] < ida;
+    d.perm[s + rank] = ia;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_copy_state(Dev d, int n, int forced) {
+  if (rebuild_off(d, forced)) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  d.t_pos[i] = d.pos[i];
+  d.t_vel[i] = d.vel[i];
+  d.t_acc[i] = d.acc[i];
+  d.t_acc_old[i] = d.acc_old[i];
+  d.t_type[i] = d.type[i];
+  d.t_id[i] = d.id[i];
+  d.perm_tmp[i] = d.atom_cell[i];  // cell of old slot i (perm_tmp is free again)
+}
+
+__global__ void __launch_bounds__(256) k_gather(Dev d, Box b, int n, int forced) {
+  if (rebuild_off(d, forced)) return;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int o = d.perm[k];
+  const dbl4 x = d.t_pos[o];
+  d.pos[k] = x;
+  d.pos_ref[k] = x;
+  d.vel[k] = d.t_vel[o];
+  d.acc[k] = d.t_acc[o];
+  d.acc_old[k] = d.t_acc_old[o];
+  d.type[k] = d.t_type[o];
+  d.id[k] = d.t_id[o];
+  d.cell_of[k] = d.perm_tmp[o];
+  update_rel(d, b, k, x);
+}
+
+// Verlet-list build over the 27-cell stencil with periodic image shifts.
+// Predicate: r^2 < cutoff_extra^2 evaluated in FP64 exactly as the reference
+// evaluates it for a ghost image (image = x_j + s*L, then minus x_i, squares
+// summed x, y, z; no FMA contraction), pre-screened in FP32 on cell-relative
+// coordinates: only candidates inside a narrow band around the cutoff take
+// the FP64 path.  BT lanes cooperate on one atom; hits are compacted with a
+// group ballot.  mode 0 stores image codes (FP64 force), mode 1 cell-offset
+// codes (mixed force).
+template <int BT>
+__global__ void __launch_bounds__(256) k_build(Dev d, Box b, int n, int mode, int forced) {
+  if (rebuild_off(d, forced)) return;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = gt / BT, g = threadIdx.x % BT;
+  if (i >= n) return;  // uniform per group
+  const int lane = threadIdx.x & 31;
+  const unsigned gmask = (BT == 32) ? FULL_MASK : (((1u << BT) - 1u) << (lane & ~(BT - 1)));
+  const int gbase = lane & ~(BT - 1);
+  const dbl4 xi = d.pos[i];
+  const float4 ri = d.rel[i];
+  const int ci = d.cell_of[i];
+  const int cx = ci % b.nc[0], cy = (ci / b.nc[0]) % b.nc[1], cz = ci / (b.nc[0] * b.nc[1]);
+  const int cap = d.cap, tpa = d.tpa;
+  int cnt = 0;
+  for (int dz = -1; dz <= 1; ++dz) {
+    int nz = cz + dz, sz = 0;
+    if (nz < 0) { nz += b.nc[2]; sz = -1; } else if (nz >= b.nc[2]) { nz -= b.nc[2]; sz = 1; }
+    for (int dy = -1; dy <= 1; ++dy) {
+      int ny = cy + dy, sy = 0;
+      if (ny < 0) { ny += b.nc[1]; sy = -1; } else if (ny >= b.nc[1]) { ny -= b.nc[1]; sy = 1; }
+      for (int dx = -1; dx <= 1; ++dx) {
+        int nx = cx + dx, sx = 0;
+        if (nx < 0) { nx += b.nc[0]; sx = -1; } else if (nx >= b.nc[0]) { nx -= b.nc[0]; sx = 1; }
+        const int c2 = nx + b.nc[0] * (ny + b.nc[1] * nz);
+        const double shx = sx * b.L[0], shy = sy * b.L[1], shz = sz * b.L[2];
+        const float ox = dx * b.wf[0] - ri.x, oy = dy * b.wf[1] - ri.y, oz = dz * b.wf[2] - ri.z;
+        const uint32_t code = (uint32_t)(mode == 0 ? image_code(sx, sy, sz) : image_code(dx, dy, dz));
+        const bool self_img = (sx | sy | sz) == 0;
+        const int jb = d.cell_start[c2], je = d.cell_start[c2 + 1];
+        for (int base = jb; base < je; base += BT) {
+          const int j = base + g;
+          bool hit = false;
+          if (j < je && !(self_img && j == i)) {
+            const float4 rj = d.rel[j];
+            const float fx = rj.x + ox, fy = rj.y + oy, fz = rj.z + oz;
+            const float r2f = fx * fx + fy * fy + fz * fz;
+            if (r2f < b.ce2_lo) {
+              hit = true;
+            } else if (r2f <= b.ce2_hi) {
+              const dbl4 xj = d.pos[j];
+              const double ddx = __dsub_rn(__dadd_rn(xj.x, shx), xi.x);
+              const double ddy = __dsub_rn(__dadd_rn(xj.y, shy), xi.y);
+              const double ddz = __dsub_rn(__dadd_rn(xj.z, shz), xi.z);
+              const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)), __dmul_rn(ddz, ddz));
+              hit = r2 < b.ce2;
+            }
+          }
+          const unsigned bal = __ballot_sync(gmask, hit) >> gbase;
+          if (hit) {
+            const int k = cnt + __popc(bal & ((1u << g) - 1u));
+            if (k < cap) d.nbr[nbr_index(i, k, cap, tpa)] = (uint32_t)j | (code << CODE_SHIFT);
+          }
+          cnt += __popc(bal);
+        }
+      }
+    }
+  }
+  if (g == 0) {
+    d.nnbr[i] = min(cnt, cap);
+    atomicMax(&d.flags[F_MAXNB], cnt);
+    if (cnt > cap) atomicMax(&d.flags[F_OVERFLOW], cnt);
+    if (i == 0) atomicAdd(&d.flags[F_REBUILDS], 1);
+  }
+}
+
+__global__ void k_clear_rebuild_flag(Dev d) { d.flags[F_REBUILD] = 0; }
+
+// ---------------------------------------------------------------------------
+// thermo: fold the per-block partials (fixed order) into KE, T, P, virial, PE
+// (Atom_data::kinetic_energy_mpi_domain / finalize_temperature / finalize_pressure,
+//  src/atom_data/kinetic_energy.cpp:26-134, 189-198, 238-303)
+// thermo[] = {KE, T, P, virial, PE, sum m, -, -}
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_thermo_final(Dev d, ThermoCfg tc, int nb_ke, int nb_ev, int ring_slot) {
+  double v[6] = {0, 0, 0, 0, 0, 0};
+  for (int k = threadIdx.x; k < nb_ke; k += blockDim.x)
+    for (int q = 0; q < 4; ++q) v[q] += d.partials_ke[(size_t)k * 4 + q];
+  const double *ev = d.partials_ev;
+  for (int k = threadIdx.x; k < nb_ev; k += blockDim.x) {
+    v[4] += ev[(size_t)k * 2];
+    v[5] += ev[(size_t)k * 2 + 1];
+  }
+  __shared__ double out[6];
+  block_sum_store<6>(v, out);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double msum = 0.0;
+    const PairTab &t = *d.tab;
+    // total mass from per-type counts is not tracked; KE with n_r_df in 1..3 uses
+    // sum m v^2 - |P|^2 / M with M computed once on the host (stored in thermo[5])
+    msum = d.thermo[5];
+    double ke2 = out[0];
+    if (tc.n_r_df >= 1 && tc.n_r_df <= 3 && msum > 0)
+      ke2 -= (out[1] * out[1] + out[2] * out[2] + out[3] * out[3]) / msum;
+    const double ke = 0.5 * ke2;
+    const int dof = 3 * tc.n - tc.n_r_df;
+    const double T = 2.0 * ke / (tc.k_b * dof);
+    const double vir = 0.5 * out[4];  // each pair was visited from both sides
+    const double pe = 0.5 * out[5];
+    const double P = ((double)tc.n * tc.k_b * T) / tc.volume + (tc.langevin ? 0.0 : vir) / (3.0 * tc.volume);
+    d.thermo[0] = ke; d.thermo[1] = T; d.thermo[2] = P; d.thermo[3] = vir; d.thermo[4] = pe;
+    if (ring_slot >= 0) {
+      double *r = d.thermo_ring + (size_t)ring_slot * 4;
+      r[0] = ke; r[1] = T; r[2] = P; r[3] = vir;
+    }
+    (void)t;
+  }
+}
+
+__global__ void k_advance_step(Dev d, int nsteps) { *d.step_base += nsteps; }
+
+// ---------------------------------------------------------------------------
+// parity exports
+// ---------------------------------------------------------------------------
+// what: 0 = positions (wrapped as Domain::fix_position), 1 = velocities, 2 = accelerations
+__global__ void __launch_bounds__(256) k_to_host_order(Dev d, Box b, int n, int what) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  dbl4 v = what == 0 ? d.pos[k] : (what == 1 ? d.vel[k] : d.acc[k]);
+  if (what == 0) {
+    if (v.x < b.lo[0]) v.x += b.L[0]; else if (v.x > b.hi[0]) v.x -= b.L[0];
+    if (v.y < b.lo[1]) v.y += b.L[1]; else if (v.y > b.hi[1]) v.y -= b.L[1];
+    if (v.z < b.lo[2]) v.z += b.L[2]; else if (v.z > b.hi[2]) v.z -= b.L[2];
+  }
+  const size_t h = (size_t)d.id[k] * 3;
+  d.h3[h] = v.x; d.h3[h + 1] = v.y; d.h3[h + 2] = v.z;
+}
+
+__global__ void __launch_bounds__(256) k_export_pairs(Dev d, Box b, int n, int mode, int32_t *rows,
+                                                      unsigned long long *counter, long long cap) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int ci = d.cell_of[i];
+  const int c3[3] = {ci % b.nc[0], (ci / b.nc[0]) % b.nc[1], ci / (b.nc[0] * b.nc[1])};
+  const int nn = d.nnbr[i];
+  for (int k = 0; k < nn; ++k) {
+    const uint32_t e = d.nbr[nbr_index(i, k, d.cap, d.tpa)];
+    const int j = (int)(e & IDX_MASK), code = (int)(e >> CODE_SHIFT);
+    int s[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
+    if (mode == 1)  // cell-offset code -> image shift
+      for (int q = 0; q < 3; ++q) {
+        const int c = c3[q] + s[q];
+        s[q] = c < 0 ? -1 : (c >= b.nc[q] ? 1 : 0);
+      }
+    const unsigned long long r = atomicAdd(counter, 1ull);
+    if ((long long)r < cap) {
+      int32_t *o = rows + r * 5;
+      o[0] = (int32_t)d.id[i]; o[1] = (int32_t)d.id[j]; o[2] = s[0]; o[3] = s[1]; o[4] = s[2];
+    }
+  }
+}
+
+struct RefBins {
+  double lo[3], inv;
+  int nb[3];
+};
+
+__device__ inline void ref_bin(const RefBins &rb, double x, double y, double z, int32_t *o) {
+  const double q[3] = {x, y, z};
+  for (int a = 0; a < 3; ++a) {
+    int v = (int)floor((q[a] - rb.lo[a]) * rb.inv);
+    if (v < 0) v = 0;
+    if (v >= rb.nb[a]) v = rb.nb[a] - 1;
+    o[a] = v;
+  }
+}
+
+// Neighborlist::binlist_index of each atom at its wrapped position (host order)
+__global__ void __launch_bounds__(256) k_ref_bins(Dev d, int n, RefBins rb) {
+  const int h = blockIdx.x * blockDim.x + threadIdx.x;
+  if (h >= n) return;
+  ref_bin(rb, d.h3[3 * (size_t)h], d.h3[3 * (size_t)h + 1], d.h3[3 * (size_t)h + 2], &d.hi3[3 * (size_t)h]);
+}
+
+struct GhostCfg {
+  double llow[3], lupp[3], L[3];
+};
+
+__device__ inline int ghost_vals(const GhostCfg &g, const double *q, int v[3]) {
+  for (int a = 0; a < 3; ++a) v[a] = q[a] < g.llow[a] ? -1 : (q[a] > g.lupp[a] ? 1 : 0);
+  const int nx = v[0] != 0, ny = v[1] != 0, nz = v[2] != 0;
+  return nx + ny + nz + (nx & ny) + (nx & nz) + (ny & nz) + (nx & ny & nz);
+}
+
+__global__ void __launch_bounds__(256) k_ghost_count(Dev d, int n, GhostCfg g, int *counts) {
+  const int h = blockIdx.x * blockDim.x + threadIdx.x;
+  if (h >= n) return;
+  int v[3];
+  counts[h] = ghost_vals(g, &d.h3[3 * (size_t)h], v);
+}
+
+// images in the order x, y, z, xy, xz, yz, xyz with coordinate pos - val*width
+// (src/atom_data/exchange_ghost_single_md_domain.cpp:163-214)
+__global__ void __launch_bounds__(256) k_ghost_emit(Dev d, int n, GhostCfg g, const int *starts, int32_t *src,
+                                                    int32_t *shift3, double *pos3, int32_t *bins3, long long cap,
+                                                    RefBins rb) {
+  const int h = blockIdx.x * blockDim.x + threadIdx.x;
+  if (h >= n) return;
+  const double *q = &d.h3[3 * (size_t)h];
+  int v[3];
+  ghost_vals(g, q, v);
+  const double gx = q[0] - v[0] * g.L[0], gy = q[1] - v[1] * g.L[1], gz = q[2] - v[2] * g.L[2];
+  const int combos[7][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {1, 1, 0}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
+  long long o = starts[h];
+  for (int c = 0; c < 7; ++c) {
+    const int ux = combos[c][0], uy = combos[c][1], uz = combos[c][2];
+    if ((ux && !v[0]) || (uy && !v[1]) || (uz && !v[2])) continue;
+    if (o < cap) {
+      const double p[3] = {ux ? gx : q[0], uy ? gy : q[1], uz ? gz : q[2]};
+      src[o] = h;
+      shift3[3 * o] = ux ? -v[0] : 0; shift3[3 * o + 1] = uy ? -v[1] : 0; shift3[3 * o + 2] = uz ? -v[2] : 0;
+      pos3[3 * o] = p[0]; pos3[3 * o + 1] = p[1]; pos3[3 * o + 2] = p[2];
+      ref_bin(rb, p[0], p[1], p[2], &bins3[3 * o]);
+    }
+    ++o;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+static inline int chk() { return cudaPeekAtLastError() == cudaSuccess ? CAVGPU_OK : CAVGPU_E_CUDA; }
+
+int drift_grid_blocks(const LaunchCfg &lc) { return ceil_div(lc.n, 256); }
+
+int launch_drift(const Dev &d, const Box &b, const StepConsts &sc, const LaunchCfg &lc, int k, int thermo,
+                 cudaStream_t st) {
+  const int g = drift_grid_blocks(lc);
+  const bool mixed = lc.precision == CAVGPU_MIXED;
+  if (lc.integrator == CAVGPU_VELOCITY_VERLET) {
+    if (mixed) k_drift_vv<true><<<g, 256, 0, st>>>(d, b, sc);
+    else k_drift_vv<false><<<g, 256, 0, st>>>(d, b, sc);
+  } else {
+    if (mixed) {
+      if (thermo) k_lang_a<true, true><<<g, 256, 0, st>>>(d, b, sc, k);
+      else k_lang_a<true, false><<<g, 256, 0, st>>>(d, b, sc, k);
+    } else {
+      if (thermo) k_lang_a<false, true><<<g, 256, 0, st>>>(d, b, sc, k);
+      else k_lang_a<false, false><<<g, 256, 0, st>>>(d, b, sc, k);
+    }
+  }
+  return chk();
+}
+
+int launch_rebuild(const Dev &d, const Box &b, const LaunchCfg &lc, int forced, cudaStream_t st) {
+  const int n = lc.n, g = ceil_div(n, 256);
+  k_bin<<<g, 256, 0, st>>>(d, b, n, forced);
+  k_scan<<<1, 1024, 0, st>>>(d, d.cell_count, d.cell_start, d.cell_cursor, b.ncell, forced);
+  k_scatter<<<g, 256, 0, st>>>(d, n, forced);
+  k_cell_sort<<<ceil_div((long long)b.ncell * 32, 256), 256, 0, st>>>(d, b.ncell, forced);
+  k_copy_state<<<g, 256, 0, st>>>(d, n, forced);
+  k_gather<<<g, 256, 0, st>>>(d, b, n, forced);
+  const int mode = lc.precision == CAVGPU_MIXED ? 1 : 0;
+  k_build<8><<<ceil_div((long long)n * 8, 256), 256, 0, st>>>(d, b, n, mode, forced);
+  k_clear_rebuild_flag<<<1, 1, 0, st>>>(d);
+  return chk();
+}
+
+int launch_thermo_final(const Dev &d, const ThermoCfg &tc, int nb_ke, int nb_ev, int ring_slot, cudaStream_t st) {
+  k_thermo_final<<<1, 256, 0, st>>>(d, tc, nb_ke, nb_ev, ring_slot);
+  return chk();
+}
+
+int launch_advance_step(const Dev &d, int nsteps, cudaStream_t st) {
+  k_advance_step<<<1, 1, 0, st>>>(d, nsteps);
+  return chk();
+}
+
+int launch_to_host_order(const Dev &d, const Box &b, int n, int what, cudaStream_t st) {
+  k_to_host_order<<<ceil_div(n, 256), 256, 0, st>>>(d, b, n, what);
+  return chk();
+}
+
+int launch_export_pairs(const Dev &d, const Box &b, int n, int mode, int32_t *rows, unsigned long long *counter,
+                        int64_t cap, cudaStream_t st) {
+  k_export_pairs<<<ceil_div(n, 256), 256, 0, st>>>(d, b, n, mode, rows, counter, (long long)cap);
+  return chk();
+}
+
+int launch_ref_bins(const Dev &d, int n, double cutoff_inv, const int nb[3], const double lo_local[3],
+                    cudaStream_t st) {
+  RefBins rb;
+  for (int a = 0; a < 3; ++a) { rb.lo[a] = lo_local[a]; rb.nb[a] = nb[a]; }
+  rb.inv = cutoff_inv;
+  k_ref_bins<<<ceil_div(n, 256), 256, 0, st>>>(d, n, rb);
+  return chk();
+}
+
+int launch_ghosts(const Dev &d, const Box &b, int n, double gc, int *counts, int *starts, int32_t *src,
+                  int32_t *shift3, double *pos3, int32_t *bins3, int64_t cap, double cutoff_inv, const int nb[3],
+                  const double lo_local[3], cudaStream_t st) {
+  GhostCfg g;
+  RefBins rb;
+  for (int a = 0; a < 3; ++a) {
+    g.llow[a] = b.lo[a] + gc;
+    g.lupp[a] = b.hi[a] - gc;
+    g.L[a] = b.L[a];
+    rb.lo[a] = lo_local[a];
+    rb.nb[a] = nb[a];
+  }
+  rb.inv = cutoff_inv;
+  k_ghost_count<<<ceil_div(n, 256), 256, 0, st>>>(d, n, g, counts);
+  k_scan<<<1, 1024, 0, st>>>(d, counts, starts, nullptr, n, 1);
+  k_ghost_emit<<<ceil_div(n, 256), 256, 0, st>>>(d, n, g, starts, src, shift3, pos3, bins3, (long long)cap, rb);
+  return chk();
+}
+
+}  // namespace cav

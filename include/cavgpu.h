@@ -1,0 +1,167 @@
+/*
+ * cavgpu.h -- C ABI of the GB300 (sm_103a) molecular-dynamics step of CAVIAR2.
+ *
+ * This is the drop-in boundary for the hot path of caviar-md/caviar-v2:
+ * the Lennard-Jones pair force over a Verlet list, cell-list binning with a
+ * half-skin-triggered list rebuild, and the velocity-Verlet and Langevin
+ * integrate stages of Md_simulator.  Plain pointers and sizes only; every
+ * host array uses the reference's own layouts (std::vector<Vector3d<double>>
+ * is three contiguous doubles per atom, so `data()` passes as `const double*`
+ * with stride 3; types and ids are size_t in Atom_struct and pass as
+ * `const uint64_t*`).
+ *
+ * One context = one periodic system on one GPU, bound to one CUDA stream;
+ * calls on one context are not thread-safe (the reference's Caviar2 object
+ * is not re-entrant either).  There is no CPU fallback: without a GPU,
+ * cavgpu_create returns CAVGPU_E_CUDA.
+ *
+ * Error convention: every call returns CAVGPU_OK (0) or a negative status;
+ * cavgpu_strerror() names it.  The C++ host API above this layer turns the
+ * statuses into the reference's behaviour (Log::error_all -> exit(1),
+ * src/log.cpp:190-228; setters throw std::runtime_error, src/force/lj.cpp:76-77).
+ */
+#ifndef CAVGPU_H
+#define CAVGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CAVGPU_MAX_TYPES 8
+
+/* status codes */
+#define CAVGPU_OK 0
+#define CAVGPU_E_ARG -1            /* invalid argument or configuration */
+#define CAVGPU_E_CUDA -2           /* CUDA runtime error or no device */
+#define CAVGPU_E_NAN -3            /* NaN acceleration (src/md_simulator.cpp:646-652) */
+#define CAVGPU_E_NLIST_OVERFLOW -4 /* neighbour capacity exceeded and could not grow */
+#define CAVGPU_E_STATE -5          /* call out of order (e.g. step before upload) */
+#define CAVGPU_E_NOMEM -6          /* device allocation failed */
+#define CAVGPU_E_RANGE -7          /* size beyond a stated maximum */
+
+/* precision of the pair force */
+#define CAVGPU_FP64 0              /* all-FP64 kernels (the parity form) */
+#define CAVGPU_MIXED 1             /* FP32 pair math on cell-relative coordinates, FP64 state */
+
+/* integrators (Integrator_t, inc/caviar2/md_simulator.hpp:34-41) */
+#define CAVGPU_VELOCITY_VERLET 0
+#define CAVGPU_VELOCITY_VERLET_LANGEVIN 1
+
+typedef struct cavgpu_params {
+  double lo[3], hi[3];            /* Domain::set_lower_global / set_upper_global */
+  int32_t bc[3];                  /* Domain::set_boundary_condition; must be {1,1,1} */
+  int32_t ntypes;                 /* 1..CAVGPU_MAX_TYPES */
+  double nl_cutoff;               /* Neighborlist::set_cutoff */
+  double nl_coef;                 /* Neighborlist::set_cutoff_extra_coef (>= 1) */
+  double lj_cutoff;               /* force_field::Lj::set_cutoff */
+  double eps[CAVGPU_MAX_TYPES * CAVGPU_MAX_TYPES];          /* Lj::set_epsilon, [ti*ntypes+tj] */
+  double sigma[CAVGPU_MAX_TYPES * CAVGPU_MAX_TYPES];        /* Lj::set_sigma */
+  double cutoff_list[CAVGPU_MAX_TYPES * CAVGPU_MAX_TYPES];  /* Lj::set_cutoff_list */
+  int32_t cutoff_list_on;
+  int32_t integrator;             /* CAVGPU_VELOCITY_VERLET or ..._LANGEVIN */
+  double mass[CAVGPU_MAX_TYPES];  /* Atom_data::add_type_mass */
+  double k_b;                     /* Atom_data::set_k_b */
+  double dt;                      /* Md_simulator::set_dt */
+  double lang_temperature;        /* Md_simulator::langevin_temperature */
+  double lang_friction;           /* Md_simulator::langevin_friction */
+  double lang_kb;                 /* Md_simulator::langevin_kb */
+  double lang_kbt;                /* Md_simulator::langevin_kbt (<= 0: use kb*T) */
+  uint64_t seed;                  /* Philox key of the Langevin noise */
+  int32_t n_r_df;                 /* Atom_data::set_n_r_df, 0..3 */
+  int32_t pressure_process;       /* Atom_data::set_pressure_process */
+  int32_t precision;              /* CAVGPU_FP64 or CAVGPU_MIXED */
+  int32_t noise_off;              /* Langevin with eta = 0 (exactness checks) */
+  int32_t nbr_capacity;           /* neighbour slots per atom; 0 = sized at set-up */
+  int32_t threads_per_atom;       /* force kernel lanes per atom (1,2,4,8,16,32); 0 = tuned */
+  int32_t block_size;             /* force kernel block size; 0 = tuned */
+  int32_t steps_per_graph;        /* steps captured per CUDA graph; 0 = default */
+} cavgpu_params;
+
+typedef struct cavgpu_ctx cavgpu_ctx;
+
+/* Fill *p with the reference's defaults (coef 1.12347, k_b 1, unit masses ...). */
+void cavgpu_default_params(cavgpu_params *p);
+
+/* Create a context on the current CUDA device.
+ * Replaces: Caviar2 construction + Domain::generate (src/caviar2.cpp:20-28,
+ * src/domain.cpp:295-307) for one periodic single-rank domain. */
+int cavgpu_create(const cavgpu_params *p, cavgpu_ctx **out);
+void cavgpu_destroy(cavgpu_ctx *ctx);
+
+/* Upload n atoms (host order = insertion order; id defaults to the index).
+ * pos3/vel3: Vector3d<double> arrays; type/id: Atom_struct size_t arrays.
+ * Atoms must lie inside [lo, hi) (Atom_data::add_atom(tools::Atom&) rejects
+ * others, src/atom_data/add_unique_atom_molecule.cpp:29-38).
+ * Replaces: Atom_data::add_atom (src/atom_data.cpp:603-637). */
+int cavgpu_upload(cavgpu_ctx *ctx, int64_t n, const double *pos3, const double *vel3, const uint64_t *type,
+                  const uint64_t *id);
+
+/* Initialise and set up: wrap, bin, build the list, first force, temperature.
+ * Replaces: Md_simulator::initialize + setup (src/md_simulator.cpp:366-420, 565-611). */
+int cavgpu_setup(cavgpu_ctx *ctx);
+
+/* Advance nsteps steps of the configured integrator entirely on the device.
+ * Replaces: Md_simulator::step / run loop (src/md_simulator.cpp:317-356, 445-546),
+ * integrate_velocity_verlet (:617-729), integrate_velocity_verlet_langevin (:731-869),
+ * re_calculate_acc (:422-437), Neighborlist::build (src/neighborlist.cpp:77-148). */
+int cavgpu_step(cavgpu_ctx *ctx, int64_t nsteps);
+
+/* Same as cavgpu_step, recording thermo every `every` steps into
+ * out4[k*4 + {0,1,2,3}] = {KE, T, P, virialForce} for k < nsteps/every. */
+int cavgpu_run(cavgpu_ctx *ctx, int64_t nsteps, int64_t every, double *out4);
+
+/* Recompute the force at the current positions (list rebuilt if the half-skin
+ * test asks for it) and return the virial and the potential energy.
+ * Replaces: force_field::Lj::calculate_acceleration (src/force/lj.cpp:393-517). */
+int cavgpu_forces(cavgpu_ctx *ctx, double *virial, double *pe);
+
+/* out6 = {KE, T, P, virialForce, PE, rebuild count} of the last thermo point.
+ * Replaces: Atom_data::kinetic_energy / temperature / pressure
+ * (src/atom_data/kinetic_energy.cpp:26-303). */
+int cavgpu_thermo(cavgpu_ctx *ctx, double *out6);
+
+/* Download in host (insertion) order; positions wrapped as Domain::fix_position
+ * would (src/domain.cpp:443-493).  Any pointer may be NULL. */
+int cavgpu_download(cavgpu_ctx *ctx, double *pos3, double *vel3, double *acc3);
+
+/* Canonical pair set of the current list: rows (id_i, id_j, sx, sy, sz), the
+ * image of j being pos_j + s*L; both orders of every pair.  Returns the row
+ * count (negative on error); writes at most cap rows.
+ * Replaces: Neighborlist::neighlist (inc/caviar2/neighborlist.hpp:102). */
+int64_t cavgpu_export_pairs(cavgpu_ctx *ctx, int32_t *out5, int64_t cap);
+
+/* Reference cell assignment of every atom (host order) at the current
+ * positions: Neighborlist::binlist_index (src/neighborlist.cpp:392-414) with
+ * no_bins = ceil(L / cutoff_extra) (src/neighborlist.cpp:336-342). */
+int cavgpu_export_bins(cavgpu_ctx *ctx, int32_t *owned3, int32_t *nbins3);
+
+/* Periodic images in the reference's ghost order (owned atom by atom; face,
+ * edge, corner images x, y, z, xy, xz, yz, xyz) for a ghost cutoff, with their
+ * reference bins.  Returns the ghost count; writes at most cap entries.
+ * Replaces: Atom_data::exchange_ghost_single_md_domain
+ * (src/atom_data/exchange_ghost_single_md_domain.cpp:24-215). */
+int64_t cavgpu_export_ghosts(cavgpu_ctx *ctx, double ghost_cutoff, int32_t *src, int32_t *shift3, double *pos3,
+                             int32_t *bins3, int64_t cap);
+
+/* Statistics: out8 = {steps done, rebuilds, max neighbours, capacity,
+ * threads per atom, block size, graph launches, kernel launches}. */
+int cavgpu_stats(cavgpu_ctx *ctx, int64_t *out8);
+
+/* The CUDA stream the context launches on (a cudaStream_t). */
+void *cavgpu_stream(cavgpu_ctx *ctx);
+
+/* Kernel timing: when on, CUDA events bracket every force-kernel launch (on
+ * the context's stream, also inside captured graphs) and the totals
+ * accumulate until read.  out: {force launches, force ms total}. */
+int cavgpu_set_profiling(cavgpu_ctx *ctx, int32_t on);
+int cavgpu_read_profile(cavgpu_ctx *ctx, double *out2);
+
+const char *cavgpu_strerror(int status);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -374,7 +374,7 @@ static int update_is_needed(orc_sys *s) {
 static int nl_build(orc_sys *s, int update) {
   int rc;
   if (s->p.use_cell_list && (rc = update_cell_list(s))) return rc;
-  if (!update) update = update_is_needed(s);
+  if (!update) update = s->p.rebuild_test ? 1 : update_is_needed(s);
   if (update) {
     if (s->p.use_cell_list) return update_verlet_list_from_cell_list(s);
     return update_verlet_list(s);

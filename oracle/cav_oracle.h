@@ -61,6 +61,7 @@ typedef struct orc_params {
   int32_t integrator;           /* 0 velocity-Verlet, 1 velocity-Verlet-Langevin */
   int32_t noise_mode;           /* Langevin: 0 eta = 0, 1 Philox */
   int32_t pressure_process;     /* Atom_data::set_pressure_process */
+  int32_t rebuild_test;         /* Neighborlist::set_rebuild_test: rebuild on every step */
 } orc_params;
 
 typedef struct orc_sys orc_sys;

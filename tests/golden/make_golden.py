@@ -127,15 +127,16 @@ def cases():
     pos, vel, typ, p = W.lj_fluid((5, 5, 5), seed=21)
     rng = np.random.default_rng(22)
     L = p["hi"]
-    pos = np.mod(pos + rng.normal(0.0, 0.06, pos.shape), L)
-    # snap coordinates that lie within 0.5 of a face onto the face (moves of <= 0.5 keep atoms apart)
-    for k in np.where(pos[:, 0] < 0.5)[0][:3]:
+    # move lattice planes next to the faces (x planes just above 0, y and z planes just below L),
+    # perturb, then snap coordinates within 0.08 of a face onto it (small moves keep atoms apart)
+    pos = np.mod(pos + np.array([-0.40, 0.40, 0.40]) + rng.normal(0.0, 0.03, pos.shape), L)
+    for k in np.where(pos[:, 0] < 0.08)[0][:3]:
         pos[k, 0] = 0.0
-    for k in np.where(pos[:, 1] > L[1] - 0.5)[0][:3]:
+    for k in np.where(pos[:, 1] > L[1] - 0.08)[0][:3]:
         pos[k, 1] = np.nextafter(L[1], 0.0)
-    both = np.where((pos[:, 0] > L[0] - 0.5) & (pos[:, 2] < 0.5))[0][:2]
-    pos[both, 0] = np.nextafter(L[0], 0.0)
-    pos[both, 2] = 0.0
+    both = np.where((pos[:, 0] < 0.08) & (pos[:, 2] > L[2] - 0.08))[0][:2]
+    pos[both, 0] = 0.0
+    pos[both, 2] = np.nextafter(L[2], 0.0)
     yield "perturbed500_cell", pos, vel, typ, p, 40
     # pairs at exactly the list cutoff, inside and across the periodic boundary
     L = 6.0
