@@ -1,0 +1,389 @@
+#!/usr/bin/env python3
+"""Headline benchmark of the GB300 CAVIAR2 MD step.
+
+Workload (the configuration the metric is quoted on): N = 1,048,576 atoms
+(64^3 FCC cells x 4) of LJ fluid, rho 0.8442, T 1.44, r_c 2.5, skin 0.3,
+dt 0.005, velocity-Verlet NVE with the list rebuilt on half-skin
+displacement.  Seeded synthetic input (no dataset exists for this path).
+
+`value` is the mixed-precision form's atom-steps/s with the state resident
+in HBM; the all-FP64 form is timed the same way and reported beside it, with
+the ratio.  `e2e` runs the same workload through the C ABI from pinned host
+arrays: upload, set-up, K steps with every step's thermo read back, and the
+download of the final state all inside the timed region.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+With torchrun (N > 1) every rank runs its own replica (weak scaling, no
+data-path collective); the time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "caviar-v2_gb300"))
+
+METRIC = json.load(open(os.path.join(ROOT, "BASELINE.json")))["metric"]
+UNIT = "atom-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=100)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cells", type=int, default=64, help="FCC cells per edge (64 -> 1,048,576 atoms)")
+    ap.add_argument("--drift-steps", type=int, default=20000)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=ws)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(ws, x):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev_id):
+        self.dev_id = dev_id
+        self.proc = None
+
+    def __enter__(self):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        cmd = ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200"]
+        if self.dev_id:
+            cmd += ["-i", self.dev_id]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            self.proc.wait()
+        self.f.flush()
+
+    def summary(self):
+        try:
+            rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines()]
+            os.unlink(self.f.name)
+        except OSError:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        sm, smax, reasons = [], [], set()
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def gpu_uuid():
+    try:
+        import torch
+
+        u = str(torch.cuda.get_device_properties(0).uuid)
+        return u if u.startswith("GPU-") else "GPU-" + u
+    except Exception:
+        return None
+
+
+# ---------------------------------------------------------------------------
+def cpu_reference_rate(pos, vel, typ, params, steps, warmup):
+    """The reference's CPU path (oracle/cav_oracle.c, a restatement of the reference's
+    single-rank serial loop: ghost exchange, cell list, Verlet list, LJ, VV) on a
+    bounded sample: set-up untimed, `warmup` steps untimed, `steps` steps timed."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import cav_oracle
+
+    cav_oracle.build()
+    s = cav_oracle.System(pos, vel, typ, params, noise_mode=0)
+    s.setup()
+    if warmup:
+        s.step(warmup)
+    t0 = time.perf_counter()
+    s.step(steps)
+    dt = time.perf_counter() - t0
+    return len(pos) * steps / dt, dt
+
+
+def read_profile_traffic(name):
+    """dram bytes per launch recorded in a committed ncu summary, or None."""
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        for line in open(path):
+            if line.strip().startswith("dram_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        return {}
+
+
+def time_device(cavgpu, torch, pos, vel, typ, params, precision, steps, warmup, ws, sampler_id):
+    """Device-resident timing: events on the context's stream around K steps."""
+    s = cavgpu.System(pos, vel, typ, params, precision=precision)
+    s.setup()
+    s.step(warmup)
+    stream = torch.cuda.ExternalStream(s.stream())
+    s.set_profiling(True)
+    st0 = s.stats()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    barrier(ws)
+    with ClockSampler(sampler_id) as cs:
+        e0.record(stream)
+        s.step(steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier(ws)
+    ms = e0.elapsed_time(e1)
+    st1 = s.stats()
+    nlaunch, force_ms = s.read_profile()
+    s.set_profiling(False)
+    nbar = s._check(cavgpu.lib().cavgpu_export_pairs(s._h, None, 0), "pairs") / len(pos)
+    out = dict(ms=ms, force_ms=force_ms, force_launches=nlaunch, rebuilds=st1["rebuilds"] - st0["rebuilds"],
+               kernel_launches=st1["kernel_launches"] - st0["kernel_launches"], nbar=nbar,
+               clocks=cs.summary(), tpa=st1["threads_per_atom"], block=st1["block_size"],
+               capacity=st1["capacity"])
+    return s, out
+
+
+def nve_drift(cavgpu, pos, vel, typ, params, precision, steps, every=100):
+    """Relative energy drift per 1e6 steps: least-squares slope of (KE+PE)(t)."""
+    s = cavgpu.System(pos, vel, typ, params, precision=precision)
+    s.setup()
+    th = s.run(steps, every)
+    s.close()
+    e = th[:, 0] + th[:, 4]
+    t = (1 + __import__("numpy").arange(len(e))) * every
+    import numpy as np
+
+    slope = np.polyfit(t, e, 1)[0]
+    return float(abs(slope) * 1e6 / abs(e[0])), float(abs(e[-1] - e[0]) / abs(e[0]))
+
+
+def time_e2e(cavgpu, torch, pos, vel, typ, params, precision, steps):
+    """Through the C ABI with host buffers: pinned host arrays -> upload -> set-up ->
+    K steps (thermo of every step read back) -> download of the final state."""
+    import numpy as np
+
+    n = len(pos)
+    hp = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    hv = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    ht = torch.empty(n, dtype=torch.int64, pin_memory=True).numpy()
+    hp[:] = pos
+    hv[:] = vel
+    ht[:] = typ
+    op = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    ov = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    oa = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s = cavgpu.System(hp, hv, ht.view(np.uint64), params, precision=precision)
+    s.setup()
+    thermo = np.zeros((steps, 5))
+    rc = cavgpu.lib().cavgpu_run(s._h, steps, 1, cavgpu._ptr(thermo))
+    if rc:
+        raise cavgpu.CavError(rc, "run")
+    cavgpu.lib().cavgpu_download(s._h, cavgpu._ptr(op), cavgpu._ptr(ov), cavgpu._ptr(oa))
+    dt = time.perf_counter() - t0
+    s.close()
+    h2d = n * (3 * 8 + 3 * 8 + 8)
+    d2h = steps * 5 * 8 + n * 3 * 3 * 8
+    return n * steps / dt, h2d / steps, d2h / steps
+
+
+# ---------------------------------------------------------------------------
+def main():
+    args = parse()
+    ws, rank, local = dist_setup()
+    import numpy as np
+
+    import workloads as W
+
+    pos, vel, typ, params = W.lj_fluid((args.cells,) * 3, seed=1002)
+    n = len(pos)
+    workload = f"lj_fluid_{n}_atoms_nve"
+    config = {"workload": workload, "atoms": n, "fcc_cells": [args.cells] * 3, "rho": 0.8442, "T": 1.44,
+              "rc": 2.5, "skin": 0.3, "dt": 0.005, "integrator": "velocity_verlet_nve",
+              "rebuild": "half-skin displacement", "replicas_per_gpu": 1,
+              "l2": "inputs larger than L2 (the Verlet list alone is ~310 MB per step; L2 is 126 MB)"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        steps = max(1, min(args.steps, 3))
+        warm = min(args.warmup, 1)
+        rate, secs = cpu_reference_rate(pos, vel, typ, params, steps, warm)
+        sample = (f"{n} atoms, set-up + {warm} warm-up step untimed, {steps} timed steps ({secs:.1f} s); "
+                  "cell-list Verlet build, rebuild checks as the reference")
+        line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": steps, "warmup": warm, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+                "cpu_baseline": {"value": rate, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+                "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+
+    import cavgpu
+
+    torch.cuda.set_device(local)
+    sid = gpu_uuid()
+
+    # mixed precision (headline) and all-FP64, state resident in HBM
+    sm, rm = time_device(cavgpu, torch, pos, vel, typ, params, cavgpu.MIXED, args.steps, args.warmup, ws, sid)
+    s64, r64 = time_device(cavgpu, torch, pos, vel, typ, params, cavgpu.FP64, max(args.steps // 4, 50),
+                           min(args.warmup, 20), ws, sid)
+    ms_mixed = max_over_ranks(ws, rm["ms"])
+    ms_fp64 = max_over_ranks(ws, r64["ms"])
+    k64 = max(args.steps // 4, 50)
+    value = ws * n * args.steps / (ms_mixed * 1e-3)
+    value64 = ws * n * k64 / (ms_fp64 * 1e-3)
+
+    # accuracy of the mixed form against FP64 at one thermalised state (the melted
+    # fluid after the FP64 run; the initial lattice has zero net forces)
+    p_eq, v_eq, _ = s64.state()
+    sm.close()
+    s64.close()
+    f64 = cavgpu.System(p_eq, v_eq, typ, params, precision=cavgpu.FP64)
+    f64.setup()
+    fm = cavgpu.System(p_eq, v_eq, typ, params, precision=cavgpu.MIXED)
+    fm.setup()
+    a_ref, a_mix = f64.state()[2], fm.state()[2]
+    t_ref, t_mix = f64.thermo(), fm.thermo()
+    f64.close()
+    fm.close()
+    force_rms = float(np.sqrt(((a_mix - a_ref) ** 2).sum(1).mean() / (a_ref ** 2).sum(1).mean()))
+
+    d64 = max(args.drift_steps // 4, 500)
+    drift_m, dE_m = nve_drift(cavgpu, p_eq, v_eq, typ, params, cavgpu.MIXED, args.drift_steps)
+    drift_64, dE_64 = nve_drift(cavgpu, p_eq, v_eq, typ, params, cavgpu.FP64, d64)
+
+    e2e_rate, h2d, d2h = time_e2e(cavgpu, torch, pos, vel, typ, params, cavgpu.MIXED, args.steps)
+    e2e_rate = ws * n * args.steps / max_over_ranks(ws, n * args.steps / e2e_rate)
+
+    # roofline of the dominant kernel (mixed force kernel): algorithmic bytes per launch
+    #   per atom: 4 * nbar list words + rel_i 16 + nnbr 4 + vel r/w 64 + acc_old r 32 + acc w 32
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs")
+    peak_note = "measured" if hbm else "fallback"
+    hbm = hbm or 6800.0
+    bytes_per_atom = 4.0 * rm["nbar"] + 148.0
+    launch_ms = rm["force_ms"] / max(rm["force_launches"], 1)
+    achieved = bytes_per_atom * n / (launch_ms * 1e-3) / 1e9
+    traffic = read_profile_traffic("lj_force_mixed_1M.md")
+    # FP64 form: FP64-pipe roofline, FLOPs per atom = 8 n_list + 17 n_cut (n_cut = n_list (rc/ce)^3)
+    fp64_peak, fp32_peak = cavgpu.measure_peaks()
+    ncut = r64["nbar"] * (2.5 / 2.8) ** 3
+    flops_atom = 8 * r64["nbar"] + 17 * ncut
+    l64 = r64["force_ms"] / max(r64["force_launches"], 1)
+    fp64_achieved = flops_atom * n / (l64 * 1e-3) / 1e12
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        rate, secs = cpu_reference_rate(pos, vel, typ, params, 3, 0)
+        cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"{n} atoms, set-up untimed, 3 timed steps ({secs:.1f} s) of the reference's serial "
+                         "cell-list path restated in oracle/cav_oracle.c"}
+
+    if rank != 0:
+        return
+    config.update({"fp64_value": value64, "mixed_over_fp64": value / value64, "fp64_steps": k64,
+                   "rebuilds_in_timed_region": rm["rebuilds"], "mean_neighbours": rm["nbar"],
+                   "threads_per_atom": rm["tpa"], "block": rm["block"], "capacity": rm["capacity"],
+                   "parallelism": f"replicas x{ws}"})
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_mixed / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "mixed (f32 pair math, f64 state and reductions)",
+        "data": "synthetic seeded FCC LJ fluid (no dataset exists for this path)", "config": config,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": traffic, "kernel": "k_force<mixed>", "peak_source": peak_note,
+                     "bytes_per_atom": bytes_per_atom, "launch_ms": launch_ms},
+        "fp64": {"value": value64, "ms_per_step": ms_fp64 / k64, "kernel": "k_force<fp64>",
+                 "roofline": {"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                              "frac": fp64_achieved / fp64_peak, "flops_per_atom": flops_atom, "launch_ms": l64,
+                              "peak_source": "measured by cavgpu_measure_peaks (DFMA chains)"},
+                 "clocks": r64["clocks"]},
+        "accuracy": {"mixed_force_rms_rel": force_rms,
+                     "mixed_pe_rel": abs(t_mix["pe"] - t_ref["pe"]) / abs(t_ref["pe"]),
+                     "mixed_pressure_rel": abs(t_mix["pressure"] - t_ref["pressure"]) / abs(t_ref["pressure"]),
+                     "nve_drift_per_1e6_steps": {"mixed": drift_m, "fp64": drift_64},
+                     "nve_rel_dE_over_run": {"mixed": dE_m, "fp64": dE_64},
+                     "drift_steps": {"mixed": args.drift_steps, "fp64": d64},
+                     "drift_start": "melted fluid after the FP64 timed run; slope of KE+PE sampled every 100 steps"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_rate, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": rm["kernel_launches"],
+        "clocks": rm["clocks"],
+        "peaks": {"fp64_tflops": fp64_peak, "fp32_tflops": fp32_peak},
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

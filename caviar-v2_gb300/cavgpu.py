@@ -40,7 +40,10 @@ class Params(C.Structure):
 class CavError(RuntimeError):
     def __init__(self, status, what):
         self.status = status
-        super().__init__(f"{what}: {lib().cavgpu_strerror(status).decode()} ({status})")
+        extra = ""
+        if status == E_CUDA:
+            extra = f" [{lib().cavgpu_last_cuda_error().decode()}]"
+        super().__init__(f"{what}: {lib().cavgpu_strerror(status).decode()} ({status}){extra}")
 
 
 # every function include/cavgpu.h declares, with its ctypes signature
@@ -64,7 +67,18 @@ _SIGS = {
     "cavgpu_set_profiling": (C.c_int, [C.c_void_p, C.c_int32]),
     "cavgpu_read_profile": (C.c_int, [C.c_void_p, C.c_void_p]),
     "cavgpu_strerror": (C.c_char_p, [C.c_int]),
+    "cavgpu_measure_peaks": (C.c_int, [C.c_void_p]),
+    "cavgpu_last_cuda_error": (C.c_char_p, []),
 }
+
+
+def measure_peaks():
+    """Measured {fp64, fp32} FMA TFLOP/s of the current device."""
+    o = np.zeros(2)
+    rc = lib().cavgpu_measure_peaks(_ptr(o))
+    if rc:
+        raise CavError(rc, "measure_peaks")
+    return float(o[0]), float(o[1])
 
 _lib = None
 
@@ -157,7 +171,7 @@ class System:
         self._check(lib().cavgpu_step(self._h, n), "step")
 
     def run(self, n, every):
-        out = np.zeros((max(n // every, 1), 4))
+        out = np.zeros((max(n // every, 1), 5))
         self._check(lib().cavgpu_run(self._h, n, every, _ptr(out)), "run")
         return out[: n // every]
 

@@ -54,7 +54,14 @@ struct cavgpu_ctx {
 
 namespace {
 
-int cuda_rc(cudaError_t e) { return e == cudaSuccess ? CAVGPU_OK : (e == cudaErrorMemoryAllocation ? CAVGPU_E_NOMEM : CAVGPU_E_CUDA); }
+// name of the last CUDA error seen by this library (process-wide, for diagnostics)
+thread_local const char *g_last_cuda_error = "none";
+
+int cuda_rc(cudaError_t e) {
+  if (e == cudaSuccess) return CAVGPU_OK;
+  g_last_cuda_error = cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? CAVGPU_E_NOMEM : CAVGPU_E_CUDA;
+}
 
 #define CK(x)                        \
   do {                               \
@@ -89,9 +96,11 @@ int enqueue_step(cavgpu_ctx *c, int k, bool thermo, int ring_slot) {
   const bool lang = c->p.integrator == CAVGPU_VELOCITY_VERLET_LANGEVIN;
   RK(launch_drift(c->d, c->b, c->sc, c->lc, k, thermo && lang, c->st));
   RK(launch_rebuild(c->d, c->b, c->lc, 0, c->st));
-  if (c->prof && k < (int)c->ev0.size()) CK(cudaEventRecord(c->ev0[k], c->st));
+  // External: inside a stream capture this becomes an event-record node that records
+  // at every replay (a plain record would only order work within the capture)
+  if (c->prof && k < (int)c->ev0.size()) CK(cudaEventRecordWithFlags(c->ev0[k], c->st, cudaEventRecordExternal));
   RK(launch_force(c->d, c->b, c->sc, c->lc, lang ? 2 : 1, thermo, k, c->st));
-  if (c->prof && k < (int)c->ev1.size()) CK(cudaEventRecord(c->ev1[k], c->st));
+  if (c->prof && k < (int)c->ev1.size()) CK(cudaEventRecordWithFlags(c->ev1[k], c->st, cudaEventRecordExternal));
   c->kernel_launches += kernels_per_step(c);
   if (thermo) {
     const int nb_ke = lang ? drift_grid_blocks(c->lc) : force_grid_blocks(c->lc);
@@ -236,6 +245,11 @@ void cavgpu_default_params(cavgpu_params *p) {
   p->precision = CAVGPU_FP64;
 }
 
+const char *cavgpu_last_cuda_error(void) {
+  const cudaError_t e = cudaPeekAtLastError();  // a failed kernel launch leaves its error here
+  return e != cudaSuccess ? cudaGetErrorString(e) : g_last_cuda_error;
+}
+
 const char *cavgpu_strerror(int s) {
   switch (s) {
     case CAVGPU_OK: return "ok";
@@ -337,7 +351,7 @@ int cavgpu_create(const cavgpu_params *p, cavgpu_ctx **out) {
   if (!rc) rc = dalloc(c, &c->d.flags, F_NWORDS);
   if (!rc) rc = dalloc(c, &c->d.thermo, 8);
   if (!rc) rc = dalloc(c, &c->d.step_base, 1);
-  if (!rc) rc = dalloc(c, &c->d.thermo_ring, 4 * (size_t)MAX_GRAPH_STEPS);
+  if (!rc) rc = dalloc(c, &c->d.thermo_ring, THERMO_REC * (size_t)MAX_GRAPH_STEPS);
   if (!rc) rc = cuda_rc(cudaMemcpyAsync(c->d.tab, &c->tab_h, sizeof(PairTab), cudaMemcpyHostToDevice, c->st));
   if (!rc) rc = cuda_rc(cudaMemsetAsync(c->d.flags, 0, F_NWORDS * sizeof(int), c->st));
   if (!rc) rc = cuda_rc(cudaMemsetAsync(c->d.thermo, 0, 8 * sizeof(double), c->st));
@@ -447,35 +461,45 @@ int cavgpu_setup(cavgpu_ctx *c) {
   return CAVGPU_OK;
 }
 
-int cavgpu_run(cavgpu_ctx *c, int64_t nsteps, int64_t every, double *out4) {
-  if (!c || nsteps < 0 || every < 0 || (every > 0 && !out4)) return CAVGPU_E_ARG;
+int cavgpu_run(cavgpu_ctx *c, int64_t nsteps, int64_t every, double *out5) {
+  if (!c || nsteps < 0 || every < 0 || (every > 0 && !out5)) return CAVGPU_E_ARG;
   if (!c->set_up) return CAVGPU_E_STATE;
   if (nsteps == 0) return CAVGPU_OK;
   const bool lang = c->p.integrator == CAVGPU_VELOCITY_VERLET_LANGEVIN;
   int S = c->p.steps_per_graph > 0 ? std::min(c->p.steps_per_graph, MAX_GRAPH_STEPS) : 50;
   if (every > 0) S = (int)std::max<int64_t>(every, (S / every) * every);
-  const int nrec = every > 0 ? (int)(S / every) : 0;
   int64_t done = 0, rec = 0;
   int rc = CAVGPU_OK;
-  // whole chunks through the graph
-  while (nsteps - done >= S && nsteps - done > 1) {
-    // keep the last step out of the graph when no thermo recording is asked, so that the
-    // final state always carries a fresh temperature (finalize_temperature runs every step)
-    if (every == 0 && nsteps - done == S) break;
-    GraphEntry *g = get_graph(c, S, (int)every, &rc);
+  int chunks_since_check = 0;
+  // chunks of up to S steps, each one captured CUDA graph (cached per size).  Without
+  // recording, the last chunk computes the thermo of its final step, so that the state
+  // after the call carries a fresh temperature (finalize_temperature runs every step).
+  while (done < nsteps) {
+    const int64_t left = nsteps - done;
+    const int sz = (int)std::min<int64_t>(left, S);
+    int ev;
+    if (every == 0) ev = (left == sz) ? sz : 0;
+    else if (sz % every == 0) ev = (int)every;
+    else break;  // a tail that does not hold whole recording periods runs eagerly below
+    GraphEntry *g = get_graph(c, sz, ev, &rc);
     if (!g) return rc;
     CK(cudaGraphLaunch(g->exec, c->st));
+    const int nrec = ev > 0 ? sz / ev : 0;
     c->graph_launches += 1;
-    c->kernel_launches += (long long)S * kernels_per_step(c) + 1 + (every > 0 ? nrec : 0);
-    if (c->prof) RK(collect_profile(c, S));
-    RK(check_status(c));
+    c->kernel_launches += (long long)sz * kernels_per_step(c) + 1 + nrec;
+    if (c->prof) RK(collect_profile(c, sz));
     if (every > 0) {
-      CK(cudaMemcpyAsync(out4 + 4 * rec, c->d.thermo_ring, 4 * sizeof(double) * nrec, cudaMemcpyDeviceToHost, c->st));
-      CK(cudaStreamSynchronize(c->st));
+      CK(cudaMemcpyAsync(out5 + THERMO_REC * rec, c->d.thermo_ring, THERMO_REC * sizeof(double) * nrec,
+                         cudaMemcpyDeviceToHost, c->st));
       rec += nrec;
     }
-    done += S;
-    c->steps_done += S;
+    done += sz;
+    c->steps_done += sz;
+    // status (NaN, list overflow) is read back every 20 chunks and at the end
+    if (++chunks_since_check == 20) {
+      RK(check_status(c));
+      chunks_since_check = 0;
+    }
   }
   // remaining steps eagerly
   while (done < nsteps) {
@@ -487,7 +511,7 @@ int cavgpu_run(cavgpu_ctx *c, int64_t nsteps, int64_t every, double *out4) {
     c->kernel_launches += 1;
     if (c->prof) RK(collect_profile(c, 1));
     if (every > 0 && th) {
-      CK(cudaMemcpyAsync(out4 + 4 * rec, c->d.thermo_ring, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+      CK(cudaMemcpyAsync(out5 + THERMO_REC * rec, c->d.thermo_ring, THERMO_REC * sizeof(double), cudaMemcpyDeviceToHost, c->st));
       rec += 1;
     }
     ++done;

@@ -24,6 +24,7 @@ __device__ inline dbl4 ldg_dbl4(const dbl4 *p) {
 }
 
 constexpr int MAXT = CAVGPU_MAX_TYPES;
+constexpr int THERMO_REC = 5;  // {KE, T, P, virialForce, PE} per recorded step
 // neighbour entry: bits 0..26 = atom slot j, bits 27..31 = image code (0..26)
 constexpr int CODE_SHIFT = 27;
 constexpr uint32_t IDX_MASK = (1u << CODE_SHIFT) - 1u;
@@ -93,7 +94,7 @@ struct Dev {
   double *partials_ke;        // per-block {sum m v^2, sum m v} (4 per block)
   double *partials_ev;        // per-block {sum -coef r^2, sum V} over both pair orders (2 per block)
   double *thermo;             // {KE, T, P, virialForce, PE, total mass, -, -}
-  double *thermo_ring;        // recorded thermo points (4 per record)
+  double *thermo_ring;        // recorded thermo points (THERMO_REC per record)
   long long *step_base;       // step counter read by the Langevin kernels
   PairTab *tab;
   // host-order staging for downloads

@@ -354,8 +354,8 @@ __global__ void __launch_bounds__(256) k_thermo_final(Dev d, ThermoCfg tc, int n
     const double P = ((double)tc.n * tc.k_b * T) / tc.volume + (tc.langevin ? 0.0 : vir) / (3.0 * tc.volume);
     d.thermo[0] = ke; d.thermo[1] = T; d.thermo[2] = P; d.thermo[3] = vir; d.thermo[4] = pe;
     if (ring_slot >= 0) {
-      double *r = d.thermo_ring + (size_t)ring_slot * 4;
-      r[0] = ke; r[1] = T; r[2] = P; r[3] = vir;
+      double *r = d.thermo_ring + (size_t)ring_slot * THERMO_REC;
+      r[0] = ke; r[1] = T; r[2] = P; r[3] = vir; r[4] = pe;
     }
     (void)t;
   }

@@ -110,8 +110,8 @@ int cavgpu_setup(cavgpu_ctx *ctx);
 int cavgpu_step(cavgpu_ctx *ctx, int64_t nsteps);
 
 /* Same as cavgpu_step, recording thermo every `every` steps into
- * out4[k*4 + {0,1,2,3}] = {KE, T, P, virialForce} for k < nsteps/every. */
-int cavgpu_run(cavgpu_ctx *ctx, int64_t nsteps, int64_t every, double *out4);
+ * out5[k*5 + {0..4}] = {KE, T, P, virialForce, PE} for k < nsteps/every. */
+int cavgpu_run(cavgpu_ctx *ctx, int64_t nsteps, int64_t every, double *out5);
 
 /* Recompute the force at the current positions (list rebuilt if the half-skin
  * test asks for it) and return the virial and the potential energy.
@@ -160,6 +160,15 @@ int cavgpu_set_profiling(cavgpu_ctx *ctx, int32_t on);
 int cavgpu_read_profile(cavgpu_ctx *ctx, double *out2);
 
 const char *cavgpu_strerror(int status);
+
+/* Text of the last CUDA runtime error this library saw on the calling thread
+ * ("none" if none); complements CAVGPU_E_CUDA (the reference logs the reason
+ * before exiting, src/log.cpp:190-228). */
+const char *cavgpu_last_cuda_error(void);
+
+/* Diagnostic (no counterpart in the reference): measured FMA throughput of the
+ * current device, out2 = {FP64 TFLOP/s, FP32 TFLOP/s}, for roofline denominators. */
+int cavgpu_measure_peaks(double *out2);
 
 #ifdef __cplusplus
 }
