@@ -19,7 +19,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + os.path.join(ROOT, "include"),
          "-diag-suppress", "1444"]
-SOURCES = ["cav_kernels.cu", "cav_force.cu", "cav_api.cu", "cav_peaks.cu"]
+SOURCES = ["cav_kernels.cu", "cav_force.cu", "cav_api.cu", "cav_peaks.cu", "cav_noalloc.cu"]
 
 
 def _compile(src, verbose):

@@ -69,6 +69,8 @@ _SIGS = {
     "cavgpu_strerror": (C.c_char_p, [C.c_int]),
     "cavgpu_measure_peaks": (C.c_int, [C.c_void_p]),
     "cavgpu_last_cuda_error": (C.c_char_p, []),
+    "cavgpu_kinetic_energy_noalloc": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                                C.c_int32, C.c_double, C.c_void_p, C.c_void_p]),
 }
 
 

@@ -166,6 +166,22 @@ const char *cavgpu_strerror(int status);
  * before exiting, src/log.cpp:190-228). */
 const char *cavgpu_last_cuda_error(void);
 
+/* Kinetic energy and temperature of n atoms held in caller-owned DEVICE memory,
+ * without any device allocation (no counterpart in the reference; the result is
+ * that of Atom_data::kinetic_energy / finalize_temperature for n_r_df 0..3).
+ * For callers that cannot call cudaMalloc: work enqueued inside a CUDA-graph
+ * stream capture, memory owned by another allocator, loops that must not
+ * synchronise.  vel3: 3 doubles per atom; type: uint64 per atom (types >= ntypes
+ * count as massless); mass: HOST array of ntypes masses; out2: DEVICE array that
+ * receives {KE, T} when `stream` (a cudaStream_t, NULL = legacy default) reaches it.
+ * Scratch: a fixed 320 KiB __device__ array (per-block partial sums) that every
+ * device loading this library keeps until exit; n > 16,777,216 returns
+ * CAVGPU_E_RANGE.  The first call on a device looks up that array's device
+ * address once; make that first call before any stream capture.  Calls share
+ * the array: two calls that overlap on the GPU race. */
+int cavgpu_kinetic_energy_noalloc(int64_t n, const double *vel3, const uint64_t *type, const double *mass,
+                                  int32_t ntypes, int32_t n_r_df, double k_b, double *out2, void *stream);
+
 /* Diagnostic (no counterpart in the reference): measured FMA throughput of the
  * current device, out2 = {FP64 TFLOP/s, FP32 TFLOP/s}, for roofline denominators. */
 int cavgpu_measure_peaks(double *out2);
