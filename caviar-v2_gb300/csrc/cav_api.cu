@@ -179,10 +179,9 @@ int check_status(cavgpu_ctx *c) {
 
 // (re)allocate the neighbour list for `cap` slots per atom
 int alloc_nbr(cavgpu_ctx *c, int cap) {
-  cap = (cap + 31) / 32 * 32;
-  const int A = 32 / c->d.tpa;
-  const size_t rows = (size_t)((c->n + A - 1) / A) * A;
-  const size_t bytes = rows * (size_t)cap * sizeof(uint32_t);
+  cap = (cap + 63) / 64 * 64;  // nbr_index needs cap % (4 * tpa) == 0, tpa <= 16
+  const int A = 32 / c->d.tpa;  // whole blocks of A slots (nbr_index)
+  const size_t bytes = (size_t)((c->n + A - 1) / A) * A * (size_t)cap * sizeof(uint32_t);
   if (c->d.nbr) {
     auto it = std::find(c->allocs.begin(), c->allocs.end(), (void *)c->d.nbr);
     if (it != c->allocs.end()) c->allocs.erase(it);
@@ -303,6 +302,7 @@ int cavgpu_create(const cavgpu_params *p, cavgpu_ctx **out) {
   b.ce2_lo = (float)(b.ce2 * (1.0 - 2e-4));
   b.ce2_hi = (float)(b.ce2 * (1.0 + 2e-4));
   b.thr2 = 0.25 * (ce - p->nl_cutoff) * (ce - p->nl_cutoff);
+  b.thr2f = (float)(b.thr2 * (1.0 - 1e-6));
   // pair table (force_field::Lj, src/force/lj.cpp:453-484)
   PairTab &t = c->tab_h;
   const int nt = p->ntypes;
@@ -328,6 +328,7 @@ int cavgpu_create(const cavgpu_params *p, cavgpu_ctx **out) {
   StepConsts &sc = c->sc;
   sc.dt = p->dt;
   sc.hdt = 0.5 * p->dt;
+  sc.hdt2 = 0.5 * p->dt * p->dt;
   if (p->integrator == CAVGPU_VELOCITY_VERLET_LANGEVIN) {
     const double fr = p->lang_friction, dt = p->dt;
     sc.la = (2.0 - fr * dt) / (2.0 + fr * dt);
@@ -417,6 +418,7 @@ int cavgpu_upload(cavgpu_ctx *c, int64_t n, const double *pos3, const double *ve
   dbl4 **d4[] = {&d.pos, &d.vel, &d.acc, &d.acc_old, &d.pos_ref, &d.t_pos, &d.t_vel, &d.t_acc, &d.t_acc_old};
   for (auto pp : d4) if (!rc) rc = dalloc(c, pp, N);
   if (!rc) rc = dalloc(c, &d.rel, N);
+  if (!rc) rc = dalloc(c, &d.rel_ref, N);
   int **di[] = {&d.type, &d.cell_of, &d.t_type, &d.atom_cell, &d.perm, &d.perm_tmp, &d.nnbr};
   for (auto pp : di) if (!rc) rc = dalloc(c, pp, N);
   if (!rc) rc = dalloc(c, &d.id, N);

@@ -61,11 +61,12 @@ struct Box {
   double ce2;         // cutoff_extra^2, the list predicate r^2 < ce2 (src/neighborlist.cpp:258, :508)
   float ce2_lo, ce2_hi;  // FP32 pre-screen band around ce2
   double thr2;        // 0.25 (cutoff_extra - cutoff)^2 (src/neighborlist.cpp:318)
+  float thr2f;        // thr2 * (1 - 1e-6) in FP32: the mixed form's test may only fire early
   int ncell;
 };
 
 struct StepConsts {
-  double dt, hdt, dt2h;       // dt, 0.5*dt, unused
+  double dt, hdt, hdt2;       // dt, 0.5*dt, 0.5*dt*dt
   double la, lb, lc;          // Langevin a, b, c (src/md_simulator.cpp:398-405)
   uint64_t seed;
   int noise_off;
@@ -76,6 +77,7 @@ struct StepConsts {
 struct Dev {
   dbl4 *pos, *vel, *acc, *acc_old, *pos_ref;
   float4 *rel;                // position relative to the build cell's origin; w = type bits
+  float4 *rel_ref;            // rel at the last build (mixed form: rel = rel_ref + (x - pos_ref))
   int *type;
   uint32_t *id;               // host (insertion) index
   int *cell_of;               // build cell of each slot
@@ -103,11 +105,26 @@ struct Dev {
 };
 
 // ---- neighbour-list layout -------------------------------------------------
-// For a force kernel with `tpa` lanes per atom, a warp serves A = 32/tpa atoms;
-// entry k of atom i sits so that one warp-wide load reads 32 consecutive words.
+// A warp of the force kernel serves A = 32/tpa atoms (a block of A consecutive
+// slots).  Within a block, entries come in chunks of four: chunk g of atom i
+// holds entries 4g..4g+3 at block_base + g*4A + (i % A)*4.  Force-kernel lane
+// (t, a) reads chunks g = t + tpa*q with one 128-bit load, so a warp reads 512
+// consecutive bytes per step of q.  A and tpa are powers of two: shifts only.
+// `cap` is a multiple of 4*tpa (64 covers every tpa up to 16).
+__host__ __device__ inline int log2_pow2(int v) {
+#ifdef __CUDA_ARCH__
+  return __ffs(v) - 1;
+#else
+  return __builtin_ctz((unsigned)v);
+#endif
+}
+__host__ __device__ inline size_t nbr_block_base(int i, int cap, int tpa) {
+  const int as = 5 - log2_pow2(tpa);  // log2(A)
+  return ((size_t)(i >> as) * (size_t)cap << as) + ((size_t)(i & ((1 << as) - 1)) << 2);
+}
 __host__ __device__ inline size_t nbr_index(int i, int k, int cap, int tpa) {
-  const int A = 32 / tpa;
-  return (size_t)(i / A) * (size_t)cap * A + (size_t)(k / tpa) * 32 + (size_t)(k % tpa) * A + (i % A);
+  const int as = 5 - log2_pow2(tpa);
+  return nbr_block_base(i, cap, tpa) + ((size_t)(k >> 2) << (as + 2)) + (k & 3);
 }
 
 __host__ __device__ inline int image_code(int sx, int sy, int sz) { return (sx + 1) + 3 * (sy + 1) + 9 * (sz + 1); }

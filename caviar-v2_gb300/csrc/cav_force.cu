@@ -84,27 +84,37 @@ __global__ void __launch_bounds__(256) k_force(Dev d, Box b, StepConsts sc, int 
     int ti = 0;
     if (act) {
       const int nn = d.nnbr[i];
-      const uint32_t *row = d.nbr + (size_t)task * cap * A + t * A + a;
+      // this lane's neighbour words: chunk g = t + TPA q (entries 4g..4g+3), one 128-bit
+      // load each; the warp's loads for one q cover 512 consecutive bytes (nbr_index)
+      const uint4 *row4 = reinterpret_cast<const uint4 *>(d.nbr + (size_t)task * cap * A) + (t * A + a);
       if constexpr (MIXED) {
         const float4 ri = d.rel[i];
         ti = __float_as_int(ri.w);
         float ax = 0.f, ay = 0.f, az = 0.f, vr = 0.f, pp = 0.f;
-        for (int k = t, it = 0; k < nn; k += TPA, ++it) {
-          const uint32_t e = __ldg(row + (size_t)it * 32);
-          const float4 rj = __ldg(&d.rel[e & IDX_MASK]);
-          const float3 o = tab.off[e >> CODE_SHIFT];
-          const float dx = (rj.x + o.x) - ri.x, dy = (rj.y + o.y) - ri.y, dz = (rj.z + o.z) - ri.z;
-          const float r2 = dx * dx + dy * dy + dz * dz;
-          const int tt = ti * nt + __float_as_int(rj.w);
-          if (r2 <= tab.rc2[tt]) {
-            const float r2i = __frcp_rn(r2);
-            const float s2 = tab.sig2[tt] * r2i;
-            const float s6 = s2 * s2 * s2;
-            const float coef = tab.eps4[tt] * r2i * s6 * (6.0f - 12.0f * s6) - tab.gc[tt];
-            ax += coef * dx; ay += coef * dy; az += coef * dz;
-            if (EV) {
-              vr -= coef * r2;
-              pp += tab.eps4[tt] * (s6 * s6 - s6) - tab.uc[tt] - 0.5f * tab.gc[tt] * (r2 - tab.rc2[tt]);
+        for (int q = 0, k0 = 4 * t; k0 < nn; ++q, k0 += 4 * TPA) {
+          const uint4 w4 = __ldg(row4 + (size_t)q * 32);
+          const uint32_t e[4] = {w4.x, w4.y, w4.z, w4.w};
+          float4 rj[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u)  // four independent gathers in flight
+            if (k0 + u < nn) rj[u] = __ldg(&d.rel[e[u] & IDX_MASK]);
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            if (k0 + u >= nn) break;
+            const float3 o = tab.off[e[u] >> CODE_SHIFT];
+            const float dx = (rj[u].x + o.x) - ri.x, dy = (rj[u].y + o.y) - ri.y, dz = (rj[u].z + o.z) - ri.z;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            const int tt = ti * nt + __float_as_int(rj[u].w);
+            if (r2 <= tab.rc2[tt]) {
+              const float r2i = __frcp_rn(r2);
+              const float s2 = tab.sig2[tt] * r2i;
+              const float s6 = s2 * s2 * s2;
+              const float coef = tab.eps4[tt] * r2i * s6 * (6.0f - 12.0f * s6) - tab.gc[tt];
+              ax += coef * dx; ay += coef * dy; az += coef * dz;
+              if (EV) {
+                vr -= coef * r2;
+                pp += tab.eps4[tt] * (s6 * s6 - s6) - tab.uc[tt] - 0.5f * tab.gc[tt] * (r2 - tab.rc2[tt]);
+              }
             }
           }
         }
@@ -112,22 +122,30 @@ __global__ void __launch_bounds__(256) k_force(Dev d, Box b, StepConsts sc, int 
       } else {
         const dbl4 xi = d.pos[i];
         ti = (int)xi.w;
-        for (int k = t, it = 0; k < nn; k += TPA, ++it) {
-          const uint32_t e = __ldg(row + (size_t)it * 32);
-          const dbl4 xj = ldg_dbl4(&d.pos[e & IDX_MASK]);
-          const double3 s = tab.shift[e >> CODE_SHIFT];
-          const double dx = (xj.x + s.x) - xi.x, dy = (xj.y + s.y) - xi.y, dz = (xj.z + s.z) - xi.z;
-          const double r2 = dx * dx + dy * dy + dz * dz;
-          const int tt = ti * nt + (int)xj.w;
-          if (r2 <= tab.rc2[tt]) {
-            const double r2i = __drcp_rn(r2);
-            const double s2 = tab.sig2[tt] * r2i;
-            const double s6 = s2 * s2 * s2;
-            const double coef = tab.eps4[tt] * r2i * s6 * (6.0 - 12.0 * s6) - tab.gc[tt];
-            fx += coef * dx; fy += coef * dy; fz += coef * dz;
-            if (EV) {
-              vir -= coef * r2;
-              pe += tab.eps4[tt] * (s6 * s6 - s6) - tab.uc[tt] - 0.5 * tab.gc[tt] * (r2 - tab.rc2[tt]);
+        for (int q = 0, k0 = 4 * t; k0 < nn; ++q, k0 += 4 * TPA) {
+          const uint4 w4 = __ldg(row4 + (size_t)q * 32);
+          const uint32_t e[4] = {w4.x, w4.y, w4.z, w4.w};
+          dbl4 xj[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            if (k0 + u < nn) xj[u] = ldg_dbl4(&d.pos[e[u] & IDX_MASK]);
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            if (k0 + u >= nn) break;
+            const double3 s = tab.shift[e[u] >> CODE_SHIFT];
+            const double dx = (xj[u].x + s.x) - xi.x, dy = (xj[u].y + s.y) - xi.y, dz = (xj[u].z + s.z) - xi.z;
+            const double r2 = dx * dx + dy * dy + dz * dz;
+            const int tt = ti * nt + (int)xj[u].w;
+            if (r2 <= tab.rc2[tt]) {
+              const double r2i = __drcp_rn(r2);
+              const double s2 = tab.sig2[tt] * r2i;
+              const double s6 = s2 * s2 * s2;
+              const double coef = tab.eps4[tt] * r2i * s6 * (6.0 - 12.0 * s6) - tab.gc[tt];
+              fx += coef * dx; fy += coef * dy; fz += coef * dz;
+              if (EV) {
+                vir -= coef * r2;
+                pe += tab.eps4[tt] * (s6 * s6 - s6) - tab.uc[tt] - 0.5 * tab.gc[tt] * (r2 - tab.rc2[tt]);
+              }
             }
           }
         }
@@ -158,9 +176,15 @@ __global__ void __launch_bounds__(256) k_force(Dev d, Box b, StepConsts sc, int 
       } else if (KICK == 1) {
         dbl4 v = d.vel[i];
         const dbl4 ao = d.acc_old[i];
-        v.x = __dadd_rn(v.x, __dmul_rn(__dadd_rn(an.x, ao.x), sc.hdt));
-        v.y = __dadd_rn(v.y, __dmul_rn(__dadd_rn(an.y, ao.y), sc.hdt));
-        v.z = __dadd_rn(v.z, __dmul_rn(__dadd_rn(an.z, ao.z), sc.hdt));
+        if (MIXED) {
+          v.x = fma(an.x + ao.x, sc.hdt, v.x);
+          v.y = fma(an.y + ao.y, sc.hdt, v.y);
+          v.z = fma(an.z + ao.z, sc.hdt, v.z);
+        } else {  // v += (a + a_old) * (0.5 dt), the reference's order
+          v.x = __dadd_rn(v.x, __dmul_rn(__dadd_rn(an.x, ao.x), sc.hdt));
+          v.y = __dadd_rn(v.y, __dmul_rn(__dadd_rn(an.y, ao.y), sc.hdt));
+          v.z = __dadd_rn(v.z, __dmul_rn(__dadd_rn(an.z, ao.z), sc.hdt));
+        }
         d.acc[i] = an;
         d.vel[i] = v;
         if (EV) {
@@ -175,9 +199,15 @@ __global__ void __launch_bounds__(256) k_force(Dev d, Box b, StepConsts sc, int 
           if (MIXED) langevin_eta_f(sc.seed, step, d.id[i], e0, e1, e2);
           else langevin_eta(sc.seed, step, d.id[i], e0, e1, e2);
         }
-        v.x = __dadd_rn(__dadd_rn(__dmul_rn(v.x, sc.la), __dmul_rn(e0, sc.lb)), __dmul_rn(__dmul_rn(an.x, 0.5), sc.dt));
-        v.y = __dadd_rn(__dadd_rn(__dmul_rn(v.y, sc.la), __dmul_rn(e1, sc.lb)), __dmul_rn(__dmul_rn(an.y, 0.5), sc.dt));
-        v.z = __dadd_rn(__dadd_rn(__dmul_rn(v.z, sc.la), __dmul_rn(e2, sc.lb)), __dmul_rn(__dmul_rn(an.z, 0.5), sc.dt));
+        if (MIXED) {
+          v.x = fma(an.x, sc.hdt, fma(v.x, sc.la, e0 * sc.lb));
+          v.y = fma(an.y, sc.hdt, fma(v.y, sc.la, e1 * sc.lb));
+          v.z = fma(an.z, sc.hdt, fma(v.z, sc.la, e2 * sc.lb));
+        } else {  // v = (v a + eta b) + (a*0.5) dt, the reference's order
+          v.x = __dadd_rn(__dadd_rn(__dmul_rn(v.x, sc.la), __dmul_rn(e0, sc.lb)), __dmul_rn(__dmul_rn(an.x, 0.5), sc.dt));
+          v.y = __dadd_rn(__dadd_rn(__dmul_rn(v.y, sc.la), __dmul_rn(e1, sc.lb)), __dmul_rn(__dmul_rn(an.y, 0.5), sc.dt));
+          v.z = __dadd_rn(__dadd_rn(__dmul_rn(v.z, sc.la), __dmul_rn(e2, sc.lb)), __dmul_rn(__dmul_rn(an.z, 0.5), sc.dt));
+        }
         d.acc[i] = an;
         d.vel[i] = v;
       }

@@ -1,6 +1,8 @@
 // cav_kernels.cu -- sm_103a kernels of the CAVIAR2 MD step (cell binning,
 // Verlet-list build, integrator stages, thermo reductions, parity exports).
 // The pair-force kernels live in cav_force.cu.
+#include <algorithm>
+
 #include "cav_common.cuh"
 
 namespace cav {
@@ -8,6 +10,17 @@ namespace cav {
 #define FULL_MASK 0xffffffffu
 
 static inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+static int num_sms() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 148;
+  }
+  return sms;
+}
 
 // ---------------------------------------------------------------------------
 // block reduction of NV doubles in a fixed order (deterministic)
@@ -54,6 +67,18 @@ __device__ inline void half_skin_test(const Dev &d, const Box &b, int i, const d
   if (dx * dx + dy * dy + dz * dz > b.thr2) d.flags[F_REBUILD] = 1;
 }
 
+// Mixed form: the displacement since the build is taken once in FP64 (3
+// subtractions) and serves both the half-skin test (in FP32 against a threshold
+// shrunk by 1e-6, so it can only fire early) and the FP32 cell-relative
+// coordinates, rel = rel_at_build + (float)(x - x_at_build).
+__device__ inline void mixed_track(const Dev &d, const Box &b, int i, const dbl4 &x) {
+  const dbl4 r = d.pos_ref[i];
+  const float fx = (float)(x.x - r.x), fy = (float)(x.y - r.y), fz = (float)(x.z - r.z);
+  if (fx * fx + fy * fy + fz * fz > b.thr2f) d.flags[F_REBUILD] = 1;
+  const float4 q = d.rel_ref[i];
+  d.rel[i] = make_float4(q.x + fx, q.y + fy, q.z + fz, q.w);
+}
+
 __device__ inline void nan_check(const Dev &d, int i, const dbl4 &a) {
   if (isnan(a.x) || isnan(a.y) || isnan(a.z)) {
     d.flags[F_NAN] = 1;
@@ -61,6 +86,10 @@ __device__ inline void nan_check(const Dev &d, int i, const dbl4 &a) {
   }
 }
 
+// FP64 form: pos += vel*dt + ((acc*0.5)*dt)*dt, unfused, in the reference's order
+// (src/md_simulator.cpp:654), so that equal forces give equal trajectories.
+// Mixed form: the same update with two FMAs per component (the FP64 pipe of
+// this part is its scarcest resource).
 template <bool MIXED>
 __global__ void __launch_bounds__(256) k_drift_vv(Dev d, Box b, StepConsts sc) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -68,14 +97,19 @@ __global__ void __launch_bounds__(256) k_drift_vv(Dev d, Box b, StepConsts sc) {
   dbl4 x = d.pos[i];
   const dbl4 v = d.vel[i], a = d.acc[i];
   nan_check(d, i, a);
-  // pos += vel*dt + ((acc*0.5)*dt)*dt, unfused as in the reference expression
-  x.x = __dadd_rn(x.x, __dadd_rn(__dmul_rn(v.x, sc.dt), __dmul_rn(__dmul_rn(__dmul_rn(a.x, 0.5), sc.dt), sc.dt)));
-  x.y = __dadd_rn(x.y, __dadd_rn(__dmul_rn(v.y, sc.dt), __dmul_rn(__dmul_rn(__dmul_rn(a.y, 0.5), sc.dt), sc.dt)));
-  x.z = __dadd_rn(x.z, __dadd_rn(__dmul_rn(v.z, sc.dt), __dmul_rn(__dmul_rn(__dmul_rn(a.z, 0.5), sc.dt), sc.dt)));
+  if (MIXED) {
+    x.x = fma(a.x, sc.hdt2, fma(v.x, sc.dt, x.x));
+    x.y = fma(a.y, sc.hdt2, fma(v.y, sc.dt, x.y));
+    x.z = fma(a.z, sc.hdt2, fma(v.z, sc.dt, x.z));
+  } else {
+    x.x = __dadd_rn(x.x, __dadd_rn(__dmul_rn(v.x, sc.dt), __dmul_rn(__dmul_rn(__dmul_rn(a.x, 0.5), sc.dt), sc.dt)));
+    x.y = __dadd_rn(x.y, __dadd_rn(__dmul_rn(v.y, sc.dt), __dmul_rn(__dmul_rn(__dmul_rn(a.y, 0.5), sc.dt), sc.dt)));
+    x.z = __dadd_rn(x.z, __dadd_rn(__dmul_rn(v.z, sc.dt), __dmul_rn(__dmul_rn(__dmul_rn(a.z, 0.5), sc.dt), sc.dt)));
+  }
   d.pos[i] = x;
   d.acc_old[i] = a;
-  half_skin_test(d, b, i, x);
-  if (MIXED) update_rel(d, b, i, x);
+  if (MIXED) mixed_track(d, b, i, x);
+  else half_skin_test(d, b, i, x);
 }
 
 // Langevin first half (src/md_simulator.cpp:748-837):
@@ -94,21 +128,33 @@ __global__ void __launch_bounds__(256) k_lang_a(Dev d, Box b, StepConsts sc, int
       if (MIXED) langevin_eta_f(sc.seed, step, d.id[i], e0, e1, e2);
       else langevin_eta(sc.seed, step, d.id[i], e0, e1, e2);
     }
-    v.x = __dadd_rn(v.x, __dadd_rn(__dmul_rn(__dmul_rn(a.x, 0.5), sc.dt), __dmul_rn(e0, sc.lb)));
-    v.y = __dadd_rn(v.y, __dadd_rn(__dmul_rn(__dmul_rn(a.y, 0.5), sc.dt), __dmul_rn(e1, sc.lb)));
-    v.z = __dadd_rn(v.z, __dadd_rn(__dmul_rn(__dmul_rn(a.z, 0.5), sc.dt), __dmul_rn(e2, sc.lb)));
+    if (MIXED) {
+      v.x = fma(a.x, sc.hdt, fma(e0, sc.lb, v.x));
+      v.y = fma(a.y, sc.hdt, fma(e1, sc.lb, v.y));
+      v.z = fma(a.z, sc.hdt, fma(e2, sc.lb, v.z));
+    } else {
+      v.x = __dadd_rn(v.x, __dadd_rn(__dmul_rn(__dmul_rn(a.x, 0.5), sc.dt), __dmul_rn(e0, sc.lb)));
+      v.y = __dadd_rn(v.y, __dadd_rn(__dmul_rn(__dmul_rn(a.y, 0.5), sc.dt), __dmul_rn(e1, sc.lb)));
+      v.z = __dadd_rn(v.z, __dadd_rn(__dmul_rn(__dmul_rn(a.z, 0.5), sc.dt), __dmul_rn(e2, sc.lb)));
+    }
     if (THERMO) {
       const double m = d.tab->mass[(int)x.w];
       part[0] = m * (v.x * v.x + v.y * v.y + v.z * v.z);
       part[1] = m * v.x; part[2] = m * v.y; part[3] = m * v.z;
     }
-    x.x = __dadd_rn(x.x, __dmul_rn(v.x, sc.lc));
-    x.y = __dadd_rn(x.y, __dmul_rn(v.y, sc.lc));
-    x.z = __dadd_rn(x.z, __dmul_rn(v.z, sc.lc));
+    if (MIXED) {
+      x.x = fma(v.x, sc.lc, x.x);
+      x.y = fma(v.y, sc.lc, x.y);
+      x.z = fma(v.z, sc.lc, x.z);
+    } else {
+      x.x = __dadd_rn(x.x, __dmul_rn(v.x, sc.lc));
+      x.y = __dadd_rn(x.y, __dmul_rn(v.y, sc.lc));
+      x.z = __dadd_rn(x.z, __dmul_rn(v.z, sc.lc));
+    }
     d.pos[i] = x;
     d.vel[i] = v;
-    half_skin_test(d, b, i, x);
-    if (MIXED) update_rel(d, b, i, x);
+    if (MIXED) mixed_track(d, b, i, x);
+    else half_skin_test(d, b, i, x);
   }
   if (THERMO) block_sum_store<4>(part, &d.partials_ke[(size_t)blockIdx.x * 4]);
 }
@@ -198,12 +244,21 @@ __global__ void __launch_bounds__(256) k_scatter(Dev d, int n, int forced) {
   d.perm_tmp[d.cell_start[c] + atomicAdd(&d.cell_cursor[c], 1)] = i;
 }
 
-// one warp per cell: order the cell's atoms by host index (deterministic lists)
+// one warp per cell: order the cell's atoms by host index (deterministic lists);
+// cells of up to 32 atoms rank in registers with warp shuffles
 __global__ void __launch_bounds__(256) k_cell_sort(Dev d, int ncell, int forced) {
   if (rebuild_off(d, forced)) return;
   const int cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (cell >= ncell) return;
   const int s = d.cell_start[cell], e = d.cell_start[cell + 1], n = e - s;
+  if (n <= 32) {
+    const int ia = lane < n ? d.perm_tmp[s + lane] : 0;
+    const uint32_t ida = lane < n ? d.id[ia] : 0xffffffffu;
+    int rank = 0;
+    for (int q = 0; q < n; ++q) rank += __shfl_sync(FULL_MASK, ida, q) < ida;
+    if (lane < n) d.perm[s + rank] = ia;
+    return;
+  }
   for (int a = lane; a < n; a += 32) {
     const int ia = d.perm_tmp[s + a];
     const uint32_t ida = d.id[ia];
@@ -241,6 +296,7 @@ __global__ void __launch_bounds__(256) k_gather(Dev d, Box b, int n, int forced)
   d.id[k] = d.t_id[o];
   d.cell_of[k] = d.perm_tmp[o];
   update_rel(d, b, k, x);
+  d.rel_ref[k] = d.rel[k];
 }
 
 // Verlet-list build over the 27-cell stencil with periodic image shifts.
@@ -248,73 +304,255 @@ __global__ void __launch_bounds__(256) k_gather(Dev d, Box b, int n, int forced)
 // evaluates it for a ghost image (image = x_j + s*L, then minus x_i, squares
 // summed x, y, z; no FMA contraction), pre-screened in FP32 on cell-relative
 // coordinates: only candidates inside a narrow band around the cutoff take
-// the FP64 path.  BT lanes cooperate on one atom; hits are compacted with a
-// group ballot.  mode 0 stores image codes (FP64 force), mode 1 cell-offset
-// codes (mixed force).
-template <int BT>
-__global__ void __launch_bounds__(256) k_build(Dev d, Box b, int n, int mode, int forced) {
-  if (rebuild_off(d, forced)) return;
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = gt / BT, g = threadIdx.x % BT;
-  if (i >= n) return;  // uniform per group
+// the FP64 path.  Hits are compacted with a warp ballot, so every atom's list
+// keeps the stencil order (deterministic).  mode 0 stores image codes (FP64
+// force), mode 1 cell-offset codes (mixed force).
+__device__ __noinline__ bool exact_pair(const Dev &d, const Box &b, int i, int j, int img) {
+  const dbl4 xi = d.pos[i], xj = d.pos[j];
+  const double shx = (img % 3 - 1) * b.L[0], shy = ((img / 3) % 3 - 1) * b.L[1], shz = (img / 9 - 1) * b.L[2];
+  const double ddx = __dsub_rn(__dadd_rn(xj.x, shx), xi.x);
+  const double ddy = __dsub_rn(__dadd_rn(xj.y, shy), xi.y);
+  const double ddz = __dsub_rn(__dadd_rn(xj.z, shz), xi.z);
+  const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)), __dmul_rn(ddz, ddz));
+  return r2 < b.ce2;
+}
+
+// the caller folds the largest count into F_MAXNB once per warp
+__device__ inline void finish_atom(const Dev &d, int i, int cnt) {
+  d.nnbr[i] = min(cnt, d.cap);
+  if (cnt > d.cap) atomicMax(&d.flags[F_OVERFLOW], cnt);
+}
+
+// One warp builds the list of atom i straight from global memory (stencils too
+// dense for the shared-memory stage).
+__device__ int build_atom_global(const Dev &d, const Box &b, int i, int mode) {
   const int lane = threadIdx.x & 31;
-  const unsigned gmask = (BT == 32) ? FULL_MASK : (((1u << BT) - 1u) << (lane & ~(BT - 1)));
-  const int gbase = lane & ~(BT - 1);
-  const dbl4 xi = d.pos[i];
   const float4 ri = d.rel[i];
   const int ci = d.cell_of[i];
   const int cx = ci % b.nc[0], cy = (ci / b.nc[0]) % b.nc[1], cz = ci / (b.nc[0] * b.nc[1]);
-  const int cap = d.cap, tpa = d.tpa;
   int cnt = 0;
-  for (int dz = -1; dz <= 1; ++dz) {
-    int nz = cz + dz, sz = 0;
+  for (int k = 0; k < 27; ++k) {
+    const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
+    int nx = cx + dx, ny = cy + dy, nz = cz + dz, sx = 0, sy = 0, sz = 0;
+    if (nx < 0) { nx += b.nc[0]; sx = -1; } else if (nx >= b.nc[0]) { nx -= b.nc[0]; sx = 1; }
+    if (ny < 0) { ny += b.nc[1]; sy = -1; } else if (ny >= b.nc[1]) { ny -= b.nc[1]; sy = 1; }
     if (nz < 0) { nz += b.nc[2]; sz = -1; } else if (nz >= b.nc[2]) { nz -= b.nc[2]; sz = 1; }
-    for (int dy = -1; dy <= 1; ++dy) {
-      int ny = cy + dy, sy = 0;
-      if (ny < 0) { ny += b.nc[1]; sy = -1; } else if (ny >= b.nc[1]) { ny -= b.nc[1]; sy = 1; }
-      for (int dx = -1; dx <= 1; ++dx) {
-        int nx = cx + dx, sx = 0;
+    const int c2 = nx + b.nc[0] * (ny + b.nc[1] * nz);
+    const int img = image_code(sx, sy, sz);
+    const uint32_t code = (uint32_t)(mode == 0 ? img : k);
+    const float ox = dx * b.wf[0] - ri.x, oy = dy * b.wf[1] - ri.y, oz = dz * b.wf[2] - ri.z;
+    const int jb = d.cell_start[c2], je = d.cell_start[c2 + 1];
+    for (int base = jb; base < je; base += 32) {
+      const int j = base + lane;
+      bool hit = false;
+      if (j < je && !(img == CODE_ZERO && j == i)) {
+        const float4 rj = d.rel[j];
+        const float fx = rj.x + ox, fy = rj.y + oy, fz = rj.z + oz;
+        const float r2f = fx * fx + fy * fy + fz * fz;
+        hit = r2f < b.ce2_lo || (r2f <= b.ce2_hi && exact_pair(d, b, i, j, img));
+      }
+      const unsigned bal = __ballot_sync(FULL_MASK, hit);
+      if (hit) {
+        const int q = cnt + __popc(bal & ((1u << lane) - 1u));
+        if (q < d.cap) d.nbr[nbr_index(i, q, d.cap, d.tpa)] = (uint32_t)j | (code << CODE_SHIFT);
+      }
+      cnt += __popc(bal);
+    }
+  }
+  if (lane == 0) finish_atom(d, i, cnt);
+  return cnt;
+}
+
+constexpr int BUILD_THREADS = 128;
+constexpr int BUILD_MAXC = 2048;  // staged candidates per cell: 2048 x 21 B = 42 KiB of shared memory
+constexpr size_t BUILD_SMEM = (size_t)BUILD_MAXC * (sizeof(float4) + sizeof(uint32_t) + 1);
+
+// One CTA per home cell (grid-stride over cells): the 27 neighbour cells are
+// staged once in shared memory as FP32 coordinates already shifted into the home
+// cell's frame, then each warp scans them for one home atom at a time.
+__global__ void __launch_bounds__(BUILD_THREADS) k_build_cell(Dev d, Box b, int mode, int forced) {
+  if (rebuild_off(d, forced)) return;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float4 *s_rel = reinterpret_cast<float4 *>(smem);
+  uint32_t *s_word = reinterpret_cast<uint32_t *>(s_rel + BUILD_MAXC);
+  unsigned char *s_img = reinterpret_cast<unsigned char *>(s_word + BUILD_MAXC);
+  __shared__ int s_pre[28], s_cell[27];
+  __shared__ float s_off[27][3];
+  __shared__ uint32_t s_code[27];
+  __shared__ unsigned char s_sc[27];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = BUILD_THREADS / 32;
+  int wmax = 0;
+  for (int cell = blockIdx.x; cell < b.ncell; cell += gridDim.x) {
+    const int hs = d.cell_start[cell], he = d.cell_start[cell + 1];
+    if (hs == he) continue;  // uniform over the block
+    const int cx = cell % b.nc[0], cy = (cell / b.nc[0]) % b.nc[1], cz = cell / (b.nc[0] * b.nc[1]);
+    if (warp == 0) {
+      int cntk = 0;
+      if (lane < 27) {
+        const int dx = lane % 3 - 1, dy = (lane / 3) % 3 - 1, dz = lane / 9 - 1;
+        int nx = cx + dx, ny = cy + dy, nz = cz + dz, sx = 0, sy = 0, sz = 0;
         if (nx < 0) { nx += b.nc[0]; sx = -1; } else if (nx >= b.nc[0]) { nx -= b.nc[0]; sx = 1; }
+        if (ny < 0) { ny += b.nc[1]; sy = -1; } else if (ny >= b.nc[1]) { ny -= b.nc[1]; sy = 1; }
+        if (nz < 0) { nz += b.nc[2]; sz = -1; } else if (nz >= b.nc[2]) { nz -= b.nc[2]; sz = 1; }
         const int c2 = nx + b.nc[0] * (ny + b.nc[1] * nz);
-        const double shx = sx * b.L[0], shy = sy * b.L[1], shz = sz * b.L[2];
-        const float ox = dx * b.wf[0] - ri.x, oy = dy * b.wf[1] - ri.y, oz = dz * b.wf[2] - ri.z;
-        const uint32_t code = (uint32_t)(mode == 0 ? image_code(sx, sy, sz) : image_code(dx, dy, dz));
-        const bool self_img = (sx | sy | sz) == 0;
-        const int jb = d.cell_start[c2], je = d.cell_start[c2 + 1];
-        for (int base = jb; base < je; base += BT) {
-          const int j = base + g;
-          bool hit = false;
-          if (j < je && !(self_img && j == i)) {
-            const float4 rj = d.rel[j];
-            const float fx = rj.x + ox, fy = rj.y + oy, fz = rj.z + oz;
-            const float r2f = fx * fx + fy * fy + fz * fz;
-            if (r2f < b.ce2_lo) {
-              hit = true;
-            } else if (r2f <= b.ce2_hi) {
-              const dbl4 xj = d.pos[j];
-              const double ddx = __dsub_rn(__dadd_rn(xj.x, shx), xi.x);
-              const double ddy = __dsub_rn(__dadd_rn(xj.y, shy), xi.y);
-              const double ddz = __dsub_rn(__dadd_rn(xj.z, shz), xi.z);
-              const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)), __dmul_rn(ddz, ddz));
-              hit = r2 < b.ce2;
-            }
-          }
-          const unsigned bal = __ballot_sync(gmask, hit) >> gbase;
-          if (hit) {
-            const int k = cnt + __popc(bal & ((1u << g) - 1u));
-            if (k < cap) d.nbr[nbr_index(i, k, cap, tpa)] = (uint32_t)j | (code << CODE_SHIFT);
-          }
-          cnt += __popc(bal);
+        const int img = image_code(sx, sy, sz);
+        s_cell[lane] = c2;
+        s_off[lane][0] = dx * b.wf[0]; s_off[lane][1] = dy * b.wf[1]; s_off[lane][2] = dz * b.wf[2];
+        s_code[lane] = (uint32_t)(mode == 0 ? img : lane);
+        s_sc[lane] = (unsigned char)img;
+        cntk = d.cell_start[c2 + 1] - d.cell_start[c2];
+      }
+      int inc = cntk;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL_MASK, inc, o);
+        if (lane >= o) inc += y;
+      }
+      if (lane < 27) s_pre[lane + 1] = inc;
+      if (lane == 0) s_pre[0] = 0;
+    }
+    __syncthreads();
+    const int total = s_pre[27];
+    if (total <= BUILD_MAXC) {
+      for (int idx = threadIdx.x; idx < total; idx += BUILD_THREADS) {
+        int k = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1)
+          if (k + step < 27 && s_pre[k + step] <= idx) k += step;
+        const int j = d.cell_start[s_cell[k]] + (idx - s_pre[k]);
+        float4 r = d.rel[j];
+        r.x += s_off[k][0]; r.y += s_off[k][1]; r.z += s_off[k][2];
+        s_rel[idx] = r;
+        s_word[idx] = (uint32_t)j | (s_code[k] << CODE_SHIFT);
+        s_img[idx] = s_sc[k];
+      }
+      __syncthreads();
+      // NA home atoms per warp: every staged candidate read serves all of them
+      constexpr int NA = 4;
+      const unsigned lt = (1u << lane) - 1u;
+      const int cap = d.cap;
+      for (int i0 = hs + NA * warp; i0 < he; i0 += NA * nwarps) {
+        int ii[NA], cnt[NA];
+        bool has[NA];
+        float4 rr[NA];
+        uint32_t *row[NA];
+#pragma unroll
+        for (int u = 0; u < NA; ++u) {
+          has[u] = i0 + u < he;
+          ii[u] = has[u] ? i0 + u : i0;
+          rr[u] = d.rel[ii[u]];
+          row[u] = d.nbr + (size_t)ii[u] * cap;
+          cnt[u] = 0;
         }
+        for (int base = 0; base < total; base += 32) {
+          const int idx = base + lane;
+          const bool valid = idx < total;
+          const int sidx = valid ? idx : total - 1;  // in-range read; the lane is masked below
+          const float4 c = s_rel[sidx];
+          const uint32_t w = s_word[sidx];
+          const bool zero_img = s_img[sidx] == CODE_ZERO;
+          const int j = (int)(w & IDX_MASK);
+          bool hit[NA], band[NA], any_band = false;
+#pragma unroll
+          for (int u = 0; u < NA; ++u) {
+            const float ax = c.x - rr[u].x, ay = c.y - rr[u].y, az = c.z - rr[u].z;
+            const float q = ax * ax + ay * ay + az * az;
+            const bool ok = valid & has[u] & !((j == ii[u]) & zero_img);
+            hit[u] = ok & (q < b.ce2_lo);
+            band[u] = ok & (q >= b.ce2_lo) & (q <= b.ce2_hi);
+            any_band |= band[u];
+          }
+          if (__ballot_sync(FULL_MASK, any_band)) {  // rare: exact FP64 predicate
+#pragma unroll
+            for (int u = 0; u < NA; ++u)
+              if (band[u]) hit[u] = exact_pair(d, b, ii[u], j, s_img[sidx]);
+          }
+#pragma unroll
+          for (int u = 0; u < NA; ++u) {
+            const unsigned bal = __ballot_sync(FULL_MASK, hit[u]);
+            if (hit[u]) {
+              const int q = cnt[u] + __popc(bal & lt);
+              if (q < cap) row[u][q] = w;
+            }
+            cnt[u] += __popc(bal);
+          }
+        }
+        if (lane == 0) {
+#pragma unroll
+          for (int u = 0; u < NA; ++u)
+            if (has[u]) {
+              finish_atom(d, ii[u], cnt[u]);
+              wmax = max(wmax, cnt[u]);
+            }
+        }
+      }
+    } else {
+      for (int i = hs + warp; i < he; i += nwarps) wmax = max(wmax, build_atom_global(d, b, i, mode));
+    }
+    __syncthreads();  // the stage is reused by the next cell
+  }
+  // one atomic per warp for the largest list length (not one per atom)
+  if (lane == 0 && wmax > 0) atomicMax(&d.flags[F_MAXNB], wmax);
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&d.flags[F_REBUILDS], 1);
+}
+
+// One warp per home cell, one lane per home atom (cells of more than 32 atoms
+// loop).  The warp walks the 27 stencil cells' atoms in order; every candidate
+// is one warp-broadcast load of its FP32 cell-relative coordinates (the stencil
+// is L1-resident), tested against all home atoms at once.  Hits append to the
+// lane's own row, so the list keeps the stencil order (deterministic) and no
+// ballot or barrier is needed.
+__global__ void __launch_bounds__(256) k_build_warp(Dev d, Box b, int mode, int forced) {
+  if (rebuild_off(d, forced)) return;
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  const int cap = d.cap;
+  int wmax = 0;
+  for (int cell = gw; cell < b.ncell; cell += nw) {
+    const int hs = d.cell_start[cell], he = d.cell_start[cell + 1];
+    const int cx = cell % b.nc[0], cy = (cell / b.nc[0]) % b.nc[1], cz = cell / (b.nc[0] * b.nc[1]);
+    for (int i0 = hs; i0 < he; i0 += 32) {
+      const int i = i0 + lane;
+      const bool act = i < he;
+      const float4 ri = act ? d.rel[i] : make_float4(1e18f, 1e18f, 1e18f, 0.f);
+      uint32_t *row = d.nbr + nbr_block_base(act ? i : hs, cap, d.tpa);
+      const int cshift = 7 - log2_pow2(d.tpa);  // chunk stride 4A words = 2^(as+2)
+      int cnt = 0;
+      for (int k = 0; k < 27; ++k) {
+        const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
+        int nx = cx + dx, ny = cy + dy, nz = cz + dz, sx = 0, sy = 0, sz = 0;
+        if (nx < 0) { nx += b.nc[0]; sx = -1; } else if (nx >= b.nc[0]) { nx -= b.nc[0]; sx = 1; }
+        if (ny < 0) { ny += b.nc[1]; sy = -1; } else if (ny >= b.nc[1]) { ny -= b.nc[1]; sy = 1; }
+        if (nz < 0) { nz += b.nc[2]; sz = -1; } else if (nz >= b.nc[2]) { nz -= b.nc[2]; sz = 1; }
+        const int c2 = nx + b.nc[0] * (ny + b.nc[1] * nz);
+        const int img = image_code(sx, sy, sz);
+        const uint32_t code = (uint32_t)(mode == 0 ? img : k) << CODE_SHIFT;
+        const float ox = dx * b.wf[0] - ri.x, oy = dy * b.wf[1] - ri.y, oz = dz * b.wf[2] - ri.z;
+        const int jb = d.cell_start[c2], je = d.cell_start[c2 + 1];
+        const int self = (img == CODE_ZERO && act) ? i : -1;  // the home atom itself is not a neighbour
+        const float lo = act ? b.ce2_lo : -1.0f;               // idle lanes never hit
+        for (int j = jb; j < je; ++j) {
+          const float4 rj = __ldg(&d.rel[j]);  // same address in every lane: one broadcast
+          const float fx = rj.x + ox, fy = rj.y + oy, fz = rj.z + oz;
+          const float q = fx * fx + fy * fy + fz * fz;
+          bool hit = (q < lo) & (j != self);
+          if (__any_sync(FULL_MASK, (q >= lo) & (q <= b.ce2_hi) & act)) {  // rare: exact FP64 predicate
+            if ((q >= lo) & (q <= b.ce2_hi) & act & (j != self)) hit = exact_pair(d, b, i, j, img);
+          }
+          if (hit & (cnt < cap)) row[((cnt >> 2) << cshift) + (cnt & 3)] = (uint32_t)j | code;
+          cnt += hit;
+        }
+      }
+      if (act) {
+        finish_atom(d, i, cnt);
+        wmax = max(wmax, cnt);
       }
     }
   }
-  if (g == 0) {
-    d.nnbr[i] = min(cnt, cap);
-    atomicMax(&d.flags[F_MAXNB], cnt);
-    if (cnt > cap) atomicMax(&d.flags[F_OVERFLOW], cnt);
-    if (i == 0) atomicAdd(&d.flags[F_REBUILDS], 1);
-  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(FULL_MASK, wmax, o));
+  if (lane == 0 && wmax > 0) atomicMax(&d.flags[F_MAXNB], wmax);
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&d.flags[F_REBUILDS], 1);
 }
 
 __global__ void k_clear_rebuild_flag(Dev d) { d.flags[F_REBUILD] = 0; }
@@ -505,7 +743,8 @@ int launch_rebuild(const Dev &d, const Box &b, const LaunchCfg &lc, int forced, 
   k_copy_state<<<g, 256, 0, st>>>(d, n, forced);
   k_gather<<<g, 256, 0, st>>>(d, b, n, forced);
   const int mode = lc.precision == CAVGPU_MIXED ? 1 : 0;
-  k_build<8><<<ceil_div((long long)n * 8, 256), 256, 0, st>>>(d, b, n, mode, forced);
+  const int build_grid = std::min(ceil_div((long long)b.ncell * 32, 256), num_sms() * 8);
+  k_build_warp<<<build_grid, 256, 0, st>>>(d, b, mode, forced);
   k_clear_rebuild_flag<<<1, 1, 0, st>>>(d);
   return chk();
 }
