@@ -46,7 +46,29 @@ def build(verbose=False):
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
+    build_host()
     return LIB
+
+
+HOST_LIB = os.path.join(HERE, "libcaviar2_gpu.so")
+HOST_HARNESS = os.path.join(OBJ, "host_harness")
+
+
+def build_host():
+    """The CAVIAR2-shaped C++ API (host/) over libcavgpu.so, and its test harness."""
+    inc = ["-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(HERE, "host")]
+    cxx = os.environ.get("CXX", "g++")
+    steps = [
+        [cxx, "-O2", "-std=c++17", "-fPIC", "-shared", *inc, os.path.join(HERE, "host", "caviar2_gpu.cpp"),
+         "-o", HOST_LIB, "-L" + HERE, "-lcavgpu", "-Wl,-rpath,$ORIGIN"],
+        [cxx, "-O2", "-std=c++17", *inc, os.path.join(ROOT, "tests", "cpp", "host_harness.cpp"), "-o",
+         HOST_HARNESS, "-L" + HERE, "-lcaviar2_gpu", "-lcavgpu", "-Wl,-rpath," + HERE],
+    ]
+    for cmd in steps:
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"host build failed ({' '.join(cmd[:3])} ...):\n{r.stderr}")
+    return HOST_LIB
 
 
 if __name__ == "__main__":

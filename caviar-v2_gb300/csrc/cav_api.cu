@@ -33,6 +33,8 @@ struct cavgpu_ctx {
   ThermoCfg tc{};
   PairTab tab_h{};
   cudaStream_t st = nullptr;
+  cudaStream_t side = nullptr;  // captures the bodies of the conditional rebuild nodes
+  long long rebuilds_counted = 0;
   int n = 0;
   bool uploaded = false, set_up = false;
   long long steps_done = 0;
@@ -110,6 +112,50 @@ int enqueue_step(cavgpu_ctx *c, int k, bool thermo, int ring_slot) {
   return CAVGPU_OK;
 }
 
+// One MD step recorded into the graph being captured on c->st.  The rebuild
+// kernels sit in the body of an IF conditional node whose value the step's
+// half-skin flag sets on the device, so steps without a rebuild launch three
+// kernels (drift, condition, force) instead of eleven.
+int capture_step(cavgpu_ctx *c, int k, bool thermo, int ring_slot) {
+  const bool lang = c->p.integrator == CAVGPU_VELOCITY_VERLET_LANGEVIN;
+  RK(launch_drift(c->d, c->b, c->sc, c->lc, k, thermo && lang, c->st));
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamGetCaptureInfo(c->st, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+  cudaGraphConditionalHandle h;
+  CK(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
+  RK(launch_set_rebuild_cond(c->d, h, c->st));
+  const cudaGraphNode_t *deps = nullptr;
+  size_t nd = 0;
+  CK(cudaStreamGetCaptureInfo(c->st, &cs, nullptr, &g, &deps, nullptr, &nd));
+  // the params struct holds a union without a default constructor: zeroed storage
+  alignas(cudaGraphNodeParams) unsigned char cp_raw[sizeof(cudaGraphNodeParams)];
+  std::memset(cp_raw, 0, sizeof(cp_raw));
+  cudaGraphNodeParams &cp = *reinterpret_cast<cudaGraphNodeParams *>(cp_raw);
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeIf;
+  cp.conditional.size = 1;
+  cudaGraphNode_t cond = nullptr;
+  CK(cudaGraphAddNode(&cond, g, deps, nullptr, nd, &cp));
+  CK(cudaStreamBeginCaptureToGraph(c->side, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                   cudaStreamCaptureModeThreadLocal));
+  const int brc = launch_rebuild(c->d, c->b, c->lc, 1, c->side);
+  cudaGraph_t body = nullptr;
+  const cudaError_t be = cudaStreamEndCapture(c->side, &body);
+  RK(brc);
+  CK(be);
+  CK(cudaStreamUpdateCaptureDependencies(c->st, &cond, nullptr, 1, cudaStreamSetCaptureDependencies));
+  if (c->prof && k < (int)c->ev0.size()) CK(cudaEventRecordWithFlags(c->ev0[k], c->st, cudaEventRecordExternal));
+  RK(launch_force(c->d, c->b, c->sc, c->lc, lang ? 2 : 1, thermo, k, c->st));
+  if (c->prof && k < (int)c->ev1.size()) CK(cudaEventRecordWithFlags(c->ev1[k], c->st, cudaEventRecordExternal));
+  if (thermo) {
+    const int nb_ke = lang ? drift_grid_blocks(c->lc) : force_grid_blocks(c->lc);
+    RK(launch_thermo_final(c->d, c->tc, nb_ke, force_grid_blocks(c->lc), ring_slot, c->st));
+  }
+  return CAVGPU_OK;
+}
+
 int ensure_events(cavgpu_ctx *c, int S) {
   while ((int)c->ev0.size() < S) {
     cudaEvent_t a, b;
@@ -139,15 +185,13 @@ GraphEntry *get_graph(cavgpu_ctx *c, int S, int every, int *rc) {
   if (c->prof && (*rc = ensure_events(c, S))) return nullptr;
   cudaGraph_t graph = nullptr;
   if ((*rc = cuda_rc(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal)))) return nullptr;
-  const long long kl = c->kernel_launches;
   int erc = CAVGPU_OK;
   for (int k = 0; k < S && !erc; ++k) {
     const bool th = every > 0 && ((k + 1) % every == 0);
-    erc = enqueue_step(c, k, th, th ? (k + 1) / every - 1 : -1);
+    erc = capture_step(c, k, th, th ? (k + 1) / every - 1 : -1);
   }
   if (!erc) erc = launch_advance_step(c->d, S, c->st);
   cudaError_t e = cudaStreamEndCapture(c->st, &graph);
-  c->kernel_launches = kl;  // capture does not launch
   if (erc || e != cudaSuccess) {
     if (graph) cudaGraphDestroy(graph);
     cudaGetLastError();
@@ -348,6 +392,11 @@ int cavgpu_create(const cavgpu_params *p, cavgpu_ctx **out) {
   if (c->lc.block < 32 || c->lc.block > 256 || c->lc.block % 32) { delete c; return CAVGPU_E_ARG; }
   c->d.tpa = c->lc.tpa;
   if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) { delete c; return CAVGPU_E_CUDA; }
+  if (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaStreamDestroy(c->st);
+    delete c;
+    return CAVGPU_E_CUDA;
+  }
   int rc = dalloc(c, &c->d.tab, 1);
   if (!rc) rc = dalloc(c, &c->d.flags, F_NWORDS);
   if (!rc) rc = dalloc(c, &c->d.thermo, 8);
@@ -371,6 +420,7 @@ void cavgpu_destroy(cavgpu_ctx *c) {
   for (auto e : c->ev1) cudaEventDestroy(e);
   for (void *q : c->allocs) cudaFree(q);
   if (c->st) cudaStreamDestroy(c->st);
+  if (c->side) cudaStreamDestroy(c->side);
   delete c;
 }
 
@@ -470,9 +520,15 @@ int cavgpu_run(cavgpu_ctx *c, int64_t nsteps, int64_t every, double *out5) {
   const bool lang = c->p.integrator == CAVGPU_VELOCITY_VERLET_LANGEVIN;
   int S = c->p.steps_per_graph > 0 ? std::min(c->p.steps_per_graph, MAX_GRAPH_STEPS) : 50;
   if (every > 0) S = (int)std::max<int64_t>(every, (S / every) * every);
-  int64_t done = 0, rec = 0;
+  int64_t done = 0, rec = 0, eager_steps = 0;
   int rc = CAVGPU_OK;
   int chunks_since_check = 0;
+  int rebuilds_at_start = 0;
+  {
+    int f[F_NWORDS];
+    RK(read_flags(c, f));
+    rebuilds_at_start = f[F_REBUILDS];
+  }
   // chunks of up to S steps, each one captured CUDA graph (cached per size).  Without
   // recording, the last chunk computes the thermo of its final step, so that the state
   // after the call carries a fresh temperature (finalize_temperature runs every step).
@@ -488,7 +544,9 @@ int cavgpu_run(cavgpu_ctx *c, int64_t nsteps, int64_t every, double *out5) {
     CK(cudaGraphLaunch(g->exec, c->st));
     const int nrec = ev > 0 ? sz / ev : 0;
     c->graph_launches += 1;
-    c->kernel_launches += (long long)sz * kernels_per_step(c) + 1 + nrec;
+    // drift + condition + force per step, the thermo folds, the step counter; the
+    // rebuild kernels that ran are added from the device's rebuild count below
+    c->kernel_launches += (long long)sz * 3 + 1 + nrec;
     if (c->prof) RK(collect_profile(c, sz));
     if (every > 0) {
       CK(cudaMemcpyAsync(out5 + THERMO_REC * rec, c->d.thermo_ring, THERMO_REC * sizeof(double) * nrec,
@@ -517,9 +575,16 @@ int cavgpu_run(cavgpu_ctx *c, int64_t nsteps, int64_t every, double *out5) {
       rec += 1;
     }
     ++done;
+    ++eager_steps;
     c->steps_done += 1;
   }
   RK(check_status(c));
+  {
+    // rebuild kernels launched by the graphs' conditional nodes (eager steps counted theirs)
+    int f[F_NWORDS];
+    RK(read_flags(c, f));
+    if (eager_steps == 0) c->kernel_launches += (long long)REBUILD_KERNELS * (f[F_REBUILDS] - rebuilds_at_start);
+  }
   (void)lang;
   return CAVGPU_OK;
 }

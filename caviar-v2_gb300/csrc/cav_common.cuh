@@ -198,6 +198,8 @@ int force_grid_blocks(const LaunchCfg &lc);
 int launch_drift(const Dev &d, const Box &b, const StepConsts &sc, const LaunchCfg &lc, int k_in_chunk,
                  int thermo, cudaStream_t st);
 int launch_rebuild(const Dev &d, const Box &b, const LaunchCfg &lc, int forced, cudaStream_t st);
+int launch_set_rebuild_cond(const Dev &d, cudaGraphConditionalHandle h, cudaStream_t st);
+constexpr int REBUILD_KERNELS = 8;  // kernels launch_rebuild enqueues
 // kick: 0 = force only, 1 = VV closing kick, 2 = Langevin closing update.
 // thermo: virial/PE partials (and KE partials unless kick == 2).
 int launch_force(const Dev &d, const Box &b, const StepConsts &sc, const LaunchCfg &lc, int kick, int thermo,

@@ -198,42 +198,58 @@ __global__ void __launch_bounds__(256) k_bin(Dev d, Box b, int n, int forced) {
 
 // exclusive scan of `count[0..m)` into start[0..m] with one block; zeroes
 // count and (if non-null) cursor for the next use
+// Tiles of 4 x 1024 consecutive counts: coalesced loads, a warp-shuffle block
+// scan per tile, and a running carry between tiles.
 __global__ void __launch_bounds__(1024) k_scan(const Dev d, int *count, int *start, int *cursor, int m, int forced) {
   if (rebuild_off(d, forced)) return;
   __shared__ int warp_tot[32];
-  const int t = threadIdx.x, nt = blockDim.x;
-  const int per = (m + nt - 1) / nt;
-  const int beg = min(t * per, m), end = min(beg + per, m);
-  int s = 0;
-  for (int k = beg; k < end; ++k) s += count[k];
-  // block exclusive scan of s
-  const int lane = t & 31, wid = t >> 5;
-  int inc = s;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int y = __shfl_up_sync(FULL_MASK, inc, o);
-    if (lane >= o) inc += y;
-  }
-  if (lane == 31) warp_tot[wid] = inc;
+  __shared__ int carry_s;
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  if (t == 0) carry_s = 0;
   __syncthreads();
-  if (wid == 0) {
-    int wv = lane < (nt >> 5) ? warp_tot[lane] : 0;
+  for (int base = 0; base < m; base += 4 * 1024) {
+    int v[4], s = 0;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int k = base + 4 * t + u;
+      v[u] = k < m ? count[k] : 0;
+      s += v[u];
+    }
+    int inc = s;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(FULL_MASK, wv, o);
-      if (lane >= o) wv += y;
+      const int y = __shfl_up_sync(FULL_MASK, inc, o);
+      if (lane >= o) inc += y;
     }
-    warp_tot[lane] = wv;
+    if (lane == 31) warp_tot[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+      int wv = warp_tot[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL_MASK, wv, o);
+        if (lane >= o) wv += y;
+      }
+      warp_tot[lane] = wv;
+    }
+    __syncthreads();
+    const int carry = carry_s;
+    int run = carry + inc - s + (wid ? warp_tot[wid - 1] : 0);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int k = base + 4 * t + u;
+      if (k < m) {
+        start[k] = run;
+        count[k] = 0;
+        if (cursor) cursor[k] = 0;
+      }
+      run += v[u];
+    }
+    __syncthreads();  // every thread has read carry_s and warp_tot
+    if (t == 1023) carry_s = run;
+    __syncthreads();
   }
-  __syncthreads();
-  int run = inc - s + (wid ? warp_tot[wid - 1] : 0);
-  for (int k = beg; k < end; ++k) {
-    start[k] = run;
-    run += count[k];
-    count[k] = 0;
-    if (cursor) cursor[k] = 0;
-  }
-  if (t == nt - 1) start[m] = run;
+  if (t == 0) start[m] = carry_s;
 }
 
 __global__ void __launch_bounds__(256) k_scatter(Dev d, int n, int forced) {
@@ -556,6 +572,17 @@ __global__ void __launch_bounds__(256) k_build_warp(Dev d, Box b, int mode, int 
 }
 
 __global__ void k_clear_rebuild_flag(Dev d) { d.flags[F_REBUILD] = 0; }
+
+// Inside a captured step: the half-skin flag becomes the value of the graph's
+// conditional node that wraps the rebuild kernels.
+__global__ void k_set_rebuild_cond(Dev d, cudaGraphConditionalHandle h) {
+  cudaGraphSetConditional(h, d.flags[F_REBUILD] != 0 ? 1u : 0u);
+}
+
+int launch_set_rebuild_cond(const Dev &d, cudaGraphConditionalHandle h, cudaStream_t st) {
+  k_set_rebuild_cond<<<1, 1, 0, st>>>(d, h);
+  return cudaPeekAtLastError() == cudaSuccess ? CAVGPU_OK : CAVGPU_E_CUDA;
+}
 
 // ---------------------------------------------------------------------------
 // thermo: fold the per-block partials (fixed order) into KE, T, P, virial, PE

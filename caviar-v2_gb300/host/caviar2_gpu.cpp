@@ -1,0 +1,334 @@
+// caviar2_gpu.cpp -- CAVIAR2 object API over the cavgpu C ABI (see caviar2_gpu.hpp).
+#include "caviar2_gpu.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <unordered_map>
+
+namespace caviar2 {
+
+// ---------------------------------------------------------------- Log
+void Log::info(const std::string &s) { std::fprintf(stdout, "[INF] %s\n", s.c_str()); }
+void Log::warning(const std::string &s) { std::fprintf(stdout, "[WRN] %s\n", s.c_str()); }
+void Log::error_all(const std::string &s) {
+  std::fprintf(stderr, "[ERR] %s\n", s.c_str());
+  std::fflush(stdout);
+  std::exit(1);
+}
+
+// ---------------------------------------------------------------- Caviar2
+Caviar2::Caviar2() {
+  atom_data.set_caviar(this);
+  domain.set_caviar(this);
+  md_simulator.set_caviar(this);
+  neighborlist.set_caviar(this);
+}
+
+// ---------------------------------------------------------------- Domain
+void Domain::generate() {
+  // one rank: grid index 0 of 1 (src/domain.cpp:309-328, 495-502)
+  lower_local.x = lower_global.x + (upper_global.x - lower_global.x) * 0 / 1;
+  lower_local.y = lower_global.y + (upper_global.y - lower_global.y) * 0 / 1;
+  lower_local.z = lower_global.z + (upper_global.z - lower_global.z) * 0 / 1;
+  upper_local.x = lower_global.x + (upper_global.x - lower_global.x) * 1 / 1;
+  upper_local.y = lower_global.y + (upper_global.y - lower_global.y) * 1 / 1;
+  upper_local.z = lower_global.z + (upper_global.z - lower_global.z) * 1 / 1;
+  size_local = Vector3d<double>{upper_local.x - lower_local.x, upper_local.y - lower_local.y,
+                                upper_local.z - lower_local.z};
+  size_global = Vector3d<double>{upper_global.x - lower_global.x, upper_global.y - lower_global.y,
+                                 upper_global.z - lower_global.z};
+  half_edge = Vector3d<double>{0.5 * size_global.x, 0.5 * size_global.y, 0.5 * size_global.z};
+}
+
+// ---------------------------------------------------------------- Atom_data
+void Atom_data::add_type_mass(int type, double m) {
+  if ((int)atom_type_params.mass.size() < type + 1) {
+    atom_type_params.mass.resize(type + 1);
+    atom_type_params.mass_inv.resize(type + 1);
+  }
+  atom_type_params.mass[type] = m;
+  atom_type_params.mass_inv[type] = m == 0.0 ? 0.0 : 1.0 / m;
+  if (m < 0) caviar_->log.warning("you have entered a negative value for atom mass.");
+}
+
+bool Atom_data::add_atom(size_t id, size_t type, const Vector3d<double> &pos, const Vector3d<double> &vel) {
+  atom_struct_owned.id.push_back(id);
+  atom_struct_owned.type.push_back(type);
+  atom_struct_owned.position.push_back(pos);
+  atom_struct_owned.velocity.push_back(vel);
+  atom_struct_owned.acceleration.push_back(Vector3d<double>{0, 0, 0});
+  return true;
+}
+
+bool Atom_data::add_atom(tools::Atom &a) {
+  const Domain &d = caviar_->domain;
+  const auto &p = a.position;
+  if (p.x < d.lower_global.x || p.x >= d.upper_global.x || p.y < d.lower_global.y || p.y >= d.upper_global.y ||
+      p.z < d.lower_global.z || p.z >= d.upper_global.z)
+    return false;
+  return add_atom(atom_struct_owned.id.size(), a.type, a.position, a.velocity);
+}
+
+void Atom_data::reset_owned_acceleration() {
+  for (auto &v : atom_struct_owned.acceleration) v = Vector3d<double>{0, 0, 0};
+}
+
+int Atom_data::get_n_r_df() {
+  if (n_r_df == -1) {
+    if (stochastic_force_present) {
+      n_r_df = 0;
+    } else {
+      const auto bc = caviar_->domain.boundary_condition;
+      const int s = bc.x + bc.y + bc.z;
+      n_r_df = s == 0 ? 6 : (s == 3 ? 3 : 6 - s);
+    }
+  }
+  return n_r_df;
+}
+
+// ---------------------------------------------------------------- Neighborlist
+void Neighborlist::set_cutoff(double v) {
+  if (v <= 0.0) caviar_->log.error_all("cutoff have to non-negative.");
+  cutoff = v;
+}
+void Neighborlist::set_cutoff_extra_coef(double v) {
+  if (v < 1.0) caviar_->log.error_all("cutoff_extra_coef must be larger than 1.0");
+  cutoff_extra_coef = v;
+}
+
+// ---------------------------------------------------------------- Lj
+namespace force_field {
+void Lj::set_cutoff(double v) {
+  if (v < 0.0) throw std::runtime_error("Force field cutoff must be non-negative.");
+  cutoff = v;
+}
+void Lj::set_epsilon(int t1, int t2, double v) {
+  if ((int)epsilon.size() < t1 + 1) epsilon.resize(t1 + 1);
+  if ((int)epsilon[t1].size() < t2 + 1) epsilon[t1].resize(t2 + 1, 0);
+  epsilon[t1][t2] = v;
+}
+void Lj::set_sigma(int t1, int t2, double v) {
+  if ((int)sigma.size() < t1 + 1) sigma.resize(t1 + 1);
+  if ((int)sigma[t1].size() < t2 + 1) sigma[t1].resize(t2 + 1, 0);
+  sigma[t1][t2] = v;
+}
+void Lj::set_cutoff_list(const std::vector<std::vector<double>> &v) {
+  for (auto &r : v)
+    for (double x : r)
+      if (x < 0.0) throw std::runtime_error("Cutoff list values must be non-negative.");
+  cutoff_list = v;
+  cutoff_list_activated = true;
+}
+void Lj::calculate_acceleration() {
+  Md_simulator &md = caviar_->md_simulator;
+  if (!md.initialized) {
+    md.initialize();
+    md.setup();  // computes the force
+  } else {
+    md.sync_host();
+  }
+}
+}  // namespace force_field
+
+// ---------------------------------------------------------------- Md_simulator
+void Md_simulator::check(int status, const char *what) {
+  if (status == CAVGPU_OK) return;
+  std::string s = std::string(what) + ": " + cavgpu_strerror(status);
+  if (status == CAVGPU_E_CUDA) s += std::string(" (") + cavgpu_last_cuda_error() + ")";
+  caviar_->log.error_all(s);
+}
+
+void Md_simulator::set_integrator_type(Integrator_t t) {
+  integrator_type = t;
+  if (t == Integrator_t::Unknown) caviar_->log.error_all("invalid or non-implemented integrator");
+}
+void Md_simulator::langevin_temperature(double v) {
+  langevin_param.temperature = v;
+  if (v < 0.0) caviar_->log.error_all("Temperature have to non-negative.");
+}
+void Md_simulator::langevin_friction(double v) {
+  langevin_param.friction = v;
+  if (v < 0.0) caviar_->log.error_all("friction have to non-negative.");
+}
+void Md_simulator::langevin_kb(double v) {
+  langevin_param.kb = v;
+  if (v < 0.0) caviar_->log.error_all("kb have to non-negative.");
+}
+void Md_simulator::langevin_kbt(double v) {
+  langevin_param.kbt = v;
+  if (v < 0.0) caviar_->log.error_all("kbt have to non-negative.");
+}
+
+Md_simulator::~Md_simulator() {
+  if (ctx_) cavgpu_destroy(ctx_);
+}
+
+void Md_simulator::initialize() {
+  if (dt < 0.0) caviar_->log.error_all("expected 'dt' input");
+  if (integrator_type != Integrator_t::Velocity_verlet && integrator_type != Integrator_t::Velocity_verlet_langevin)
+    caviar_->log.error_all("integrator not on the GPU path (velocity-Verlet and Langevin are)");
+  if (caviar_->forces.size() != 1) caviar_->log.error_all("the GPU path runs exactly one force_field::Lj");
+  auto *lj = dynamic_cast<force_field::Lj *>(caviar_->forces[0]);
+  if (!lj) caviar_->log.error_all("the GPU path runs force_field::Lj");
+  Atom_data &ad = caviar_->atom_data;
+  Domain &dom = caviar_->domain;
+  Neighborlist &nl = caviar_->neighborlist;
+  if (ad.k_b < 0) caviar_->log.error_all("k_b is not set.");
+
+  cavgpu_params p;
+  cavgpu_default_params(&p);
+  p.lo[0] = dom.lower_global.x; p.lo[1] = dom.lower_global.y; p.lo[2] = dom.lower_global.z;
+  p.hi[0] = dom.upper_global.x; p.hi[1] = dom.upper_global.y; p.hi[2] = dom.upper_global.z;
+  p.bc[0] = dom.boundary_condition.x; p.bc[1] = dom.boundary_condition.y; p.bc[2] = dom.boundary_condition.z;
+  const int nt = (int)std::max<size_t>(ad.atom_type_params.mass.size(), 1);
+  if (nt > CAVGPU_MAX_TYPES) caviar_->log.error_all("too many atom types for the GPU path");
+  p.ntypes = nt;
+  p.nl_cutoff = nl.cutoff;
+  p.nl_coef = nl.cutoff_extra_coef;
+  p.lj_cutoff = lj->cutoff;
+  for (int a = 0; a < nt; ++a)
+    for (int b = 0; b < nt; ++b) {
+      // tables as the reference reads them: entries never set are 0 (src/force/lj.cpp:121-140)
+      auto at = [](const std::vector<std::vector<double>> &t, int i, int j) {
+        return (i < (int)t.size() && j < (int)t[i].size()) ? t[i][j] : 0.0;
+      };
+      p.eps[a * nt + b] = at(lj->epsilon, a, b);
+      p.sigma[a * nt + b] = at(lj->sigma, a, b);
+      p.cutoff_list[a * nt + b] = at(lj->cutoff_list, a, b);
+    }
+  p.cutoff_list_on = lj->cutoff_list_activated ? 1 : 0;
+  for (int t = 0; t < nt; ++t) p.mass[t] = t < (int)ad.atom_type_params.mass.size() ? ad.atom_type_params.mass[t] : 0.0;
+  p.k_b = ad.k_b;
+  p.dt = dt;
+  p.integrator = integrator_type == Integrator_t::Velocity_verlet_langevin ? CAVGPU_VELOCITY_VERLET_LANGEVIN
+                                                                           : CAVGPU_VELOCITY_VERLET;
+  p.lang_temperature = langevin_param.temperature;
+  p.lang_friction = langevin_param.friction;
+  p.lang_kb = langevin_param.kb;
+  p.lang_kbt = langevin_param.kbt;
+  p.seed = seed;
+  p.n_r_df = ad.get_n_r_df();
+  p.pressure_process = ad.pressure_process ? 1 : 0;
+  p.precision = precision;
+  if (ctx_) cavgpu_destroy(ctx_);
+  ctx_ = nullptr;
+  check(cavgpu_create(&p, &ctx_), "cavgpu_create");
+  const auto &o = ad.atom_struct_owned;
+  static_assert(sizeof(Vector3d<double>) == 3 * sizeof(double), "Vector3d<double> must be three packed doubles");
+  static_assert(sizeof(size_t) == sizeof(uint64_t), "size_t must be 64-bit");
+  // slot order = insertion order (the noise key is the index, as the reference's
+  // per-index draw loop, src/md_simulator.cpp:748-757)
+  check(cavgpu_upload(ctx_, (int64_t)o.position.size(), &o.position[0].x, &o.velocity[0].x,
+                      reinterpret_cast<const uint64_t *>(o.type.data()), nullptr),
+        "cavgpu_upload");
+  initialized = true;
+}
+
+void Md_simulator::setup() {
+  check(cavgpu_setup(ctx_), "cavgpu_setup");
+  time = dt * initial_step;
+  sync_host();
+}
+
+void Md_simulator::sync_host() {
+  Atom_data &ad = caviar_->atom_data;
+  auto &o = ad.atom_struct_owned;
+  check(cavgpu_download(ctx_, &o.position[0].x, &o.velocity[0].x, &o.acceleration[0].x), "cavgpu_download");
+  double th[6];
+  check(cavgpu_thermo(ctx_, th), "cavgpu_thermo");
+  ad.kinetic_energy_ = th[0];
+  ad.temperature_ = th[1];
+  ad.pressure_ = th[2];
+  ad.virialForce = th[3];
+  ad.potential_energy_ = th[4];
+  host_dirty_ = false;
+}
+
+void Md_simulator::step() {
+  if (!initialized) {
+    initialize();
+    setup();
+  }
+  check(cavgpu_step(ctx_, 1), "cavgpu_step");
+  double th[6];
+  check(cavgpu_thermo(ctx_, th), "cavgpu_thermo");
+  Atom_data &ad = caviar_->atom_data;
+  ad.kinetic_energy_ = th[0];
+  ad.temperature_ = th[1];
+  ad.pressure_ = th[2];
+  ad.virialForce = th[3];
+  ad.potential_energy_ = th[4];
+  host_dirty_ = true;  // positions stay on the device until sync_host() / run() / cleanup()
+  time += dt;
+}
+
+bool Md_simulator::run() {
+  if (use_time && use_step) caviar_->log.error_all("simulator md: verify_settings: cannot use both 'time' and 'step'.");
+  if (!(use_time || use_step)) caviar_->log.error_all("simulator md: verify_settings: please assign 'time' or 'step' variables.");
+  caviar_->log.info("MD started.");
+  if (!initialized) {
+    initialize();
+    setup();
+  }
+  const int64_t n = final_step - initial_step;
+  if (n > 0) check(cavgpu_step(ctx_, n), "cavgpu_step");
+  current_step = final_step;
+  time = dt * final_step;
+  sync_host();
+  caviar_->log.info("MD finished.");
+  return true;
+}
+
+void Md_simulator::cleanup() {
+  if (!ctx_) return;
+  if (host_dirty_) sync_host();
+  cavgpu_destroy(ctx_);
+  ctx_ = nullptr;
+  initialized = false;
+}
+
+void Md_simulator::export_neighborlist() {
+  if (!ctx_) caviar_->log.error_all("export_neighborlist: no GPU state yet");
+  Atom_data &ad = caviar_->atom_data;
+  Neighborlist &nl = caviar_->neighborlist;
+  const size_t n = ad.atom_struct_owned.position.size();
+  const int64_t np = cavgpu_export_pairs(ctx_, nullptr, 0);
+  if (np < 0) check((int)np, "cavgpu_export_pairs");
+  std::vector<int32_t> rows(5 * (size_t)std::max<int64_t>(np, 1));
+  check((int)std::min<int64_t>(0, cavgpu_export_pairs(ctx_, rows.data(), np)), "cavgpu_export_pairs");
+  // ghost images in the reference's order, for a ghost cutoff no smaller than the list cutoff
+  const double ce = nl.cutoff * nl.cutoff_extra_coef;
+  const double gc = std::max(ad.ghost_cutoff, ce);
+  const int64_t ng = cavgpu_export_ghosts(ctx_, gc, nullptr, nullptr, nullptr, nullptr, 0);
+  if (ng < 0) check((int)ng, "cavgpu_export_ghosts");
+  std::vector<int32_t> src(std::max<int64_t>(ng, 1)), sh(3 * (size_t)std::max<int64_t>(ng, 1));
+  std::vector<double> gp(3 * (size_t)std::max<int64_t>(ng, 1));
+  check((int)std::min<int64_t>(0, cavgpu_export_ghosts(ctx_, gc, src.data(), sh.data(), gp.data(), nullptr, ng)),
+        "cavgpu_export_ghosts");
+  std::unordered_map<int64_t, uint32_t> ghost_of;
+  ghost_source.assign(src.begin(), src.begin() + ng);
+  ghost_position.resize(ng);
+  for (int64_t g = 0; g < ng; ++g) {
+    const int code = (sh[3 * g] + 1) + 3 * (sh[3 * g + 1] + 1) + 9 * (sh[3 * g + 2] + 1);
+    ghost_of[(int64_t)src[g] * 27 + code] = (uint32_t)g;
+    ghost_position[g] = Vector3d<double>{gp[3 * g], gp[3 * g + 1], gp[3 * g + 2]};
+  }
+  nl.neighlist.assign(n, {});
+  for (int64_t r = 0; r < np; ++r) {
+    const int32_t *q = &rows[5 * r];
+    const int code = (q[2] + 1) + 3 * (q[3] + 1) + 9 * (q[4] + 1);
+    if (code == 13) {
+      if (q[1] > q[0]) nl.neighlist[q[0]].push_back((unsigned)q[1]);
+    } else {
+      auto it = ghost_of.find((int64_t)q[1] * 27 + code);
+      if (it == ghost_of.end()) caviar_->log.error_all("export_neighborlist: image pair without a ghost");
+      nl.neighlist[q[0]].push_back((unsigned)(n + it->second));
+    }
+  }
+  for (auto &r : nl.neighlist) std::sort(r.begin(), r.end());  // the O(N^2) build's order
+  nl.cutoff_extra = ce;
+}
+
+}  // namespace caviar2

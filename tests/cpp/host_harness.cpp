@@ -1,0 +1,152 @@
+// host_harness.cpp -- drives the GPU MD step through the CAVIAR2-shaped C++ API
+// (caviar-v2_gb300/host/caviar2_gpu.hpp) with the same set-up code a CAVIAR2
+// user writes, reading and writing the file formats of oracle/ref_harness.cpp so
+// that tests/test_host_api.py compares it with the fixtures the reference made.
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "caviar2_gpu.hpp"
+
+using namespace caviar2;
+
+template <class T> static bool rd(FILE *f, T *p, size_t n) { return fread(p, sizeof(T), n, f) == n; }
+template <class T> static void wr(FILE *f, const T *p, size_t n) { fwrite(p, sizeof(T), n, f); }
+
+int main(int argc, char **argv) {
+  if (argc < 3) {
+    fprintf(stderr, "usage: %s in.bin out.bin [mixed]\n", argv[0]);
+    return 2;
+  }
+  FILE *fi = fopen(argv[1], "rb");
+  if (!fi) return 3;
+  int32_t h[10];
+  double dp[15];
+  if (!rd(fi, h, 10) || h[0] != 0x48564143 || !rd(fi, dp, 15)) return 4;
+  const int N = h[1], nt = h[2], nsteps = h[3], integ = h[4], cell = h[5], nrdf = h[6], pproc = h[7], clon = h[8];
+  std::vector<double> eps(nt * nt), sig(nt * nt), cl(nt * nt), mass(nt), pos(3 * N), vel(3 * N);
+  std::vector<int32_t> type(N);
+  if (!rd(fi, eps.data(), eps.size()) || !rd(fi, sig.data(), sig.size()) || !rd(fi, cl.data(), cl.size()) ||
+      !rd(fi, mass.data(), mass.size()) || !rd(fi, pos.data(), pos.size()) || !rd(fi, vel.data(), vel.size()) ||
+      !rd(fi, type.data(), type.size()))
+    return 5;
+  fclose(fi);
+
+  Caviar2 caviar;
+  caviar.domain.set_lower_global(Vector3d<double>{dp[0], dp[1], dp[2]});
+  caviar.domain.set_upper_global(Vector3d<double>{dp[3], dp[4], dp[5]});
+  caviar.domain.set_boundary_condition(Vector3d<int>{1, 1, 1});
+  caviar.domain.generate();
+
+  caviar.atom_data.set_ghost_cutoff(dp[8]);
+  for (int i = 0; i < N; ++i) {
+    tools::Atom a(&caviar);
+    a.set_type((size_t)type[i]);
+    a.set_position(Vector3d<double>{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]});
+    a.set_velocity(Vector3d<double>{vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]});
+    if (!caviar.atom_data.add_atom(a)) return 6;  // outside the box
+  }
+  for (int t = 0; t < nt; ++t) caviar.atom_data.add_type_mass(t, mass[t]);
+  caviar.atom_data.set_k_b(dp[10]);
+  caviar.atom_data.set_n_r_df(nrdf);
+  caviar.atom_data.set_temperature_process(true);
+  caviar.atom_data.set_pressure_process(pproc != 0);
+
+  caviar.neighborlist.set_cutoff(dp[6]);
+  caviar.neighborlist.set_cutoff_extra_coef(dp[7]);
+  caviar.neighborlist.set_dt(dp[11]);
+  if (cell) caviar.neighborlist.set_make_verlet_list_from_cell_list(true);
+
+  force_field::Lj lj(&caviar);
+  lj.set_cutoff(dp[9]);
+  for (int a = 0; a < nt; ++a)
+    for (int b = 0; b < nt; ++b) {
+      lj.set_epsilon(a, b, eps[a * nt + b]);
+      lj.set_sigma(a, b, sig[a * nt + b]);
+    }
+  if (clon) {
+    std::vector<std::vector<double>> cll(nt, std::vector<double>(nt));
+    for (int a = 0; a < nt; ++a)
+      for (int b = 0; b < nt; ++b) cll[a][b] = cl[a * nt + b];
+    lj.set_cutoff_list(cll);
+  }
+  caviar.add_force_field(&lj);
+
+  Md_simulator &md = caviar.md_simulator;
+  if (integ == 1) {
+    md.set_integrator_type(Integrator_t::Velocity_verlet_langevin);
+    md.langevin_friction(dp[13]);
+    md.langevin_kb(dp[14]);
+    md.langevin_temperature(dp[12]);
+  } else {
+    md.set_integrator_type(Integrator_t::Velocity_verlet);
+  }
+  if (argc > 3 && !std::strcmp(argv[3], "mixed")) md.set_precision(CAVGPU_MIXED);
+  md.set_dt(dp[11]);
+  md.set_initial_step(0);
+  md.set_final_step(nsteps);
+  md.initialize();
+  md.setup();
+
+  FILE *fo = fopen(argv[2], "wb");
+  if (!fo) return 7;
+  const auto &o = caviar.atom_data.atom_struct_owned;
+  md.export_neighborlist();
+  const int32_t g = (int32_t)md.ghost_source.size();
+  wr(fo, &N, 1);
+  wr(fo, &g, 1);
+  wr(fo, &o.acceleration[0].x, 3 * (size_t)N);
+  double th[3] = {caviar.atom_data.virialForce, caviar.atom_data.kinetic_energy(), caviar.atom_data.temperature()};
+  wr(fo, th, 3);
+  int32_t nb[3] = {0, 0, 0};
+  std::vector<int32_t> ib(3 * (size_t)N, 0);
+  if (cell) cavgpu_export_bins(md.gpu_context(), ib.data(), nb);
+  std::vector<int32_t> gb(3 * (size_t)g, 0), gsrc(md.ghost_source.begin(), md.ghost_source.end()), gsh(3 * (size_t)g);
+  std::vector<double> gpos(3 * (size_t)g);
+  if (g > 0) {
+    const double gc = caviar.neighborlist.cutoff_extra > caviar.atom_data.ghost_cutoff ? caviar.neighborlist.cutoff_extra
+                                                                                    : caviar.atom_data.ghost_cutoff;
+    cavgpu_export_ghosts(md.gpu_context(), gc, gsrc.data(), gsh.data(), gpos.data(), gb.data(), g);
+  }
+  if (!cell) std::fill(gb.begin(), gb.end(), 0);
+  wr(fo, nb, 3);
+  wr(fo, ib.data(), ib.size());
+  wr(fo, gsrc.data(), gsrc.size());
+  wr(fo, gpos.data(), gpos.size());
+  wr(fo, gb.data(), gb.size());
+  // canonical rows from Neighborlist::neighlist (reference encoding)
+  std::vector<int32_t> rows;
+  const auto &L = caviar.domain.size_global;
+  for (int i = 0; i < N; ++i)
+    for (unsigned j : caviar.neighborlist.neighlist[i]) {
+      if ((int)j >= N) {
+        const int gi = (int)j - N, s = md.ghost_source[gi];
+        const auto &q = md.ghost_position[gi];
+        const double dd[3] = {q.x - o.position[s].x, q.y - o.position[s].y, q.z - o.position[s].z};
+        const double LL[3] = {L.x, L.y, L.z};
+        int32_t r[5] = {i, s, 0, 0, 0};
+        for (int k = 0; k < 3; ++k) r[2 + k] = dd[k] > 0.5 * LL[k] ? 1 : (dd[k] < -0.5 * LL[k] ? -1 : 0);
+        rows.insert(rows.end(), r, r + 5);
+      } else {
+        int32_t r1[5] = {i, (int32_t)j, 0, 0, 0}, r2[5] = {(int32_t)j, i, 0, 0, 0};
+        rows.insert(rows.end(), r1, r1 + 5);
+        rows.insert(rows.end(), r2, r2 + 5);
+      }
+    }
+  int64_t np = (int64_t)rows.size() / 5;
+  wr(fo, &np, 1);
+  wr(fo, rows.data(), rows.size());
+  wr(fo, &nsteps, 1);
+  for (int s = 0; s < nsteps; ++s) {
+    md.step((int64_t)s);
+    double t[3] = {caviar.atom_data.temperature(), caviar.atom_data.virialForce, caviar.atom_data.pressure()};
+    wr(fo, t, 3);
+  }
+  md.sync_host();
+  wr(fo, &o.position[0].x, 3 * (size_t)N);
+  wr(fo, &o.velocity[0].x, 3 * (size_t)N);
+  wr(fo, &o.acceleration[0].x, 3 * (size_t)N);
+  fclose(fo);
+  md.cleanup();
+  return 0;
+}
