@@ -71,6 +71,10 @@ _SIGS = {
     "cavgpu_last_cuda_error": (C.c_char_p, []),
     "cavgpu_kinetic_energy_noalloc": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                                 C.c_int32, C.c_double, C.c_void_p, C.c_void_p]),
+    "cavgpu_create_batch": (C.c_int, [C.POINTER(Params), C.c_int32, C.c_void_p, C.c_void_p,
+                                      C.POINTER(C.c_void_p)]),
+    "cavgpu_upload_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "cavgpu_thermo_batch": (C.c_int, [C.c_void_p, C.c_void_p]),
 }
 
 
@@ -228,6 +232,42 @@ class System:
         o = np.zeros(2)
         self._check(lib().cavgpu_read_profile(self._h, _ptr(o)), "read_profile")
         return int(o[0]), float(o[1])
+
+
+class Batch(System):
+    """R independent periodic systems advanced together in one context.
+
+    systems: list of (pos, vel, typ, lo3, hi3); all share `params` (pair table,
+    integrator, dt, cutoffs).  state() returns the concatenation in that order.
+    """
+
+    def __init__(self, systems, params, precision=FP64, noise_off=False, **launch):
+        self.params = make_params(params, precision, noise_off, **launch)
+        self.nrep = len(systems)
+        lo = np.ascontiguousarray([s[3] for s in systems], np.float64)
+        hi = np.ascontiguousarray([s[4] for s in systems], np.float64)
+        h = C.c_void_p()
+        rc = lib().cavgpu_create_batch(C.byref(self.params), self.nrep, _ptr(lo), _ptr(hi), C.byref(h))
+        if rc:
+            raise CavError(rc, "cavgpu_create_batch")
+        self._h = h
+        self.counts = np.ascontiguousarray([len(s[0]) for s in systems], np.int64)
+        self.n = int(self.counts.sum())
+        pos = np.ascontiguousarray(np.concatenate([s[0] for s in systems]), np.float64)
+        vel = np.ascontiguousarray(np.concatenate([s[1] for s in systems]), np.float64)
+        typ = np.ascontiguousarray(np.concatenate([s[2] for s in systems]), np.uint64)
+        self._check(lib().cavgpu_upload_batch(self._h, _ptr(self.counts), _ptr(pos), _ptr(vel), _ptr(typ)),
+                    "upload_batch")
+
+    def thermo_batch(self):
+        """Per-replica (R, 6) array: KE, T, P, virial, PE, total mass."""
+        o = np.zeros((self.nrep, 6))
+        self._check(lib().cavgpu_thermo_batch(self._h, _ptr(o)), "thermo_batch")
+        return o
+
+    def split(self, a):
+        """Split a concatenated per-atom array into the replicas' pieces."""
+        return np.split(a, np.cumsum(self.counts)[:-1])
 
 
 def sort_rows(rows):

@@ -1,6 +1,6 @@
 // cav_api.cu -- the extern "C" boundary (include/cavgpu.h): context life cycle,
 // uploads/downloads in the reference's host layouts, step orchestration with
-// CUDA graphs, and the parity exports.
+// CUDA graphs, batches of replicas, and the parity exports.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -32,16 +32,16 @@ struct cavgpu_ctx {
   LaunchCfg lc{};
   ThermoCfg tc{};
   PairTab tab_h{};
+  std::vector<RepBox> reps;     // host copy of the replica boxes
   cudaStream_t st = nullptr;
   cudaStream_t side = nullptr;  // captures the bodies of the conditional rebuild nodes
-  long long rebuilds_counted = 0;
-  int n = 0;
+  int natoms = 0;               // atoms over all replicas
   bool uploaded = false, set_up = false;
   long long steps_done = 0;
   long long graph_launches = 0, kernel_launches = 0;
   int max_nb = 0;
   std::vector<GraphEntry> graphs;
-  // reference binning (Neighborlist::init, src/neighborlist.cpp:334-342)
+  // reference binning (Neighborlist::init, src/neighborlist.cpp:334-342), single system
   double cutoff_extra = 0.0, cutoff_inv = 0.0, lo_local[3] = {0, 0, 0};
   int ref_nb[3] = {0, 0, 0};
   // profiling
@@ -56,7 +56,7 @@ struct cavgpu_ctx {
 
 namespace {
 
-// name of the last CUDA error seen by this library (process-wide, for diagnostics)
+// name of the last CUDA error seen by this library (per thread, for diagnostics)
 thread_local const char *g_last_cuda_error = "none";
 
 int cuda_rc(cudaError_t e) {
@@ -91,34 +91,54 @@ void free_graphs(cavgpu_ctx *c) {
   c->graphs.clear();
 }
 
-int kernels_per_step(const cavgpu_ctx *c) { (void)c; return 1 /*drift*/ + 8 /*rebuild*/ + 1 /*force*/; }
+bool is_lang(const cavgpu_ctx *c) { return c->p.integrator == CAVGPU_VELOCITY_VERLET_LANGEVIN; }
 
-// one MD step on the stream (captured or eager).  k = step index inside the chunk.
-int enqueue_step(cavgpu_ctx *c, int k, bool thermo, int ring_slot) {
-  const bool lang = c->p.integrator == CAVGPU_VELOCITY_VERLET_LANGEVIN;
-  RK(launch_drift(c->d, c->b, c->sc, c->lc, k, thermo && lang, c->st));
-  RK(launch_rebuild(c->d, c->b, c->lc, 0, c->st));
-  // External: inside a stream capture this becomes an event-record node that records
-  // at every replay (a plain record would only order work within the capture)
-  if (c->prof && k < (int)c->ev0.size()) CK(cudaEventRecordWithFlags(c->ev0[k], c->st, cudaEventRecordExternal));
-  RK(launch_force(c->d, c->b, c->sc, c->lc, lang ? 2 : 1, thermo, k, c->st));
-  if (c->prof && k < (int)c->ev1.size()) CK(cudaEventRecordWithFlags(c->ev1[k], c->st, cudaEventRecordExternal));
-  c->kernel_launches += kernels_per_step(c);
-  if (thermo) {
+// thermo folds after the force kernel of a thermo step
+int enqueue_thermo_after_force(cavgpu_ctx *c, int ring_slot) {
+  const bool lang = is_lang(c);
+  if (c->b.nrep == 1) {
     const int nb_ke = lang ? drift_grid_blocks(c->lc) : force_grid_blocks(c->lc);
     RK(launch_thermo_final(c->d, c->tc, nb_ke, force_grid_blocks(c->lc), ring_slot, c->st));
+  } else {
+    RK(launch_thermo_replicas(c->d, c->b, c->tc, lang ? 0 : 1, 1, c->st));
+  }
+  c->kernel_launches += 1;
+  return CAVGPU_OK;
+}
+
+// drift (VV) or first Langevin half; batches fold their per-replica KE right after
+// the Langevin half kick, where the reference takes the temperature
+int enqueue_drift(cavgpu_ctx *c, int k, bool thermo) {
+  RK(launch_drift(c->d, c->b, c->sc, c->lc, k, thermo && is_lang(c), c->st));
+  c->kernel_launches += 1;
+  if (thermo && is_lang(c) && c->b.nrep > 1) {
+    RK(launch_thermo_replicas(c->d, c->b, c->tc, 1, 0, c->st));
     c->kernel_launches += 1;
   }
   return CAVGPU_OK;
 }
 
+// one MD step on the stream, launched directly; the rebuild kernels return at
+// once unless a replica's half-skin flag is set.  k = step index inside the chunk.
+int enqueue_step(cavgpu_ctx *c, int k, bool thermo, int ring_slot) {
+  RK(enqueue_drift(c, k, thermo));
+  RK(launch_rebuild(c->d, c->b, c->lc, 0, c->st));
+  // External: inside a stream capture this becomes an event-record node that records
+  // at every replay (a plain record would only order work within the capture)
+  if (c->prof && k < (int)c->ev0.size()) CK(cudaEventRecordWithFlags(c->ev0[k], c->st, cudaEventRecordExternal));
+  RK(launch_force(c->d, c->b, c->sc, c->lc, is_lang(c) ? 2 : 1, thermo, k, c->st));
+  if (c->prof && k < (int)c->ev1.size()) CK(cudaEventRecordWithFlags(c->ev1[k], c->st, cudaEventRecordExternal));
+  c->kernel_launches += REBUILD_KERNELS + 1;
+  if (thermo) RK(enqueue_thermo_after_force(c, ring_slot));
+  return CAVGPU_OK;
+}
+
 // One MD step recorded into the graph being captured on c->st.  The rebuild
 // kernels sit in the body of an IF conditional node whose value the step's
-// half-skin flag sets on the device, so steps without a rebuild launch three
+// half-skin flags set on the device, so steps without a rebuild launch three
 // kernels (drift, condition, force) instead of eleven.
 int capture_step(cavgpu_ctx *c, int k, bool thermo, int ring_slot) {
-  const bool lang = c->p.integrator == CAVGPU_VELOCITY_VERLET_LANGEVIN;
-  RK(launch_drift(c->d, c->b, c->sc, c->lc, k, thermo && lang, c->st));
+  RK(enqueue_drift(c, k, thermo));
   cudaStreamCaptureStatus cs;
   cudaGraph_t g = nullptr;
   CK(cudaStreamGetCaptureInfo(c->st, &cs, nullptr, &g, nullptr, nullptr, nullptr));
@@ -140,19 +160,16 @@ int capture_step(cavgpu_ctx *c, int k, bool thermo, int ring_slot) {
   CK(cudaGraphAddNode(&cond, g, deps, nullptr, nd, &cp));
   CK(cudaStreamBeginCaptureToGraph(c->side, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
                                    cudaStreamCaptureModeThreadLocal));
-  const int brc = launch_rebuild(c->d, c->b, c->lc, 1, c->side);
+  const int brc = launch_rebuild(c->d, c->b, c->lc, 0, c->side);
   cudaGraph_t body = nullptr;
   const cudaError_t be = cudaStreamEndCapture(c->side, &body);
   RK(brc);
   CK(be);
   CK(cudaStreamUpdateCaptureDependencies(c->st, &cond, nullptr, 1, cudaStreamSetCaptureDependencies));
   if (c->prof && k < (int)c->ev0.size()) CK(cudaEventRecordWithFlags(c->ev0[k], c->st, cudaEventRecordExternal));
-  RK(launch_force(c->d, c->b, c->sc, c->lc, lang ? 2 : 1, thermo, k, c->st));
+  RK(launch_force(c->d, c->b, c->sc, c->lc, is_lang(c) ? 2 : 1, thermo, k, c->st));
   if (c->prof && k < (int)c->ev1.size()) CK(cudaEventRecordWithFlags(c->ev1[k], c->st, cudaEventRecordExternal));
-  if (thermo) {
-    const int nb_ke = lang ? drift_grid_blocks(c->lc) : force_grid_blocks(c->lc);
-    RK(launch_thermo_final(c->d, c->tc, nb_ke, force_grid_blocks(c->lc), ring_slot, c->st));
-  }
+  if (thermo) RK(enqueue_thermo_after_force(c, ring_slot));
   return CAVGPU_OK;
 }
 
@@ -185,6 +202,7 @@ GraphEntry *get_graph(cavgpu_ctx *c, int S, int every, int *rc) {
   if (c->prof && (*rc = ensure_events(c, S))) return nullptr;
   cudaGraph_t graph = nullptr;
   if ((*rc = cuda_rc(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal)))) return nullptr;
+  const long long kl = c->kernel_launches;
   int erc = CAVGPU_OK;
   for (int k = 0; k < S && !erc; ++k) {
     const bool th = every > 0 && ((k + 1) % every == 0);
@@ -192,6 +210,7 @@ GraphEntry *get_graph(cavgpu_ctx *c, int S, int every, int *rc) {
   }
   if (!erc) erc = launch_advance_step(c->d, S, c->st);
   cudaError_t e = cudaStreamEndCapture(c->st, &graph);
+  c->kernel_launches = kl;  // capture launches nothing; replays are counted in cavgpu_run
   if (erc || e != cudaSuccess) {
     if (graph) cudaGraphDestroy(graph);
     cudaGetLastError();
@@ -225,7 +244,7 @@ int check_status(cavgpu_ctx *c) {
 int alloc_nbr(cavgpu_ctx *c, int cap) {
   cap = (cap + 63) / 64 * 64;  // nbr_index needs cap % (4 * tpa) == 0, tpa <= 16
   const int A = 32 / c->d.tpa;  // whole blocks of A slots (nbr_index)
-  const size_t bytes = (size_t)((c->n + A - 1) / A) * A * (size_t)cap * sizeof(uint32_t);
+  const size_t bytes = (size_t)((c->b.nslot + A - 1) / A) * A * (size_t)cap * sizeof(uint32_t);
   if (c->d.nbr) {
     auto it = std::find(c->allocs.begin(), c->allocs.end(), (void *)c->d.nbr);
     if (it != c->allocs.end()) c->allocs.erase(it);
@@ -242,16 +261,17 @@ int alloc_nbr(cavgpu_ctx *c, int cap) {
   return CAVGPU_OK;
 }
 
-// forced list build; grows the capacity until the build fits
+// forced list build of every replica; grows the capacity until the build fits
 int forced_build(cavgpu_ctx *c) {
   for (int attempt = 0; attempt < 4; ++attempt) {
     int zero[F_NWORDS] = {0};
     int f[F_NWORDS];
     RK(read_flags(c, f));
     zero[F_REBUILDS] = f[F_REBUILDS];
+    zero[F_PASSES] = f[F_PASSES];
     CK(cudaMemcpyAsync(c->d.flags, zero, sizeof(zero), cudaMemcpyHostToDevice, c->st));
     RK(launch_rebuild(c->d, c->b, c->lc, 1, c->st));
-    c->kernel_launches += 8;
+    c->kernel_launches += REBUILD_KERNELS;
     RK(read_flags(c, f));
     c->max_nb = f[F_MAXNB];
     if (!f[F_OVERFLOW]) return CAVGPU_OK;
@@ -260,55 +280,26 @@ int forced_build(cavgpu_ctx *c) {
   return CAVGPU_E_NLIST_OVERFLOW;
 }
 
-int thermo_now(cavgpu_ctx *c, bool langevin_ke_from_drift) {
-  const int nb_ke = langevin_ke_from_drift ? drift_grid_blocks(c->lc) : force_grid_blocks(c->lc);
-  RK(launch_thermo_final(c->d, c->tc, nb_ke, force_grid_blocks(c->lc), -1, c->st));
-  c->kernel_launches += 1;
+// box and search grid of one replica; L >= 2 cutoff_extra (one image per pair)
+int make_repbox(double ce, const double lo[3], const double hi[3], RepBox *rb) {
+  for (int a = 0; a < 3; ++a) {
+    rb->lo[a] = lo[a];
+    rb->hi[a] = hi[a];
+    rb->L[a] = hi[a] - lo[a];  // Domain::update_after_domain_change (src/domain.cpp:498)
+    if (!(rb->L[a] >= 2.0 * ce)) return CAVGPU_E_ARG;
+    int nc = (int)std::floor(rb->L[a] / ce);
+    while (nc > 1 && rb->L[a] / nc < ce * (1.0 + 1e-10)) --nc;  // cell width safely >= ce
+    rb->nc[a] = std::max(nc, 1);
+    rb->w[a] = rb->L[a] / rb->nc[a];
+    rb->inv_w[a] = 1.0 / rb->w[a];
+    rb->wf[a] = (float)rb->w[a];
+  }
+  rb->ncell = rb->nc[0] * rb->nc[1] * rb->nc[2];
   return CAVGPU_OK;
 }
 
-}  // namespace
-
-extern "C" {
-
-void cavgpu_default_params(cavgpu_params *p) {
-  std::memset(p, 0, sizeof(*p));
-  for (int a = 0; a < 3; ++a) { p->bc[a] = 1; p->hi[a] = 1.0; }
-  p->ntypes = 1;
-  p->nl_cutoff = 2.5;
-  p->nl_coef = 1.12347;  // Neighborlist::cutoff_extra_coef default (inc/caviar2/neighborlist.hpp:147)
-  p->lj_cutoff = 2.5;
-  for (int k = 0; k < CAVGPU_MAX_TYPES * CAVGPU_MAX_TYPES; ++k) { p->eps[k] = 1.0; p->sigma[k] = 1.0; }
-  for (int t = 0; t < CAVGPU_MAX_TYPES; ++t) p->mass[t] = 1.0;
-  p->k_b = 1.0;
-  p->dt = 0.001;
-  p->lang_kb = 1.0;
-  p->lang_kbt = -1.0;
-  p->n_r_df = 3;
-  p->precision = CAVGPU_FP64;
-}
-
-const char *cavgpu_last_cuda_error(void) {
-  const cudaError_t e = cudaPeekAtLastError();  // a failed kernel launch leaves its error here
-  return e != cudaSuccess ? cudaGetErrorString(e) : g_last_cuda_error;
-}
-
-const char *cavgpu_strerror(int s) {
-  switch (s) {
-    case CAVGPU_OK: return "ok";
-    case CAVGPU_E_ARG: return "invalid argument";
-    case CAVGPU_E_CUDA: return "CUDA error (or no CUDA device)";
-    case CAVGPU_E_NAN: return "NaN acceleration";
-    case CAVGPU_E_NLIST_OVERFLOW: return "neighbour list capacity exceeded";
-    case CAVGPU_E_STATE: return "call out of order";
-    case CAVGPU_E_NOMEM: return "device allocation failed";
-    case CAVGPU_E_RANGE: return "size beyond the stated maximum";
-    default: return "unknown status";
-  }
-}
-
-int cavgpu_create(const cavgpu_params *p, cavgpu_ctx **out) {
-  if (!p || !out) return CAVGPU_E_ARG;
+int create_common(const cavgpu_params *p, int nrep, const double *lo3, const double *hi3, cavgpu_ctx **out) {
+  if (!p || !out || nrep < 1 || !lo3 || !hi3) return CAVGPU_E_ARG;
   *out = nullptr;
   if (p->ntypes < 1 || p->ntypes > CAVGPU_MAX_TYPES) return CAVGPU_E_ARG;
   if (p->bc[0] != 1 || p->bc[1] != 1 || p->bc[2] != 1) return CAVGPU_E_ARG;
@@ -321,27 +312,21 @@ int cavgpu_create(const cavgpu_params *p, cavgpu_ctx **out) {
   cavgpu_ctx *c = new (std::nothrow) cavgpu_ctx();
   if (!c) return CAVGPU_E_NOMEM;
   c->p = *p;
-  Box &b = c->b;
   const double ce = p->nl_cutoff * p->nl_coef;  // Neighborlist::init (src/neighborlist.cpp:317)
   c->cutoff_extra = ce;
+  c->reps.resize(nrep);
+  for (int r = 0; r < nrep; ++r)
+    if (make_repbox(ce, lo3 + 3 * r, hi3 + 3 * r, &c->reps[r])) { delete c; return CAVGPU_E_ARG; }
+  // reference binning of a single system: Domain::calculate_local_domain with grid
+  // index 0 of 1 (src/domain.cpp:320-326), no_bins = ceil(size * 1/cutoff_extra)
+  c->cutoff_inv = 1.0 / ce;
   for (int a = 0; a < 3; ++a) {
-    b.lo[a] = p->lo[a];
-    b.hi[a] = p->hi[a];
-    b.L[a] = p->hi[a] - p->lo[a];  // Domain::update_after_domain_change (src/domain.cpp:498)
-    if (!(b.L[a] >= 2.0 * ce)) { delete c; return CAVGPU_E_ARG; }  // one image per pair
-    int nc = (int)std::floor(b.L[a] / ce);
-    while (nc > 1 && b.L[a] / nc < ce * (1.0 + 1e-10)) --nc;
-    b.nc[a] = std::max(nc, 1);
-    b.w[a] = b.L[a] / b.nc[a];
-    b.inv_w[a] = 1.0 / b.w[a];
-    b.wf[a] = (float)b.w[a];
-    // Domain::calculate_local_domain with grid index 0 of 1 (src/domain.cpp:320-326)
-    c->lo_local[a] = p->lo[a] + (p->hi[a] - p->lo[a]) * 0 / 1;
-    const double hi_local = p->lo[a] + (p->hi[a] - p->lo[a]) * 1 / 1;
-    c->cutoff_inv = 1.0 / ce;
+    c->lo_local[a] = lo3[a] + (hi3[a] - lo3[a]) * 0 / 1;
+    const double hi_local = lo3[a] + (hi3[a] - lo3[a]) * 1 / 1;
     c->ref_nb[a] = (int)std::ceil((hi_local - c->lo_local[a]) * c->cutoff_inv);
   }
-  b.ncell = b.nc[0] * b.nc[1] * b.nc[2];
+  Box &b = c->b;
+  b.nrep = nrep;
   b.ce2 = ce * ce;
   b.ce2_lo = (float)(b.ce2 * (1.0 - 2e-4));
   b.ce2_hi = (float)(b.ce2 * (1.0 + 2e-4));
@@ -386,7 +371,7 @@ int cavgpu_create(const cavgpu_params *p, cavgpu_ctx **out) {
   // launch shape
   c->lc.precision = p->precision;
   c->lc.integrator = p->integrator;
-  c->lc.tpa = p->threads_per_atom ? p->threads_per_atom : (p->precision == CAVGPU_MIXED ? 4 : 4);
+  c->lc.tpa = p->threads_per_atom ? p->threads_per_atom : 4;
   c->lc.block = p->block_size ? p->block_size : 128;
   if (c->lc.tpa != 1 && c->lc.tpa != 2 && c->lc.tpa != 4 && c->lc.tpa != 8 && c->lc.tpa != 16) { delete c; return CAVGPU_E_ARG; }
   if (c->lc.block < 32 || c->lc.block > 256 || c->lc.block % 32) { delete c; return CAVGPU_E_ARG; }
@@ -412,6 +397,207 @@ int cavgpu_create(const cavgpu_params *p, cavgpu_ctx **out) {
   return CAVGPU_OK;
 }
 
+// Lay the replicas out (32-aligned slot ranges, consecutive cell ranges with one
+// padding cell each), allocate every per-slot array and upload the atoms.
+int upload_common(cavgpu_ctx *c, const int64_t *counts, const double *pos3, const double *vel3,
+                  const uint64_t *type, const uint64_t *id) {
+  if (c->uploaded) return CAVGPU_E_STATE;
+  const int R = c->b.nrep;
+  int64_t total = 0, nslot = 0, ncell_all = 0;
+  for (int r = 0; r < R; ++r) {
+    if (counts[r] < 1) return CAVGPU_E_ARG;
+    total += counts[r];
+  }
+  if (!pos3 || !type || total > MAX_ATOMS) return total > MAX_ATOMS ? CAVGPU_E_RANGE : CAVGPU_E_ARG;
+  for (int r = 0; r < R; ++r) {
+    RepBox &rb = c->reps[r];
+    rb.slot_off = (int)nslot;
+    rb.natoms = (int)counts[r];
+    const int64_t end = nslot + counts[r];
+    const int64_t next = R == 1 ? end : (end + SLOT_ALIGN - 1) / SLOT_ALIGN * SLOT_ALIGN;
+    rb.pad = (int)(next - end);
+    nslot = next;
+    rb.cell_off = (int)ncell_all;
+    ncell_all += rb.ncell + 1;
+  }
+  if (nslot > MAX_ATOMS || ncell_all > (1ll << 30)) return CAVGPU_E_RANGE;
+  const int N = (int)total, NS = (int)nslot;
+  std::vector<dbl4> hp(NS, make_dbl4(0, 0, 0, 0)), hv(NS, make_dbl4(0, 0, 0, 0));
+  std::vector<int> ht(NS, 0), rep_of(NS, -1), cell_rep(ncell_all, -1);
+  std::vector<uint32_t> hid(NS, 0);
+  std::vector<char> seen(id ? N : 0, 0);
+  std::vector<double> msum(R, 0.0);
+  int64_t h = 0;
+  for (int r = 0; r < R; ++r) {
+    RepBox &rb = c->reps[r];
+    rb.id_off = (int)h;
+    for (int k = 0; k < rb.natoms; ++k, ++h) {
+      const int s = rb.slot_off + k;
+      for (int a = 0; a < 3; ++a) {
+        const double x = pos3[3 * h + a];
+        // Atom_data::position_inside_global_domain (src/atom_data.cpp:548-559)
+        if (!(x >= rb.lo[a] && x < rb.hi[a])) return CAVGPU_E_ARG;
+      }
+      if (type[h] >= (uint64_t)c->p.ntypes) return CAVGPU_E_ARG;
+      const uint64_t ii = id ? id[h] : (uint64_t)k;  // batches: ids local to the replica
+      if (ii >= (uint64_t)N || (id && seen[ii]++)) return CAVGPU_E_ARG;  // ids: a permutation of 0..n-1
+      hp[s] = make_dbl4(pos3[3 * h], pos3[3 * h + 1], pos3[3 * h + 2], (double)type[h]);
+      if (vel3) hv[s] = make_dbl4(vel3[3 * h], vel3[3 * h + 1], vel3[3 * h + 2], 0.0);
+      ht[s] = (int)type[h];
+      hid[s] = (uint32_t)ii;
+      rep_of[s] = r;
+      msum[r] += c->p.mass[type[h]];
+    }
+    for (int k = 0; k < rb.ncell; ++k) cell_rep[rb.cell_off + k] = r;
+  }
+  Box &b = c->b;
+  b.nslot = NS;
+  b.ncell_all = (int)ncell_all;
+  b.r0 = c->reps[0];
+  c->natoms = N;
+  c->sc.n = NS;
+  c->lc.n = NS;
+  c->tc.n = N;
+  c->tc.n_r_df = c->p.n_r_df;
+  c->tc.k_b = c->p.k_b;
+  // finalize_pressure_mpi_domain volume (src/atom_data/kinetic_energy.cpp:242-243) of the
+  // single system: local domain of grid index 0 of 1; replicas use their box volume
+  double vol = 1.0;
+  for (int a = 0; a < 3; ++a) vol *= (c->reps[0].lo[a] + c->reps[0].L[a] * 1 / 1) - c->lo_local[a];
+  c->tc.volume = vol;
+  c->tc.langevin = is_lang(c);
+  Dev &d = c->d;
+  const size_t nblk = (size_t)std::max(force_grid_blocks(c->lc), 1);
+  const size_t nblk_d = (size_t)std::max((NS + 255) / 256, 1);
+  int rc = CAVGPU_OK;
+  dbl4 **d4[] = {&d.pos, &d.vel, &d.acc, &d.acc_old, &d.pos_ref, &d.t_pos, &d.t_vel, &d.t_acc, &d.t_acc_old};
+  for (auto pp : d4) if (!rc) rc = dalloc(c, pp, NS);
+  if (!rc) rc = dalloc(c, &d.rel, NS);
+  if (!rc) rc = dalloc(c, &d.rel_ref, NS);
+  int **di[] = {&d.type, &d.cell_of, &d.t_type, &d.atom_cell, &d.perm, &d.perm_tmp, &d.nnbr};
+  for (auto pp : di) if (!rc) rc = dalloc(c, pp, NS);
+  if (!rc) rc = dalloc(c, &d.id, NS);
+  if (!rc) rc = dalloc(c, &d.t_id, NS);
+  if (!rc) rc = dalloc(c, &d.cell_count, ncell_all);
+  if (!rc) rc = dalloc(c, &d.cell_cursor, ncell_all);
+  if (!rc) rc = dalloc(c, &d.cell_start, (size_t)ncell_all + 1);
+  if (!rc) rc = dalloc(c, &d.partials_ke, 4 * std::max(nblk, nblk_d));
+  if (!rc) rc = dalloc(c, &d.partials_ev, 2 * nblk);
+  if (!rc) rc = dalloc(c, &d.h3, 3 * (size_t)N);
+  if (!rc) rc = dalloc(c, &d.hi3, 3 * (size_t)N);
+  RepBox *drep = nullptr;
+  int *dflag = nullptr;
+  if (!rc) rc = dalloc(c, &drep, R);
+  if (!rc) rc = dalloc(c, &dflag, R);
+  if (R > 1) {
+    int *drep_of = nullptr, *dcell_rep = nullptr;
+    if (!rc) rc = dalloc(c, &drep_of, NS);
+    if (!rc) rc = dalloc(c, &dcell_rep, ncell_all);
+    if (!rc) rc = dalloc(c, &d.ev_atom, NS);
+    if (!rc) rc = dalloc(c, &d.thermo_rep, 8 * (size_t)R);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(drep_of, rep_of.data(), NS * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(dcell_rep, cell_rep.data(), ncell_all * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemsetAsync(d.ev_atom, 0, NS * sizeof(double2), c->st));
+    CK(cudaMemsetAsync(d.thermo_rep, 0, 8 * (size_t)R * sizeof(double), c->st));
+    b.rep_of = drep_of;
+    b.cell_rep = dcell_rep;
+  }
+  if (rc) return rc;
+  b.rep = drep;
+  b.rep_flag = dflag;
+  CK(cudaMemcpyAsync(drep, c->reps.data(), R * sizeof(RepBox), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemsetAsync(dflag, 0, R * sizeof(int), c->st));
+  // initial capacity from the densest replica: 1.4 x the mean count in the cutoff sphere, plus headroom
+  double rho = 0.0;
+  for (const RepBox &rb : c->reps) rho = std::max(rho, rb.natoms / (rb.L[0] * rb.L[1] * rb.L[2]));
+  const double ce = c->cutoff_extra;
+  const int cap = c->p.nbr_capacity > 0 ? c->p.nbr_capacity : (int)(1.4 * rho * 4.18879020479 * ce * ce * ce) + 48;
+  RK(alloc_nbr(c, cap));
+  CK(cudaMemcpyAsync(d.pos, hp.data(), NS * sizeof(dbl4), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(d.vel, hv.data(), NS * sizeof(dbl4), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemsetAsync(d.acc, 0, NS * sizeof(dbl4), c->st));
+  CK(cudaMemsetAsync(d.acc_old, 0, NS * sizeof(dbl4), c->st));
+  CK(cudaMemsetAsync(d.nnbr, 0, NS * sizeof(int), c->st));
+  CK(cudaMemcpyAsync(d.type, ht.data(), NS * sizeof(int), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(d.id, hid.data(), NS * sizeof(uint32_t), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemsetAsync(d.cell_count, 0, ncell_all * sizeof(int), c->st));
+  CK(cudaMemsetAsync(d.cell_cursor, 0, ncell_all * sizeof(int), c->st));
+  const int end_slot = NS;  // the start after the last cell (the per-replica scans never write it)
+  CK(cudaMemcpyAsync(d.cell_start + ncell_all, &end_slot, sizeof(int), cudaMemcpyHostToDevice, c->st));
+  double th[8] = {0, 0, 0, 0, 0, msum[0], 0, 0};
+  CK(cudaMemcpyAsync(d.thermo, th, sizeof(th), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->uploaded = true;
+  return CAVGPU_OK;
+}
+
+int setup_common(cavgpu_ctx *c) {
+  if (!c->uploaded) return CAVGPU_E_STATE;
+  RK(forced_build(c));
+  RK(launch_force(c->d, c->b, c->sc, c->lc, 0, 1, 0, c->st));
+  c->kernel_launches += 1;
+  if (c->b.nrep == 1) {
+    RK(launch_thermo_final(c->d, c->tc, force_grid_blocks(c->lc), force_grid_blocks(c->lc), -1, c->st));
+  } else {
+    RK(launch_thermo_replicas(c->d, c->b, c->tc, 1, 1, c->st));
+  }
+  c->kernel_launches += 1;
+  RK(check_status(c));
+  c->set_up = true;
+  return CAVGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void cavgpu_default_params(cavgpu_params *p) {
+  std::memset(p, 0, sizeof(*p));
+  for (int a = 0; a < 3; ++a) { p->bc[a] = 1; p->hi[a] = 1.0; }
+  p->ntypes = 1;
+  p->nl_cutoff = 2.5;
+  p->nl_coef = 1.12347;  // Neighborlist::cutoff_extra_coef default (inc/caviar2/neighborlist.hpp:147)
+  p->lj_cutoff = 2.5;
+  for (int k = 0; k < CAVGPU_MAX_TYPES * CAVGPU_MAX_TYPES; ++k) { p->eps[k] = 1.0; p->sigma[k] = 1.0; }
+  for (int t = 0; t < CAVGPU_MAX_TYPES; ++t) p->mass[t] = 1.0;
+  p->k_b = 1.0;
+  p->dt = 0.001;
+  p->lang_kb = 1.0;
+  p->lang_kbt = -1.0;
+  p->n_r_df = 3;
+  p->precision = CAVGPU_FP64;
+}
+
+const char *cavgpu_last_cuda_error(void) {
+  const cudaError_t e = cudaPeekAtLastError();  // a failed kernel launch leaves its error here
+  return e != cudaSuccess ? cudaGetErrorString(e) : g_last_cuda_error;
+}
+
+const char *cavgpu_strerror(int s) {
+  switch (s) {
+    case CAVGPU_OK: return "ok";
+    case CAVGPU_E_ARG: return "invalid argument";
+    case CAVGPU_E_CUDA: return "CUDA error (or no CUDA device)";
+    case CAVGPU_E_NAN: return "NaN acceleration";
+    case CAVGPU_E_NLIST_OVERFLOW: return "neighbour list capacity exceeded";
+    case CAVGPU_E_STATE: return "call out of order";
+    case CAVGPU_E_NOMEM: return "device allocation failed";
+    case CAVGPU_E_RANGE: return "size beyond the stated maximum";
+    default: return "unknown status";
+  }
+}
+
+int cavgpu_create(const cavgpu_params *p, cavgpu_ctx **out) {
+  if (!p) return CAVGPU_E_ARG;
+  return create_common(p, 1, p->lo, p->hi, out);
+}
+
+int cavgpu_create_batch(const cavgpu_params *p, int32_t nrep, const double *lo3, const double *hi3,
+                        cavgpu_ctx **out) {
+  return create_common(p, nrep, lo3, hi3, out);
+}
+
 void cavgpu_destroy(cavgpu_ctx *c) {
   if (!c) return;
   if (c->st) cudaStreamSynchronize(c->st);
@@ -426,98 +612,26 @@ void cavgpu_destroy(cavgpu_ctx *c) {
 
 int cavgpu_upload(cavgpu_ctx *c, int64_t n, const double *pos3, const double *vel3, const uint64_t *type,
                   const uint64_t *id) {
-  if (!c || n < 1 || !pos3 || !type) return CAVGPU_E_ARG;
-  if (c->uploaded) return CAVGPU_E_STATE;
-  if (n > MAX_ATOMS) return CAVGPU_E_RANGE;
-  const int N = (int)n;
-  std::vector<dbl4> hp(N), hv(N);
-  std::vector<int> ht(N);
-  std::vector<uint32_t> hid(N);
-  std::vector<char> seen(id ? N : 0, 0);
-  double msum = 0.0;
-  for (int i = 0; i < N; ++i) {
-    for (int a = 0; a < 3; ++a) {
-      const double x = pos3[3 * i + a];
-      // Atom_data::position_inside_global_domain (src/atom_data.cpp:548-559)
-      if (!(x >= c->p.lo[a] && x < c->p.hi[a])) return CAVGPU_E_ARG;
-    }
-    if (type[i] >= (uint64_t)c->p.ntypes) return CAVGPU_E_ARG;
-    const uint64_t ii = id ? id[i] : (uint64_t)i;
-    if (ii >= (uint64_t)N || (id && seen[ii]++)) return CAVGPU_E_ARG;  // ids must be a permutation of 0..n-1
-    hp[i] = make_dbl4(pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2], (double)type[i]);
-    hv[i] = vel3 ? make_dbl4(vel3[3 * i], vel3[3 * i + 1], vel3[3 * i + 2], 0.0) : make_dbl4(0, 0, 0, 0);
-    ht[i] = (int)type[i];
-    hid[i] = (uint32_t)ii;
-    msum += c->p.mass[type[i]];
-  }
-  c->n = N;
-  c->sc.n = N;
-  c->lc.n = N;
-  c->tc.n = N;
-  c->tc.n_r_df = c->p.n_r_df;
-  c->tc.k_b = c->p.k_b;
-  // finalize_pressure_mpi_domain volume (src/atom_data/kinetic_energy.cpp:242-243)
-  double vol = 1.0;
-  for (int a = 0; a < 3; ++a) vol *= (c->p.lo[a] + (c->p.hi[a] - c->p.lo[a]) * 1 / 1) - c->lo_local[a];
-  c->tc.volume = vol;
-  c->tc.langevin = c->p.integrator == CAVGPU_VELOCITY_VERLET_LANGEVIN;
-  Dev &d = c->d;
-  const size_t nblk = (size_t)std::max(force_grid_blocks(c->lc), 1);
-  const size_t nblk_d = (size_t)std::max((N + 255) / 256, 1);
-  int rc = CAVGPU_OK;
-  dbl4 **d4[] = {&d.pos, &d.vel, &d.acc, &d.acc_old, &d.pos_ref, &d.t_pos, &d.t_vel, &d.t_acc, &d.t_acc_old};
-  for (auto pp : d4) if (!rc) rc = dalloc(c, pp, N);
-  if (!rc) rc = dalloc(c, &d.rel, N);
-  if (!rc) rc = dalloc(c, &d.rel_ref, N);
-  int **di[] = {&d.type, &d.cell_of, &d.t_type, &d.atom_cell, &d.perm, &d.perm_tmp, &d.nnbr};
-  for (auto pp : di) if (!rc) rc = dalloc(c, pp, N);
-  if (!rc) rc = dalloc(c, &d.id, N);
-  if (!rc) rc = dalloc(c, &d.t_id, N);
-  if (!rc) rc = dalloc(c, &d.cell_count, c->b.ncell);
-  if (!rc) rc = dalloc(c, &d.cell_cursor, c->b.ncell);
-  if (!rc) rc = dalloc(c, &d.cell_start, (size_t)c->b.ncell + 1);
-  if (!rc) rc = dalloc(c, &d.partials_ke, 4 * std::max(nblk, nblk_d));
-  if (!rc) rc = dalloc(c, &d.partials_ev, 2 * nblk);
-  if (!rc) rc = dalloc(c, &d.h3, 3 * (size_t)N);
-  if (!rc) rc = dalloc(c, &d.hi3, 3 * (size_t)N);
-  if (rc) return rc;
-  // initial capacity from the density: 1.4 x the mean count in the cutoff sphere, plus headroom
-  const double rho = N / (c->b.L[0] * c->b.L[1] * c->b.L[2]);
-  const double ce = c->cutoff_extra;
-  int cap = c->p.nbr_capacity > 0 ? c->p.nbr_capacity : (int)(1.4 * rho * 4.18879020479 * ce * ce * ce) + 48;
-  RK(alloc_nbr(c, cap));
-  CK(cudaMemcpyAsync(d.pos, hp.data(), N * sizeof(dbl4), cudaMemcpyHostToDevice, c->st));
-  CK(cudaMemcpyAsync(d.vel, hv.data(), N * sizeof(dbl4), cudaMemcpyHostToDevice, c->st));
-  CK(cudaMemsetAsync(d.acc, 0, N * sizeof(dbl4), c->st));
-  CK(cudaMemsetAsync(d.acc_old, 0, N * sizeof(dbl4), c->st));
-  CK(cudaMemcpyAsync(d.type, ht.data(), N * sizeof(int), cudaMemcpyHostToDevice, c->st));
-  CK(cudaMemcpyAsync(d.id, hid.data(), N * sizeof(uint32_t), cudaMemcpyHostToDevice, c->st));
-  CK(cudaMemsetAsync(d.cell_count, 0, c->b.ncell * sizeof(int), c->st));
-  CK(cudaMemsetAsync(d.cell_cursor, 0, c->b.ncell * sizeof(int), c->st));
-  double th[8] = {0, 0, 0, 0, 0, msum, 0, 0};
-  CK(cudaMemcpyAsync(d.thermo, th, sizeof(th), cudaMemcpyHostToDevice, c->st));
-  CK(cudaStreamSynchronize(c->st));
-  c->uploaded = true;
-  return CAVGPU_OK;
+  if (!c || n < 1 || c->b.nrep != 1) return CAVGPU_E_ARG;
+  return upload_common(c, &n, pos3, vel3, type, id);
+}
+
+int cavgpu_upload_batch(cavgpu_ctx *c, const int64_t *counts, const double *pos3, const double *vel3,
+                        const uint64_t *type) {
+  if (!c || !counts) return CAVGPU_E_ARG;
+  return upload_common(c, counts, pos3, vel3, type, nullptr);
 }
 
 int cavgpu_setup(cavgpu_ctx *c) {
   if (!c) return CAVGPU_E_ARG;
-  if (!c->uploaded) return CAVGPU_E_STATE;
-  RK(forced_build(c));
-  RK(launch_force(c->d, c->b, c->sc, c->lc, 0, 1, 0, c->st));
-  c->kernel_launches += 1;
-  RK(thermo_now(c, false));
-  RK(check_status(c));
-  c->set_up = true;
-  return CAVGPU_OK;
+  return setup_common(c);
 }
 
 int cavgpu_run(cavgpu_ctx *c, int64_t nsteps, int64_t every, double *out5) {
   if (!c || nsteps < 0 || every < 0 || (every > 0 && !out5)) return CAVGPU_E_ARG;
+  if (every > 0 && c->b.nrep > 1) return CAVGPU_E_ARG;  // batches: cavgpu_thermo_batch after the call
   if (!c->set_up) return CAVGPU_E_STATE;
   if (nsteps == 0) return CAVGPU_OK;
-  const bool lang = c->p.integrator == CAVGPU_VELOCITY_VERLET_LANGEVIN;
   int S = c->p.steps_per_graph > 0 ? std::min(c->p.steps_per_graph, MAX_GRAPH_STEPS) : 50;
   if (every > 0) S = (int)std::max<int64_t>(every, (S / every) * every);
   int64_t done = 0, rec = 0, eager_steps = 0;
@@ -527,7 +641,7 @@ int cavgpu_run(cavgpu_ctx *c, int64_t nsteps, int64_t every, double *out5) {
   {
     int f[F_NWORDS];
     RK(read_flags(c, f));
-    rebuilds_at_start = f[F_REBUILDS];
+    rebuilds_at_start = f[F_PASSES];
   }
   // chunks of up to S steps, each one captured CUDA graph (cached per size).  Without
   // recording, the last chunk computes the thermo of its final step, so that the state
@@ -546,7 +660,7 @@ int cavgpu_run(cavgpu_ctx *c, int64_t nsteps, int64_t every, double *out5) {
     c->graph_launches += 1;
     // drift + condition + force per step, the thermo folds, the step counter; the
     // rebuild kernels that ran are added from the device's rebuild count below
-    c->kernel_launches += (long long)sz * 3 + 1 + nrec;
+    c->kernel_launches += (long long)sz * 3 + 1 + nrec * (c->b.nrep > 1 && is_lang(c) ? 2 : 1);
     if (c->prof) RK(collect_profile(c, sz));
     if (every > 0) {
       CK(cudaMemcpyAsync(out5 + THERMO_REC * rec, c->d.thermo_ring, THERMO_REC * sizeof(double) * nrec,
@@ -571,7 +685,8 @@ int cavgpu_run(cavgpu_ctx *c, int64_t nsteps, int64_t every, double *out5) {
     c->kernel_launches += 1;
     if (c->prof) RK(collect_profile(c, 1));
     if (every > 0 && th) {
-      CK(cudaMemcpyAsync(out5 + THERMO_REC * rec, c->d.thermo_ring, THERMO_REC * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+      CK(cudaMemcpyAsync(out5 + THERMO_REC * rec, c->d.thermo_ring, THERMO_REC * sizeof(double),
+                         cudaMemcpyDeviceToHost, c->st));
       rec += 1;
     }
     ++done;
@@ -583,9 +698,9 @@ int cavgpu_run(cavgpu_ctx *c, int64_t nsteps, int64_t every, double *out5) {
     // rebuild kernels launched by the graphs' conditional nodes (eager steps counted theirs)
     int f[F_NWORDS];
     RK(read_flags(c, f));
-    if (eager_steps == 0) c->kernel_launches += (long long)REBUILD_KERNELS * (f[F_REBUILDS] - rebuilds_at_start);
+    if (eager_steps == 0 && f[F_PASSES] > rebuilds_at_start)
+      c->kernel_launches += (long long)REBUILD_KERNELS * (f[F_PASSES] - rebuilds_at_start);
   }
-  (void)lang;
   return CAVGPU_OK;
 }
 
@@ -597,19 +712,35 @@ int cavgpu_forces(cavgpu_ctx *c, double *virial, double *pe) {
   RK(forced_build(c));
   RK(launch_force(c->d, c->b, c->sc, c->lc, 0, 1, 0, c->st));
   c->kernel_launches += 1;
-  RK(thermo_now(c, false));
+  if (c->b.nrep == 1) {
+    RK(launch_thermo_final(c->d, c->tc, force_grid_blocks(c->lc), force_grid_blocks(c->lc), -1, c->st));
+  } else {
+    RK(launch_thermo_replicas(c->d, c->b, c->tc, 1, 1, c->st));
+  }
+  c->kernel_launches += 1;
   RK(check_status(c));
-  double th[8];
-  CK(cudaMemcpyAsync(th, c->d.thermo, sizeof(th), cudaMemcpyDeviceToHost, c->st));
-  CK(cudaStreamSynchronize(c->st));
-  if (virial) *virial = th[3];
-  if (pe) *pe = th[4];
+  if (c->b.nrep == 1) {
+    double th[8];
+    CK(cudaMemcpyAsync(th, c->d.thermo, sizeof(th), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    if (virial) *virial = th[3];
+    if (pe) *pe = th[4];
+  } else {  // sums over the replicas
+    std::vector<double> th(8 * (size_t)c->b.nrep);
+    CK(cudaMemcpyAsync(th.data(), c->d.thermo_rep, th.size() * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    double v = 0.0, e = 0.0;
+    for (int r = 0; r < c->b.nrep; ++r) { v += th[8 * r + 3]; e += th[8 * r + 4]; }
+    if (virial) *virial = v;
+    if (pe) *pe = e;
+  }
   return CAVGPU_OK;
 }
 
 int cavgpu_thermo(cavgpu_ctx *c, double *out6) {
   if (!c || !out6) return CAVGPU_E_ARG;
   if (!c->set_up) return CAVGPU_E_STATE;
+  if (c->b.nrep > 1) return CAVGPU_E_ARG;  // cavgpu_thermo_batch
   double th[8];
   int f[F_NWORDS];
   CK(cudaMemcpyAsync(th, c->d.thermo, sizeof(th), cudaMemcpyDeviceToHost, c->st));
@@ -619,24 +750,37 @@ int cavgpu_thermo(cavgpu_ctx *c, double *out6) {
   return CAVGPU_OK;
 }
 
+int cavgpu_thermo_batch(cavgpu_ctx *c, double *out6) {
+  if (!c || !out6) return CAVGPU_E_ARG;
+  if (!c->set_up) return CAVGPU_E_STATE;
+  const int R = c->b.nrep;
+  if (R == 1) return cavgpu_thermo(c, out6);
+  std::vector<double> th(8 * (size_t)R);
+  CK(cudaMemcpyAsync(th.data(), c->d.thermo_rep, th.size() * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  for (int r = 0; r < R; ++r)
+    for (int k = 0; k < 6; ++k) out6[6 * r + k] = th[8 * r + k];
+  return CAVGPU_OK;
+}
+
 int cavgpu_download(cavgpu_ctx *c, double *pos3, double *vel3, double *acc3) {
   if (!c) return CAVGPU_E_ARG;
   if (!c->uploaded) return CAVGPU_E_STATE;
   double *outs[3] = {pos3, vel3, acc3};
   for (int w = 0; w < 3; ++w) {
     if (!outs[w]) continue;
-    RK(launch_to_host_order(c->d, c->b, c->n, w, c->st));
-    CK(cudaMemcpyAsync(outs[w], c->d.h3, 3 * sizeof(double) * c->n, cudaMemcpyDeviceToHost, c->st));
+    RK(launch_to_host_order(c->d, c->b, w, c->st));
+    CK(cudaMemcpyAsync(outs[w], c->d.h3, 3 * sizeof(double) * c->natoms, cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
   }
   return CAVGPU_OK;
 }
 
 int64_t cavgpu_export_pairs(cavgpu_ctx *c, int32_t *out5, int64_t cap) {
-  if (!c || (cap > 0 && !out5)) return CAVGPU_E_ARG;
+  if (!c || (cap > 0 && !out5) || c->b.nrep != 1) return CAVGPU_E_ARG;
   if (!c->set_up) return CAVGPU_E_STATE;
-  std::vector<int> nn(c->n);
-  if (cudaMemcpyAsync(nn.data(), c->d.nnbr, c->n * sizeof(int), cudaMemcpyDeviceToHost, c->st) != cudaSuccess ||
+  std::vector<int> nn(c->b.nslot);
+  if (cudaMemcpyAsync(nn.data(), c->d.nnbr, c->b.nslot * sizeof(int), cudaMemcpyDeviceToHost, c->st) != cudaSuccess ||
       cudaStreamSynchronize(c->st) != cudaSuccess)
     return CAVGPU_E_CUDA;
   int64_t total = 0;
@@ -648,7 +792,7 @@ int64_t cavgpu_export_pairs(cavgpu_ctx *c, int32_t *out5, int64_t cap) {
   if (cudaMalloc(&rows, (size_t)take * 5 * sizeof(int32_t)) != cudaSuccess) { cudaGetLastError(); return CAVGPU_E_NOMEM; }
   if (cudaMalloc(&cnt, sizeof(unsigned long long)) != cudaSuccess) { cudaFree(rows); cudaGetLastError(); return CAVGPU_E_NOMEM; }
   int rc = cuda_rc(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), c->st));
-  if (!rc) rc = launch_export_pairs(c->d, c->b, c->n, c->p.precision == CAVGPU_MIXED ? 1 : 0, rows, cnt, take, c->st);
+  if (!rc) rc = launch_export_pairs(c->d, c->b, c->p.precision == CAVGPU_MIXED ? 1 : 0, rows, cnt, take, c->st);
   if (!rc) rc = cuda_rc(cudaMemcpyAsync(out5, rows, (size_t)take * 5 * sizeof(int32_t), cudaMemcpyDeviceToHost, c->st));
   if (!rc) rc = cuda_rc(cudaStreamSynchronize(c->st));
   cudaFree(rows);
@@ -657,22 +801,22 @@ int64_t cavgpu_export_pairs(cavgpu_ctx *c, int32_t *out5, int64_t cap) {
 }
 
 int cavgpu_export_bins(cavgpu_ctx *c, int32_t *owned3, int32_t *nbins3) {
-  if (!c) return CAVGPU_E_ARG;
+  if (!c || c->b.nrep != 1) return CAVGPU_E_ARG;
   if (!c->uploaded) return CAVGPU_E_STATE;
   if (nbins3) for (int a = 0; a < 3; ++a) nbins3[a] = c->ref_nb[a];
   if (!owned3) return CAVGPU_OK;
-  RK(launch_to_host_order(c->d, c->b, c->n, 0, c->st));
-  RK(launch_ref_bins(c->d, c->n, c->cutoff_inv, c->ref_nb, c->lo_local, c->st));
-  CK(cudaMemcpyAsync(owned3, c->d.hi3, 3 * sizeof(int32_t) * c->n, cudaMemcpyDeviceToHost, c->st));
+  RK(launch_to_host_order(c->d, c->b, 0, c->st));
+  RK(launch_ref_bins(c->d, c->natoms, c->cutoff_inv, c->ref_nb, c->lo_local, c->st));
+  CK(cudaMemcpyAsync(owned3, c->d.hi3, 3 * sizeof(int32_t) * c->natoms, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
   return CAVGPU_OK;
 }
 
 int64_t cavgpu_export_ghosts(cavgpu_ctx *c, double ghost_cutoff, int32_t *src, int32_t *shift3, double *pos3,
                              int32_t *bins3, int64_t cap) {
-  if (!c || ghost_cutoff < 0.0) return CAVGPU_E_ARG;
+  if (!c || ghost_cutoff < 0.0 || c->b.nrep != 1) return CAVGPU_E_ARG;
   if (!c->uploaded) return CAVGPU_E_STATE;
-  const int N = c->n;
+  const int N = c->natoms;
   int *counts = nullptr, *starts = nullptr;
   int32_t *gs = nullptr, *gsh = nullptr, *gb = nullptr;
   double *gp = nullptr;
@@ -688,7 +832,7 @@ int64_t cavgpu_export_ghosts(cavgpu_ctx *c, double ghost_cutoff, int32_t *src, i
   M((void **)&gp, (size_t)gcap * 3 * sizeof(double));
   M((void **)&gb, (size_t)gcap * 3 * sizeof(int32_t));
   int total = 0;
-  if (!rc) rc = launch_to_host_order(c->d, c->b, N, 0, c->st);
+  if (!rc) rc = launch_to_host_order(c->d, c->b, 0, c->st);
   if (!rc) rc = launch_ghosts(c->d, c->b, N, ghost_cutoff, counts, starts, gs, gsh, gp, gb, gcap, c->cutoff_inv,
                               c->ref_nb, c->lo_local, c->st);
   if (!rc) rc = cuda_rc(cudaMemcpyAsync(&total, starts + N, sizeof(int), cudaMemcpyDeviceToHost, c->st));

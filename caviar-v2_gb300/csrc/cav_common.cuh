@@ -1,5 +1,11 @@
 // cav_common.cuh -- device state, constants and small device helpers shared by
 // the sm_103a kernels of the CAVIAR2 MD step.
+//
+// One context holds R >= 1 independent periodic systems ("replicas"); a single
+// system is R = 1.  Replica r owns a contiguous, 32-aligned range of atom slots
+// (so that no warp of any kernel straddles two replicas) and a contiguous range
+// of search cells; the slots after its atoms, up to the next aligned start, are
+// padding that no kernel updates and no list refers to.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -28,17 +34,19 @@ constexpr int THERMO_REC = 5;  // {KE, T, P, virialForce, PE} per recorded step
 // neighbour entry: bits 0..26 = atom slot j, bits 27..31 = image code (0..26)
 constexpr int CODE_SHIFT = 27;
 constexpr uint32_t IDX_MASK = (1u << CODE_SHIFT) - 1u;
-constexpr int64_t MAX_ATOMS = (int64_t)IDX_MASK;  // 134,217,727
+constexpr int64_t MAX_ATOMS = (int64_t)IDX_MASK;  // 134,217,727 slots
 constexpr int CODE_ZERO = 13;                      // (0,0,0)
+constexpr int SLOT_ALIGN = 32;                     // replica slot ranges start on warp boundaries
 
 // device flag words
 enum Flag : int {
-  F_REBUILD = 0,   // list must be rebuilt before the next force (half-skin test fired)
+  F_REBUILD = 0,   // some replica must rebuild its list before the next force (half-skin test fired)
   F_MAXNB = 1,     // largest neighbour count seen by the last build
   F_OVERFLOW = 2,  // a build wanted more than `cap` slots
   F_NAN = 3,       // NaN acceleration seen
   F_NAN_ATOM = 4,  // host index of one NaN atom
-  F_REBUILDS = 5,  // rebuild count
+  F_REBUILDS = 5,  // replica list builds (a single system: its rebuild count)
+  F_PASSES = 6,    // rebuild passes that built at least one replica
   F_NWORDS = 8
 };
 
@@ -53,27 +61,44 @@ struct PairTab {
   int nt;
 };
 
-struct Box {
+// One replica's periodic box and search grid.
+struct RepBox {
   double lo[3], hi[3], L[3];
-  int nc[3];          // search grid cells per axis (cell width >= list cutoff)
-  double w[3], inv_w[3];
+  double w[3], inv_w[3];  // search cell width >= list cutoff
   float wf[3];
-  double ce2;         // cutoff_extra^2, the list predicate r^2 < ce2 (src/neighborlist.cpp:258, :508)
-  float ce2_lo, ce2_hi;  // FP32 pre-screen band around ce2
-  double thr2;        // 0.25 (cutoff_extra - cutoff)^2 (src/neighborlist.cpp:318)
-  float thr2f;        // thr2 * (1 - 1e-6) in FP32: the mixed form's test may only fire early
-  int ncell;
+  int nc[3];
+  int cell_off, ncell;    // cells [cell_off, cell_off + ncell); cell cell_off + ncell holds the padding
+  int slot_off, natoms, pad;
+  int id_off;             // host index of the replica's first atom; atom ids are local (0..natoms-1)
 };
+
+// Batch-wide geometry (by value in every launch).
+struct Box {
+  const RepBox *rep;    // [nrep] (device)
+  const int *rep_of;    // slot -> replica, -1 for padding (device; null when nrep == 1)
+  const int *cell_rep;  // cell -> replica, -1 for a padding cell (device; null when nrep == 1)
+  int *rep_flag;        // per replica: rebuild requested (device)
+  int nrep, nslot, ncell_all;  // ncell_all counts the padding cells
+  double ce2;           // cutoff_extra^2, the list predicate r^2 < ce2 (src/neighborlist.cpp:258, :508)
+  float ce2_lo, ce2_hi; // FP32 pre-screen band around ce2
+  double thr2;          // 0.25 (cutoff_extra - cutoff)^2 (src/neighborlist.cpp:318)
+  float thr2f;          // thr2 * (1 - 1e-6) in FP32: the mixed form's test may only fire early
+  RepBox r0;            // replica 0 by value: the single-system path reads no replica table
+};
+
+__device__ inline const RepBox &repbox(const Box &b, int r) { return b.nrep == 1 ? b.r0 : b.rep[r]; }
+__device__ inline int rep_of_slot(const Box &b, int i) { return b.nrep == 1 ? 0 : b.rep_of[i]; }
+__device__ inline int rep_of_cell(const Box &b, int c) { return b.nrep == 1 ? (c < b.r0.ncell ? 0 : -1) : b.cell_rep[c]; }
 
 struct StepConsts {
   double dt, hdt, hdt2;       // dt, 0.5*dt, 0.5*dt*dt
   double la, lb, lc;          // Langevin a, b, c (src/md_simulator.cpp:398-405)
   uint64_t seed;
   int noise_off;
-  int n;
+  int n;                      // slots
 };
 
-// Device arrays of one system, in cell-sorted slot order.
+// Device arrays, in cell-sorted slot order.
 struct Dev {
   dbl4 *pos, *vel, *acc, *acc_old, *pos_ref;
   float4 *rel;                // position relative to the build cell's origin; w = type bits
@@ -89,13 +114,15 @@ struct Dev {
   // neighbour list
   uint32_t *nbr;
   int *nnbr;
-  int cap;                    // slots per atom (multiple of 32)
+  int cap;                    // slots per atom (multiple of 64)
   int tpa;                    // force-kernel lanes per atom (fixes the list layout)
   // status, reductions
   int *flags;
   double *partials_ke;        // per-block {sum m v^2, sum m v} (4 per block)
   double *partials_ev;        // per-block {sum -coef r^2, sum V} over both pair orders (2 per block)
+  double2 *ev_atom;           // per-slot {-coef r^2, V} sums (batches: per-replica folds)
   double *thermo;             // {KE, T, P, virialForce, PE, total mass, -, -}
+  double *thermo_rep;         // batches: per replica {KE, T, P, virialForce, PE, total mass, -, -}
   double *thermo_ring;        // recorded thermo points (THERMO_REC per record)
   long long *step_base;       // step counter read by the Langevin kernels
   PairTab *tab;
@@ -175,24 +202,24 @@ __device__ inline void langevin_eta_f(uint64_t seed, long long step, uint32_t id
   e2 = (double)(r1 * cospif(2.0f * u3));
 }
 
-// ---- host-side launch helpers (defined in cav_kernels.cu) -------------------
+// ---- host-side launch helpers ----------------------------------------------
 struct LaunchCfg {
   int precision;   // CAVGPU_FP64 / CAVGPU_MIXED
   int integrator;  // CAVGPU_VELOCITY_VERLET / ..._LANGEVIN
   int tpa, block;
-  int n;
-  int pressure;    // n_r_df etc. are in ThermoCfg
+  int n;           // slots
 };
 
 struct ThermoCfg {
   int n_r_df;
   double k_b, volume;
-  int n;
-  int langevin;  // pressure without the force virial (computed before the force)
+  int n;           // atoms (single system)
+  int langevin;    // pressure without the force virial (the reference computes it before the force)
 };
 
-// Kernel launchers.  `forced` rebuilds regardless of the device flag; otherwise
-// the rebuild kernels return at once unless the half-skin test set F_REBUILD.
+// Kernel launchers (cav_kernels.cu, cav_force.cu).  `forced` rebuilds every
+// replica regardless of the flags; otherwise the rebuild kernels skip replicas
+// whose half-skin test did not fire.
 int drift_grid_blocks(const LaunchCfg &lc);
 int force_grid_blocks(const LaunchCfg &lc);
 int launch_drift(const Dev &d, const Box &b, const StepConsts &sc, const LaunchCfg &lc, int k_in_chunk,
@@ -205,9 +232,11 @@ constexpr int REBUILD_KERNELS = 8;  // kernels launch_rebuild enqueues
 int launch_force(const Dev &d, const Box &b, const StepConsts &sc, const LaunchCfg &lc, int kick, int thermo,
                  int k_in_chunk, cudaStream_t st);
 int launch_thermo_final(const Dev &d, const ThermoCfg &tc, int nb_ke, int nb_ev, int ring_slot, cudaStream_t st);
+// batches: per-replica KE (ke = 1, from the current velocities) and/or virial+PE folds
+int launch_thermo_replicas(const Dev &d, const Box &b, const ThermoCfg &tc, int ke, int ev, cudaStream_t st);
 int launch_advance_step(const Dev &d, int nsteps, cudaStream_t st);
-int launch_to_host_order(const Dev &d, const Box &b, int n, int what, cudaStream_t st);
-int launch_export_pairs(const Dev &d, const Box &b, int n, int mode, int32_t *rows, unsigned long long *counter,
+int launch_to_host_order(const Dev &d, const Box &b, int what, cudaStream_t st);
+int launch_export_pairs(const Dev &d, const Box &b, int mode, int32_t *rows, unsigned long long *counter,
                         int64_t cap, cudaStream_t st);
 int launch_ref_bins(const Dev &d, int n, double cutoff_inv, const int nb[3], const double lo_local[3],
                     cudaStream_t st);

@@ -37,22 +37,34 @@ __device__ inline void block_sum_store_f(double (&v)[NV], double *out) {
 struct SmemTabD {
   double rc2[MAXT * MAXT], sig2[MAXT * MAXT], eps4[MAXT * MAXT], gc[MAXT * MAXT], uc[MAXT * MAXT];
   double minv[MAXT], mass[MAXT];
-  double3 shift[27];
 };
 struct SmemTabF {
   float rc2[MAXT * MAXT], sig2[MAXT * MAXT], eps4[MAXT * MAXT], gc[MAXT * MAXT], uc[MAXT * MAXT];
   double minv[MAXT], mass[MAXT];
-  float3 off[27];
+};
+// per warp: the 27 image shifts s*L (FP64) or cell offsets d*w (mixed) of the
+// replica the warp's current atoms belong to (a warp never straddles two)
+template <bool MIXED>
+struct WarpImages;
+template <>
+struct WarpImages<true> {
+  float3 v[27];
+};
+template <>
+struct WarpImages<false> {
+  double3 v[27];
 };
 
 // KICK: 0 = store the acceleration only; 1 = velocity-Verlet closing kick
 // v += (a + a_old) * (0.5 dt) (src/md_simulator.cpp:672-679); 2 = Langevin closing
 // update v = (v a_L + eta b) + (a*0.5) dt (src/md_simulator.cpp:853-862).
-// EV: accumulate virial and potential energy (and KE unless KICK == 2).
+// EV: accumulate virial and potential energy (and KE unless KICK == 2); batches
+// also store them per slot for the per-replica folds.
 template <int TPA, bool MIXED, int KICK, bool EV>
 __global__ void __launch_bounds__(256) k_force(Dev d, Box b, StepConsts sc, int k_in_chunk) {
   constexpr int A = 32 / TPA;
   __shared__ typename std::conditional<MIXED, SmemTabF, SmemTabD>::type tab;
+  __shared__ WarpImages<MIXED> wimg[8];
   const PairTab &T = *d.tab;
   const int nt = T.nt;
   for (int k = threadIdx.x; k < nt * nt; k += blockDim.x) {
@@ -60,14 +72,9 @@ __global__ void __launch_bounds__(256) k_force(Dev d, Box b, StepConsts sc, int 
     tab.uc[k] = T.uc[k];
   }
   for (int k = threadIdx.x; k < nt; k += blockDim.x) { tab.minv[k] = T.minv[k]; tab.mass[k] = T.mass[k]; }
-  for (int k = threadIdx.x; k < 27; k += blockDim.x) {
-    const int sx = k % 3 - 1, sy = (k / 3) % 3 - 1, sz = k / 9 - 1;
-    if constexpr (MIXED) tab.off[k] = make_float3(sx * b.wf[0], sy * b.wf[1], sz * b.wf[2]);
-    else tab.shift[k] = make_double3(sx * b.L[0], sy * b.L[1], sz * b.L[2]);
-  }
   __syncthreads();
 
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int a = lane % A, t = lane / A;
   const int n = sc.n, cap = d.cap;
   const int warps_total = (gridDim.x * blockDim.x) >> 5;
@@ -76,10 +83,24 @@ __global__ void __launch_bounds__(256) k_force(Dev d, Box b, StepConsts sc, int 
   double ev_p[2] = {0.0, 0.0};
   long long step = 0;
   if (KICK == 2) step = *d.step_base + k_in_chunk;
+  auto &img = wimg[wid].v;
+  int img_rep = -1;
 
   for (int task = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; task < ntask; task += warps_total) {
+    const int rep = rep_of_slot(b, task * A);
+    if (rep < 0) continue;  // a task of padding slots (uniform over the warp)
+    if (rep != img_rep) {
+      const RepBox &rb = repbox(b, rep);
+      if (lane < 27) {
+        const int sx = lane % 3 - 1, sy = (lane / 3) % 3 - 1, sz = lane / 9 - 1;
+        if constexpr (MIXED) img[lane] = make_float3(sx * rb.wf[0], sy * rb.wf[1], sz * rb.wf[2]);
+        else img[lane] = make_double3(sx * rb.L[0], sy * rb.L[1], sz * rb.L[2]);
+      }
+      __syncwarp();
+      img_rep = rep;
+    }
     const int i = task * A + a;
-    const bool act = i < n;
+    const bool act = i < n && rep_of_slot(b, i) >= 0;
     double fx = 0.0, fy = 0.0, fz = 0.0, vir = 0.0, pe = 0.0;
     int ti = 0;
     if (act) {
@@ -101,7 +122,7 @@ __global__ void __launch_bounds__(256) k_force(Dev d, Box b, StepConsts sc, int 
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
             if (k0 + u >= nn) break;
-            const float3 o = tab.off[e[u] >> CODE_SHIFT];
+            const float3 o = img[e[u] >> CODE_SHIFT];
             const float dx = (rj[u].x + o.x) - ri.x, dy = (rj[u].y + o.y) - ri.y, dz = (rj[u].z + o.z) - ri.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
             const int tt = ti * nt + __float_as_int(rj[u].w);
@@ -132,7 +153,7 @@ __global__ void __launch_bounds__(256) k_force(Dev d, Box b, StepConsts sc, int 
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
             if (k0 + u >= nn) break;
-            const double3 s = tab.shift[e[u] >> CODE_SHIFT];
+            const double3 s = img[e[u] >> CODE_SHIFT];
             const double dx = (xj[u].x + s.x) - xi.x, dy = (xj[u].y + s.y) - xi.y, dz = (xj[u].z + s.z) - xi.z;
             const double r2 = dx * dx + dy * dy + dz * dz;
             const int tt = ti * nt + (int)xj[u].w;
@@ -196,8 +217,8 @@ __global__ void __launch_bounds__(256) k_force(Dev d, Box b, StepConsts sc, int 
         dbl4 v = d.vel[i];
         double e0 = 0.0, e1 = 0.0, e2 = 0.0;
         if (!sc.noise_off) {
-          if (MIXED) langevin_eta_f(sc.seed, step, d.id[i], e0, e1, e2);
-          else langevin_eta(sc.seed, step, d.id[i], e0, e1, e2);
+          if (MIXED) langevin_eta_f(sc.seed + rep, step, d.id[i], e0, e1, e2);
+          else langevin_eta(sc.seed + rep, step, d.id[i], e0, e1, e2);
         }
         if (MIXED) {
           v.x = fma(an.x, sc.hdt, fma(v.x, sc.la, e0 * sc.lb));
@@ -211,7 +232,11 @@ __global__ void __launch_bounds__(256) k_force(Dev d, Box b, StepConsts sc, int 
         d.acc[i] = an;
         d.vel[i] = v;
       }
-      if (EV) { ev_p[0] += vir; ev_p[1] += pe; }
+      if (EV) {
+        ev_p[0] += vir;
+        ev_p[1] += pe;
+        if (d.ev_atom) d.ev_atom[i] = make_double2(vir, pe);
+      }
     }
   }
   if (EV) {

@@ -1,6 +1,7 @@
-// cav_kernels.cu -- sm_103a kernels of the CAVIAR2 MD step (cell binning,
-// Verlet-list build, integrator stages, thermo reductions, parity exports).
-// The pair-force kernels live in cav_force.cu.
+// cav_kernels.cu -- sm_103a kernels of the CAVIAR2 MD step (integrator stages,
+// cell binning, Verlet-list build, thermo reductions, parity exports).  The
+// pair-force kernels live in cav_force.cu.  Every kernel serves R >= 1 replicas
+// (see cav_common.cuh); a single system is R = 1.
 #include <algorithm>
 
 #include "cav_common.cuh"
@@ -47,34 +48,39 @@ __device__ inline void block_sum_store(double (&v)[NV], double *out /* NV double
 }
 
 // ---------------------------------------------------------------------------
-// integrator stage 1: drift (velocity Verlet) -- src/md_simulator.cpp:640-656
-//   r(t+dt) = r + v dt + 0.5 a dt^2 ; a_old = a ; NaN check ; half-skin test
+// integrator stage 1 -- src/md_simulator.cpp:640-656 (velocity Verlet) and
+// :748-837 (Langevin first half); NaN check; half-skin test per replica
 // ---------------------------------------------------------------------------
-__device__ inline void update_rel(const Dev &d, const Box &b, int i, const dbl4 &x) {
-  const int c = d.cell_of[i];
-  const int cx = c % b.nc[0], cy = (c / b.nc[0]) % b.nc[1], cz = c / (b.nc[0] * b.nc[1]);
+__device__ inline void update_rel(const Dev &d, const RepBox &rb, int i, const dbl4 &x) {
+  const int c = d.cell_of[i] - rb.cell_off;
+  const int cx = c % rb.nc[0], cy = (c / rb.nc[0]) % rb.nc[1], cz = c / (rb.nc[0] * rb.nc[1]);
   float4 r;
-  r.x = (float)(x.x - (b.lo[0] + cx * b.w[0]));
-  r.y = (float)(x.y - (b.lo[1] + cy * b.w[1]));
-  r.z = (float)(x.z - (b.lo[2] + cz * b.w[2]));
+  r.x = (float)(x.x - (rb.lo[0] + cx * rb.w[0]));
+  r.y = (float)(x.y - (rb.lo[1] + cy * rb.w[1]));
+  r.z = (float)(x.z - (rb.lo[2] + cz * rb.w[2]));
   r.w = __int_as_float((int)x.w);
   d.rel[i] = r;
 }
 
-__device__ inline void half_skin_test(const Dev &d, const Box &b, int i, const dbl4 &x) {
+__device__ inline void request_rebuild(const Dev &d, const Box &b, int rep) {
+  b.rep_flag[rep] = 1;
+  d.flags[F_REBUILD] = 1;
+}
+
+__device__ inline void half_skin_test(const Dev &d, const Box &b, int rep, int i, const dbl4 &x) {
   const dbl4 r = d.pos_ref[i];
   const double dx = x.x - r.x, dy = x.y - r.y, dz = x.z - r.z;
-  if (dx * dx + dy * dy + dz * dz > b.thr2) d.flags[F_REBUILD] = 1;
+  if (dx * dx + dy * dy + dz * dz > b.thr2) request_rebuild(d, b, rep);
 }
 
 // Mixed form: the displacement since the build is taken once in FP64 (3
 // subtractions) and serves both the half-skin test (in FP32 against a threshold
 // shrunk by 1e-6, so it can only fire early) and the FP32 cell-relative
 // coordinates, rel = rel_at_build + (float)(x - x_at_build).
-__device__ inline void mixed_track(const Dev &d, const Box &b, int i, const dbl4 &x) {
+__device__ inline void mixed_track(const Dev &d, const Box &b, int rep, int i, const dbl4 &x) {
   const dbl4 r = d.pos_ref[i];
   const float fx = (float)(x.x - r.x), fy = (float)(x.y - r.y), fz = (float)(x.z - r.z);
-  if (fx * fx + fy * fy + fz * fz > b.thr2f) d.flags[F_REBUILD] = 1;
+  if (fx * fx + fy * fy + fz * fz > b.thr2f) request_rebuild(d, b, rep);
   const float4 q = d.rel_ref[i];
   d.rel[i] = make_float4(q.x + fx, q.y + fy, q.z + fz, q.w);
 }
@@ -94,6 +100,8 @@ template <bool MIXED>
 __global__ void __launch_bounds__(256) k_drift_vv(Dev d, Box b, StepConsts sc) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= sc.n) return;
+  const int rep = rep_of_slot(b, i);
+  if (rep < 0) return;  // padding slot
   dbl4 x = d.pos[i];
   const dbl4 v = d.vel[i], a = d.acc[i];
   nan_check(d, i, a);
@@ -108,8 +116,8 @@ __global__ void __launch_bounds__(256) k_drift_vv(Dev d, Box b, StepConsts sc) {
   }
   d.pos[i] = x;
   d.acc_old[i] = a;
-  if (MIXED) mixed_track(d, b, i, x);
-  else half_skin_test(d, b, i, x);
+  if (MIXED) mixed_track(d, b, rep, i, x);
+  else half_skin_test(d, b, rep, i, x);
 }
 
 // Langevin first half (src/md_simulator.cpp:748-837):
@@ -118,15 +126,17 @@ template <bool MIXED, bool THERMO>
 __global__ void __launch_bounds__(256) k_lang_a(Dev d, Box b, StepConsts sc, int k_in_chunk) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double part[4] = {0.0, 0.0, 0.0, 0.0};
-  if (i < sc.n) {
+  const int rep = i < sc.n ? rep_of_slot(b, i) : -1;
+  if (rep >= 0) {
     dbl4 x = d.pos[i], v = d.vel[i];
     const dbl4 a = d.acc[i];
     nan_check(d, i, a);
     double e0 = 0.0, e1 = 0.0, e2 = 0.0;
     if (!sc.noise_off) {
       const long long step = *d.step_base + k_in_chunk;
-      if (MIXED) langevin_eta_f(sc.seed, step, d.id[i], e0, e1, e2);
-      else langevin_eta(sc.seed, step, d.id[i], e0, e1, e2);
+      // replica r draws the noise stream of seed + r with its local ids
+      if (MIXED) langevin_eta_f(sc.seed + rep, step, d.id[i], e0, e1, e2);
+      else langevin_eta(sc.seed + rep, step, d.id[i], e0, e1, e2);
     }
     if (MIXED) {
       v.x = fma(a.x, sc.hdt, fma(e0, sc.lb, v.x));
@@ -153,41 +163,43 @@ __global__ void __launch_bounds__(256) k_lang_a(Dev d, Box b, StepConsts sc, int
     }
     d.pos[i] = x;
     d.vel[i] = v;
-    if (MIXED) mixed_track(d, b, i, x);
-    else half_skin_test(d, b, i, x);
+    if (MIXED) mixed_track(d, b, rep, i, x);
+    else half_skin_test(d, b, rep, i, x);
   }
   if (THERMO) block_sum_store<4>(part, &d.partials_ke[(size_t)blockIdx.x * 4]);
 }
 
 // ---------------------------------------------------------------------------
-// list rebuild: wrap + bin -> scan -> scatter -> per-cell sort -> gather -> build
+// list rebuild of the flagged replicas: wrap + bin -> per-replica scan ->
+// scatter -> per-cell sort -> gather -> build
 // (Neighborlist::update_cell_list + update_verlet_list_from_cell_list,
 //  src/neighborlist.cpp:422-455, 496-553; Domain::fix_position, src/domain.cpp:443-493)
 // ---------------------------------------------------------------------------
-__device__ inline bool rebuild_off(const Dev &d, int forced) { return !forced && d.flags[F_REBUILD] == 0; }
+__device__ inline bool rebuild_on(const Box &b, int rep, int forced) { return forced || b.rep_flag[rep] != 0; }
 
-__global__ void __launch_bounds__(256) k_bin(Dev d, Box b, int n, int forced) {
-  if (rebuild_off(d, forced)) return;
+__global__ void __launch_bounds__(256) k_bin(Dev d, Box b, int forced) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool act = i < n;
+  if (i == 0) d.flags[F_MAXNB] = 0;
+  int rep = i < b.nslot ? rep_of_slot(b, i) : -1;
+  const bool act = rep >= 0 && rebuild_on(b, rep, forced);
   int c = 0;
   if (act) {
+    const RepBox &rb = repbox(b, rep);
     dbl4 p = d.pos[i];
     // single-image wrap exactly as Domain::fix_position
-    if (p.x < b.lo[0]) p.x += b.L[0]; else if (p.x > b.hi[0]) p.x -= b.L[0];
-    if (p.y < b.lo[1]) p.y += b.L[1]; else if (p.y > b.hi[1]) p.y -= b.L[1];
-    if (p.z < b.lo[2]) p.z += b.L[2]; else if (p.z > b.hi[2]) p.z -= b.L[2];
+    if (p.x < rb.lo[0]) p.x += rb.L[0]; else if (p.x > rb.hi[0]) p.x -= rb.L[0];
+    if (p.y < rb.lo[1]) p.y += rb.L[1]; else if (p.y > rb.hi[1]) p.y -= rb.L[1];
+    if (p.z < rb.lo[2]) p.z += rb.L[2]; else if (p.z > rb.hi[2]) p.z -= rb.L[2];
     d.pos[i] = p;
-    int cx = (int)floor((p.x - b.lo[0]) * b.inv_w[0]);
-    int cy = (int)floor((p.y - b.lo[1]) * b.inv_w[1]);
-    int cz = (int)floor((p.z - b.lo[2]) * b.inv_w[2]);
-    cx = min(max(cx, 0), b.nc[0] - 1);
-    cy = min(max(cy, 0), b.nc[1] - 1);
-    cz = min(max(cz, 0), b.nc[2] - 1);
-    c = cx + b.nc[0] * (cy + b.nc[1] * cz);
+    int cx = (int)floor((p.x - rb.lo[0]) * rb.inv_w[0]);
+    int cy = (int)floor((p.y - rb.lo[1]) * rb.inv_w[1]);
+    int cz = (int)floor((p.z - rb.lo[2]) * rb.inv_w[2]);
+    cx = min(max(cx, 0), rb.nc[0] - 1);
+    cy = min(max(cy, 0), rb.nc[1] - 1);
+    cz = min(max(cz, 0), rb.nc[2] - 1);
+    c = rb.cell_off + cx + rb.nc[0] * (cy + rb.nc[1] * cz);
     d.atom_cell[i] = c;
   }
-  if (i == 0) d.flags[F_MAXNB] = 0;
   // warp-aggregated counting: one atomic per distinct cell in the warp
   const unsigned m = __ballot_sync(FULL_MASK, act);
   if (act) {
@@ -196,23 +208,26 @@ __global__ void __launch_bounds__(256) k_bin(Dev d, Box b, int n, int forced) {
   }
 }
 
-// exclusive scan of `count[0..m)` into start[0..m] with one block; zeroes
-// count and (if non-null) cursor for the next use
-// Tiles of 4 x 1024 consecutive counts: coalesced loads, a warp-shuffle block
-// scan per tile, and a running carry between tiles.
-__global__ void __launch_bounds__(1024) k_scan(const Dev d, int *count, int *start, int *cursor, int m, int forced) {
-  if (rebuild_off(d, forced)) return;
+// One block per replica: exclusive scan of its cell counts, starting at the
+// replica's first slot; the padding cell counts the replica's padding slots.
+// Tiles of 4 x 1024 counts, a warp-shuffle block scan per tile, a running carry.
+// Zeroes the counts and cursors it read.
+__global__ void __launch_bounds__(1024) k_scan_rep(Dev d, Box b, int forced) {
+  const int rep = blockIdx.x;
+  if (!rebuild_on(b, rep, forced)) return;
+  const RepBox &rb = repbox(b, rep);
+  const int m = rb.ncell + 1, off = rb.cell_off;
   __shared__ int warp_tot[32];
   __shared__ int carry_s;
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-  if (t == 0) carry_s = 0;
+  if (t == 0) carry_s = rb.slot_off;
   __syncthreads();
   for (int base = 0; base < m; base += 4 * 1024) {
     int v[4], s = 0;
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int k = base + 4 * t + u;
-      v[u] = k < m ? count[k] : 0;
+      v[u] = k < m ? (k == m - 1 ? rb.pad : d.cell_count[off + k]) : 0;
       s += v[u];
     }
     int inc = s;
@@ -233,15 +248,14 @@ __global__ void __launch_bounds__(1024) k_scan(const Dev d, int *count, int *sta
       warp_tot[lane] = wv;
     }
     __syncthreads();
-    const int carry = carry_s;
-    int run = carry + inc - s + (wid ? warp_tot[wid - 1] : 0);
+    int run = carry_s + inc - s + (wid ? warp_tot[wid - 1] : 0);
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int k = base + 4 * t + u;
       if (k < m) {
-        start[k] = run;
-        count[k] = 0;
-        if (cursor) cursor[k] = 0;
+        d.cell_start[off + k] = run;
+        d.cell_count[off + k] = 0;
+        d.cell_cursor[off + k] = 0;
       }
       run += v[u];
     }
@@ -249,23 +263,24 @@ __global__ void __launch_bounds__(1024) k_scan(const Dev d, int *count, int *sta
     if (t == 1023) carry_s = run;
     __syncthreads();
   }
-  if (t == 0) start[m] = carry_s;
 }
 
-__global__ void __launch_bounds__(256) k_scatter(Dev d, int n, int forced) {
-  if (rebuild_off(d, forced)) return;
+__global__ void __launch_bounds__(256) k_scatter(Dev d, Box b, int forced) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= b.nslot) return;
+  const int rep = rep_of_slot(b, i);
+  if (rep < 0 || !rebuild_on(b, rep, forced)) return;
   const int c = d.atom_cell[i];
   d.perm_tmp[d.cell_start[c] + atomicAdd(&d.cell_cursor[c], 1)] = i;
 }
 
 // one warp per cell: order the cell's atoms by host index (deterministic lists);
 // cells of up to 32 atoms rank in registers with warp shuffles
-__global__ void __launch_bounds__(256) k_cell_sort(Dev d, int ncell, int forced) {
-  if (rebuild_off(d, forced)) return;
+__global__ void __launch_bounds__(256) k_cell_sort(Dev d, Box b, int forced) {
   const int cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (cell >= ncell) return;
+  if (cell >= b.ncell_all) return;
+  const int rep = rep_of_cell(b, cell);
+  if (rep < 0 || !rebuild_on(b, rep, forced)) return;
   const int s = d.cell_start[cell], e = d.cell_start[cell + 1], n = e - s;
   if (n <= 32) {
     const int ia = lane < n ? d.perm_tmp[s + lane] : 0;
@@ -284,10 +299,11 @@ __global__ void __launch_bounds__(256) k_cell_sort(Dev d, int ncell, int forced)
   }
 }
 
-__global__ void __launch_bounds__(256) k_copy_state(Dev d, int n, int forced) {
-  if (rebuild_off(d, forced)) return;
+__global__ void __launch_bounds__(256) k_copy_state(Dev d, Box b, int forced) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= b.nslot) return;
+  const int rep = rep_of_slot(b, i);
+  if (rep < 0 || !rebuild_on(b, rep, forced)) return;
   d.t_pos[i] = d.pos[i];
   d.t_vel[i] = d.vel[i];
   d.t_acc[i] = d.acc[i];
@@ -297,10 +313,11 @@ __global__ void __launch_bounds__(256) k_copy_state(Dev d, int n, int forced) {
   d.perm_tmp[i] = d.atom_cell[i];  // cell of old slot i (perm_tmp is free again)
 }
 
-__global__ void __launch_bounds__(256) k_gather(Dev d, Box b, int n, int forced) {
-  if (rebuild_off(d, forced)) return;
+__global__ void __launch_bounds__(256) k_gather(Dev d, Box b, int forced) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
+  if (k >= b.nslot) return;
+  const int rep = rep_of_slot(b, k);
+  if (rep < 0 || !rebuild_on(b, rep, forced)) return;
   const int o = d.perm[k];
   const dbl4 x = d.t_pos[o];
   d.pos[k] = x;
@@ -311,7 +328,7 @@ __global__ void __launch_bounds__(256) k_gather(Dev d, Box b, int n, int forced)
   d.type[k] = d.t_type[o];
   d.id[k] = d.t_id[o];
   d.cell_of[k] = d.perm_tmp[o];
-  update_rel(d, b, k, x);
+  update_rel(d, repbox(b, rep), k, x);
   d.rel_ref[k] = d.rel[k];
 }
 
@@ -320,196 +337,16 @@ __global__ void __launch_bounds__(256) k_gather(Dev d, Box b, int n, int forced)
 // evaluates it for a ghost image (image = x_j + s*L, then minus x_i, squares
 // summed x, y, z; no FMA contraction), pre-screened in FP32 on cell-relative
 // coordinates: only candidates inside a narrow band around the cutoff take
-// the FP64 path.  Hits are compacted with a warp ballot, so every atom's list
-// keeps the stencil order (deterministic).  mode 0 stores image codes (FP64
-// force), mode 1 cell-offset codes (mixed force).
-__device__ __noinline__ bool exact_pair(const Dev &d, const Box &b, int i, int j, int img) {
+// the FP64 path.  mode 0 stores image codes (FP64 force), mode 1 cell-offset
+// codes (mixed force).
+__device__ __noinline__ bool exact_pair(const Dev &d, const RepBox &rb, double ce2, int i, int j, int img) {
   const dbl4 xi = d.pos[i], xj = d.pos[j];
-  const double shx = (img % 3 - 1) * b.L[0], shy = ((img / 3) % 3 - 1) * b.L[1], shz = (img / 9 - 1) * b.L[2];
+  const double shx = (img % 3 - 1) * rb.L[0], shy = ((img / 3) % 3 - 1) * rb.L[1], shz = (img / 9 - 1) * rb.L[2];
   const double ddx = __dsub_rn(__dadd_rn(xj.x, shx), xi.x);
   const double ddy = __dsub_rn(__dadd_rn(xj.y, shy), xi.y);
   const double ddz = __dsub_rn(__dadd_rn(xj.z, shz), xi.z);
   const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)), __dmul_rn(ddz, ddz));
-  return r2 < b.ce2;
-}
-
-// the caller folds the largest count into F_MAXNB once per warp
-__device__ inline void finish_atom(const Dev &d, int i, int cnt) {
-  d.nnbr[i] = min(cnt, d.cap);
-  if (cnt > d.cap) atomicMax(&d.flags[F_OVERFLOW], cnt);
-}
-
-// One warp builds the list of atom i straight from global memory (stencils too
-// dense for the shared-memory stage).
-__device__ int build_atom_global(const Dev &d, const Box &b, int i, int mode) {
-  const int lane = threadIdx.x & 31;
-  const float4 ri = d.rel[i];
-  const int ci = d.cell_of[i];
-  const int cx = ci % b.nc[0], cy = (ci / b.nc[0]) % b.nc[1], cz = ci / (b.nc[0] * b.nc[1]);
-  int cnt = 0;
-  for (int k = 0; k < 27; ++k) {
-    const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
-    int nx = cx + dx, ny = cy + dy, nz = cz + dz, sx = 0, sy = 0, sz = 0;
-    if (nx < 0) { nx += b.nc[0]; sx = -1; } else if (nx >= b.nc[0]) { nx -= b.nc[0]; sx = 1; }
-    if (ny < 0) { ny += b.nc[1]; sy = -1; } else if (ny >= b.nc[1]) { ny -= b.nc[1]; sy = 1; }
-    if (nz < 0) { nz += b.nc[2]; sz = -1; } else if (nz >= b.nc[2]) { nz -= b.nc[2]; sz = 1; }
-    const int c2 = nx + b.nc[0] * (ny + b.nc[1] * nz);
-    const int img = image_code(sx, sy, sz);
-    const uint32_t code = (uint32_t)(mode == 0 ? img : k);
-    const float ox = dx * b.wf[0] - ri.x, oy = dy * b.wf[1] - ri.y, oz = dz * b.wf[2] - ri.z;
-    const int jb = d.cell_start[c2], je = d.cell_start[c2 + 1];
-    for (int base = jb; base < je; base += 32) {
-      const int j = base + lane;
-      bool hit = false;
-      if (j < je && !(img == CODE_ZERO && j == i)) {
-        const float4 rj = d.rel[j];
-        const float fx = rj.x + ox, fy = rj.y + oy, fz = rj.z + oz;
-        const float r2f = fx * fx + fy * fy + fz * fz;
-        hit = r2f < b.ce2_lo || (r2f <= b.ce2_hi && exact_pair(d, b, i, j, img));
-      }
-      const unsigned bal = __ballot_sync(FULL_MASK, hit);
-      if (hit) {
-        const int q = cnt + __popc(bal & ((1u << lane) - 1u));
-        if (q < d.cap) d.nbr[nbr_index(i, q, d.cap, d.tpa)] = (uint32_t)j | (code << CODE_SHIFT);
-      }
-      cnt += __popc(bal);
-    }
-  }
-  if (lane == 0) finish_atom(d, i, cnt);
-  return cnt;
-}
-
-constexpr int BUILD_THREADS = 128;
-constexpr int BUILD_MAXC = 2048;  // staged candidates per cell: 2048 x 21 B = 42 KiB of shared memory
-constexpr size_t BUILD_SMEM = (size_t)BUILD_MAXC * (sizeof(float4) + sizeof(uint32_t) + 1);
-
-// One CTA per home cell (grid-stride over cells): the 27 neighbour cells are
-// staged once in shared memory as FP32 coordinates already shifted into the home
-// cell's frame, then each warp scans them for one home atom at a time.
-__global__ void __launch_bounds__(BUILD_THREADS) k_build_cell(Dev d, Box b, int mode, int forced) {
-  if (rebuild_off(d, forced)) return;
-  extern __shared__ __align__(16) unsigned char smem[];
-  float4 *s_rel = reinterpret_cast<float4 *>(smem);
-  uint32_t *s_word = reinterpret_cast<uint32_t *>(s_rel + BUILD_MAXC);
-  unsigned char *s_img = reinterpret_cast<unsigned char *>(s_word + BUILD_MAXC);
-  __shared__ int s_pre[28], s_cell[27];
-  __shared__ float s_off[27][3];
-  __shared__ uint32_t s_code[27];
-  __shared__ unsigned char s_sc[27];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = BUILD_THREADS / 32;
-  int wmax = 0;
-  for (int cell = blockIdx.x; cell < b.ncell; cell += gridDim.x) {
-    const int hs = d.cell_start[cell], he = d.cell_start[cell + 1];
-    if (hs == he) continue;  // uniform over the block
-    const int cx = cell % b.nc[0], cy = (cell / b.nc[0]) % b.nc[1], cz = cell / (b.nc[0] * b.nc[1]);
-    if (warp == 0) {
-      int cntk = 0;
-      if (lane < 27) {
-        const int dx = lane % 3 - 1, dy = (lane / 3) % 3 - 1, dz = lane / 9 - 1;
-        int nx = cx + dx, ny = cy + dy, nz = cz + dz, sx = 0, sy = 0, sz = 0;
-        if (nx < 0) { nx += b.nc[0]; sx = -1; } else if (nx >= b.nc[0]) { nx -= b.nc[0]; sx = 1; }
-        if (ny < 0) { ny += b.nc[1]; sy = -1; } else if (ny >= b.nc[1]) { ny -= b.nc[1]; sy = 1; }
-        if (nz < 0) { nz += b.nc[2]; sz = -1; } else if (nz >= b.nc[2]) { nz -= b.nc[2]; sz = 1; }
-        const int c2 = nx + b.nc[0] * (ny + b.nc[1] * nz);
-        const int img = image_code(sx, sy, sz);
-        s_cell[lane] = c2;
-        s_off[lane][0] = dx * b.wf[0]; s_off[lane][1] = dy * b.wf[1]; s_off[lane][2] = dz * b.wf[2];
-        s_code[lane] = (uint32_t)(mode == 0 ? img : lane);
-        s_sc[lane] = (unsigned char)img;
-        cntk = d.cell_start[c2 + 1] - d.cell_start[c2];
-      }
-      int inc = cntk;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(FULL_MASK, inc, o);
-        if (lane >= o) inc += y;
-      }
-      if (lane < 27) s_pre[lane + 1] = inc;
-      if (lane == 0) s_pre[0] = 0;
-    }
-    __syncthreads();
-    const int total = s_pre[27];
-    if (total <= BUILD_MAXC) {
-      for (int idx = threadIdx.x; idx < total; idx += BUILD_THREADS) {
-        int k = 0;
-#pragma unroll
-        for (int step = 16; step > 0; step >>= 1)
-          if (k + step < 27 && s_pre[k + step] <= idx) k += step;
-        const int j = d.cell_start[s_cell[k]] + (idx - s_pre[k]);
-        float4 r = d.rel[j];
-        r.x += s_off[k][0]; r.y += s_off[k][1]; r.z += s_off[k][2];
-        s_rel[idx] = r;
-        s_word[idx] = (uint32_t)j | (s_code[k] << CODE_SHIFT);
-        s_img[idx] = s_sc[k];
-      }
-      __syncthreads();
-      // NA home atoms per warp: every staged candidate read serves all of them
-      constexpr int NA = 4;
-      const unsigned lt = (1u << lane) - 1u;
-      const int cap = d.cap;
-      for (int i0 = hs + NA * warp; i0 < he; i0 += NA * nwarps) {
-        int ii[NA], cnt[NA];
-        bool has[NA];
-        float4 rr[NA];
-        uint32_t *row[NA];
-#pragma unroll
-        for (int u = 0; u < NA; ++u) {
-          has[u] = i0 + u < he;
-          ii[u] = has[u] ? i0 + u : i0;
-          rr[u] = d.rel[ii[u]];
-          row[u] = d.nbr + (size_t)ii[u] * cap;
-          cnt[u] = 0;
-        }
-        for (int base = 0; base < total; base += 32) {
-          const int idx = base + lane;
-          const bool valid = idx < total;
-          const int sidx = valid ? idx : total - 1;  // in-range read; the lane is masked below
-          const float4 c = s_rel[sidx];
-          const uint32_t w = s_word[sidx];
-          const bool zero_img = s_img[sidx] == CODE_ZERO;
-          const int j = (int)(w & IDX_MASK);
-          bool hit[NA], band[NA], any_band = false;
-#pragma unroll
-          for (int u = 0; u < NA; ++u) {
-            const float ax = c.x - rr[u].x, ay = c.y - rr[u].y, az = c.z - rr[u].z;
-            const float q = ax * ax + ay * ay + az * az;
-            const bool ok = valid & has[u] & !((j == ii[u]) & zero_img);
-            hit[u] = ok & (q < b.ce2_lo);
-            band[u] = ok & (q >= b.ce2_lo) & (q <= b.ce2_hi);
-            any_band |= band[u];
-          }
-          if (__ballot_sync(FULL_MASK, any_band)) {  // rare: exact FP64 predicate
-#pragma unroll
-            for (int u = 0; u < NA; ++u)
-              if (band[u]) hit[u] = exact_pair(d, b, ii[u], j, s_img[sidx]);
-          }
-#pragma unroll
-          for (int u = 0; u < NA; ++u) {
-            const unsigned bal = __ballot_sync(FULL_MASK, hit[u]);
-            if (hit[u]) {
-              const int q = cnt[u] + __popc(bal & lt);
-              if (q < cap) row[u][q] = w;
-            }
-            cnt[u] += __popc(bal);
-          }
-        }
-        if (lane == 0) {
-#pragma unroll
-          for (int u = 0; u < NA; ++u)
-            if (has[u]) {
-              finish_atom(d, ii[u], cnt[u]);
-              wmax = max(wmax, cnt[u]);
-            }
-        }
-      }
-    } else {
-      for (int i = hs + warp; i < he; i += nwarps) wmax = max(wmax, build_atom_global(d, b, i, mode));
-    }
-    __syncthreads();  // the stage is reused by the next cell
-  }
-  // one atomic per warp for the largest list length (not one per atom)
-  if (lane == 0 && wmax > 0) atomicMax(&d.flags[F_MAXNB], wmax);
-  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&d.flags[F_REBUILDS], 1);
+  return r2 < ce2;
 }
 
 // One warp per home cell, one lane per home atom (cells of more than 32 atoms
@@ -519,31 +356,35 @@ __global__ void __launch_bounds__(BUILD_THREADS) k_build_cell(Dev d, Box b, int 
 // lane's own row, so the list keeps the stencil order (deterministic) and no
 // ballot or barrier is needed.
 __global__ void __launch_bounds__(256) k_build_warp(Dev d, Box b, int mode, int forced) {
-  if (rebuild_off(d, forced)) return;
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
   const int cap = d.cap;
+  const int cshift = 7 - log2_pow2(d.tpa);  // chunk stride 4A words = 2^(log2 A + 2)
   int wmax = 0;
-  for (int cell = gw; cell < b.ncell; cell += nw) {
+  for (int cell = gw; cell < b.ncell_all; cell += nw) {
+    const int rep = rep_of_cell(b, cell);
+    if (rep < 0 || !rebuild_on(b, rep, forced)) continue;
+    const RepBox &rb = repbox(b, rep);
+    const int lc = cell - rb.cell_off;
+    if (lc >= rb.ncell) continue;  // the padding cell
     const int hs = d.cell_start[cell], he = d.cell_start[cell + 1];
-    const int cx = cell % b.nc[0], cy = (cell / b.nc[0]) % b.nc[1], cz = cell / (b.nc[0] * b.nc[1]);
+    const int cx = lc % rb.nc[0], cy = (lc / rb.nc[0]) % rb.nc[1], cz = lc / (rb.nc[0] * rb.nc[1]);
     for (int i0 = hs; i0 < he; i0 += 32) {
       const int i = i0 + lane;
       const bool act = i < he;
       const float4 ri = act ? d.rel[i] : make_float4(1e18f, 1e18f, 1e18f, 0.f);
       uint32_t *row = d.nbr + nbr_block_base(act ? i : hs, cap, d.tpa);
-      const int cshift = 7 - log2_pow2(d.tpa);  // chunk stride 4A words = 2^(as+2)
       int cnt = 0;
       for (int k = 0; k < 27; ++k) {
         const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
         int nx = cx + dx, ny = cy + dy, nz = cz + dz, sx = 0, sy = 0, sz = 0;
-        if (nx < 0) { nx += b.nc[0]; sx = -1; } else if (nx >= b.nc[0]) { nx -= b.nc[0]; sx = 1; }
-        if (ny < 0) { ny += b.nc[1]; sy = -1; } else if (ny >= b.nc[1]) { ny -= b.nc[1]; sy = 1; }
-        if (nz < 0) { nz += b.nc[2]; sz = -1; } else if (nz >= b.nc[2]) { nz -= b.nc[2]; sz = 1; }
-        const int c2 = nx + b.nc[0] * (ny + b.nc[1] * nz);
+        if (nx < 0) { nx += rb.nc[0]; sx = -1; } else if (nx >= rb.nc[0]) { nx -= rb.nc[0]; sx = 1; }
+        if (ny < 0) { ny += rb.nc[1]; sy = -1; } else if (ny >= rb.nc[1]) { ny -= rb.nc[1]; sy = 1; }
+        if (nz < 0) { nz += rb.nc[2]; sz = -1; } else if (nz >= rb.nc[2]) { nz -= rb.nc[2]; sz = 1; }
+        const int c2 = rb.cell_off + nx + rb.nc[0] * (ny + rb.nc[1] * nz);
         const int img = image_code(sx, sy, sz);
         const uint32_t code = (uint32_t)(mode == 0 ? img : k) << CODE_SHIFT;
-        const float ox = dx * b.wf[0] - ri.x, oy = dy * b.wf[1] - ri.y, oz = dz * b.wf[2] - ri.z;
+        const float ox = dx * rb.wf[0] - ri.x, oy = dy * rb.wf[1] - ri.y, oz = dz * rb.wf[2] - ri.z;
         const int jb = d.cell_start[c2], je = d.cell_start[c2 + 1];
         const int self = (img == CODE_ZERO && act) ? i : -1;  // the home atom itself is not a neighbour
         const float lo = act ? b.ce2_lo : -1.0f;               // idle lanes never hit
@@ -553,35 +394,52 @@ __global__ void __launch_bounds__(256) k_build_warp(Dev d, Box b, int mode, int 
           const float q = fx * fx + fy * fy + fz * fz;
           bool hit = (q < lo) & (j != self);
           if (__any_sync(FULL_MASK, (q >= lo) & (q <= b.ce2_hi) & act)) {  // rare: exact FP64 predicate
-            if ((q >= lo) & (q <= b.ce2_hi) & act & (j != self)) hit = exact_pair(d, b, i, j, img);
+            if ((q >= lo) & (q <= b.ce2_hi) & act & (j != self)) hit = exact_pair(d, rb, b.ce2, i, j, img);
           }
           if (hit & (cnt < cap)) row[((cnt >> 2) << cshift) + (cnt & 3)] = (uint32_t)j | code;
           cnt += hit;
         }
       }
       if (act) {
-        finish_atom(d, i, cnt);
+        d.nnbr[i] = min(cnt, cap);
+        if (cnt > cap) atomicMax(&d.flags[F_OVERFLOW], cnt);
         wmax = max(wmax, cnt);
       }
     }
   }
+  // one atomic per warp for the largest list length (not one per atom)
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(FULL_MASK, wmax, o));
   if (lane == 0 && wmax > 0) atomicMax(&d.flags[F_MAXNB], wmax);
-  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&d.flags[F_REBUILDS], 1);
 }
 
-__global__ void k_clear_rebuild_flag(Dev d) { d.flags[F_REBUILD] = 0; }
+// after the build: count the rebuilt replicas, clear their flags and the global one
+__global__ void __launch_bounds__(256) k_finish_rebuild(Dev d, Box b, int forced) {
+  __shared__ int total;
+  if (threadIdx.x == 0) total = 0;
+  __syncthreads();
+  int n = 0;
+  for (int r = threadIdx.x; r < b.nrep; r += blockDim.x) {
+    n += rebuild_on(b, r, forced) ? 1 : 0;
+    b.rep_flag[r] = 0;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(FULL_MASK, n, o);
+  if ((threadIdx.x & 31) == 0 && n) atomicAdd_block(&total, n);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (total) {
+      d.flags[F_REBUILDS] += total;
+      d.flags[F_PASSES] += 1;
+    }
+    d.flags[F_REBUILD] = 0;
+  }
+}
 
 // Inside a captured step: the half-skin flag becomes the value of the graph's
 // conditional node that wraps the rebuild kernels.
 __global__ void k_set_rebuild_cond(Dev d, cudaGraphConditionalHandle h) {
   cudaGraphSetConditional(h, d.flags[F_REBUILD] != 0 ? 1u : 0u);
-}
-
-int launch_set_rebuild_cond(const Dev &d, cudaGraphConditionalHandle h, cudaStream_t st) {
-  k_set_rebuild_cond<<<1, 1, 0, st>>>(d, h);
-  return cudaPeekAtLastError() == cudaSuccess ? CAVGPU_OK : CAVGPU_E_CUDA;
 }
 
 // ---------------------------------------------------------------------------
@@ -590,6 +448,20 @@ int launch_set_rebuild_cond(const Dev &d, cudaGraphConditionalHandle h, cudaStre
 //  src/atom_data/kinetic_energy.cpp:26-134, 189-198, 238-303)
 // thermo[] = {KE, T, P, virial, PE, sum m, -, -}
 // ---------------------------------------------------------------------------
+__device__ inline void thermo_finish(double ke2, const double P3[3], double msum, double vir2, double pe2, int natoms,
+                                     int n_r_df, double k_b, double volume, int langevin, double *out) {
+  if (n_r_df >= 1 && n_r_df <= 3 && msum > 0) ke2 -= (P3[0] * P3[0] + P3[1] * P3[1] + P3[2] * P3[2]) / msum;
+  const double ke = 0.5 * ke2;
+  const int dof = 3 * natoms - n_r_df;
+  const double T = 2.0 * ke / (k_b * dof);
+  const double vir = 0.5 * vir2;  // each pair was visited from both sides
+  out[0] = ke;
+  out[1] = T;
+  out[2] = ((double)natoms * k_b * T) / volume + (langevin ? 0.0 : vir) / (3.0 * volume);
+  out[3] = vir;
+  out[4] = 0.5 * pe2;
+}
+
 __global__ void __launch_bounds__(256) k_thermo_final(Dev d, ThermoCfg tc, int nb_ke, int nb_ev, int ring_slot) {
   double v[6] = {0, 0, 0, 0, 0, 0};
   for (int k = threadIdx.x; k < nb_ke; k += blockDim.x)
@@ -603,26 +475,56 @@ __global__ void __launch_bounds__(256) k_thermo_final(Dev d, ThermoCfg tc, int n
   block_sum_store<6>(v, out);
   __syncthreads();
   if (threadIdx.x == 0) {
-    double msum = 0.0;
-    const PairTab &t = *d.tab;
-    // total mass from per-type counts is not tracked; KE with n_r_df in 1..3 uses
-    // sum m v^2 - |P|^2 / M with M computed once on the host (stored in thermo[5])
-    msum = d.thermo[5];
-    double ke2 = out[0];
-    if (tc.n_r_df >= 1 && tc.n_r_df <= 3 && msum > 0)
-      ke2 -= (out[1] * out[1] + out[2] * out[2] + out[3] * out[3]) / msum;
-    const double ke = 0.5 * ke2;
-    const int dof = 3 * tc.n - tc.n_r_df;
-    const double T = 2.0 * ke / (tc.k_b * dof);
-    const double vir = 0.5 * out[4];  // each pair was visited from both sides
-    const double pe = 0.5 * out[5];
-    const double P = ((double)tc.n * tc.k_b * T) / tc.volume + (tc.langevin ? 0.0 : vir) / (3.0 * tc.volume);
-    d.thermo[0] = ke; d.thermo[1] = T; d.thermo[2] = P; d.thermo[3] = vir; d.thermo[4] = pe;
+    double res[5];
+    const double P3[3] = {out[1], out[2], out[3]};
+    // total mass is fixed at upload (thermo[5])
+    thermo_finish(out[0], P3, d.thermo[5], out[4], out[5], tc.n, tc.n_r_df, tc.k_b, tc.volume, tc.langevin, res);
+    for (int q = 0; q < 5; ++q) d.thermo[q] = res[q];
     if (ring_slot >= 0) {
       double *r = d.thermo_ring + (size_t)ring_slot * THERMO_REC;
-      r[0] = ke; r[1] = T; r[2] = P; r[3] = vir; r[4] = pe;
+      for (int q = 0; q < THERMO_REC; ++q) r[q] = res[q];
     }
-    (void)t;
+  }
+}
+
+// Batches: one block per replica folds its slots in a fixed order.  ke: KE/T/P
+// from the current velocities; ev: virial and PE from the per-slot sums the
+// force kernel wrote (VV: P gets the virial term).  thermo_rep[r*8 + 0..5].
+__global__ void __launch_bounds__(256) k_thermo_rep(Dev d, Box b, ThermoCfg tc, int ke, int ev) {
+  const int rep = blockIdx.x;
+  const RepBox &rb = repbox(b, rep);
+  double v[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (int i = rb.slot_off + threadIdx.x; i < rb.slot_off + rb.natoms; i += blockDim.x) {
+    if (ke) {
+      const dbl4 vv = d.vel[i];
+      const double m = d.tab->mass[d.type[i]];
+      v[0] += m * (vv.x * vv.x + vv.y * vv.y + vv.z * vv.z);
+      v[1] += m * vv.x; v[2] += m * vv.y; v[3] += m * vv.z;
+      v[4] += m;
+    }
+    if (ev) {
+      const double2 e = d.ev_atom[i];
+      v[5] += e.x;
+      v[6] += e.y;
+    }
+  }
+  __shared__ double out[7];
+  block_sum_store<7>(v, out);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double *o = d.thermo_rep + (size_t)rep * 8;
+    const double volume = rb.L[0] * rb.L[1] * rb.L[2];
+    if (ke) {
+      double res[5];
+      const double P3[3] = {out[1], out[2], out[3]};
+      thermo_finish(out[0], P3, out[4], 0.0, 0.0, rb.natoms, tc.n_r_df, tc.k_b, volume, 1, res);
+      o[0] = res[0]; o[1] = res[1]; o[2] = res[2]; o[5] = out[4];
+    }
+    if (ev) {
+      o[3] = 0.5 * out[5];
+      o[4] = 0.5 * out[6];
+      if (!tc.langevin) o[2] += o[3] / (3.0 * volume);
+    }
   }
 }
 
@@ -632,25 +534,30 @@ __global__ void k_advance_step(Dev d, int nsteps) { *d.step_base += nsteps; }
 // parity exports
 // ---------------------------------------------------------------------------
 // what: 0 = positions (wrapped as Domain::fix_position), 1 = velocities, 2 = accelerations
-__global__ void __launch_bounds__(256) k_to_host_order(Dev d, Box b, int n, int what) {
+__global__ void __launch_bounds__(256) k_to_host_order(Dev d, Box b, int what) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
+  if (k >= b.nslot) return;
+  const int rep = rep_of_slot(b, k);
+  if (rep < 0) return;
   dbl4 v = what == 0 ? d.pos[k] : (what == 1 ? d.vel[k] : d.acc[k]);
+  const RepBox &rb = repbox(b, rep);
   if (what == 0) {
-    if (v.x < b.lo[0]) v.x += b.L[0]; else if (v.x > b.hi[0]) v.x -= b.L[0];
-    if (v.y < b.lo[1]) v.y += b.L[1]; else if (v.y > b.hi[1]) v.y -= b.L[1];
-    if (v.z < b.lo[2]) v.z += b.L[2]; else if (v.z > b.hi[2]) v.z -= b.L[2];
+    if (v.x < rb.lo[0]) v.x += rb.L[0]; else if (v.x > rb.hi[0]) v.x -= rb.L[0];
+    if (v.y < rb.lo[1]) v.y += rb.L[1]; else if (v.y > rb.hi[1]) v.y -= rb.L[1];
+    if (v.z < rb.lo[2]) v.z += rb.L[2]; else if (v.z > rb.hi[2]) v.z -= rb.L[2];
   }
-  const size_t h = (size_t)d.id[k] * 3;
+  const size_t h = ((size_t)rb.id_off + d.id[k]) * 3;
   d.h3[h] = v.x; d.h3[h + 1] = v.y; d.h3[h + 2] = v.z;
 }
 
-__global__ void __launch_bounds__(256) k_export_pairs(Dev d, Box b, int n, int mode, int32_t *rows,
+// canonical rows (id_i, id_j, sx, sy, sz) of the current list (single system)
+__global__ void __launch_bounds__(256) k_export_pairs(Dev d, Box b, int mode, int32_t *rows,
                                                       unsigned long long *counter, long long cap) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int ci = d.cell_of[i];
-  const int c3[3] = {ci % b.nc[0], (ci / b.nc[0]) % b.nc[1], ci / (b.nc[0] * b.nc[1])};
+  if (i >= b.nslot) return;
+  const RepBox &rb = b.r0;
+  const int ci = d.cell_of[i] - rb.cell_off;
+  const int c3[3] = {ci % rb.nc[0], (ci / rb.nc[0]) % rb.nc[1], ci / (rb.nc[0] * rb.nc[1])};
   const int nn = d.nnbr[i];
   for (int k = 0; k < nn; ++k) {
     const uint32_t e = d.nbr[nbr_index(i, k, d.cap, d.tpa)];
@@ -659,7 +566,7 @@ __global__ void __launch_bounds__(256) k_export_pairs(Dev d, Box b, int n, int m
     if (mode == 1)  // cell-offset code -> image shift
       for (int q = 0; q < 3; ++q) {
         const int c = c3[q] + s[q];
-        s[q] = c < 0 ? -1 : (c >= b.nc[q] ? 1 : 0);
+        s[q] = c < 0 ? -1 : (c >= rb.nc[q] ? 1 : 0);
       }
     const unsigned long long r = atomicAdd(counter, 1ull);
     if ((long long)r < cap) {
@@ -735,6 +642,43 @@ __global__ void __launch_bounds__(256) k_ghost_emit(Dev d, int n, GhostCfg g, co
   }
 }
 
+// exclusive scan of counts[0..m) into starts[0..m] (ghost export; one block)
+__global__ void __launch_bounds__(1024) k_scan_plain(const int *count, int *start, int m) {
+  __shared__ int warp_tot[32];
+  __shared__ int carry_s;
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  if (t == 0) carry_s = 0;
+  __syncthreads();
+  for (int base = 0; base < m; base += 1024) {
+    const int k = base + t;
+    const int s = k < m ? count[k] : 0;
+    int inc = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(FULL_MASK, inc, o);
+      if (lane >= o) inc += y;
+    }
+    if (lane == 31) warp_tot[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+      int wv = warp_tot[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL_MASK, wv, o);
+        if (lane >= o) wv += y;
+      }
+      warp_tot[lane] = wv;
+    }
+    __syncthreads();
+    const int run = carry_s + inc - s + (wid ? warp_tot[wid - 1] : 0);
+    if (k < m) start[k] = run;
+    __syncthreads();
+    if (t == 1023) carry_s = run + s;
+    __syncthreads();
+  }
+  if (t == 0) start[m] = carry_s;
+}
+
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
@@ -762,17 +706,22 @@ int launch_drift(const Dev &d, const Box &b, const StepConsts &sc, const LaunchC
 }
 
 int launch_rebuild(const Dev &d, const Box &b, const LaunchCfg &lc, int forced, cudaStream_t st) {
-  const int n = lc.n, g = ceil_div(n, 256);
-  k_bin<<<g, 256, 0, st>>>(d, b, n, forced);
-  k_scan<<<1, 1024, 0, st>>>(d, d.cell_count, d.cell_start, d.cell_cursor, b.ncell, forced);
-  k_scatter<<<g, 256, 0, st>>>(d, n, forced);
-  k_cell_sort<<<ceil_div((long long)b.ncell * 32, 256), 256, 0, st>>>(d, b.ncell, forced);
-  k_copy_state<<<g, 256, 0, st>>>(d, n, forced);
-  k_gather<<<g, 256, 0, st>>>(d, b, n, forced);
+  const int g = ceil_div(b.nslot, 256);
+  k_bin<<<g, 256, 0, st>>>(d, b, forced);
+  k_scan_rep<<<b.nrep, 1024, 0, st>>>(d, b, forced);
+  k_scatter<<<g, 256, 0, st>>>(d, b, forced);
+  k_cell_sort<<<ceil_div((long long)b.ncell_all * 32, 256), 256, 0, st>>>(d, b, forced);
+  k_copy_state<<<g, 256, 0, st>>>(d, b, forced);
+  k_gather<<<g, 256, 0, st>>>(d, b, forced);
   const int mode = lc.precision == CAVGPU_MIXED ? 1 : 0;
-  const int build_grid = std::min(ceil_div((long long)b.ncell * 32, 256), num_sms() * 8);
+  const int build_grid = std::min(ceil_div((long long)b.ncell_all * 32, 256), num_sms() * 8);
   k_build_warp<<<build_grid, 256, 0, st>>>(d, b, mode, forced);
-  k_clear_rebuild_flag<<<1, 1, 0, st>>>(d);
+  k_finish_rebuild<<<1, 256, 0, st>>>(d, b, forced);
+  return chk();
+}
+
+int launch_set_rebuild_cond(const Dev &d, cudaGraphConditionalHandle h, cudaStream_t st) {
+  k_set_rebuild_cond<<<1, 1, 0, st>>>(d, h);
   return chk();
 }
 
@@ -781,19 +730,24 @@ int launch_thermo_final(const Dev &d, const ThermoCfg &tc, int nb_ke, int nb_ev,
   return chk();
 }
 
+int launch_thermo_replicas(const Dev &d, const Box &b, const ThermoCfg &tc, int ke, int ev, cudaStream_t st) {
+  k_thermo_rep<<<b.nrep, 256, 0, st>>>(d, b, tc, ke, ev);
+  return chk();
+}
+
 int launch_advance_step(const Dev &d, int nsteps, cudaStream_t st) {
   k_advance_step<<<1, 1, 0, st>>>(d, nsteps);
   return chk();
 }
 
-int launch_to_host_order(const Dev &d, const Box &b, int n, int what, cudaStream_t st) {
-  k_to_host_order<<<ceil_div(n, 256), 256, 0, st>>>(d, b, n, what);
+int launch_to_host_order(const Dev &d, const Box &b, int what, cudaStream_t st) {
+  k_to_host_order<<<ceil_div(b.nslot, 256), 256, 0, st>>>(d, b, what);
   return chk();
 }
 
-int launch_export_pairs(const Dev &d, const Box &b, int n, int mode, int32_t *rows, unsigned long long *counter,
+int launch_export_pairs(const Dev &d, const Box &b, int mode, int32_t *rows, unsigned long long *counter,
                         int64_t cap, cudaStream_t st) {
-  k_export_pairs<<<ceil_div(n, 256), 256, 0, st>>>(d, b, n, mode, rows, counter, (long long)cap);
+  k_export_pairs<<<ceil_div(b.nslot, 256), 256, 0, st>>>(d, b, mode, rows, counter, (long long)cap);
   return chk();
 }
 
@@ -812,15 +766,15 @@ int launch_ghosts(const Dev &d, const Box &b, int n, double gc, int *counts, int
   GhostCfg g;
   RefBins rb;
   for (int a = 0; a < 3; ++a) {
-    g.llow[a] = b.lo[a] + gc;
-    g.lupp[a] = b.hi[a] - gc;
-    g.L[a] = b.L[a];
+    g.llow[a] = b.r0.lo[a] + gc;
+    g.lupp[a] = b.r0.hi[a] - gc;
+    g.L[a] = b.r0.L[a];
     rb.lo[a] = lo_local[a];
     rb.nb[a] = nb[a];
   }
   rb.inv = cutoff_inv;
   k_ghost_count<<<ceil_div(n, 256), 256, 0, st>>>(d, n, g, counts);
-  k_scan<<<1, 1024, 0, st>>>(d, counts, starts, nullptr, n, 1);
+  k_scan_plain<<<1, 1024, 0, st>>>(counts, starts, n);
   k_ghost_emit<<<ceil_div(n, 256), 256, 0, st>>>(d, n, g, starts, src, shift3, pos3, bins3, (long long)cap, rb);
   return chk();
 }

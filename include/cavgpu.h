@@ -75,8 +75,8 @@ typedef struct cavgpu_params {
   int32_t precision;              /* CAVGPU_FP64 or CAVGPU_MIXED */
   int32_t noise_off;              /* Langevin with eta = 0 (exactness checks) */
   int32_t nbr_capacity;           /* neighbour slots per atom; 0 = sized at set-up */
-  int32_t threads_per_atom;       /* force kernel lanes per atom (1,2,4,8,16,32); 0 = tuned */
-  int32_t block_size;             /* force kernel block size; 0 = tuned */
+  int32_t threads_per_atom;       /* force kernel lanes per atom (1,2,4,8,16); 0 = default */
+  int32_t block_size;             /* force kernel block size (32..256, multiple of 32); 0 = default */
   int32_t steps_per_graph;        /* steps captured per CUDA graph; 0 = default */
 } cavgpu_params;
 
@@ -181,6 +181,30 @@ const char *cavgpu_last_cuda_error(void);
  * the array: two calls that overlap on the GPU race. */
 int cavgpu_kinetic_energy_noalloc(int64_t n, const double *vel3, const uint64_t *type, const double *mass,
                                   int32_t ntypes, int32_t n_r_df, double k_b, double *out2, void *stream);
+
+/* ---- batches of independent replicas (no counterpart in the reference: one
+ * CAVIAR2 process runs one Md_simulator; a batch is R of them in one context,
+ * each with its own periodic box, atom count, cell grid and half-skin rebuild,
+ * sharing params, pair table and integrator).  A batch advances with
+ * cavgpu_step / cavgpu_run(every = 0) and each replica's trajectory equals that
+ * of its own single-system context in FP64 form.  The single-system exports
+ * (pairs, bins, ghosts) and cavgpu_thermo refuse batches (CAVGPU_E_ARG). */
+
+/* Create a batch of nrep >= 1 replicas; replica r's box is [lo3[3r..3r+2],
+ * hi3[3r..3r+2]) (p->lo / p->hi are ignored); each edge >= 2 (nl_cutoff * nl_coef). */
+int cavgpu_create_batch(const cavgpu_params *p, int32_t nrep, const double *lo3, const double *hi3,
+                        cavgpu_ctx **out);
+
+/* Upload counts[r] >= 1 atoms per replica, concatenated in replica order
+ * (pos3/vel3: 3 doubles per atom; vel3 may be NULL; type: uint64 per atom).
+ * download returns the atoms in the same concatenated order. */
+int cavgpu_upload_batch(cavgpu_ctx *ctx, const int64_t *counts, const double *pos3, const double *vel3,
+                        const uint64_t *type);
+
+/* Per-replica thermo of the last thermo point: out6[6r + {0..5}] = {KE, T, P,
+ * virialForce, PE, total mass} (Atom_data::kinetic_energy / temperature /
+ * pressure of replica r alone). */
+int cavgpu_thermo_batch(cavgpu_ctx *ctx, double *out6);
 
 /* Diagnostic (no counterpart in the reference): measured FMA throughput of the
  * current device, out2 = {FP64 TFLOP/s, FP32 TFLOP/s}, for roofline denominators. */
