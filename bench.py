@@ -45,6 +45,7 @@ def parse():
     ap.add_argument("--cells", type=int, default=64, help="FCC cells per edge (64 -> 1,048,576 atoms)")
     ap.add_argument("--drift-steps", type=int, default=20000)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-extra", action="store_true", help="skip the batched and Langevin configurations")
     return ap.parse_args()
 
 
@@ -181,10 +182,12 @@ def measured_peaks():
         return {}
 
 
-def time_device(cavgpu, torch, pos, vel, typ, params, precision, steps, warmup, ws, sampler_id):
-    """Device-resident timing: events on the context's stream around K steps."""
+def time_device(cavgpu, torch, pos, vel, typ, params, precision, steps, warmup, ws, sampler_id, tune=True):
+    """Device-resident timing: events on the context's stream around K steps
+    (launch shape chosen by cavgpu_autotune first, outside the timed region)."""
     s = cavgpu.System(pos, vel, typ, params, precision=precision)
     s.setup()
+    choice = s.autotune(trial_steps=30) if tune else None
     s.step(warmup)
     stream = torch.cuda.ExternalStream(s.stream())
     s.set_profiling(True)
@@ -206,8 +209,84 @@ def time_device(cavgpu, torch, pos, vel, typ, params, precision, steps, warmup, 
     out = dict(ms=ms, force_ms=force_ms, force_launches=nlaunch, rebuilds=st1["rebuilds"] - st0["rebuilds"],
                kernel_launches=st1["kernel_launches"] - st0["kernel_launches"], nbar=nbar,
                clocks=cs.summary(), tpa=st1["threads_per_atom"], block=st1["block_size"],
-               capacity=st1["capacity"])
+               capacity=st1["capacity"], autotune=choice)
     return s, out
+
+
+def time_batch(cavgpu, torch, systems, params, precision, steps, warmup, trial_steps):
+    """A batch of replicas, device-resident: autotune, warm-up, K timed steps.
+    Returns throughput over all replicas and the per-replica thermo after the run."""
+    b = cavgpu.Batch(systems, params, precision=precision)
+    b.setup()
+    choice = b.autotune(trial_steps=trial_steps)
+    b.step(warmup)
+    stream = torch.cuda.ExternalStream(b.stream())
+    b.set_profiling(True)
+    st0 = b.stats()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    b.step(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    st1 = b.stats()
+    nl, fms = b.read_profile()
+    th = b.thermo_batch()
+    out = dict(value=b.n * steps / (ms * 1e-3), ms_per_step=ms / steps, steps=steps, warmup=warmup,
+               atoms=b.n, replicas=b.nrep, force_ms_per_launch=fms / max(nl, 1),
+               replica_rebuilds=st1["rebuilds"] - st0["rebuilds"],
+               gpu_launches=st1["kernel_launches"] - st0["kernel_launches"], autotune=choice)
+    b.close()
+    return out, th
+
+
+def extra_workloads(cavgpu, torch, W, np, single_mixed):
+    """The other benchmark configurations, each timed on this GPU beside the headline:
+    4096 uneven replicas (mixed and FP64), 64 Kob-Andersen replicas (mixed Langevin)
+    and the 4,194,304-atom Langevin fluid (mixed and FP64)."""
+    res = {}
+    sets = W.replica_set(4096)
+    systems = [(p, v, np.zeros(len(p), np.int32), np.zeros(3), b) for p, v, b, _, _ in sets]
+    params = W.lj_params(systems[0][4])
+    m, _ = time_batch(cavgpu, torch, systems, params, cavgpu.MIXED, 200, 20, 10)
+    f, _ = time_batch(cavgpu, torch, systems, params, cavgpu.FP64, 20, 3, 4)
+    res["replicas_4096"] = {
+        "workload": "4096 periodic LJ replicas, N_r ~ U[256, 8192], rho_r ~ U[0.6, 1.0], T_r ~ U[0.7, 2.0], "
+                    "random FCC fill + N(0, 0.05) displacement, rc 2.5, skin 0.3, dt 0.005, NVE",
+        "mixed": m, "fp64": f, "mixed_over_single_system_mixed": m["value"] / single_mixed}
+    del systems, sets
+    systems = []
+    for r in range(64):
+        pos, vel, typ, p = W.kob_andersen(n=32768, seed=1005 + r)
+        systems.append((pos, vel, typ, np.zeros(3), p["hi"]))
+    params = W.kob_andersen(n=32768, seed=1005)[3]
+    k, th = time_batch(cavgpu, torch, systems, params, cavgpu.MIXED, 400, 20, 20)
+    k["mean_T_over_replicas"] = float(th[:, 1].mean())
+    res["kob_andersen_64x32768"] = {
+        "workload": "64 replicas x 32768 atoms, Kob-Andersen 80:20, rho 1.2, Langevin T 0.45 gamma 1, dt 0.003",
+        "mixed": k}
+    del systems
+    pos, vel, typ, params = W.config_langevin()
+    lang = {"workload": "Langevin LJ fluid, 4,194,304 atoms (128x128x64 FCC cells), T 1.0, gamma 1, skin 0.4"}
+    for prec, name, steps in ((cavgpu.MIXED, "mixed", 400), (cavgpu.FP64, "fp64", 40)):
+        s = cavgpu.System(pos, vel, typ, params, precision=prec)
+        s.setup()
+        s.autotune(trial_steps=10)
+        s.step(10)
+        stream = torch.cuda.ExternalStream(s.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        s.step(steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        lang[name] = {"value": len(pos) * steps / (ms * 1e-3), "ms_per_step": ms / steps, "steps": steps,
+                      "T_end": s.thermo()["temperature"]}
+        s.close()
+    res["langevin_4M"] = lang
+    return res
 
 
 def nve_drift(cavgpu, pos, vel, typ, params, precision, steps, every=100):
@@ -224,7 +303,7 @@ def nve_drift(cavgpu, pos, vel, typ, params, precision, steps, every=100):
     return float(abs(slope) * 1e6 / abs(e[0])), float(abs(e[-1] - e[0]) / abs(e[0]))
 
 
-def time_e2e(cavgpu, torch, pos, vel, typ, params, precision, steps):
+def time_e2e(cavgpu, torch, pos, vel, typ, params, precision, steps, **launch):
     """Through the C ABI with host buffers: pinned host arrays -> upload -> set-up ->
     K steps (thermo of every step read back) -> download of the final state."""
     import numpy as np
@@ -241,7 +320,7 @@ def time_e2e(cavgpu, torch, pos, vel, typ, params, precision, steps):
     oa = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    s = cavgpu.System(hp, hv, ht.view(np.uint64), params, precision=precision)
+    s = cavgpu.System(hp, hv, ht.view(np.uint64), params, precision=precision, **launch)
     s.setup()
     thermo = np.zeros((steps, 5))
     rc = cavgpu.lib().cavgpu_run(s._h, steps, 1, cavgpu._ptr(thermo))
@@ -323,7 +402,9 @@ def main():
     drift_m, dE_m = nve_drift(cavgpu, p_eq, v_eq, typ, params, cavgpu.MIXED, args.drift_steps)
     drift_64, dE_64 = nve_drift(cavgpu, p_eq, v_eq, typ, params, cavgpu.FP64, d64)
 
-    e2e_rate, h2d, d2h = time_e2e(cavgpu, torch, pos, vel, typ, params, cavgpu.MIXED, args.steps)
+    tuned = rm["autotune"] or {}
+    e2e_rate, h2d, d2h = time_e2e(cavgpu, torch, pos, vel, typ, params, cavgpu.MIXED, args.steps,
+                                  tpa=rm["tpa"], block=rm["block"], steps_per_graph=tuned.get("steps_per_graph", 0))
     e2e_rate = ws * n * args.steps / max_over_ranks(ws, n * args.steps / e2e_rate)
 
     # roofline of the dominant kernel (mixed force kernel): algorithmic bytes per launch
@@ -343,6 +424,10 @@ def main():
     l64 = r64["force_ms"] / max(r64["force_launches"], 1)
     fp64_achieved = flops_atom * n / (l64 * 1e-3) / 1e12
 
+    extra = None
+    if rank == 0 and not args.no_extra:
+        extra = extra_workloads(cavgpu, torch, W, np, value / ws)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         rate, secs = cpu_reference_rate(pos, vel, typ, params, 3, 0)
@@ -355,7 +440,7 @@ def main():
     config.update({"fp64_value": value64, "mixed_over_fp64": value / value64, "fp64_steps": k64,
                    "rebuilds_in_timed_region": rm["rebuilds"], "mean_neighbours": rm["nbar"],
                    "threads_per_atom": rm["tpa"], "block": rm["block"], "capacity": rm["capacity"],
-                   "parallelism": f"replicas x{ws}"})
+                   "autotune": rm["autotune"], "parallelism": f"replicas x{ws}"})
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_mixed / args.steps, "higher_is_better": True,
@@ -381,6 +466,7 @@ def main():
         "gpu_launches": rm["kernel_launches"],
         "clocks": rm["clocks"],
         "peaks": {"fp64_tflops": fp64_peak, "fp32_tflops": fp32_peak},
+        "other_configs": extra,
     }
     print(json.dumps(line), flush=True)
 

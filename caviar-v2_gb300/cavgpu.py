@@ -75,6 +75,7 @@ _SIGS = {
                                       C.POINTER(C.c_void_p)]),
     "cavgpu_upload_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "cavgpu_thermo_batch": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "cavgpu_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),
 }
 
 
@@ -224,6 +225,12 @@ class System:
 
     def stream(self):
         return lib().cavgpu_stream(self._h)
+
+    def autotune(self, trial_steps=0, force=False):
+        """Choose the launch shape by timed trials (state restored afterwards)."""
+        o = np.zeros(4, np.int64)
+        self._check(lib().cavgpu_autotune(self._h, int(trial_steps), int(bool(force)), _ptr(o)), "autotune")
+        return dict(threads_per_atom=int(o[0]), block_size=int(o[1]), steps_per_graph=int(o[2]), trials=int(o[3]))
 
     def set_profiling(self, on):
         self._check(lib().cavgpu_set_profiling(self._h, int(on)), "set_profiling")

@@ -6,7 +6,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <new>
+#include <utility>
 #include <vector>
 
 #include "cav_common.cuh"
@@ -21,6 +23,21 @@ struct GraphEntry {
   int S, every, prof;
   cudaGraphExec_t exec;
 };
+
+// autotuner results, per process: a system of the same kind and size on the same
+// device reuses the launch shape measured for the first one
+struct TuneKey {
+  int dev, precision, integrator, nrep, natoms, ntypes;
+  bool operator==(const TuneKey &o) const {
+    return dev == o.dev && precision == o.precision && integrator == o.integrator && nrep == o.nrep &&
+           natoms == o.natoms && ntypes == o.ntypes;
+  }
+};
+struct TuneChoice {
+  int tpa, block, spg;
+};
+std::mutex g_tune_mu;
+std::vector<std::pair<TuneKey, TuneChoice>> g_tune_cache;
 
 }  // namespace
 
@@ -467,8 +484,18 @@ int upload_common(cavgpu_ctx *c, const int64_t *counts, const double *pos3, cons
   c->tc.volume = vol;
   c->tc.langevin = is_lang(c);
   Dev &d = c->d;
-  const size_t nblk = (size_t)std::max(force_grid_blocks(c->lc), 1);
+  // partial sums for the largest force grid of any launch shape (the autotuner
+  // changes the shape later) and for the drift grid
+  size_t nblk = 1;
+  for (int tpa = 1; tpa <= 16; tpa *= 2)
+    for (int blk = 32; blk <= 256; blk += 32) {
+      LaunchCfg t = c->lc;
+      t.tpa = tpa;
+      t.block = blk;
+      nblk = std::max(nblk, (size_t)force_grid_blocks(t));
+    }
   const size_t nblk_d = (size_t)std::max((NS + 255) / 256, 1);
+  d.partials_blocks = (int)nblk;
   int rc = CAVGPU_OK;
   dbl4 **d4[] = {&d.pos, &d.vel, &d.acc, &d.acc_old, &d.pos_ref, &d.t_pos, &d.t_vel, &d.t_acc, &d.t_acc_old};
   for (auto pp : d4) if (!rc) rc = dalloc(c, pp, NS);
@@ -675,7 +702,15 @@ int cavgpu_run(cavgpu_ctx *c, int64_t nsteps, int64_t every, double *out5) {
       chunks_since_check = 0;
     }
   }
-  // remaining steps eagerly
+  // rebuild kernels launched by the graphs' conditional nodes
+  auto count_graph_rebuilds = [&]() -> int {
+    int f[F_NWORDS];
+    RK(read_flags(c, f));
+    if (f[F_PASSES] > rebuilds_at_start) c->kernel_launches += (long long)REBUILD_KERNELS * (f[F_PASSES] - rebuilds_at_start);
+    return CAVGPU_OK;
+  };
+  if (done < nsteps) RK(count_graph_rebuilds());
+  // remaining steps eagerly (they count their own rebuild launches)
   while (done < nsteps) {
     const bool last = done == nsteps - 1;
     const bool th = (every > 0 && (done + 1) % every == 0) || (every == 0 && last);
@@ -694,17 +729,147 @@ int cavgpu_run(cavgpu_ctx *c, int64_t nsteps, int64_t every, double *out5) {
     c->steps_done += 1;
   }
   RK(check_status(c));
-  {
-    // rebuild kernels launched by the graphs' conditional nodes (eager steps counted theirs)
-    int f[F_NWORDS];
-    RK(read_flags(c, f));
-    if (eager_steps == 0 && f[F_PASSES] > rebuilds_at_start)
-      c->kernel_launches += (long long)REBUILD_KERNELS * (f[F_PASSES] - rebuilds_at_start);
-  }
+  if (eager_steps == 0) RK(count_graph_rebuilds());
   return CAVGPU_OK;
 }
 
 int cavgpu_step(cavgpu_ctx *c, int64_t nsteps) { return cavgpu_run(c, nsteps, 0, nullptr); }
+
+int cavgpu_autotune(cavgpu_ctx *c, int32_t trial_steps, int32_t flags, int64_t *out4) {
+  if (!c || trial_steps < 0) return CAVGPU_E_ARG;
+  if (!c->set_up) return CAVGPU_E_STATE;
+  const int T = trial_steps > 0 ? trial_steps : 40;
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  const TuneKey key{dev, c->p.precision, c->p.integrator, c->b.nrep, c->natoms, c->p.ntypes};
+  TuneChoice best{};
+  bool cached = false;
+  if (!(flags & CAVGPU_TUNE_FORCE)) {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    for (const auto &e : g_tune_cache)
+      if (e.first == key) { best = e.second; cached = true; }
+  }
+  // snapshot of the per-slot state and the step counters; trials run from it and
+  // the chosen shape restarts from it (a forced rebuild re-derives lists and cells)
+  const size_t NS = (size_t)c->b.nslot;
+  dbl4 *snap = nullptr;
+  int *snap_i = nullptr;
+  long long snap_step = 0;
+  int snap_flags[F_NWORDS];
+  double snap_thermo[8];
+  std::vector<double> snap_rep(c->d.thermo_rep ? 8 * (size_t)c->b.nrep : 0);
+  const long long steps0 = c->steps_done, graphs0 = c->graph_launches, kern0 = c->kernel_launches;
+  const bool prof0 = c->prof;
+  if (cudaMalloc(&snap, 4 * NS * sizeof(dbl4)) != cudaSuccess) { cudaGetLastError(); return CAVGPU_E_NOMEM; }
+  if (cudaMalloc(&snap_i, 2 * NS * sizeof(int)) != cudaSuccess) { cudaFree(snap); cudaGetLastError(); return CAVGPU_E_NOMEM; }
+  dbl4 *const src4[4] = {c->d.pos, c->d.vel, c->d.acc, c->d.acc_old};
+  int rc = CAVGPU_OK;
+  auto save = [&]() {
+    for (int k = 0; k < 4 && !rc; ++k)
+      rc = cuda_rc(cudaMemcpyAsync(snap + k * NS, src4[k], NS * sizeof(dbl4), cudaMemcpyDeviceToDevice, c->st));
+    if (!rc) rc = cuda_rc(cudaMemcpyAsync(snap_i, c->d.type, NS * sizeof(int), cudaMemcpyDeviceToDevice, c->st));
+    if (!rc) rc = cuda_rc(cudaMemcpyAsync(snap_i + NS, c->d.id, NS * sizeof(int), cudaMemcpyDeviceToDevice, c->st));
+    if (!rc) rc = cuda_rc(cudaMemcpyAsync(&snap_step, c->d.step_base, sizeof(long long), cudaMemcpyDeviceToHost, c->st));
+    if (!rc) rc = cuda_rc(cudaMemcpyAsync(snap_flags, c->d.flags, sizeof(snap_flags), cudaMemcpyDeviceToHost, c->st));
+    if (!rc) rc = cuda_rc(cudaMemcpyAsync(snap_thermo, c->d.thermo, sizeof(snap_thermo), cudaMemcpyDeviceToHost, c->st));
+    if (!rc && !snap_rep.empty())
+      rc = cuda_rc(cudaMemcpyAsync(snap_rep.data(), c->d.thermo_rep, snap_rep.size() * sizeof(double),
+                                   cudaMemcpyDeviceToHost, c->st));
+    if (!rc) rc = cuda_rc(cudaStreamSynchronize(c->st));
+  };
+  // back to the snapshot with launch shape (tpa, block): list storage for the shape,
+  // state copied back, forced rebuild
+  auto restore = [&](int tpa, int block) -> int {
+    c->lc.tpa = tpa;
+    c->lc.block = block;
+    c->d.tpa = tpa;
+    RK(alloc_nbr(c, c->d.cap));
+    for (int k = 0; k < 4; ++k)
+      CK(cudaMemcpyAsync(src4[k], snap + k * NS, NS * sizeof(dbl4), cudaMemcpyDeviceToDevice, c->st));
+    CK(cudaMemcpyAsync(c->d.type, snap_i, NS * sizeof(int), cudaMemcpyDeviceToDevice, c->st));
+    CK(cudaMemcpyAsync(c->d.id, snap_i + NS, NS * sizeof(int), cudaMemcpyDeviceToDevice, c->st));
+    CK(cudaMemcpyAsync(c->d.step_base, &snap_step, sizeof(long long), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(c->d.flags, snap_flags, sizeof(snap_flags), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(c->d.thermo, snap_thermo, sizeof(snap_thermo), cudaMemcpyHostToDevice, c->st));
+    if (!snap_rep.empty())
+      CK(cudaMemcpyAsync(c->d.thermo_rep, snap_rep.data(), snap_rep.size() * sizeof(double), cudaMemcpyHostToDevice,
+                         c->st));
+    RK(forced_build(c));
+    int f[F_NWORDS];
+    RK(read_flags(c, f));
+    // the forced build is not a rebuild of the trajectory: keep the counts of the snapshot
+    f[F_REBUILDS] = snap_flags[F_REBUILDS];
+    f[F_PASSES] = snap_flags[F_PASSES];
+    CK(cudaMemcpyAsync(c->d.flags, f, sizeof(f), cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return CAVGPU_OK;
+  };
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  save();
+  if (!rc) rc = cuda_rc(cudaEventCreate(&e0));
+  if (!rc) rc = cuda_rc(cudaEventCreate(&e1));
+  c->prof = false;
+  int trials = 0;
+  // one trial: a warm-up graph (capture, first replay) then T steps timed on the stream
+  auto trial = [&](int tpa, int block, int spg, float *ms) -> int {
+    RK(restore(tpa, block));
+    c->p.steps_per_graph = spg;
+    RK(cavgpu_run(c, std::min(T, spg), 0, nullptr));
+    CK(cudaEventRecord(e0, c->st));
+    RK(cavgpu_run(c, T, 0, nullptr));
+    CK(cudaEventRecord(e1, c->st));
+    CK(cudaEventSynchronize(e1));
+    CK(cudaEventElapsedTime(ms, e0, e1));
+    ++trials;
+    return CAVGPU_OK;
+  };
+  const int spg0 = c->p.steps_per_graph > 0 ? c->p.steps_per_graph : 50;
+  if (!rc && !cached) {
+    float best_ms = 1e30f;
+    best = {c->lc.tpa, c->lc.block, spg0};
+    const int tpas[] = {1, 2, 4, 8};
+    const int blocks[] = {64, 128, 256};
+    for (int tpa : tpas)
+      for (int block : blocks) {
+        float ms = 0.f;
+        const int trc = trial(tpa, block, spg0, &ms);
+        if (trc == CAVGPU_E_CUDA || trc == CAVGPU_E_NOMEM) { rc = trc; break; }
+        if (trc == CAVGPU_OK && ms < best_ms) { best_ms = ms; best = {tpa, block, spg0}; }
+      }
+    // graph length: the host reads status once per chunk group; longer graphs cost memory
+    for (int spg : {25, 100}) {
+      if (rc) break;
+      float ms = 0.f;
+      const int trc = trial(best.tpa, best.block, spg, &ms);
+      if (trc == CAVGPU_E_CUDA || trc == CAVGPU_E_NOMEM) { rc = trc; break; }
+      if (trc == CAVGPU_OK && ms < 0.98f * best_ms) { best_ms = ms; best.spg = spg; }
+    }
+    if (!rc) {
+      std::lock_guard<std::mutex> g(g_tune_mu);
+      g_tune_cache.push_back({key, best});
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (!rc) {
+    c->p.steps_per_graph = best.spg;
+    rc = restore(best.tpa, best.block);
+  }
+  cudaFree(snap);
+  cudaFree(snap_i);
+  c->prof = prof0;
+  c->steps_done = steps0;
+  c->graph_launches = graphs0;
+  c->kernel_launches = kern0;
+  if (rc) return rc;
+  if (out4) {
+    out4[0] = best.tpa;
+    out4[1] = best.block;
+    out4[2] = best.spg;
+    out4[3] = trials;
+  }
+  return CAVGPU_OK;
+}
 
 int cavgpu_forces(cavgpu_ctx *c, double *virial, double *pe) {
   if (!c) return CAVGPU_E_ARG;

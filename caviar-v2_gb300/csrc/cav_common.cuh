@@ -120,6 +120,7 @@ struct Dev {
   int *flags;
   double *partials_ke;        // per-block {sum m v^2, sum m v} (4 per block)
   double *partials_ev;        // per-block {sum -coef r^2, sum V} over both pair orders (2 per block)
+  int partials_blocks;        // blocks the partial arrays hold (every launch grid is checked against it)
   double2 *ev_atom;           // per-slot {-coef r^2, V} sums (batches: per-replica folds)
   double *thermo;             // {KE, T, P, virialForce, PE, total mass, -, -}
   double *thermo_rep;         // batches: per replica {KE, T, P, virialForce, PE, total mass, -, -}

@@ -299,6 +299,7 @@ int force_grid_blocks(const LaunchCfg &lc) {
 int launch_force(const Dev &d, const Box &b, const StepConsts &sc, const LaunchCfg &lc, int kick, int thermo,
                  int k, cudaStream_t st) {
   const int grid = force_grid_blocks(lc);
+  if (grid > d.partials_blocks) return CAVGPU_E_ARG;  // each block writes its own partial sums
   int rc = lc.precision == CAVGPU_MIXED ? launch_tpa<true>(lc.tpa, kick, thermo != 0, grid, lc.block, d, b, sc, k, st)
                                         : launch_tpa<false>(lc.tpa, kick, thermo != 0, grid, lc.block, d, b, sc, k, st);
   if (rc) return rc;

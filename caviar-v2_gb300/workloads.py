@@ -111,11 +111,11 @@ def replica_set(n_rep=4096, nmin=256, nmax=8192, rho_range=(0.6, 1.0), t_range=(
                 seed=1004):
     """Independent periodic LJ replicas of uneven size.
 
-    Replica r: N_r ~ U[nmin, nmax], rho_r ~ U[rho_range], T_r ~ U[t_range]; the
-    first N_r sites of a ceil((N_r/4)^(1/3))^3-cell FCC lattice, box set by rho_r
-    (so the filled lattice is slightly compressed into L = (N_r/rho_r)^(1/3)),
-    plus a seeded N(0, disp) displacement.  Returns a list of
-    (pos, vel, box) with replica seeds seed + r.
+    Replica r: N_r ~ U[nmin, nmax], rho_r ~ U[rho_range], T_r ~ U[t_range]; a
+    random fill (seeded choice of N_r sites) of a ceil((N_r/4)^(1/3))^3-cell FCC
+    lattice spanning the cubic box L = (N_r/rho_r)^(1/3) set by rho_r, plus a
+    seeded N(0, disp) displacement.  Returns a list of (pos, vel, box, T_r,
+    rho_r) with replica seeds seed + r.
     """
     out = []
     meta_rng = np.random.default_rng(seed)
@@ -128,8 +128,10 @@ def replica_set(n_rep=4096, nmin=256, nmax=8192, rho_range=(0.6, 1.0), t_range=(
         c = math.ceil((n / 4) ** (1.0 / 3.0))
         lat, _ = fcc_lattice((c, c, c), 1.0)
         L = (n / rhos[r]) ** (1.0 / 3.0)
-        pos = lat[:n] * (L / (c * (4.0 / 1.0) ** (1.0 / 3.0)))
+        sites = np.sort(rng.choice(len(lat), size=n, replace=False))
+        pos = lat[sites] * (L / (c * (4.0 / 1.0) ** (1.0 / 3.0)))
         pos = np.mod(pos + rng.normal(0.0, disp, size=pos.shape), L)
+        pos[pos >= L] = 0.0  # np.mod of a tiny negative number can round up to L
         vel = thermal_velocities(n, float(temps[r]), rng)
         out.append((pos, vel, np.array([L, L, L]), float(temps[r]), float(rhos[r])))
     return out

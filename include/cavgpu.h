@@ -182,6 +182,20 @@ const char *cavgpu_last_cuda_error(void);
 int cavgpu_kinetic_energy_noalloc(int64_t n, const double *vel3, const uint64_t *type, const double *mass,
                                   int32_t ntypes, int32_t n_r_df, double k_b, double *out2, void *stream);
 
+/* Autotuner (no counterpart in the reference, whose loop has no launch shape):
+ * times short trial runs of every launch shape -- force-kernel lanes per atom
+ * {1,2,4,8} x block size {64,128,256}, then steps per captured graph {25,50,100}
+ * -- each started from a snapshot of the current state, and keeps the fastest.
+ * The state afterwards is the snapshot's (positions, velocities, accelerations,
+ * step counter, statistics), with the list rebuilt for the chosen shape; the
+ * changed summation order perturbs later FP64 results at rounding level, as any
+ * launch-shape change does.  trial_steps: steps timed per candidate (0 = 40).
+ * Results are cached per process by (device, precision, integrator, replica
+ * count, atom count, type count); CAVGPU_TUNE_FORCE re-measures.
+ * out4 (may be NULL) = {threads per atom, block size, steps per graph, trials}. */
+#define CAVGPU_TUNE_FORCE 1
+int cavgpu_autotune(cavgpu_ctx *ctx, int32_t trial_steps, int32_t flags, int64_t *out4);
+
 /* ---- batches of independent replicas (no counterpart in the reference: one
  * CAVIAR2 process runs one Md_simulator; a batch is R of them in one context,
  * each with its own periodic box, atom count, cell grid and half-skin rebuild,
