@@ -310,6 +310,7 @@ int make_repbox(double ce, const double lo[3], const double hi[3], RepBox *rb) {
     rb->w[a] = rb->L[a] / rb->nc[a];
     rb->inv_w[a] = 1.0 / rb->w[a];
     rb->wf[a] = (float)rb->w[a];
+    rb->wlo[a] = (float)(rb->w[a] - (double)rb->wf[a]);
   }
   rb->ncell = rb->nc[0] * rb->nc[1] * rb->nc[2];
   return CAVGPU_OK;

@@ -65,7 +65,8 @@ struct PairTab {
 struct RepBox {
   double lo[3], hi[3], L[3];
   double w[3], inv_w[3];  // search cell width >= list cutoff
-  float wf[3];
+  float wf[3];            // cell width rounded to FP32 ...
+  float wlo[3];           // ... and the rest, w - wf (a cell offset is d*wf + d*wlo in the mixed form)
   int nc[3];
   int cell_off, ncell;    // cells [cell_off, cell_off + ncell); cell cell_off + ncell holds the padding
   int slot_off, natoms, pad;

@@ -43,12 +43,17 @@ struct SmemTabF {
   double minv[MAXT], mass[MAXT];
 };
 // per warp: the 27 image shifts s*L (FP64) or cell offsets d*w (mixed) of the
-// replica the warp's current atoms belong to (a warp never straddles two)
+// replica the warp's current atoms belong to (a warp never straddles two).  The
+// mixed offsets are FP32 pairs d*wf + d*wlo: with the rounded width alone, every
+// pair across a cell face would be displaced by the same d*(wf - w), a fixed
+// distortion of the potential that changes pattern at each rebuild and drifts
+// the NVE energy (measured -2.4e-4 per 1e6 steps).
 template <bool MIXED>
 struct WarpImages;
 template <>
 struct WarpImages<true> {
   float3 v[27];
+  float3 lo[27];
 };
 template <>
 struct WarpImages<false> {
@@ -93,8 +98,12 @@ __global__ void __launch_bounds__(256) k_force(Dev d, Box b, StepConsts sc, int 
       const RepBox &rb = repbox(b, rep);
       if (lane < 27) {
         const int sx = lane % 3 - 1, sy = (lane / 3) % 3 - 1, sz = lane / 9 - 1;
-        if constexpr (MIXED) img[lane] = make_float3(sx * rb.wf[0], sy * rb.wf[1], sz * rb.wf[2]);
-        else img[lane] = make_double3(sx * rb.L[0], sy * rb.L[1], sz * rb.L[2]);
+        if constexpr (MIXED) {
+          img[lane] = make_float3(sx * rb.wf[0], sy * rb.wf[1], sz * rb.wf[2]);
+          wimg[wid].lo[lane] = make_float3(sx * rb.wlo[0], sy * rb.wlo[1], sz * rb.wlo[2]);
+        } else {
+          img[lane] = make_double3(sx * rb.L[0], sy * rb.L[1], sz * rb.L[2]);
+        }
       }
       __syncwarp();
       img_rep = rep;
@@ -122,8 +131,13 @@ __global__ void __launch_bounds__(256) k_force(Dev d, Box b, StepConsts sc, int 
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
             if (k0 + u >= nn) break;
-            const float3 o = img[e[u] >> CODE_SHIFT];
-            const float dx = (rj[u].x + o.x) - ri.x, dy = (rj[u].y + o.y) - ri.y, dz = (rj[u].z + o.z) - ri.z;
+            // ((r_j - r_i) + offset_hi) + offset_lo: rounding is symmetric under negation
+            // and the offsets of i seen from j are exactly -offset, so d_ji = -d_ij bit
+            // for bit and the FP32 pair forces obey Newton's third law exactly
+            const int code = e[u] >> CODE_SHIFT;
+            const float3 o = img[code], ol = wimg[wid].lo[code];
+            const float dx = ((rj[u].x - ri.x) + o.x) + ol.x, dy = ((rj[u].y - ri.y) + o.y) + ol.y,
+                        dz = ((rj[u].z - ri.z) + o.z) + ol.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
             const int tt = ti * nt + __float_as_int(rj[u].w);
             if (r2 <= tab.rc2[tt]) {

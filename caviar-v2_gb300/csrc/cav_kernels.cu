@@ -349,12 +349,34 @@ __device__ __noinline__ bool exact_pair(const Dev &d, const RepBox &rb, double c
   return r2 < ce2;
 }
 
+// Stencil cell k of home cell (cx, cy, cz): its global index, its periodic image
+// code and the offset of its origin from the home cell's origin.
+struct StencilCell {
+  int c2, img;
+  float ox, oy, oz;
+};
+__device__ inline StencilCell stencil_cell(const RepBox &rb, int cx, int cy, int cz, int k) {
+  const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
+  int nx = cx + dx, ny = cy + dy, nz = cz + dz, sx = 0, sy = 0, sz = 0;
+  if (nx < 0) { nx += rb.nc[0]; sx = -1; } else if (nx >= rb.nc[0]) { nx -= rb.nc[0]; sx = 1; }
+  if (ny < 0) { ny += rb.nc[1]; sy = -1; } else if (ny >= rb.nc[1]) { ny -= rb.nc[1]; sy = 1; }
+  if (nz < 0) { nz += rb.nc[2]; sz = -1; } else if (nz >= rb.nc[2]) { nz -= rb.nc[2]; sz = 1; }
+  StencilCell s;
+  s.c2 = rb.cell_off + nx + rb.nc[0] * (ny + rb.nc[1] * nz);
+  s.img = image_code(sx, sy, sz);
+  s.ox = dx * rb.wf[0];
+  s.oy = dy * rb.wf[1];
+  s.oz = dz * rb.wf[2];
+  return s;
+}
+
 // One warp per home cell, one lane per home atom (cells of more than 32 atoms
-// loop).  The warp walks the 27 stencil cells' atoms in order; every candidate
-// is one warp-broadcast load of its FP32 cell-relative coordinates (the stencil
-// is L1-resident), tested against all home atoms at once.  Hits append to the
-// lane's own row, so the list keeps the stencil order (deterministic) and no
-// ballot or barrier is needed.
+// loop).  The warp walks the 27 stencil cells' atoms in order, four candidates
+// per iteration (four independent warp-broadcast loads of FP32 cell-relative
+// coordinates in flight; the stencil is L1-resident), each tested against all
+// home atoms at once.  Hits append to the lane's own row, so the list keeps the
+// stencil order (deterministic, independent of the launch shape) and no ballot
+// or barrier is needed.
 __global__ void __launch_bounds__(256) k_build_warp(Dev d, Box b, int mode, int forced) {
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
@@ -375,29 +397,30 @@ __global__ void __launch_bounds__(256) k_build_warp(Dev d, Box b, int mode, int 
       const float4 ri = act ? d.rel[i] : make_float4(1e18f, 1e18f, 1e18f, 0.f);
       uint32_t *row = d.nbr + nbr_block_base(act ? i : hs, cap, d.tpa);
       int cnt = 0;
+      const float lo = act ? b.ce2_lo : -1.0f;  // idle lanes never hit
       for (int k = 0; k < 27; ++k) {
-        const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
-        int nx = cx + dx, ny = cy + dy, nz = cz + dz, sx = 0, sy = 0, sz = 0;
-        if (nx < 0) { nx += rb.nc[0]; sx = -1; } else if (nx >= rb.nc[0]) { nx -= rb.nc[0]; sx = 1; }
-        if (ny < 0) { ny += rb.nc[1]; sy = -1; } else if (ny >= rb.nc[1]) { ny -= rb.nc[1]; sy = 1; }
-        if (nz < 0) { nz += rb.nc[2]; sz = -1; } else if (nz >= rb.nc[2]) { nz -= rb.nc[2]; sz = 1; }
-        const int c2 = rb.cell_off + nx + rb.nc[0] * (ny + rb.nc[1] * nz);
-        const int img = image_code(sx, sy, sz);
-        const uint32_t code = (uint32_t)(mode == 0 ? img : k) << CODE_SHIFT;
-        const float ox = dx * rb.wf[0] - ri.x, oy = dy * rb.wf[1] - ri.y, oz = dz * rb.wf[2] - ri.z;
-        const int jb = d.cell_start[c2], je = d.cell_start[c2 + 1];
-        const int self = (img == CODE_ZERO && act) ? i : -1;  // the home atom itself is not a neighbour
-        const float lo = act ? b.ce2_lo : -1.0f;               // idle lanes never hit
-        for (int j = jb; j < je; ++j) {
-          const float4 rj = __ldg(&d.rel[j]);  // same address in every lane: one broadcast
-          const float fx = rj.x + ox, fy = rj.y + oy, fz = rj.z + oz;
-          const float q = fx * fx + fy * fy + fz * fz;
-          bool hit = (q < lo) & (j != self);
-          if (__any_sync(FULL_MASK, (q >= lo) & (q <= b.ce2_hi) & act)) {  // rare: exact FP64 predicate
-            if ((q >= lo) & (q <= b.ce2_hi) & act & (j != self)) hit = exact_pair(d, rb, b.ce2, i, j, img);
+        const StencilCell s = stencil_cell(rb, cx, cy, cz, k);
+        const uint32_t code = (uint32_t)(mode == 0 ? s.img : k) << CODE_SHIFT;
+        const float ox = s.ox - ri.x, oy = s.oy - ri.y, oz = s.oz - ri.z;
+        const int jb = d.cell_start[s.c2], je = d.cell_start[s.c2 + 1];
+        const int self = (k == 13 && act) ? i : -1;  // the home atom itself is not a neighbour
+        for (int j0 = jb; j0 < je; j0 += 4) {
+          float4 rj[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u)  // same address in every lane: broadcasts
+            rj[u] = j0 + u < je ? __ldg(&d.rel[j0 + u]) : make_float4(1e18f, 1e18f, 1e18f, 0.f);
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int j = j0 + u;
+            const float fx = rj[u].x + ox, fy = rj[u].y + oy, fz = rj[u].z + oz;
+            const float q = fx * fx + fy * fy + fz * fz;
+            bool hit = (q < lo) & (j != self);
+            if (__any_sync(FULL_MASK, (q >= lo) & (q <= b.ce2_hi) & act)) {  // rare: exact FP64 predicate
+              if ((q >= lo) & (q <= b.ce2_hi) & act & (j != self)) hit = exact_pair(d, rb, b.ce2, i, j, s.img);
+            }
+            if (hit & (cnt < cap)) row[((cnt >> 2) << cshift) + (cnt & 3)] = (uint32_t)j | code;
+            cnt += hit;
           }
-          if (hit & (cnt < cap)) row[((cnt >> 2) << cshift) + (cnt & 3)] = (uint32_t)j | code;
-          cnt += hit;
         }
       }
       if (act) {
