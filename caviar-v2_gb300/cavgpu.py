@@ -18,6 +18,7 @@ MAXT = 8
 
 OK, E_ARG, E_CUDA, E_NAN, E_NLIST_OVERFLOW, E_STATE, E_NOMEM, E_RANGE = 0, -1, -2, -3, -4, -5, -6, -7
 FP64, MIXED = 0, 1
+FORCE_AUTO, FORCE_STRIDED, FORCE_SEGMENTS = 0, 1, 2
 VELOCITY_VERLET, VELOCITY_VERLET_LANGEVIN = 0, 1
 
 
@@ -33,7 +34,7 @@ class Params(C.Structure):
         ("lang_friction", C.c_double), ("lang_kb", C.c_double), ("lang_kbt", C.c_double), ("seed", C.c_uint64),
         ("n_r_df", C.c_int32), ("pressure_process", C.c_int32), ("precision", C.c_int32), ("noise_off", C.c_int32),
         ("nbr_capacity", C.c_int32), ("threads_per_atom", C.c_int32), ("block_size", C.c_int32),
-        ("steps_per_graph", C.c_int32),
+        ("steps_per_graph", C.c_int32), ("force_kernel", C.c_int32),
     ]
 
 
@@ -109,7 +110,8 @@ def _ptr(a):
     return None if a is None else C.c_void_p(a.ctypes.data)
 
 
-def make_params(p, precision=FP64, noise_off=False, tpa=0, block=0, nbr_capacity=0, steps_per_graph=0):
+def make_params(p, precision=FP64, noise_off=False, tpa=0, block=0, nbr_capacity=0, steps_per_graph=0,
+                force_kernel=FORCE_AUTO):
     """cavgpu_params from a parameter dict in the CAVIAR2 setter vocabulary (see workloads.lj_params)."""
     o = Params()
     lib().cavgpu_default_params(C.byref(o))
@@ -139,6 +141,7 @@ def make_params(p, precision=FP64, noise_off=False, tpa=0, block=0, nbr_capacity
     o.precision, o.noise_off = int(precision), int(bool(noise_off))
     o.threads_per_atom, o.block_size = int(tpa), int(block)
     o.nbr_capacity, o.steps_per_graph = int(nbr_capacity), int(steps_per_graph)
+    o.force_kernel = int(force_kernel)
     return o
 
 
@@ -228,9 +231,10 @@ class System:
 
     def autotune(self, trial_steps=0, force=False):
         """Choose the launch shape by timed trials (state restored afterwards)."""
-        o = np.zeros(4, np.int64)
+        o = np.zeros(6, np.int64)
         self._check(lib().cavgpu_autotune(self._h, int(trial_steps), int(bool(force)), _ptr(o)), "autotune")
-        return dict(threads_per_atom=int(o[0]), block_size=int(o[1]), steps_per_graph=int(o[2]), trials=int(o[3]))
+        return dict(threads_per_atom=int(o[0]), block_size=int(o[1]), steps_per_graph=int(o[2]), trials=int(o[3]),
+                    force_kernel="segments" if int(o[4]) == FORCE_SEGMENTS else "strided")
 
     def set_profiling(self, on):
         self._check(lib().cavgpu_set_profiling(self._h, int(on)), "set_profiling")

@@ -27,14 +27,14 @@ struct GraphEntry {
 // autotuner results, per process: a system of the same kind and size on the same
 // device reuses the launch shape measured for the first one
 struct TuneKey {
-  int dev, precision, integrator, nrep, natoms, ntypes;
+  int dev, precision, integrator, nrep, natoms, ntypes, force_kernel;
   bool operator==(const TuneKey &o) const {
     return dev == o.dev && precision == o.precision && integrator == o.integrator && nrep == o.nrep &&
-           natoms == o.natoms && ntypes == o.ntypes;
+           natoms == o.natoms && ntypes == o.ntypes && force_kernel == o.force_kernel;
   }
 };
 struct TuneChoice {
-  int tpa, block, spg;
+  int tpa, block, spg, seg;
 };
 std::mutex g_tune_mu;
 std::vector<std::pair<TuneKey, TuneChoice>> g_tune_cache;
@@ -393,6 +393,9 @@ int create_common(const cavgpu_params *p, int nrep, const double *lo3, const dou
   c->lc.block = p->block_size ? p->block_size : 128;
   if (c->lc.tpa != 1 && c->lc.tpa != 2 && c->lc.tpa != 4 && c->lc.tpa != 8 && c->lc.tpa != 16) { delete c; return CAVGPU_E_ARG; }
   if (c->lc.block < 32 || c->lc.block > 256 || c->lc.block % 32) { delete c; return CAVGPU_E_ARG; }
+  if (p->force_kernel < CAVGPU_FORCE_AUTO || p->force_kernel > CAVGPU_FORCE_SEGMENTS) { delete c; return CAVGPU_E_ARG; }
+  c->lc.use_seg = p->precision == CAVGPU_MIXED && p->force_kernel == CAVGPU_FORCE_SEGMENTS;
+  c->lc.ntypes = p->ntypes;
   c->d.tpa = c->lc.tpa;
   if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) { delete c; return CAVGPU_E_CUDA; }
   if (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess) {
@@ -413,6 +416,43 @@ int create_common(const cavgpu_params *p, int nrep, const double *lo3, const dou
   if (rc) { cavgpu_destroy(c); return rc; }
   *out = c;
   return CAVGPU_OK;
+}
+
+// Row segments of the mixed force kernel.  Replica r's x-rows are cut into
+// segments of S cells, S chosen so that the 9 x (S + 2) staged cells hold about
+// STAGE_TARGET atoms at the replica's mean cell occupancy; the stage is sized
+// for the largest estimate with 35% headroom (a segment that still overflows it
+// falls back to global gathers).
+int build_segments(cavgpu_ctx *c) {
+  constexpr double STAGE_TARGET = 4096.0;
+  constexpr int SEG_MAX = 62;  // cells per segment
+  std::vector<int4> segs;
+  int umax = 3;
+  double need = 0.0;
+  for (int r = 0; r < c->b.nrep; ++r) {
+    const RepBox &rb = c->reps[r];
+    if (rb.nc[1] > 0xffff || rb.nc[2] > 0x7fff) return CAVGPU_E_RANGE;
+    const double navg = (double)rb.natoms / rb.ncell;
+    const int smax = std::max(1, std::min(SEG_MAX, (int)(STAGE_TARGET / (9.0 * navg * 1.3)) - 2));
+    const int ncx = rb.nc[0], nsx = (ncx + smax - 1) / smax, S = (ncx + nsx - 1) / nsx;
+    for (int cz = 0; cz < rb.nc[2]; ++cz)
+      for (int cy = 0; cy < rb.nc[1]; ++cy)
+        for (int x0 = 0; x0 < ncx; x0 += S) segs.push_back(make_int4(r, cy | (cz << 16), x0, std::min(S, ncx - x0)));
+    umax = std::max(umax, S + 2);
+    need = std::max(need, 9.0 * (S + 2) * navg * 1.35);
+  }
+  // dynamic shared memory within the 227 KiB a block may hold, beside ~4 KiB of static
+  const size_t limit = 227 * 1024 - 4096 - (size_t)2 * 9 * umax * sizeof(int);
+  c->d.stage_cap = (int)std::min<double>(need + 128.0, (double)(limit / 16));
+  int4 *dseg = nullptr;
+  RK(dalloc(c, &dseg, segs.size()));
+  CK(cudaMemcpyAsync(dseg, segs.data(), segs.size() * sizeof(int4), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->d.seg = dseg;
+  c->d.nseg = (int)segs.size();
+  c->d.seg_umax = umax;
+  c->lc.nseg = c->d.nseg;
+  return prepare_force_seg(seg_smem_bytes(c->d.stage_cap, umax));
 }
 
 // Lay the replicas out (32-aligned slot ranges, consecutive cell ranges with one
@@ -485,16 +525,19 @@ int upload_common(cavgpu_ctx *c, const int64_t *counts, const double *pos3, cons
   c->tc.volume = vol;
   c->tc.langevin = is_lang(c);
   Dev &d = c->d;
-  // partial sums for the largest force grid of any launch shape (the autotuner
-  // changes the shape later) and for the drift grid
+  if (c->p.precision == CAVGPU_MIXED) RK(build_segments(c));
+  // partial sums for the largest force grid of any launch shape and kernel (the
+  // autotuner changes them later) and for the drift grid
   size_t nblk = 1;
-  for (int tpa = 1; tpa <= 16; tpa *= 2)
-    for (int blk = 32; blk <= 256; blk += 32) {
-      LaunchCfg t = c->lc;
-      t.tpa = tpa;
-      t.block = blk;
-      nblk = std::max(nblk, (size_t)force_grid_blocks(t));
-    }
+  for (int seg = 0; seg < 2; ++seg)
+    for (int tpa = 1; tpa <= 16; tpa *= 2)
+      for (int blk = 32; blk <= 256; blk += 32) {
+        LaunchCfg t = c->lc;
+        t.tpa = tpa;
+        t.block = blk;
+        t.use_seg = seg;
+        nblk = std::max(nblk, (size_t)force_grid_blocks(t));
+      }
   const size_t nblk_d = (size_t)std::max((NS + 255) / 256, 1);
   d.partials_blocks = (int)nblk;
   int rc = CAVGPU_OK;
@@ -736,13 +779,13 @@ int cavgpu_run(cavgpu_ctx *c, int64_t nsteps, int64_t every, double *out5) {
 
 int cavgpu_step(cavgpu_ctx *c, int64_t nsteps) { return cavgpu_run(c, nsteps, 0, nullptr); }
 
-int cavgpu_autotune(cavgpu_ctx *c, int32_t trial_steps, int32_t flags, int64_t *out4) {
+int cavgpu_autotune(cavgpu_ctx *c, int32_t trial_steps, int32_t flags, int64_t *out6) {
   if (!c || trial_steps < 0) return CAVGPU_E_ARG;
   if (!c->set_up) return CAVGPU_E_STATE;
   const int T = trial_steps > 0 ? trial_steps : 40;
   int dev = 0;
   CK(cudaGetDevice(&dev));
-  const TuneKey key{dev, c->p.precision, c->p.integrator, c->b.nrep, c->natoms, c->p.ntypes};
+  const TuneKey key{dev, c->p.precision, c->p.integrator, c->b.nrep, c->natoms, c->p.ntypes, c->p.force_kernel};
   TuneChoice best{};
   bool cached = false;
   if (!(flags & CAVGPU_TUNE_FORCE)) {
@@ -778,11 +821,12 @@ int cavgpu_autotune(cavgpu_ctx *c, int32_t trial_steps, int32_t flags, int64_t *
                                    cudaMemcpyDeviceToHost, c->st));
     if (!rc) rc = cuda_rc(cudaStreamSynchronize(c->st));
   };
-  // back to the snapshot with launch shape (tpa, block): list storage for the shape,
-  // state copied back, forced rebuild
-  auto restore = [&](int tpa, int block) -> int {
+  // back to the snapshot with launch shape (tpa, block, kernel): list storage for the
+  // shape, state copied back, forced rebuild
+  auto restore = [&](int tpa, int block, int seg) -> int {
     c->lc.tpa = tpa;
     c->lc.block = block;
+    c->lc.use_seg = seg;
     c->d.tpa = tpa;
     RK(alloc_nbr(c, c->d.cap));
     for (int k = 0; k < 4; ++k)
@@ -812,8 +856,8 @@ int cavgpu_autotune(cavgpu_ctx *c, int32_t trial_steps, int32_t flags, int64_t *
   c->prof = false;
   int trials = 0;
   // one trial: a warm-up graph (capture, first replay) then T steps timed on the stream
-  auto trial = [&](int tpa, int block, int spg, float *ms) -> int {
-    RK(restore(tpa, block));
+  auto trial = [&](int tpa, int block, int seg, int spg, float *ms) -> int {
+    RK(restore(tpa, block, seg));
     c->p.steps_per_graph = spg;
     RK(cavgpu_run(c, std::min(T, spg), 0, nullptr));
     CK(cudaEventRecord(e0, c->st));
@@ -827,21 +871,29 @@ int cavgpu_autotune(cavgpu_ctx *c, int32_t trial_steps, int32_t flags, int64_t *
   const int spg0 = c->p.steps_per_graph > 0 ? c->p.steps_per_graph : 50;
   if (!rc && !cached) {
     float best_ms = 1e30f;
-    best = {c->lc.tpa, c->lc.block, spg0};
+    best = {c->lc.tpa, c->lc.block, spg0, c->lc.use_seg};
     const int tpas[] = {1, 2, 4, 8};
     const int blocks[] = {64, 128, 256};
-    for (int tpa : tpas)
-      for (int block : blocks) {
-        float ms = 0.f;
-        const int trc = trial(tpa, block, spg0, &ms);
-        if (trc == CAVGPU_E_CUDA || trc == CAVGPU_E_NOMEM) { rc = trc; break; }
-        if (trc == CAVGPU_OK && ms < best_ms) { best_ms = ms; best = {tpa, block, spg0}; }
-      }
+    // kernels: the mixed form tries the segment and the grid-strided kernel unless the
+    // caller fixed one
+    int kernels[2] = {c->lc.use_seg, -1};
+    if (c->p.precision == CAVGPU_MIXED && c->p.force_kernel == CAVGPU_FORCE_AUTO) kernels[0] = 1, kernels[1] = 0;
+    for (int seg : kernels) {
+      if (seg < 0) break;
+      for (int tpa : tpas)
+        for (int block : blocks) {
+          if (rc) break;
+          float ms = 0.f;
+          const int trc = trial(tpa, block, seg, spg0, &ms);
+          if (trc == CAVGPU_E_CUDA || trc == CAVGPU_E_NOMEM) { rc = trc; break; }
+          if (trc == CAVGPU_OK && ms < best_ms) { best_ms = ms; best = {tpa, block, spg0, seg}; }
+        }
+    }
     // graph length: the host reads status once per chunk group; longer graphs cost memory
     for (int spg : {25, 100}) {
       if (rc) break;
       float ms = 0.f;
-      const int trc = trial(best.tpa, best.block, spg, &ms);
+      const int trc = trial(best.tpa, best.block, best.seg, spg, &ms);
       if (trc == CAVGPU_E_CUDA || trc == CAVGPU_E_NOMEM) { rc = trc; break; }
       if (trc == CAVGPU_OK && ms < 0.98f * best_ms) { best_ms = ms; best.spg = spg; }
     }
@@ -854,7 +906,7 @@ int cavgpu_autotune(cavgpu_ctx *c, int32_t trial_steps, int32_t flags, int64_t *
   if (e1) cudaEventDestroy(e1);
   if (!rc) {
     c->p.steps_per_graph = best.spg;
-    rc = restore(best.tpa, best.block);
+    rc = restore(best.tpa, best.block, best.seg);
   }
   cudaFree(snap);
   cudaFree(snap_i);
@@ -863,11 +915,13 @@ int cavgpu_autotune(cavgpu_ctx *c, int32_t trial_steps, int32_t flags, int64_t *
   c->graph_launches = graphs0;
   c->kernel_launches = kern0;
   if (rc) return rc;
-  if (out4) {
-    out4[0] = best.tpa;
-    out4[1] = best.block;
-    out4[2] = best.spg;
-    out4[3] = trials;
+  if (out6) {
+    out6[0] = best.tpa;
+    out6[1] = best.block;
+    out6[2] = best.spg;
+    out6[3] = trials;
+    out6[4] = best.seg ? CAVGPU_FORCE_SEGMENTS : CAVGPU_FORCE_STRIDED;
+    out6[5] = 0;
   }
   return CAVGPU_OK;
 }

@@ -131,7 +131,18 @@ struct Dev {
   // host-order staging for downloads
   double *h3;
   int32_t *hi3;
+  // row segments of the mixed force kernel: {replica, cy | cz << 16, first cell x, cells}
+  const int4 *seg;
+  int nseg;
+  int seg_umax;               // most cells a segment stages per row (segment length + 2)
+  int stage_cap;              // staged atoms the shared memory holds (float4 each)
 };
+
+// Dynamic shared memory of the segment force kernel: the staged coordinates, then
+// two int tables of 9 rows x seg_umax cells (slot offset, count).
+inline size_t seg_smem_bytes(int stage_cap, int umax) {
+  return (size_t)stage_cap * 16 + (size_t)2 * 9 * umax * sizeof(int);
+}
 
 // ---- neighbour-list layout -------------------------------------------------
 // A warp of the force kernel serves A = 32/tpa atoms (a block of A consecutive
@@ -210,6 +221,9 @@ struct LaunchCfg {
   int integrator;  // CAVGPU_VELOCITY_VERLET / ..._LANGEVIN
   int tpa, block;
   int n;           // slots
+  int nseg;        // row segments (mixed form; 0 = none)
+  int use_seg;     // mixed form: run the segment kernel (shared-memory stage)
+  int ntypes;      // 1: the mixed kernels keep the pair constants in registers
 };
 
 struct ThermoCfg {
@@ -224,6 +238,8 @@ struct ThermoCfg {
 // whose half-skin test did not fire.
 int drift_grid_blocks(const LaunchCfg &lc);
 int force_grid_blocks(const LaunchCfg &lc);
+// sets the dynamic shared-memory limit of every segment-kernel variant (call outside capture)
+int prepare_force_seg(size_t smem_bytes);
 int launch_drift(const Dev &d, const Box &b, const StepConsts &sc, const LaunchCfg &lc, int k_in_chunk,
                  int thermo, cudaStream_t st);
 int launch_rebuild(const Dev &d, const Box &b, const LaunchCfg &lc, int forced, cudaStream_t st);

@@ -42,7 +42,7 @@ struct SmemTabF {
   float rc2[MAXT * MAXT], sig2[MAXT * MAXT], eps4[MAXT * MAXT], gc[MAXT * MAXT], uc[MAXT * MAXT];
   double minv[MAXT], mass[MAXT];
 };
-// per warp: the 27 image shifts s*L (FP64) or cell offsets d*w (mixed) of the
+// per warp: the 27 image shifts s*L (FP64) or the cell widths (mixed) of the
 // replica the warp's current atoms belong to (a warp never straddles two).  The
 // mixed offsets are FP32 pairs d*wf + d*wlo: with the rounded width alone, every
 // pair across a cell face would be displaced by the same d*(wf - w), a fixed
@@ -52,24 +52,31 @@ template <bool MIXED>
 struct WarpImages;
 template <>
 struct WarpImages<true> {
-  float3 v[27];
-  float3 lo[27];
+  float4 w;   // (wf, 0): cell widths rounded to FP32; a neighbour's offset is d*wf + d*wlo,
+  float4 lo;  // (wlo, 0)  with d in {-1,0,1}^3 decoded from its stencil index
 };
+
+// Single-type systems keep the pair constants in registers (no table lookups).
+struct OneType {
+  float rc2, sig2, eps4, gc, uc;
+};
+
+// FP32 reciprocal from the hardware approximation (PTX rcp.approx.ftz.f32): one
+// instruction instead of the correctly rounded sequence; it is a function of r^2
+// alone, so both orders of a pair still see the same value.
+__device__ __forceinline__ float rcp_approx(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
 template <>
 struct WarpImages<false> {
   double3 v[27];
 };
 
-// KICK: 0 = store the acceleration only; 1 = velocity-Verlet closing kick
-// v += (a + a_old) * (0.5 dt) (src/md_simulator.cpp:672-679); 2 = Langevin closing
-// update v = (v a_L + eta b) + (a*0.5) dt (src/md_simulator.cpp:853-862).
-// EV: accumulate virial and potential energy (and KE unless KICK == 2); batches
-// also store them per slot for the per-replica folds.
-template <int TPA, bool MIXED, int KICK, bool EV>
-__global__ void __launch_bounds__(256) k_force(Dev d, Box b, StepConsts sc, int k_in_chunk) {
-  constexpr int A = 32 / TPA;
-  __shared__ typename std::conditional<MIXED, SmemTabF, SmemTabD>::type tab;
-  __shared__ WarpImages<MIXED> wimg[8];
+// Loads the pair table into shared memory (FP32 copy for the mixed form).
+template <class Tab>
+__device__ inline void load_tab(const Dev &d, Tab &tab) {
   const PairTab &T = *d.tab;
   const int nt = T.nt;
   for (int k = threadIdx.x; k < nt * nt; k += blockDim.x) {
@@ -77,8 +84,166 @@ __global__ void __launch_bounds__(256) k_force(Dev d, Box b, StepConsts sc, int 
     tab.uc[k] = T.uc[k];
   }
   for (int k = threadIdx.x; k < nt; k += blockDim.x) { tab.minv[k] = T.minv[k]; tab.mass[k] = T.mass[k]; }
-  __syncthreads();
+}
 
+// Mixed-form pair loop of one lane: list chunks t, t+TPA, ... of atom i (four words
+// per 128-bit load, four neighbour coordinates in flight); `gather(word)` returns the
+// neighbour's float4 (global memory or a shared-memory stage).  ONE: single-type
+// system, pair constants from `c1` in registers.
+template <int TPA, bool EV, bool ONE, class Gather>
+__device__ __forceinline__ void mixed_pairs(const uint4 *row4, int nn, int t, const float4 ri, int ti, int nt,
+                                            const SmemTabF &tab, const OneType c1, const float4 wf,
+                                            const float4 wl, Gather gather, float &ax, float &ay, float &az,
+                                            float &vr, float &pp) {
+  for (int q = 0, k0 = 4 * t; k0 < nn; ++q, k0 += 4 * TPA) {
+    const uint4 w4 = __ldg(row4 + (size_t)q * 32);
+    const uint32_t e[4] = {w4.x, w4.y, w4.z, w4.w};
+    float4 rj[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)  // four independent gathers in flight
+      if (k0 + u < nn) rj[u] = gather(e[u]);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (k0 + u >= nn) break;
+      // ((r_j - r_i) + d wf) + d wlo, each sum rounded once (d wf and d wlo are exact
+      // products): rounding is symmetric under negation and i seen from j has offset
+      // -d, so d_ji = -d_ij bit for bit and the FP32 pair forces obey Newton's third
+      // law exactly.  d comes from the stencil index k = (dx+1) + 3 (dy+1) + 9 (dz+1)
+      // by integer arithmetic (a table in shared memory would load the L1 pipe that
+      // the neighbour gathers saturate).
+      const int code = e[u] >> CODE_SHIFT;
+      const int kz = (code * 57) >> 9, r9 = code - 9 * kz, ky = (r9 * 11) >> 5, kx = r9 - 3 * ky;  // k/9, k/3
+      const float ddx = (float)(kx - 1), ddy = (float)(ky - 1), ddz = (float)(kz - 1);
+      const float dx = fmaf(ddx, wl.x, fmaf(ddx, wf.x, rj[u].x - ri.x));
+      const float dy = fmaf(ddy, wl.y, fmaf(ddy, wf.y, rj[u].y - ri.y));
+      const float dz = fmaf(ddz, wl.z, fmaf(ddz, wf.z, rj[u].z - ri.z));
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      float rc2, sig2, eps4, gc, uc;
+      if (ONE) {
+        rc2 = c1.rc2; sig2 = c1.sig2; eps4 = c1.eps4; gc = c1.gc; uc = c1.uc;
+      } else {
+        const int tt = ti * nt + __float_as_int(rj[u].w);
+        rc2 = tab.rc2[tt]; sig2 = tab.sig2[tt]; eps4 = tab.eps4[tt]; gc = tab.gc[tt]; uc = tab.uc[tt];
+      }
+      if (r2 <= rc2) {
+        const float r2i = rcp_approx(r2);
+        const float s2 = sig2 * r2i;
+        const float s6 = s2 * s2 * s2;
+        const float coef = eps4 * r2i * s6 * (6.0f - 12.0f * s6) - gc;
+        ax += coef * dx; ay += coef * dy; az += coef * dz;
+        if (EV) {
+          vr -= coef * r2;
+          pp += eps4 * (s6 * s6 - s6) - uc - 0.5f * gc * (r2 - rc2);
+        }
+      }
+    }
+  }
+}
+
+__device__ inline OneType one_type(const SmemTabF &tab) {
+  return OneType{tab.rc2[0], tab.sig2[0], tab.eps4[0], tab.gc[0], tab.uc[0]};
+}
+
+// Folds the TPA lanes of each atom (lanes a, a+A, a+2A, ...; every lane of the warp
+// calls this) and applies the closing update of the step to atom i on lane t == 0.
+// KICK: 0 = store the acceleration only; 1 = velocity-Verlet closing kick
+// v += (a + a_old) * (0.5 dt) (src/md_simulator.cpp:672-679); 2 = Langevin closing
+// update v = (v a_L + eta b) + (a*0.5) dt (src/md_simulator.cpp:853-862).
+// EV: accumulate virial and potential energy (and KE unless KICK == 2); batches
+// also store them per slot for the per-replica folds.
+template <int A, bool MIXED, int KICK, bool EV, class Tab>
+__device__ __forceinline__ void finish_atom(const Dev &d, const StepConsts &sc, const Tab &tab, bool act, int t,
+                                            int i, int ti, int rep, long long step, double fx, double fy,
+                                            double fz, double vir, double pe, double (&ke_p)[4],
+                                            double (&ev_p)[2]) {
+#pragma unroll
+  for (int o = A; o < 32; o <<= 1) {
+    fx += __shfl_xor_sync(FULL_MASK, fx, o);
+    fy += __shfl_xor_sync(FULL_MASK, fy, o);
+    fz += __shfl_xor_sync(FULL_MASK, fz, o);
+    if (EV) {
+      vir += __shfl_xor_sync(FULL_MASK, vir, o);
+      pe += __shfl_xor_sync(FULL_MASK, pe, o);
+    }
+  }
+  if (!(act && t == 0)) return;
+  const double mi = tab.minv[ti];
+  dbl4 an = make_dbl4(fx * mi, fy * mi, fz * mi, 0.0);
+  if (KICK == 0) {
+    d.acc[i] = an;
+    if (EV) {
+      const dbl4 v = d.vel[i];
+      const double m = tab.mass[ti];
+      ke_p[0] += m * (v.x * v.x + v.y * v.y + v.z * v.z);
+      ke_p[1] += m * v.x; ke_p[2] += m * v.y; ke_p[3] += m * v.z;
+    }
+  } else if (KICK == 1) {
+    dbl4 v = d.vel[i];
+    const dbl4 ao = d.acc_old[i];
+    if (MIXED) {
+      v.x = fma(an.x + ao.x, sc.hdt, v.x);
+      v.y = fma(an.y + ao.y, sc.hdt, v.y);
+      v.z = fma(an.z + ao.z, sc.hdt, v.z);
+    } else {  // v += (a + a_old) * (0.5 dt), the reference's order
+      v.x = __dadd_rn(v.x, __dmul_rn(__dadd_rn(an.x, ao.x), sc.hdt));
+      v.y = __dadd_rn(v.y, __dmul_rn(__dadd_rn(an.y, ao.y), sc.hdt));
+      v.z = __dadd_rn(v.z, __dmul_rn(__dadd_rn(an.z, ao.z), sc.hdt));
+    }
+    d.acc[i] = an;
+    d.vel[i] = v;
+    if (EV) {
+      const double m = tab.mass[ti];
+      ke_p[0] += m * (v.x * v.x + v.y * v.y + v.z * v.z);
+      ke_p[1] += m * v.x; ke_p[2] += m * v.y; ke_p[3] += m * v.z;
+    }
+  } else {
+    dbl4 v = d.vel[i];
+    double e0 = 0.0, e1 = 0.0, e2 = 0.0;
+    if (!sc.noise_off) {  // replica r draws the noise stream of seed + r with its local ids
+      if (MIXED) langevin_eta_f(sc.seed + rep, step, d.id[i], e0, e1, e2);
+      else langevin_eta(sc.seed + rep, step, d.id[i], e0, e1, e2);
+    }
+    if (MIXED) {
+      v.x = fma(an.x, sc.hdt, fma(v.x, sc.la, e0 * sc.lb));
+      v.y = fma(an.y, sc.hdt, fma(v.y, sc.la, e1 * sc.lb));
+      v.z = fma(an.z, sc.hdt, fma(v.z, sc.la, e2 * sc.lb));
+    } else {  // v = (v a + eta b) + (a*0.5) dt, the reference's order
+      v.x = __dadd_rn(__dadd_rn(__dmul_rn(v.x, sc.la), __dmul_rn(e0, sc.lb)), __dmul_rn(__dmul_rn(an.x, 0.5), sc.dt));
+      v.y = __dadd_rn(__dadd_rn(__dmul_rn(v.y, sc.la), __dmul_rn(e1, sc.lb)), __dmul_rn(__dmul_rn(an.y, 0.5), sc.dt));
+      v.z = __dadd_rn(__dadd_rn(__dmul_rn(v.z, sc.la), __dmul_rn(e2, sc.lb)), __dmul_rn(__dmul_rn(an.z, 0.5), sc.dt));
+    }
+    d.acc[i] = an;
+    d.vel[i] = v;
+  }
+  if (EV) {
+    ev_p[0] += vir;
+    ev_p[1] += pe;
+    if (d.ev_atom) d.ev_atom[i] = make_double2(vir, pe);
+  }
+}
+
+template <int KICK, bool EV>
+__device__ inline void store_partials(const Dev &d, double (&ke_p)[4], double (&ev_p)[2]) {
+  if (EV) {
+    block_sum_store_f<2>(ev_p, &d.partials_ev[(size_t)blockIdx.x * 2]);
+    if (KICK != 2) {
+      __syncthreads();
+      block_sum_store_f<4>(ke_p, &d.partials_ke[(size_t)blockIdx.x * 4]);
+    }
+  }
+}
+
+// Grid-strided pair kernel (the FP64 form; the mixed form when it has no segments):
+// warp-sized tasks of A consecutive slots, neighbour coordinates gathered from
+// global memory.
+template <int TPA, bool MIXED, int KICK, bool EV, bool ONE>
+__global__ void __launch_bounds__(256) k_force(Dev d, Box b, StepConsts sc, int k_in_chunk) {
+  constexpr int A = 32 / TPA;
+  __shared__ typename std::conditional<MIXED, SmemTabF, SmemTabD>::type tab;
+  __shared__ WarpImages<MIXED> wimg[8];
+  load_tab(d, tab);
+  __syncthreads();
+  const int nt = d.tab->nt;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int a = lane % A, t = lane / A;
   const int n = sc.n, cap = d.cap;
@@ -88,7 +253,6 @@ __global__ void __launch_bounds__(256) k_force(Dev d, Box b, StepConsts sc, int 
   double ev_p[2] = {0.0, 0.0};
   long long step = 0;
   if (KICK == 2) step = *d.step_base + k_in_chunk;
-  auto &img = wimg[wid].v;
   int img_rep = -1;
 
   for (int task = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; task < ntask; task += warps_total) {
@@ -96,14 +260,14 @@ __global__ void __launch_bounds__(256) k_force(Dev d, Box b, StepConsts sc, int 
     if (rep < 0) continue;  // a task of padding slots (uniform over the warp)
     if (rep != img_rep) {
       const RepBox &rb = repbox(b, rep);
-      if (lane < 27) {
-        const int sx = lane % 3 - 1, sy = (lane / 3) % 3 - 1, sz = lane / 9 - 1;
-        if constexpr (MIXED) {
-          img[lane] = make_float3(sx * rb.wf[0], sy * rb.wf[1], sz * rb.wf[2]);
-          wimg[wid].lo[lane] = make_float3(sx * rb.wlo[0], sy * rb.wlo[1], sz * rb.wlo[2]);
-        } else {
-          img[lane] = make_double3(sx * rb.L[0], sy * rb.L[1], sz * rb.L[2]);
+      if constexpr (MIXED) {
+        if (lane == 0) {
+          wimg[wid].w = make_float4(rb.wf[0], rb.wf[1], rb.wf[2], 0.f);
+          wimg[wid].lo = make_float4(rb.wlo[0], rb.wlo[1], rb.wlo[2], 0.f);
         }
+      } else if (lane < 27) {
+        const int sx = lane % 3 - 1, sy = (lane / 3) % 3 - 1, sz = lane / 9 - 1;
+        wimg[wid].v[lane] = make_double3(sx * rb.L[0], sy * rb.L[1], sz * rb.L[2]);
       }
       __syncwarp();
       img_rep = rep;
@@ -121,38 +285,9 @@ __global__ void __launch_bounds__(256) k_force(Dev d, Box b, StepConsts sc, int 
         const float4 ri = d.rel[i];
         ti = __float_as_int(ri.w);
         float ax = 0.f, ay = 0.f, az = 0.f, vr = 0.f, pp = 0.f;
-        for (int q = 0, k0 = 4 * t; k0 < nn; ++q, k0 += 4 * TPA) {
-          const uint4 w4 = __ldg(row4 + (size_t)q * 32);
-          const uint32_t e[4] = {w4.x, w4.y, w4.z, w4.w};
-          float4 rj[4];
-#pragma unroll
-          for (int u = 0; u < 4; ++u)  // four independent gathers in flight
-            if (k0 + u < nn) rj[u] = __ldg(&d.rel[e[u] & IDX_MASK]);
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            if (k0 + u >= nn) break;
-            // ((r_j - r_i) + offset_hi) + offset_lo: rounding is symmetric under negation
-            // and the offsets of i seen from j are exactly -offset, so d_ji = -d_ij bit
-            // for bit and the FP32 pair forces obey Newton's third law exactly
-            const int code = e[u] >> CODE_SHIFT;
-            const float3 o = img[code], ol = wimg[wid].lo[code];
-            const float dx = ((rj[u].x - ri.x) + o.x) + ol.x, dy = ((rj[u].y - ri.y) + o.y) + ol.y,
-                        dz = ((rj[u].z - ri.z) + o.z) + ol.z;
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            const int tt = ti * nt + __float_as_int(rj[u].w);
-            if (r2 <= tab.rc2[tt]) {
-              const float r2i = __frcp_rn(r2);
-              const float s2 = tab.sig2[tt] * r2i;
-              const float s6 = s2 * s2 * s2;
-              const float coef = tab.eps4[tt] * r2i * s6 * (6.0f - 12.0f * s6) - tab.gc[tt];
-              ax += coef * dx; ay += coef * dy; az += coef * dz;
-              if (EV) {
-                vr -= coef * r2;
-                pp += tab.eps4[tt] * (s6 * s6 - s6) - tab.uc[tt] - 0.5f * tab.gc[tt] * (r2 - tab.rc2[tt]);
-              }
-            }
-          }
-        }
+        const float4 *rel = d.rel;
+        mixed_pairs<TPA, EV, ONE>(row4, nn, t, ri, ti, nt, tab, one_type(tab), wimg[wid].w, wimg[wid].lo,
+                             [rel](uint32_t w) { return __ldg(&rel[w & IDX_MASK]); }, ax, ay, az, vr, pp);
         fx = ax; fy = ay; fz = az; vir = vr; pe = pp;
       } else {
         const dbl4 xi = d.pos[i];
@@ -167,7 +302,7 @@ __global__ void __launch_bounds__(256) k_force(Dev d, Box b, StepConsts sc, int 
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
             if (k0 + u >= nn) break;
-            const double3 s = img[e[u] >> CODE_SHIFT];
+            const double3 s = wimg[wid].v[e[u] >> CODE_SHIFT];
             const double dx = (xj[u].x + s.x) - xi.x, dy = (xj[u].y + s.y) - xi.y, dz = (xj[u].z + s.z) - xi.z;
             const double r2 = dx * dx + dy * dy + dz * dz;
             const int tt = ti * nt + (int)xj[u].w;
@@ -186,108 +321,221 @@ __global__ void __launch_bounds__(256) k_force(Dev d, Box b, StepConsts sc, int 
         }
       }
     }
-    // fold the TPA lanes of each atom (lanes a, a+A, a+2A, ...)
+    finish_atom<A, MIXED, KICK, EV>(d, sc, tab, act, t, i, ti, rep, step, fx, fy, fz, vir, pe, ke_p, ev_p);
+  }
+  store_partials<KICK, EV>(d, ke_p, ev_p);
+}
+
+// Mixed-form pair kernel over row segments.  A block takes a segment -- up to
+// seg_umax - 2 consecutive cells of one x-row of one replica -- and stages into
+// shared memory the FP32 coordinates of the atoms of the 9 neighbouring rows'
+// cells x0-1 .. x0+len (periodic), so that every neighbour gather of the
+// segment's atoms reads shared memory.  A list word (slot j, stencil index k)
+// finds its copy through a table: row r = k / 3 of the stencil, staged cell
+// u = (home cell - x0) + k % 3, index = j + (stage offset - first slot) of (r, u).
+// The arithmetic is that of the grid-strided kernel, so results are the same bit
+// for bit.  A segment whose stencil holds more atoms than the stage falls back to
+// global gathers.  Warps take the segment's A-slot tasks; lanes whose atom lies
+// outside the segment idle (their atoms belong to the adjacent segment).
+template <int TPA, int KICK, bool EV, bool ONE>
+__global__ void __launch_bounds__(256) k_force_seg(Dev d, Box b, StepConsts sc, int k_in_chunk) {
+  constexpr int A = 32 / TPA;
+  constexpr int AS = 5 - (TPA == 1 ? 0 : TPA == 2 ? 1 : TPA == 4 ? 2 : TPA == 8 ? 3 : 4);  // log2(A)
+  __shared__ SmemTabF tab;
+  __shared__ float4 s_wf, s_wl;
+  __shared__ int s_total;
+  extern __shared__ float4 stage[];
+  const int umax = d.seg_umax;
+  int *const toff = reinterpret_cast<int *>(stage + d.stage_cap);  // [9 * umax] stage offset - first slot
+  int *const tcnt = toff + 9 * umax;                                 // [9 * umax] atoms, then exclusive scan
+  load_tab(d, tab);
+  const int nt = d.tab->nt;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  const int a = lane % A, t = lane / A;
+  const int cap = d.cap;
+  double ke_p[4] = {0.0, 0.0, 0.0, 0.0};
+  double ev_p[2] = {0.0, 0.0};
+  long long step = 0;
+  if (KICK == 2) step = *d.step_base + k_in_chunk;
+  int img_rep = -1;
+
+  for (int sgi = blockIdx.x; sgi < d.nseg; sgi += gridDim.x) {
+    const int4 sg = d.seg[sgi];
+    const int rep = sg.x, cy = sg.y & 0xffff, cz = sg.y >> 16, x0 = sg.z, len = sg.w;
+    const RepBox &rb = repbox(b, rep);
+    const int U = len + 2, nq = 9 * U;
+    __syncthreads();  // the previous segment's gathers are done with the stage and tables
+    if (rep != img_rep) {
+      if (threadIdx.x == 0) {
+        s_wf = make_float4(rb.wf[0], rb.wf[1], rb.wf[2], 0.f);
+        s_wl = make_float4(rb.wlo[0], rb.wlo[1], rb.wlo[2], 0.f);
+      }
+      img_rep = rep;
+    }
+    // staged cells q = r * U + u: row r = (dy + 1) + 3 (dz + 1), x cell x0 - 1 + u (periodic)
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+      const int r = q / U, u = q - r * U;
+      int ny = cy + r % 3 - 1, nz = cz + r / 3 - 1, nx = (x0 - 1 + u) % rb.nc[0];
+      if (nx < 0) nx += rb.nc[0];
+      if (ny < 0) ny += rb.nc[1]; else if (ny >= rb.nc[1]) ny -= rb.nc[1];
+      if (nz < 0) nz += rb.nc[2]; else if (nz >= rb.nc[2]) nz -= rb.nc[2];
+      const int c = rb.cell_off + nx + rb.nc[0] * (ny + rb.nc[1] * nz);
+      const int st = d.cell_start[c];
+      toff[q] = st;
+      tcnt[q] = d.cell_start[c + 1] - st;
+    }
+    __syncthreads();
+    // exclusive scan of the counts (nq <= 9 * umax) by warp 0, 32 entries at a time
+    if (wid == 0) {
+      int carry = 0;
+      for (int base = 0; base < nq; base += 32) {
+        const int q = base + lane;
+        const int v = q < nq ? tcnt[q] : 0;
+        int inc = v;
 #pragma unroll
-    for (int o = A; o < 32; o <<= 1) {
-      fx += __shfl_xor_sync(FULL_MASK, fx, o);
-      fy += __shfl_xor_sync(FULL_MASK, fy, o);
-      fz += __shfl_xor_sync(FULL_MASK, fz, o);
-      if (EV) {
-        vir += __shfl_xor_sync(FULL_MASK, vir, o);
-        pe += __shfl_xor_sync(FULL_MASK, pe, o);
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(FULL_MASK, inc, o);
+          if (lane >= o) inc += y;
+        }
+        if (q < nq) tcnt[q] = carry + inc - v;
+        carry += __shfl_sync(FULL_MASK, inc, 31);
       }
+      if (lane == 0) s_total = carry;
     }
-    if (act && t == 0) {
-      const double mi = tab.minv[ti];
-      dbl4 an = make_dbl4(fx * mi, fy * mi, fz * mi, 0.0);
-      if (KICK == 0) {
-        d.acc[i] = an;
-        if (EV) {
-          const dbl4 v = d.vel[i];
-          const double m = tab.mass[ti];
-          ke_p[0] += m * (v.x * v.x + v.y * v.y + v.z * v.z);
-          ke_p[1] += m * v.x; ke_p[2] += m * v.y; ke_p[3] += m * v.z;
-        }
-      } else if (KICK == 1) {
-        dbl4 v = d.vel[i];
-        const dbl4 ao = d.acc_old[i];
-        if (MIXED) {
-          v.x = fma(an.x + ao.x, sc.hdt, v.x);
-          v.y = fma(an.y + ao.y, sc.hdt, v.y);
-          v.z = fma(an.z + ao.z, sc.hdt, v.z);
-        } else {  // v += (a + a_old) * (0.5 dt), the reference's order
-          v.x = __dadd_rn(v.x, __dmul_rn(__dadd_rn(an.x, ao.x), sc.hdt));
-          v.y = __dadd_rn(v.y, __dmul_rn(__dadd_rn(an.y, ao.y), sc.hdt));
-          v.z = __dadd_rn(v.z, __dmul_rn(__dadd_rn(an.z, ao.z), sc.hdt));
-        }
-        d.acc[i] = an;
-        d.vel[i] = v;
-        if (EV) {
-          const double m = tab.mass[ti];
-          ke_p[0] += m * (v.x * v.x + v.y * v.y + v.z * v.z);
-          ke_p[1] += m * v.x; ke_p[2] += m * v.y; ke_p[3] += m * v.z;
-        }
-      } else {
-        dbl4 v = d.vel[i];
-        double e0 = 0.0, e1 = 0.0, e2 = 0.0;
-        if (!sc.noise_off) {
-          if (MIXED) langevin_eta_f(sc.seed + rep, step, d.id[i], e0, e1, e2);
-          else langevin_eta(sc.seed + rep, step, d.id[i], e0, e1, e2);
-        }
-        if (MIXED) {
-          v.x = fma(an.x, sc.hdt, fma(v.x, sc.la, e0 * sc.lb));
-          v.y = fma(an.y, sc.hdt, fma(v.y, sc.la, e1 * sc.lb));
-          v.z = fma(an.z, sc.hdt, fma(v.z, sc.la, e2 * sc.lb));
-        } else {  // v = (v a + eta b) + (a*0.5) dt, the reference's order
-          v.x = __dadd_rn(__dadd_rn(__dmul_rn(v.x, sc.la), __dmul_rn(e0, sc.lb)), __dmul_rn(__dmul_rn(an.x, 0.5), sc.dt));
-          v.y = __dadd_rn(__dadd_rn(__dmul_rn(v.y, sc.la), __dmul_rn(e1, sc.lb)), __dmul_rn(__dmul_rn(an.y, 0.5), sc.dt));
-          v.z = __dadd_rn(__dadd_rn(__dmul_rn(v.z, sc.la), __dmul_rn(e2, sc.lb)), __dmul_rn(__dmul_rn(an.z, 0.5), sc.dt));
-        }
-        d.acc[i] = an;
-        d.vel[i] = v;
+    __syncthreads();
+    const bool staged = s_total <= d.stage_cap;
+    if (staged) {
+      // copy: warp w takes staged cells w, w + nwarp, ...; lanes copy the cell's atoms
+      for (int q = wid; q < nq; q += nwarp) {
+        const int st = toff[q], base = tcnt[q];
+        const int cn = (q + 1 < nq ? tcnt[q + 1] : s_total) - base;
+        for (int k = lane; k < cn; k += 32) stage[base + k] = __ldg(&d.rel[st + k]);
       }
-      if (EV) {
-        ev_p[0] += vir;
-        ev_p[1] += pe;
-        if (d.ev_atom) d.ev_atom[i] = make_double2(vir, pe);
-      }
-    }
-  }
-  if (EV) {
-    block_sum_store_f<2>(ev_p, &d.partials_ev[(size_t)blockIdx.x * 2]);
-    if (KICK != 2) {
       __syncthreads();
-      block_sum_store_f<4>(ke_p, &d.partials_ke[(size_t)blockIdx.x * 4]);
+      for (int q = threadIdx.x; q < nq; q += blockDim.x) toff[q] = tcnt[q] - toff[q];
+    }
+    __syncthreads();
+    // the segment's atoms: slots of its cells (consecutive cell indices, so one range)
+    const int rowc = rb.cell_off + rb.nc[0] * (cy + rb.nc[1] * cz);
+    const int hs = d.cell_start[rowc + x0], he = d.cell_start[rowc + x0 + len];
+    if (he > hs) {
+      const int t_first = hs >> AS, t_last = (he - 1) >> AS;
+      for (int task = t_first + wid; task <= t_last; task += nwarp) {
+        const int i = task * A + a;
+        const bool act = i >= hs && i < he;
+        double fx = 0.0, fy = 0.0, fz = 0.0, vir = 0.0, pe = 0.0;
+        int ti = 0;
+        if (act) {
+          const int nn = d.nnbr[i];
+          const uint4 *row4 = reinterpret_cast<const uint4 *>(d.nbr + (size_t)task * cap * A) + (t * A + a);
+          const float4 ri = d.rel[i];
+          ti = __float_as_int(ri.w);
+          float ax = 0.f, ay = 0.f, az = 0.f, vr = 0.f, pp = 0.f;
+          if (staged) {
+            const int hx = d.cell_of[i] - rowc - x0;  // home cell within the segment
+            const int *tr = toff + hx;
+            mixed_pairs<TPA, EV, ONE>(row4, nn, t, ri, ti, nt, tab, one_type(tab), s_wf, s_wl,
+                                 [tr, U](uint32_t w) {  // `stage` is the block's shared array
+                                   const int k = (int)(w >> CODE_SHIFT), r = (k * 11) >> 5;  // k / 3 for k < 27
+                                   return stage[(int)(w & IDX_MASK) + tr[r * U + (k - 3 * r)]];
+                                 },
+                                 ax, ay, az, vr, pp);
+          } else {
+            const float4 *rel = d.rel;
+            mixed_pairs<TPA, EV, ONE>(row4, nn, t, ri, ti, nt, tab, one_type(tab), s_wf, s_wl,
+                                 [rel](uint32_t w) { return __ldg(&rel[w & IDX_MASK]); }, ax, ay, az, vr, pp);
+          }
+          fx = ax; fy = ay; fz = az; vir = vr; pe = pp;
+        }
+        finish_atom<A, true, KICK, EV>(d, sc, tab, act, t, i, ti, rep, step, fx, fy, fz, vir, pe, ke_p, ev_p);
+      }
     }
   }
+  store_partials<KICK, EV>(d, ke_p, ev_p);
 }
 
 template <int TPA, bool MIXED, int KICK>
-static void launch_ev(bool ev, int grid, int block, const Dev &d, const Box &b, const StepConsts &sc, int k,
-                      cudaStream_t st) {
-  if (ev) k_force<TPA, MIXED, KICK, true><<<grid, block, 0, st>>>(d, b, sc, k);
-  else k_force<TPA, MIXED, KICK, false><<<grid, block, 0, st>>>(d, b, sc, k);
+static void launch_ev(bool ev, bool one, int grid, int block, const Dev &d, const Box &b, const StepConsts &sc,
+                      int k, cudaStream_t st) {
+  if (MIXED && one) {  // single-type systems: constants in registers (mixed form)
+    if (ev) k_force<TPA, MIXED, KICK, true, MIXED><<<grid, block, 0, st>>>(d, b, sc, k);
+    else k_force<TPA, MIXED, KICK, false, MIXED><<<grid, block, 0, st>>>(d, b, sc, k);
+    return;
+  }
+  if (ev) k_force<TPA, MIXED, KICK, true, false><<<grid, block, 0, st>>>(d, b, sc, k);
+  else k_force<TPA, MIXED, KICK, false, false><<<grid, block, 0, st>>>(d, b, sc, k);
 }
 
 template <int TPA, bool MIXED>
-static void launch_kick(int kick, bool ev, int grid, int block, const Dev &d, const Box &b, const StepConsts &sc,
-                        int k, cudaStream_t st) {
-  if (kick == 0) launch_ev<TPA, MIXED, 0>(ev, grid, block, d, b, sc, k, st);
-  else if (kick == 1) launch_ev<TPA, MIXED, 1>(ev, grid, block, d, b, sc, k, st);
-  else launch_ev<TPA, MIXED, 2>(ev, grid, block, d, b, sc, k, st);
+static void launch_kick(int kick, bool ev, bool one, int grid, int block, const Dev &d, const Box &b,
+                        const StepConsts &sc, int k, cudaStream_t st) {
+  if (kick == 0) launch_ev<TPA, MIXED, 0>(ev, one, grid, block, d, b, sc, k, st);
+  else if (kick == 1) launch_ev<TPA, MIXED, 1>(ev, one, grid, block, d, b, sc, k, st);
+  else launch_ev<TPA, MIXED, 2>(ev, one, grid, block, d, b, sc, k, st);
 }
 
 template <bool MIXED>
-static int launch_tpa(int tpa, int kick, bool ev, int grid, int block, const Dev &d, const Box &b,
+static int launch_tpa(int tpa, int kick, bool ev, bool one, int grid, int block, const Dev &d, const Box &b,
                       const StepConsts &sc, int k, cudaStream_t st) {
   switch (tpa) {
-    case 1: launch_kick<1, MIXED>(kick, ev, grid, block, d, b, sc, k, st); break;
-    case 2: launch_kick<2, MIXED>(kick, ev, grid, block, d, b, sc, k, st); break;
-    case 4: launch_kick<4, MIXED>(kick, ev, grid, block, d, b, sc, k, st); break;
-    case 8: launch_kick<8, MIXED>(kick, ev, grid, block, d, b, sc, k, st); break;
-    case 16: launch_kick<16, MIXED>(kick, ev, grid, block, d, b, sc, k, st); break;
+    case 1: launch_kick<1, MIXED>(kick, ev, one, grid, block, d, b, sc, k, st); break;
+    case 2: launch_kick<2, MIXED>(kick, ev, one, grid, block, d, b, sc, k, st); break;
+    case 4: launch_kick<4, MIXED>(kick, ev, one, grid, block, d, b, sc, k, st); break;
+    case 8: launch_kick<8, MIXED>(kick, ev, one, grid, block, d, b, sc, k, st); break;
+    case 16: launch_kick<16, MIXED>(kick, ev, one, grid, block, d, b, sc, k, st); break;
     default: return CAVGPU_E_ARG;
   }
+  return CAVGPU_OK;
+}
+
+// the segment kernel's variants, for launching and for their shared-memory attribute
+template <int TPA, int KICK, bool EV>
+static int seg_variant(bool launch, bool one, int grid, int block, size_t smem, const Dev &d, const Box &b,
+                       const StepConsts &sc, int k, cudaStream_t st) {
+  if (!launch) {
+    if (cudaFuncSetAttribute(k_force_seg<TPA, KICK, EV, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess ||
+        cudaFuncSetAttribute(k_force_seg<TPA, KICK, EV, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess)
+      return CAVGPU_E_CUDA;
+    return CAVGPU_OK;
+  }
+  if (one) k_force_seg<TPA, KICK, EV, true><<<grid, block, smem, st>>>(d, b, sc, k);
+  else k_force_seg<TPA, KICK, EV, false><<<grid, block, smem, st>>>(d, b, sc, k);
+  return CAVGPU_OK;
+}
+template <int TPA>
+static int seg_kick(bool launch, int kick, bool ev, bool one, int grid, int block, size_t smem, const Dev &d,
+                    const Box &b, const StepConsts &sc, int k, cudaStream_t st) {
+  if (kick == 0) return ev ? seg_variant<TPA, 0, true>(launch, one, grid, block, smem, d, b, sc, k, st)
+                           : seg_variant<TPA, 0, false>(launch, one, grid, block, smem, d, b, sc, k, st);
+  if (kick == 1) return ev ? seg_variant<TPA, 1, true>(launch, one, grid, block, smem, d, b, sc, k, st)
+                           : seg_variant<TPA, 1, false>(launch, one, grid, block, smem, d, b, sc, k, st);
+  return ev ? seg_variant<TPA, 2, true>(launch, one, grid, block, smem, d, b, sc, k, st)
+            : seg_variant<TPA, 2, false>(launch, one, grid, block, smem, d, b, sc, k, st);
+}
+static int seg_tpa(bool launch, int tpa, int kick, bool ev, bool one, int grid, int block, size_t smem,
+                   const Dev &d, const Box &b, const StepConsts &sc, int k, cudaStream_t st) {
+  switch (tpa) {
+    case 1: return seg_kick<1>(launch, kick, ev, one, grid, block, smem, d, b, sc, k, st);
+    case 2: return seg_kick<2>(launch, kick, ev, one, grid, block, smem, d, b, sc, k, st);
+    case 4: return seg_kick<4>(launch, kick, ev, one, grid, block, smem, d, b, sc, k, st);
+    case 8: return seg_kick<8>(launch, kick, ev, one, grid, block, smem, d, b, sc, k, st);
+    case 16: return seg_kick<16>(launch, kick, ev, one, grid, block, smem, d, b, sc, k, st);
+    default: return CAVGPU_E_ARG;
+  }
+}
+
+int prepare_force_seg(size_t smem_bytes) {
+  Dev d{};
+  Box b{};
+  StepConsts sc{};
+  for (int tpa = 1; tpa <= 16; tpa *= 2)
+    for (int kick = 0; kick < 3; ++kick)
+      for (int ev = 0; ev < 2; ++ev) {
+        const int rc = seg_tpa(false, tpa, kick, ev != 0, false, 0, 0, smem_bytes, d, b, sc, 0, nullptr);
+        if (rc) return rc;
+      }
   return CAVGPU_OK;
 }
 
@@ -300,6 +548,8 @@ int force_grid_blocks(const LaunchCfg &lc) {
     cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
     if (g_num_sms <= 0) g_num_sms = 148;
   }
+  if (lc.precision == CAVGPU_MIXED && lc.use_seg && lc.nseg > 0)  // one segment per block at a time
+    return lc.nseg < g_num_sms * 4 ? lc.nseg : g_num_sms * 4;
   const int A = 32 / lc.tpa;
   const long long ntask = (lc.n + A - 1) / A;
   const long long warps_per_block = lc.block / 32;
@@ -314,8 +564,17 @@ int launch_force(const Dev &d, const Box &b, const StepConsts &sc, const LaunchC
                  int k, cudaStream_t st) {
   const int grid = force_grid_blocks(lc);
   if (grid > d.partials_blocks) return CAVGPU_E_ARG;  // each block writes its own partial sums
-  int rc = lc.precision == CAVGPU_MIXED ? launch_tpa<true>(lc.tpa, kick, thermo != 0, grid, lc.block, d, b, sc, k, st)
-                                        : launch_tpa<false>(lc.tpa, kick, thermo != 0, grid, lc.block, d, b, sc, k, st);
+  int rc;
+  if (lc.precision == CAVGPU_MIXED && lc.use_seg && lc.nseg > 0) {
+    if (!d.seg || d.nseg != lc.nseg) return CAVGPU_E_ARG;
+    rc = seg_tpa(true, lc.tpa, kick, thermo != 0, lc.ntypes == 1, grid, lc.block,
+                 seg_smem_bytes(d.stage_cap, d.seg_umax), d, b, sc, k, st);
+  } else {
+    const bool one = lc.ntypes == 1;
+    rc = lc.precision == CAVGPU_MIXED
+             ? launch_tpa<true>(lc.tpa, kick, thermo != 0, one, grid, lc.block, d, b, sc, k, st)
+             : launch_tpa<false>(lc.tpa, kick, thermo != 0, one, grid, lc.block, d, b, sc, k, st);
+  }
   if (rc) return rc;
   return cudaPeekAtLastError() == cudaSuccess ? CAVGPU_OK : CAVGPU_E_CUDA;
 }

@@ -371,14 +371,22 @@ __device__ inline StencilCell stencil_cell(const RepBox &rb, int cx, int cy, int
 }
 
 // One warp per home cell, one lane per home atom (cells of more than 32 atoms
-// loop).  The warp walks the 27 stencil cells' atoms in order, four candidates
-// per iteration (four independent warp-broadcast loads of FP32 cell-relative
-// coordinates in flight; the stencil is L1-resident), each tested against all
-// home atoms at once.  Hits append to the lane's own row, so the list keeps the
-// stencil order (deterministic, independent of the launch shape) and no ballot
-// or barrier is needed.
-__global__ void __launch_bounds__(256) k_build_warp(Dev d, Box b, int mode, int forced) {
+// take several groups).  The warp first stages the 27 stencil cells' atoms, in
+// stencil order and slot order inside a cell, into its slice of shared memory as
+// {x, y, z relative to the home cell's origin, list word j | code}, padded to a
+// multiple of four with far-away entries; stencils of more than BUILD_STAGE
+// candidates are staged in passes.  The sweep is then a guard-free loop in
+// which every candidate is one shared-memory broadcast tested by all home
+// atoms at once, with one warp vote per four candidates for the rare exact
+// FP64 test and predicated stores.  Hits append to the lane's own row, so the
+// list keeps the stencil order (deterministic, independent of the launch shape).
+constexpr int BUILD_WARPS = 4;    // warps per block
+constexpr int BUILD_STAGE = 512;  // staged candidates per warp and pass (8 KiB)
+
+__global__ void __launch_bounds__(BUILD_WARPS * 32, 8) k_build_warp(Dev d, Box b, int mode, int forced) {
+  __shared__ float4 stage_all[BUILD_WARPS][BUILD_STAGE];
   const int lane = threadIdx.x & 31;
+  float4 *stage = stage_all[threadIdx.x >> 5];
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
   const int cap = d.cap;
   const int cshift = 7 - log2_pow2(d.tpa);  // chunk stride 4A words = 2^(log2 A + 2)
@@ -391,35 +399,82 @@ __global__ void __launch_bounds__(256) k_build_warp(Dev d, Box b, int mode, int 
     if (lc >= rb.ncell) continue;  // the padding cell
     const int hs = d.cell_start[cell], he = d.cell_start[cell + 1];
     const int cx = lc % rb.nc[0], cy = (lc / rb.nc[0]) % rb.nc[1], cz = lc / (rb.nc[0] * rb.nc[1]);
-    for (int i0 = hs; i0 < he; i0 += 32) {
-      const int i = i0 + lane;
+    // lane k < 27: stencil cell k's first slot and count; exclusive scan = its
+    // position in the flattened candidate sequence
+    int kb = 0, kn = 0;
+    if (lane < 27) {
+      const StencilCell s = stencil_cell(rb, cx, cy, cz, lane);
+      kb = d.cell_start[s.c2];
+      kn = d.cell_start[s.c2 + 1] - kb;
+    }
+    int kpre = kn;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(FULL_MASK, kpre, o);
+      if (lane >= o) kpre += y;
+    }
+    const int ntot = __shfl_sync(FULL_MASK, kpre, 26);
+    kpre -= kn;
+    for (int h0 = hs; h0 < he; h0 += 32) {
+      const int i = h0 + lane;
       const bool act = i < he;
-      const float4 ri = act ? d.rel[i] : make_float4(1e18f, 1e18f, 1e18f, 0.f);
+      const float4 ri = act ? d.rel[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float lo = act ? b.ce2_lo : -1.0f;  // idle lanes never hit
+      const float hi = act ? b.ce2_hi : -1.0f;
+      const uint32_t selfw = (uint32_t)i | (13u << CODE_SHIFT);  // home cell: stencil 13, image zero
       uint32_t *row = d.nbr + nbr_block_base(act ? i : hs, cap, d.tpa);
       int cnt = 0;
-      const float lo = act ? b.ce2_lo : -1.0f;  // idle lanes never hit
-      for (int k = 0; k < 27; ++k) {
-        const StencilCell s = stencil_cell(rb, cx, cy, cz, k);
-        const uint32_t code = (uint32_t)(mode == 0 ? s.img : k) << CODE_SHIFT;
-        const float ox = s.ox - ri.x, oy = s.oy - ri.y, oz = s.oz - ri.z;
-        const int jb = d.cell_start[s.c2], je = d.cell_start[s.c2 + 1];
-        const int self = (k == 13 && act) ? i : -1;  // the home atom itself is not a neighbour
-        for (int j0 = jb; j0 < je; j0 += 4) {
-          float4 rj[4];
+      for (int p0 = 0; p0 < ntot; p0 += BUILD_STAGE) {
+        const int np = min(BUILD_STAGE, ntot - p0), npad = (np + 3) & ~3;
+        __syncwarp();
+        for (int k = 0; k < 27; ++k) {
+          const int f0 = __shfl_sync(FULL_MASK, kpre, k), cn = __shfl_sync(FULL_MASK, kn, k);
+          const int lo_t = max(f0, p0), hi_t = min(f0 + cn, p0 + np);
+          if (lo_t >= hi_t) continue;
+          const StencilCell s = stencil_cell(rb, cx, cy, cz, k);
+          const int jb = __shfl_sync(FULL_MASK, kb, k);
+          const uint32_t code = (uint32_t)(mode == 0 ? s.img : k) << CODE_SHIFT;
+          for (int t = lo_t + lane; t < hi_t; t += 32) {
+            const int j = jb + (t - f0);
+            const float4 rj = __ldg(&d.rel[j]);
+            stage[t - p0] = make_float4(rj.x + s.ox, rj.y + s.oy, rj.z + s.oz, __uint_as_float((uint32_t)j | code));
+          }
+        }
+        if (lane < npad - np) stage[np + lane] = make_float4(1e18f, 1e18f, 1e18f, 0.f);
+        __syncwarp();
+        for (int t = 0; t < npad; t += 4) {
+          float4 c[4];
 #pragma unroll
-          for (int u = 0; u < 4; ++u)  // same address in every lane: broadcasts
-            rj[u] = j0 + u < je ? __ldg(&d.rel[j0 + u]) : make_float4(1e18f, 1e18f, 1e18f, 0.f);
+          for (int u = 0; u < 4; ++u) c[u] = stage[t + u];  // broadcasts
+          bool hit[4], band[4];
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
-            const int j = j0 + u;
-            const float fx = rj[u].x + ox, fy = rj[u].y + oy, fz = rj[u].z + oz;
+            const float fx = c[u].x - ri.x, fy = c[u].y - ri.y, fz = c[u].z - ri.z;
             const float q = fx * fx + fy * fy + fz * fz;
-            bool hit = (q < lo) & (j != self);
-            if (__any_sync(FULL_MASK, (q >= lo) & (q <= b.ce2_hi) & act)) {  // rare: exact FP64 predicate
-              if ((q >= lo) & (q <= b.ce2_hi) & act & (j != self)) hit = exact_pair(d, rb, b.ce2, i, j, s.img);
-            }
-            if (hit & (cnt < cap)) row[((cnt >> 2) << cshift) + (cnt & 3)] = (uint32_t)j | code;
-            cnt += hit;
+            const bool notself = __float_as_uint(c[u].w) != selfw;
+            hit[u] = (q < lo) & notself;
+            band[u] = (q >= lo) & (q <= hi) & notself;
+          }
+          // one vote per four candidates; the band around the cutoff is rare
+          if (__any_sync(FULL_MASK, band[0] | band[1] | band[2] | band[3])) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+              if (band[u]) {  // the exact FP64 predicate
+                const uint32_t w = __float_as_uint(c[u].w);
+                const int code = (int)(w >> CODE_SHIFT);
+                int img = code;
+                if (mode != 0) {  // recover the image from the stencil index
+                  const int nx = cx + code % 3 - 1, ny = cy + (code / 3) % 3 - 1, nz = cz + code / 9 - 1;
+                  img = image_code(nx < 0 ? -1 : (nx >= rb.nc[0] ? 1 : 0), ny < 0 ? -1 : (ny >= rb.nc[1] ? 1 : 0),
+                                   nz < 0 ? -1 : (nz >= rb.nc[2] ? 1 : 0));
+                }
+                hit[u] = exact_pair(d, rb, b.ce2, i, (int)(w & IDX_MASK), img);
+              }
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {  // predicated stores, no branches
+            if (hit[u] & (cnt < cap)) row[((cnt >> 2) << cshift) + (cnt & 3)] = __float_as_uint(c[u].w);
+            cnt += hit[u];
           }
         }
       }
@@ -737,8 +792,8 @@ int launch_rebuild(const Dev &d, const Box &b, const LaunchCfg &lc, int forced, 
   k_copy_state<<<g, 256, 0, st>>>(d, b, forced);
   k_gather<<<g, 256, 0, st>>>(d, b, forced);
   const int mode = lc.precision == CAVGPU_MIXED ? 1 : 0;
-  const int build_grid = std::min(ceil_div((long long)b.ncell_all * 32, 256), num_sms() * 8);
-  k_build_warp<<<build_grid, 256, 0, st>>>(d, b, mode, forced);
+  const int build_grid = std::min(ceil_div(b.ncell_all, BUILD_WARPS), num_sms() * 8);
+  k_build_warp<<<build_grid, BUILD_WARPS * 32, 0, st>>>(d, b, mode, forced);
   k_finish_rebuild<<<1, 256, 0, st>>>(d, b, forced);
   return chk();
 }

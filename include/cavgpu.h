@@ -78,7 +78,14 @@ typedef struct cavgpu_params {
   int32_t threads_per_atom;       /* force kernel lanes per atom (1,2,4,8,16); 0 = default */
   int32_t block_size;             /* force kernel block size (32..256, multiple of 32); 0 = default */
   int32_t steps_per_graph;        /* steps captured per CUDA graph; 0 = default */
+  int32_t force_kernel;           /* CAVGPU_FORCE_*: pair-kernel variant of the mixed form */
 } cavgpu_params;
+
+/* pair-kernel variants of the mixed form (the FP64 form has one kernel); both give
+ * the same results bit for bit */
+#define CAVGPU_FORCE_AUTO 0       /* grid-strided; the autotuner may switch to segments */
+#define CAVGPU_FORCE_STRIDED 1    /* grid-strided tasks, neighbour gathers from global memory */
+#define CAVGPU_FORCE_SEGMENTS 2   /* row segments staged in shared memory */
 
 typedef struct cavgpu_ctx cavgpu_ctx;
 
@@ -183,7 +190,8 @@ int cavgpu_kinetic_energy_noalloc(int64_t n, const double *vel3, const uint64_t 
                                   int32_t ntypes, int32_t n_r_df, double k_b, double *out2, void *stream);
 
 /* Autotuner (no counterpart in the reference, whose loop has no launch shape):
- * times short trial runs of every launch shape -- force-kernel lanes per atom
+ * times short trial runs of every launch shape -- pair kernel (mixed form with
+ * CAVGPU_FORCE_AUTO: segments and grid-strided) x force-kernel lanes per atom
  * {1,2,4,8} x block size {64,128,256}, then steps per captured graph {25,50,100}
  * -- each started from a snapshot of the current state, and keeps the fastest.
  * The state afterwards is the snapshot's (positions, velocities, accelerations,
@@ -191,10 +199,11 @@ int cavgpu_kinetic_energy_noalloc(int64_t n, const double *vel3, const uint64_t 
  * changed summation order perturbs later FP64 results at rounding level, as any
  * launch-shape change does.  trial_steps: steps timed per candidate (0 = 40).
  * Results are cached per process by (device, precision, integrator, replica
- * count, atom count, type count); CAVGPU_TUNE_FORCE re-measures.
- * out4 (may be NULL) = {threads per atom, block size, steps per graph, trials}. */
+ * count, atom count, type count, force_kernel); CAVGPU_TUNE_FORCE re-measures.
+ * out6 (may be NULL) = {threads per atom, block size, steps per graph, trials,
+ * pair kernel (CAVGPU_FORCE_STRIDED or _SEGMENTS), 0}. */
 #define CAVGPU_TUNE_FORCE 1
-int cavgpu_autotune(cavgpu_ctx *ctx, int32_t trial_steps, int32_t flags, int64_t *out4);
+int cavgpu_autotune(cavgpu_ctx *ctx, int32_t trial_steps, int32_t flags, int64_t *out6);
 
 /* ---- batches of independent replicas (no counterpart in the reference: one
  * CAVIAR2 process runs one Md_simulator; a batch is R of them in one context,
