@@ -46,7 +46,24 @@ def parse():
     ap.add_argument("--drift-steps", type=int, default=20000)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-extra", action="store_true", help="skip the batched and Langevin configurations")
-    return ap.parse_args()
+    ap.add_argument("--eager", action="store_true",
+                    help="launch every kernel from the host, no CUDA graphs (for profiler runs: profilers "
+                         "cannot see the kernels of graphs with conditional nodes); not for timing")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (launch shape from --tpa/--block)")
+    ap.add_argument("--tpa", type=int, default=0, help="force-kernel lanes per atom without the autotuner")
+    ap.add_argument("--block", type=int, default=0, help="force-kernel block size without the autotuner")
+    args = ap.parse_args()
+    if args.eager:
+        LAUNCH["steps_per_graph"] = -1
+    if args.tpa:
+        LAUNCH["tpa"] = args.tpa
+    if args.block:
+        LAUNCH["block"] = args.block
+    return args
+
+
+# launch options given to every context (--eager: steps_per_graph = -1)
+LAUNCH = {}
 
 
 # ---------------------------------------------------------------------------
@@ -185,7 +202,7 @@ def measured_peaks():
 def time_device(cavgpu, torch, pos, vel, typ, params, precision, steps, warmup, ws, sampler_id, tune=True):
     """Device-resident timing: events on the context's stream around K steps
     (launch shape chosen by cavgpu_autotune first, outside the timed region)."""
-    s = cavgpu.System(pos, vel, typ, params, precision=precision)
+    s = cavgpu.System(pos, vel, typ, params, precision=precision, **LAUNCH)
     s.setup()
     choice = s.autotune(trial_steps=30) if tune else None
     s.step(warmup)
@@ -216,7 +233,7 @@ def time_device(cavgpu, torch, pos, vel, typ, params, precision, steps, warmup, 
 def time_batch(cavgpu, torch, systems, params, precision, steps, warmup, trial_steps):
     """A batch of replicas, device-resident: autotune, warm-up, K timed steps.
     Returns throughput over all replicas and the per-replica thermo after the run."""
-    b = cavgpu.Batch(systems, params, precision=precision)
+    b = cavgpu.Batch(systems, params, precision=precision, **LAUNCH)
     b.setup()
     choice = b.autotune(trial_steps=trial_steps)
     b.step(warmup)
@@ -270,7 +287,7 @@ def extra_workloads(cavgpu, torch, W, np, single_mixed):
     pos, vel, typ, params = W.config_langevin()
     lang = {"workload": "Langevin LJ fluid, 4,194,304 atoms (128x128x64 FCC cells), T 1.0, gamma 1, skin 0.4"}
     for prec, name, steps in ((cavgpu.MIXED, "mixed", 400), (cavgpu.FP64, "fp64", 40)):
-        s = cavgpu.System(pos, vel, typ, params, precision=prec)
+        s = cavgpu.System(pos, vel, typ, params, precision=prec, **LAUNCH)
         s.setup()
         s.autotune(trial_steps=10)
         s.step(10)
@@ -290,17 +307,21 @@ def extra_workloads(cavgpu, torch, W, np, single_mixed):
 
 
 def nve_drift(cavgpu, pos, vel, typ, params, precision, steps, every=100):
-    """Relative energy drift per 1e6 steps: least-squares slope of (KE+PE)(t)."""
-    s = cavgpu.System(pos, vel, typ, params, precision=precision)
+    """NVE energy drift: least-squares slope of E = KE + PE sampled every `every`
+    steps over `steps` steps, per 1e6 steps and relative to the mean |E|; and the
+    largest |E - E_first| / |E| seen.  None when steps is 0."""
+    import numpy as np
+
+    if steps <= 0:
+        return None, None
+    s = cavgpu.System(pos, vel, typ, params, precision=precision, **LAUNCH)
     s.setup()
     th = s.run(steps, every)
     s.close()
     e = th[:, 0] + th[:, 4]
-    t = (1 + __import__("numpy").arange(len(e))) * every
-    import numpy as np
-
+    t = (1 + np.arange(len(e))) * every
     slope = np.polyfit(t, e, 1)[0]
-    return float(abs(slope) * 1e6 / abs(e[0])), float(abs(e[-1] - e[0]) / abs(e[0]))
+    return float(slope * 1e6 / abs(e.mean())), float(np.abs(e - e[0]).max() / abs(e.mean()))
 
 
 def time_e2e(cavgpu, torch, pos, vel, typ, params, precision, steps, **launch):
@@ -374,9 +395,10 @@ def main():
     sid = gpu_uuid()
 
     # mixed precision (headline) and all-FP64, state resident in HBM
-    sm, rm = time_device(cavgpu, torch, pos, vel, typ, params, cavgpu.MIXED, args.steps, args.warmup, ws, sid)
+    tune = not args.no_tune
+    sm, rm = time_device(cavgpu, torch, pos, vel, typ, params, cavgpu.MIXED, args.steps, args.warmup, ws, sid, tune)
     s64, r64 = time_device(cavgpu, torch, pos, vel, typ, params, cavgpu.FP64, max(args.steps // 4, 50),
-                           min(args.warmup, 20), ws, sid)
+                           min(args.warmup, 20), ws, sid, tune)
     ms_mixed = max_over_ranks(ws, rm["ms"])
     ms_fp64 = max_over_ranks(ws, r64["ms"])
     k64 = max(args.steps // 4, 50)
@@ -388,9 +410,9 @@ def main():
     p_eq, v_eq, _ = s64.state()
     sm.close()
     s64.close()
-    f64 = cavgpu.System(p_eq, v_eq, typ, params, precision=cavgpu.FP64)
+    f64 = cavgpu.System(p_eq, v_eq, typ, params, precision=cavgpu.FP64, **LAUNCH)
     f64.setup()
-    fm = cavgpu.System(p_eq, v_eq, typ, params, precision=cavgpu.MIXED)
+    fm = cavgpu.System(p_eq, v_eq, typ, params, precision=cavgpu.MIXED, **LAUNCH)
     fm.setup()
     a_ref, a_mix = f64.state()[2], fm.state()[2]
     t_ref, t_mix = f64.thermo(), fm.thermo()
@@ -398,13 +420,23 @@ def main():
     fm.close()
     force_rms = float(np.sqrt(((a_mix - a_ref) ** 2).sum(1).mean() / (a_ref ** 2).sum(1).mean()))
 
-    d64 = max(args.drift_steps // 4, 500)
+    # NVE drift from an equilibrated fluid: the melted state relaxed 3000 more steps
+    d64 = max(args.drift_steps // 4, 500) if args.drift_steps > 0 else 0
+    if args.drift_steps > 0:
+        eq = cavgpu.System(p_eq, v_eq, typ, params, precision=cavgpu.MIXED, **LAUNCH)
+        eq.setup()
+        eq.step(3000)
+        p_eq, v_eq, _ = eq.state()
+        eq.close()
     drift_m, dE_m = nve_drift(cavgpu, p_eq, v_eq, typ, params, cavgpu.MIXED, args.drift_steps)
     drift_64, dE_64 = nve_drift(cavgpu, p_eq, v_eq, typ, params, cavgpu.FP64, d64)
 
     tuned = rm["autotune"] or {}
+    kern = {"segments": cavgpu.FORCE_SEGMENTS, "strided": cavgpu.FORCE_STRIDED}.get(tuned.get("force_kernel"),
+                                                                                      cavgpu.FORCE_AUTO)
+    spg = LAUNCH.get("steps_per_graph", tuned.get("steps_per_graph", 0))
     e2e_rate, h2d, d2h = time_e2e(cavgpu, torch, pos, vel, typ, params, cavgpu.MIXED, args.steps,
-                                  tpa=rm["tpa"], block=rm["block"], steps_per_graph=tuned.get("steps_per_graph", 0))
+                                  tpa=rm["tpa"], block=rm["block"], steps_per_graph=spg, force_kernel=kern)
     e2e_rate = ws * n * args.steps / max_over_ranks(ws, n * args.steps / e2e_rate)
 
     # roofline of the dominant kernel (mixed force kernel): algorithmic bytes per launch
@@ -458,9 +490,11 @@ def main():
                      "mixed_pe_rel": abs(t_mix["pe"] - t_ref["pe"]) / abs(t_ref["pe"]),
                      "mixed_pressure_rel": abs(t_mix["pressure"] - t_ref["pressure"]) / abs(t_ref["pressure"]),
                      "nve_drift_per_1e6_steps": {"mixed": drift_m, "fp64": drift_64},
-                     "nve_rel_dE_over_run": {"mixed": dE_m, "fp64": dE_64},
+                     "nve_max_rel_dE": {"mixed": dE_m, "fp64": dE_64},
                      "drift_steps": {"mixed": args.drift_steps, "fp64": d64},
-                     "drift_start": "melted fluid after the FP64 timed run; slope of KE+PE sampled every 100 steps"},
+                     "drift_start": "melted fluid after the FP64 timed run, then 3000 mixed steps; signed "
+                                    "least-squares slope of KE+PE sampled every 100 steps, per 1e6 steps, "
+                                    "relative to the mean |E|"},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_rate, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": rm["kernel_launches"],

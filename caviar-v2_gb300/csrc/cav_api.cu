@@ -140,11 +140,10 @@ int enqueue_drift(cavgpu_ctx *c, int k, bool thermo) {
 int enqueue_step(cavgpu_ctx *c, int k, bool thermo, int ring_slot) {
   RK(enqueue_drift(c, k, thermo));
   RK(launch_rebuild(c->d, c->b, c->lc, 0, c->st));
-  // External: inside a stream capture this becomes an event-record node that records
-  // at every replay (a plain record would only order work within the capture)
-  if (c->prof && k < (int)c->ev0.size()) CK(cudaEventRecordWithFlags(c->ev0[k], c->st, cudaEventRecordExternal));
+  // launched directly, not captured: plain event records
+  if (c->prof && k < (int)c->ev0.size()) CK(cudaEventRecord(c->ev0[k], c->st));
   RK(launch_force(c->d, c->b, c->sc, c->lc, is_lang(c) ? 2 : 1, thermo, k, c->st));
-  if (c->prof && k < (int)c->ev1.size()) CK(cudaEventRecordWithFlags(c->ev1[k], c->st, cudaEventRecordExternal));
+  if (c->prof && k < (int)c->ev1.size()) CK(cudaEventRecord(c->ev1[k], c->st));
   c->kernel_launches += REBUILD_KERNELS + 1;
   if (thermo) RK(enqueue_thermo_after_force(c, ring_slot));
   return CAVGPU_OK;
@@ -717,7 +716,10 @@ int cavgpu_run(cavgpu_ctx *c, int64_t nsteps, int64_t every, double *out5) {
   // chunks of up to S steps, each one captured CUDA graph (cached per size).  Without
   // recording, the last chunk computes the thermo of its final step, so that the state
   // after the call carries a fresh temperature (finalize_temperature runs every step).
-  while (done < nsteps) {
+  // steps_per_graph < 0: no graphs, every step launched from the host (profilers
+  // cannot see the kernels of graphs that hold conditional nodes).
+  const bool eager = c->p.steps_per_graph < 0;
+  while (!eager && done < nsteps) {
     const int64_t left = nsteps - done;
     const int sz = (int)std::min<int64_t>(left, S);
     int ev;
@@ -856,10 +858,11 @@ int cavgpu_autotune(cavgpu_ctx *c, int32_t trial_steps, int32_t flags, int64_t *
   c->prof = false;
   int trials = 0;
   // one trial: a warm-up graph (capture, first replay) then T steps timed on the stream
+  // (an eager context, steps_per_graph < 0, stays eager: spg is then -1)
   auto trial = [&](int tpa, int block, int seg, int spg, float *ms) -> int {
     RK(restore(tpa, block, seg));
     c->p.steps_per_graph = spg;
-    RK(cavgpu_run(c, std::min(T, spg), 0, nullptr));
+    RK(cavgpu_run(c, spg > 0 ? std::min(T, spg) : 2, 0, nullptr));
     CK(cudaEventRecord(e0, c->st));
     RK(cavgpu_run(c, T, 0, nullptr));
     CK(cudaEventRecord(e1, c->st));
@@ -868,7 +871,7 @@ int cavgpu_autotune(cavgpu_ctx *c, int32_t trial_steps, int32_t flags, int64_t *
     ++trials;
     return CAVGPU_OK;
   };
-  const int spg0 = c->p.steps_per_graph > 0 ? c->p.steps_per_graph : 50;
+  const int spg0 = c->p.steps_per_graph > 0 ? c->p.steps_per_graph : (c->p.steps_per_graph < 0 ? -1 : 50);
   if (!rc && !cached) {
     float best_ms = 1e30f;
     best = {c->lc.tpa, c->lc.block, spg0, c->lc.use_seg};
@@ -891,7 +894,7 @@ int cavgpu_autotune(cavgpu_ctx *c, int32_t trial_steps, int32_t flags, int64_t *
     }
     // graph length: the host reads status once per chunk group; longer graphs cost memory
     for (int spg : {25, 100}) {
-      if (rc) break;
+      if (rc || spg0 < 0) break;
       float ms = 0.f;
       const int trc = trial(best.tpa, best.block, best.seg, spg, &ms);
       if (trc == CAVGPU_E_CUDA || trc == CAVGPU_E_NOMEM) { rc = trc; break; }

@@ -77,7 +77,9 @@ typedef struct cavgpu_params {
   int32_t nbr_capacity;           /* neighbour slots per atom; 0 = sized at set-up */
   int32_t threads_per_atom;       /* force kernel lanes per atom (1,2,4,8,16); 0 = default */
   int32_t block_size;             /* force kernel block size (32..256, multiple of 32); 0 = default */
-  int32_t steps_per_graph;        /* steps captured per CUDA graph; 0 = default */
+  int32_t steps_per_graph;        /* steps captured per CUDA graph; 0 = default (50); < 0 = no
+                                     graphs, every kernel launched from the host (for profilers,
+                                     which cannot see the kernels of graphs with conditional nodes) */
   int32_t force_kernel;           /* CAVGPU_FORCE_*: pair-kernel variant of the mixed form */
 } cavgpu_params;
 
