@@ -6,8 +6,8 @@
 // iteration one coalesced 128-byte read of neighbour words.  Two precisions:
 //   FP64  : image = x_j + s*L, all pair arithmetic in double;
 //   MIXED : FP32 pair arithmetic on coordinates relative to each atom's build cell
-//           (float4 x,y,z,type; cell offsets from a shared table), FP64 accumulation
-//           across lanes, FP64 acceleration/velocity/reductions.
+//           (float4 x,y,z,type; cell offsets decoded from the stencil index), FP64
+//           accumulation across lanes, FP64 acceleration/velocity/reductions.
 #include "cav_common.cuh"
 
 namespace cav {
@@ -237,7 +237,7 @@ __device__ inline void store_partials(const Dev &d, double (&ke_p)[4], double (&
 // warp-sized tasks of A consecutive slots, neighbour coordinates gathered from
 // global memory.
 template <int TPA, bool MIXED, int KICK, bool EV, bool ONE>
-__global__ void __launch_bounds__(256) k_force(Dev d, Box b, StepConsts sc, int k_in_chunk) {
+__global__ void __launch_bounds__(256, MIXED ? 4 : 1) k_force(Dev d, Box b, StepConsts sc, int k_in_chunk) {
   constexpr int A = 32 / TPA;
   __shared__ typename std::conditional<MIXED, SmemTabF, SmemTabD>::type tab;
   __shared__ WarpImages<MIXED> wimg[8];
