@@ -87,16 +87,18 @@ __device__ inline void load_tab(const Dev &d, Tab &tab) {
 }
 
 // Mixed-form pair loop of one lane: list chunks t, t+TPA, ... of atom i (four words
-// per 128-bit load, four neighbour coordinates in flight); `gather(word)` returns the
-// neighbour's float4 (global memory or a shared-memory stage).  ONE: single-type
-// system, pair constants from `c1` in registers.
+// per 128-bit load; the next chunk's load and four neighbour coordinates in
+// flight); `gather(word)` returns the neighbour's float4 (global memory or a
+// shared-memory stage).  ONE: single-type system, pair constants in registers.
 template <int TPA, bool EV, bool ONE, class Gather>
 __device__ __forceinline__ void mixed_pairs(const uint4 *row4, int nn, int t, const float4 ri, int ti, int nt,
                                             const SmemTabF &tab, const OneType c1, const float4 wf,
                                             const float4 wl, Gather gather, float &ax, float &ay, float &az,
                                             float &vr, float &pp) {
+  uint4 nxt = 4 * t < nn ? __ldg(row4) : make_uint4(0, 0, 0, 0);
   for (int q = 0, k0 = 4 * t; k0 < nn; ++q, k0 += 4 * TPA) {
-    const uint4 w4 = __ldg(row4 + (size_t)q * 32);
+    const uint4 w4 = nxt;
+    if (k0 + 4 * TPA < nn) nxt = __ldg(row4 + (size_t)(q + 1) * 32);  // the next list chunk in flight
     const uint32_t e[4] = {w4.x, w4.y, w4.z, w4.w};
     float4 rj[4];
 #pragma unroll

@@ -374,12 +374,14 @@ __device__ inline StencilCell stencil_cell(const RepBox &rb, int cx, int cy, int
 // take several groups).  The warp first stages the 27 stencil cells' atoms, in
 // stencil order and slot order inside a cell, into its slice of shared memory as
 // {x, y, z relative to the home cell's origin, list word j | code}, padded to a
-// multiple of four with far-away entries; stencils of more than BUILD_STAGE
-// candidates are staged in passes.  The sweep is then a guard-free loop in
-// which every candidate is one shared-memory broadcast tested by all home
-// atoms at once, with one warp vote per four candidates for the rare exact
-// FP64 test and predicated stores.  Hits append to the lane's own row, so the
-// list keeps the stencil order (deterministic, independent of the launch shape).
+// multiple of 32 with far-away entries; stencils of more than BUILD_STAGE
+// candidates are staged in passes.  The sweep takes 32 candidates at a time:
+// every candidate is one shared-memory broadcast tested by all home atoms, the
+// results collect in a hit and a band bit mask per lane (one warp vote per 32
+// candidates for the rare exact FP64 test), and only then are the hits (~15% of
+// the candidates) written, in candidate order.  Hits append to the lane's own
+// row, so the list keeps the stencil order (deterministic, independent of the
+// launch shape).
 constexpr int BUILD_WARPS = 4;    // warps per block
 constexpr int BUILD_STAGE = 512;  // staged candidates per warp and pass (8 KiB)
 
@@ -425,7 +427,7 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 8) k_build_warp(Dev d, Box b
       uint32_t *row = d.nbr + nbr_block_base(act ? i : hs, cap, d.tpa);
       int cnt = 0;
       for (int p0 = 0; p0 < ntot; p0 += BUILD_STAGE) {
-        const int np = min(BUILD_STAGE, ntot - p0), npad = (np + 3) & ~3;
+        const int np = min(BUILD_STAGE, ntot - p0);
         __syncwarp();
         for (int k = 0; k < 27; ++k) {
           const int f0 = __shfl_sync(FULL_MASK, kpre, k), cn = __shfl_sync(FULL_MASK, kn, k);
@@ -440,41 +442,42 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 8) k_build_warp(Dev d, Box b
             stage[t - p0] = make_float4(rj.x + s.ox, rj.y + s.oy, rj.z + s.oz, __uint_as_float((uint32_t)j | code));
           }
         }
-        if (lane < npad - np) stage[np + lane] = make_float4(1e18f, 1e18f, 1e18f, 0.f);
+        const int npad32 = (np + 31) & ~31;
+        for (int t = np + lane; t < npad32; t += 32) stage[t] = make_float4(1e18f, 1e18f, 1e18f, 0.f);
         __syncwarp();
-        for (int t = 0; t < npad; t += 4) {
-          float4 c[4];
+        for (int t0 = 0; t0 < npad32; t0 += 32) {
+          // phase 1: hit and band bits of 32 candidates
+          uint32_t hm = 0u, bm = 0u;
 #pragma unroll
-          for (int u = 0; u < 4; ++u) c[u] = stage[t + u];  // broadcasts
-          bool hit[4], band[4];
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            const float fx = c[u].x - ri.x, fy = c[u].y - ri.y, fz = c[u].z - ri.z;
+          for (int u = 0; u < 32; ++u) {
+            const float4 c = stage[t0 + u];  // broadcast
+            const float fx = c.x - ri.x, fy = c.y - ri.y, fz = c.z - ri.z;
             const float q = fx * fx + fy * fy + fz * fz;
-            const bool notself = __float_as_uint(c[u].w) != selfw;
-            hit[u] = (q < lo) & notself;
-            band[u] = (q >= lo) & (q <= hi) & notself;
+            const bool notself = __float_as_uint(c.w) != selfw;
+            hm |= (uint32_t)((q < lo) & notself) << u;
+            bm |= (uint32_t)((q >= lo) & (q <= hi) & notself) << u;
           }
-          // one vote per four candidates; the band around the cutoff is rare
-          if (__any_sync(FULL_MASK, band[0] | band[1] | band[2] | band[3])) {
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-              if (band[u]) {  // the exact FP64 predicate
-                const uint32_t w = __float_as_uint(c[u].w);
-                const int code = (int)(w >> CODE_SHIFT);
-                int img = code;
-                if (mode != 0) {  // recover the image from the stencil index
-                  const int nx = cx + code % 3 - 1, ny = cy + (code / 3) % 3 - 1, nz = cz + code / 9 - 1;
-                  img = image_code(nx < 0 ? -1 : (nx >= rb.nc[0] ? 1 : 0), ny < 0 ? -1 : (ny >= rb.nc[1] ? 1 : 0),
-                                   nz < 0 ? -1 : (nz >= rb.nc[2] ? 1 : 0));
-                }
-                hit[u] = exact_pair(d, rb, b.ce2, i, (int)(w & IDX_MASK), img);
+          if (__any_sync(FULL_MASK, bm != 0u)) {  // rare: the exact FP64 predicate
+            while (bm) {
+              const int u = __ffs(bm) - 1;
+              bm &= bm - 1u;
+              const uint32_t w = __float_as_uint(stage[t0 + u].w);
+              const int code = (int)(w >> CODE_SHIFT);
+              int img = code;
+              if (mode != 0) {  // recover the image from the stencil index
+                const int nx = cx + code % 3 - 1, ny = cy + (code / 3) % 3 - 1, nz = cz + code / 9 - 1;
+                img = image_code(nx < 0 ? -1 : (nx >= rb.nc[0] ? 1 : 0), ny < 0 ? -1 : (ny >= rb.nc[1] ? 1 : 0),
+                                 nz < 0 ? -1 : (nz >= rb.nc[2] ? 1 : 0));
               }
+              if (exact_pair(d, rb, b.ce2, i, (int)(w & IDX_MASK), img)) hm |= 1u << u;
+            }
           }
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {  // predicated stores, no branches
-            if (hit[u] & (cnt < cap)) row[((cnt >> 2) << cshift) + (cnt & 3)] = __float_as_uint(c[u].w);
-            cnt += hit[u];
+          // phase 2: the hits, in candidate order
+          while (hm) {
+            const int u = __ffs(hm) - 1;
+            hm &= hm - 1u;
+            if (cnt < cap) row[((cnt >> 2) << cshift) + (cnt & 3)] = __float_as_uint(stage[t0 + u].w);
+            ++cnt;
           }
         }
       }
