@@ -34,7 +34,7 @@ class Params(C.Structure):
         ("lang_friction", C.c_double), ("lang_kb", C.c_double), ("lang_kbt", C.c_double), ("seed", C.c_uint64),
         ("n_r_df", C.c_int32), ("pressure_process", C.c_int32), ("precision", C.c_int32), ("noise_off", C.c_int32),
         ("nbr_capacity", C.c_int32), ("threads_per_atom", C.c_int32), ("block_size", C.c_int32),
-        ("steps_per_graph", C.c_int32), ("force_kernel", C.c_int32),
+        ("steps_per_graph", C.c_int32), ("force_kernel", C.c_int32), ("jump_tol", C.c_double),
     ]
 
 
@@ -142,6 +142,7 @@ def make_params(p, precision=FP64, noise_off=False, tpa=0, block=0, nbr_capacity
     o.threads_per_atom, o.block_size = int(tpa), int(block)
     o.nbr_capacity, o.steps_per_graph = int(nbr_capacity), int(steps_per_graph)
     o.force_kernel = int(force_kernel)
+    o.jump_tol = float(p.get("jump_tol", 0.0))
     return o
 
 

@@ -322,7 +322,9 @@ int create_common(const cavgpu_params *p, int nrep, const double *lo3, const dou
   if (p->bc[0] != 1 || p->bc[1] != 1 || p->bc[2] != 1) return CAVGPU_E_ARG;
   if (!(p->nl_cutoff > 0.0) || !(p->nl_coef >= 1.0) || !(p->lj_cutoff >= 0.0) || !(p->dt >= 0.0)) return CAVGPU_E_ARG;
   if (p->precision != CAVGPU_FP64 && p->precision != CAVGPU_MIXED) return CAVGPU_E_ARG;
-  if (p->integrator != CAVGPU_VELOCITY_VERLET && p->integrator != CAVGPU_VELOCITY_VERLET_LANGEVIN) return CAVGPU_E_ARG;
+  if (p->integrator != CAVGPU_VELOCITY_VERLET && p->integrator != CAVGPU_VELOCITY_VERLET_LANGEVIN &&
+      p->integrator != CAVGPU_LEAP_FROG)
+    return CAVGPU_E_ARG;
   if (p->n_r_df < 0 || p->n_r_df > 3) return CAVGPU_E_ARG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) { cudaGetLastError(); return CAVGPU_E_CUDA; }
@@ -385,6 +387,9 @@ int create_common(const cavgpu_params *p, int nrep, const double *lo3, const dou
   }
   sc.seed = p->seed;
   sc.noise_off = p->noise_off;
+  if (p->jump_tol < 0.0) { delete c; return CAVGPU_E_ARG; }
+  sc.jump_tol = p->jump_tol;  // Lj::set_jump_tol (src/force/lj.cpp:82-86); 0 = off
+  sc.jump_tolf = (float)p->jump_tol;
   // launch shape
   c->lc.precision = p->precision;
   c->lc.integrator = p->integrator;

@@ -97,6 +97,8 @@ struct StepConsts {
   uint64_t seed;
   int noise_off;
   int n;                      // slots
+  double jump_tol;            // Lj jump_fix: floor of r^2 inside the cutoff (0 = off)
+  float jump_tolf;
 };
 
 // Device arrays, in cell-sorted slot order.

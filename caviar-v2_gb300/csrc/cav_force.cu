@@ -93,8 +93,8 @@ __device__ inline void load_tab(const Dev &d, Tab &tab) {
 template <int TPA, bool EV, bool ONE, class Gather>
 __device__ __forceinline__ void mixed_pairs(const uint4 *row4, int nn, int t, const float4 ri, int ti, int nt,
                                             const SmemTabF &tab, const OneType c1, const float4 wf,
-                                            const float4 wl, Gather gather, float &ax, float &ay, float &az,
-                                            float &vr, float &pp) {
+                                            const float4 wl, const float jtol, Gather gather, float &ax,
+                                            float &ay, float &az, float &vr, float &pp) {
   uint4 nxt = 4 * t < nn ? __ldg(row4) : make_uint4(0, 0, 0, 0);
   for (int q = 0, k0 = 4 * t; k0 < nn; ++q, k0 += 4 * TPA) {
     const uint4 w4 = nxt;
@@ -119,7 +119,7 @@ __device__ __forceinline__ void mixed_pairs(const uint4 *row4, int nn, int t, co
       const float dx = fmaf(ddx, wl.x, fmaf(ddx, wf.x, rj[u].x - ri.x));
       const float dy = fmaf(ddy, wl.y, fmaf(ddy, wf.y, rj[u].y - ri.y));
       const float dz = fmaf(ddz, wl.z, fmaf(ddz, wf.z, rj[u].z - ri.z));
-      const float r2 = dx * dx + dy * dy + dz * dz;
+      const float r2d = dx * dx + dy * dy + dz * dz;
       float rc2, sig2, eps4, gc, uc;
       if (ONE) {
         rc2 = c1.rc2; sig2 = c1.sig2; eps4 = c1.eps4; gc = c1.gc; uc = c1.uc;
@@ -127,7 +127,8 @@ __device__ __forceinline__ void mixed_pairs(const uint4 *row4, int nn, int t, co
         const int tt = ti * nt + __float_as_int(rj[u].w);
         rc2 = tab.rc2[tt]; sig2 = tab.sig2[tt]; eps4 = tab.eps4[tt]; gc = tab.gc[tt]; uc = tab.uc[tt];
       }
-      if (r2 <= rc2) {
+      if (r2d <= rc2) {
+        const float r2 = fmaxf(r2d, jtol);  // Lj jump_fix floor (0 when off)
         const float r2i = rcp_approx(r2);
         const float s2 = sig2 * r2i;
         const float s6 = s2 * s2 * s2;
@@ -288,7 +289,7 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 1) k_force(Dev d, Box b, Step
         ti = __float_as_int(ri.w);
         float ax = 0.f, ay = 0.f, az = 0.f, vr = 0.f, pp = 0.f;
         const float4 *rel = d.rel;
-        mixed_pairs<TPA, EV, ONE>(row4, nn, t, ri, ti, nt, tab, one_type(tab), wimg[wid].w, wimg[wid].lo,
+        mixed_pairs<TPA, EV, ONE>(row4, nn, t, ri, ti, nt, tab, one_type(tab), wimg[wid].w, wimg[wid].lo, sc.jump_tolf,
                              [rel](uint32_t w) { return __ldg(&rel[w & IDX_MASK]); }, ax, ay, az, vr, pp);
         fx = ax; fy = ay; fz = az; vir = vr; pe = pp;
       } else {
@@ -306,9 +307,12 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 1) k_force(Dev d, Box b, Step
             if (k0 + u >= nn) break;
             const double3 s = wimg[wid].v[e[u] >> CODE_SHIFT];
             const double dx = (xj[u].x + s.x) - xi.x, dy = (xj[u].y + s.y) - xi.y, dz = (xj[u].z + s.z) - xi.z;
-            const double r2 = dx * dx + dy * dy + dz * dz;
+            const double r2d = dx * dx + dy * dy + dz * dz;
             const int tt = ti * nt + (int)xj[u].w;
-            if (r2 <= tab.rc2[tt]) {
+            if (r2d <= tab.rc2[tt]) {
+              // Lj jump_fix (src/force/lj.cpp:459-468): r^2 floored at jump_tol after the
+              // cutoff test (jump_tol = 0 when off); the direction stays dx, dy, dz
+              const double r2 = r2d < sc.jump_tol ? sc.jump_tol : r2d;
               const double r2i = __drcp_rn(r2);
               const double s2 = tab.sig2[tt] * r2i;
               const double s6 = s2 * s2 * s2;
@@ -436,7 +440,7 @@ __global__ void __launch_bounds__(256) k_force_seg(Dev d, Box b, StepConsts sc, 
           if (staged) {
             const int hx = d.cell_of[i] - rowc - x0;  // home cell within the segment
             const int *tr = toff + hx;
-            mixed_pairs<TPA, EV, ONE>(row4, nn, t, ri, ti, nt, tab, one_type(tab), s_wf, s_wl,
+            mixed_pairs<TPA, EV, ONE>(row4, nn, t, ri, ti, nt, tab, one_type(tab), s_wf, s_wl, sc.jump_tolf,
                                  [tr, U](uint32_t w) {  // `stage` is the block's shared array
                                    const int k = (int)(w >> CODE_SHIFT), r = (k * 11) >> 5;  // k / 3 for k < 27
                                    return stage[(int)(w & IDX_MASK) + tr[r * U + (k - 3 * r)]];
@@ -444,7 +448,7 @@ __global__ void __launch_bounds__(256) k_force_seg(Dev d, Box b, StepConsts sc, 
                                  ax, ay, az, vr, pp);
           } else {
             const float4 *rel = d.rel;
-            mixed_pairs<TPA, EV, ONE>(row4, nn, t, ri, ti, nt, tab, one_type(tab), s_wf, s_wl,
+            mixed_pairs<TPA, EV, ONE>(row4, nn, t, ri, ti, nt, tab, one_type(tab), s_wf, s_wl, sc.jump_tolf,
                                  [rel](uint32_t w) { return __ldg(&rel[w & IDX_MASK]); }, ax, ay, az, vr, pp);
           }
           fx = ax; fy = ay; fz = az; vir = vr; pe = pp;

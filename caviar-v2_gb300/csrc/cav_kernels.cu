@@ -120,6 +120,36 @@ __global__ void __launch_bounds__(256) k_drift_vv(Dev d, Box b, StepConsts sc) {
   else half_skin_test(d, b, rep, i, x);
 }
 
+// Leap-frog first half (src/md_simulator.cpp:890-905): v += (0.5 dt) a ; r += dt v.
+// The closing half, v += (0.5 dt) a(t + dt), is the velocity-Verlet kick of the pair
+// kernel with a_old = 0: v + (a + 0)(0.5 dt) rounds exactly as v + (0.5 dt) a.
+template <bool MIXED>
+__global__ void __launch_bounds__(256) k_drift_lf(Dev d, Box b, StepConsts sc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= sc.n) return;
+  const int rep = rep_of_slot(b, i);
+  if (rep < 0) return;  // padding slot
+  dbl4 x = d.pos[i], v = d.vel[i];
+  const dbl4 a = d.acc[i];
+  nan_check(d, i, a);
+  if (MIXED) {
+    v.x = fma(a.x, sc.hdt, v.x); v.y = fma(a.y, sc.hdt, v.y); v.z = fma(a.z, sc.hdt, v.z);
+    x.x = fma(v.x, sc.dt, x.x); x.y = fma(v.y, sc.dt, x.y); x.z = fma(v.z, sc.dt, x.z);
+  } else {
+    v.x = __dadd_rn(v.x, __dmul_rn(sc.hdt, a.x));
+    v.y = __dadd_rn(v.y, __dmul_rn(sc.hdt, a.y));
+    v.z = __dadd_rn(v.z, __dmul_rn(sc.hdt, a.z));
+    x.x = __dadd_rn(x.x, __dmul_rn(sc.dt, v.x));
+    x.y = __dadd_rn(x.y, __dmul_rn(sc.dt, v.y));
+    x.z = __dadd_rn(x.z, __dmul_rn(sc.dt, v.z));
+  }
+  d.pos[i] = x;
+  d.vel[i] = v;
+  d.acc_old[i] = make_dbl4(0.0, 0.0, 0.0, 0.0);
+  if (MIXED) mixed_track(d, b, rep, i, x);
+  else half_skin_test(d, b, rep, i, x);
+}
+
 // Langevin first half (src/md_simulator.cpp:748-837):
 //   v += (a*0.5)*dt + eta*b ; [temperature here] ; r += v*c
 template <bool MIXED, bool THERMO>
@@ -774,6 +804,9 @@ int launch_drift(const Dev &d, const Box &b, const StepConsts &sc, const LaunchC
   if (lc.integrator == CAVGPU_VELOCITY_VERLET) {
     if (mixed) k_drift_vv<true><<<g, 256, 0, st>>>(d, b, sc);
     else k_drift_vv<false><<<g, 256, 0, st>>>(d, b, sc);
+  } else if (lc.integrator == CAVGPU_LEAP_FROG) {
+    if (mixed) k_drift_lf<true><<<g, 256, 0, st>>>(d, b, sc);
+    else k_drift_lf<false><<<g, 256, 0, st>>>(d, b, sc);
   } else {
     if (mixed) {
       if (thermo) k_lang_a<true, true><<<g, 256, 0, st>>>(d, b, sc, k);

@@ -108,11 +108,106 @@ void Lj::set_epsilon(int t1, int t2, double v) {
   if ((int)epsilon.size() < t1 + 1) epsilon.resize(t1 + 1);
   if ((int)epsilon[t1].size() < t2 + 1) epsilon[t1].resize(t2 + 1, 0);
   epsilon[t1][t2] = v;
+  input_by_array = true;
 }
 void Lj::set_sigma(int t1, int t2, double v) {
   if ((int)sigma.size() < t1 + 1) sigma.resize(t1 + 1);
   if ((int)sigma[t1].size() < t2 + 1) sigma[t1].resize(t2 + 1, 0);
   sigma[t1][t2] = v;
+  input_by_array = true;
+}
+void Lj::set_jump_tol(double v) {
+  jump_fix = true;
+  jump_tol = v;
+}
+void Lj::enable_wca(bool flag) {
+  wca = flag;
+  if (flag) cutoff_list_activated = true;
+}
+static void check_non_negative(const std::vector<std::vector<double>> &v, const char *what) {
+  for (auto &r : v)
+    for (double x : r)
+      if (x < 0.0) throw std::runtime_error(std::string(what) + " values must be non-negative.");
+}
+void Lj::set_lambda_s(const std::vector<std::vector<double>> &v) {
+  check_non_negative(v, "Lambda_s");
+  lambda_s = v;
+  lambda_s_is_set = true;
+}
+void Lj::set_lambda_e(const std::vector<std::vector<double>> &v) {
+  check_non_negative(v, "Lambda_e");
+  lambda_e = v;
+  lambda_e_is_set = true;
+}
+void Lj::set_epsilon_atom(int t, double v) {
+  if ((int)epsilon_atom.size() < t + 1) epsilon_atom.resize(t + 1, 0);
+  epsilon_atom[t] = v;
+  input_by_atom = true;
+}
+void Lj::set_sigma_atom(int t, double v) {
+  if ((int)sigma_atom.size() < t + 1) sigma_atom.resize(t + 1, 0);
+  sigma_atom[t] = v;
+  input_by_atom = true;
+}
+
+// The table resolution of the reference's Lj::verify_settings, step by step: the
+// tables cover every type present; per-atom input mixes by Lorentz-Berthelot
+// (sigma_ij = (sigma_i + sigma_j) / 2, epsilon_ij = sqrt(epsilon_i epsilon_j),
+// the diagonal as given); WCA sets cutoff_ij = 2^(1/6) sigma_ij from the mixed
+// sigma; lambda_s / lambda_e (missing entries 1) then scale sigma and epsilon.
+void Lj::verify_settings() {
+  if (input_by_atom && input_by_array) caviar_->log.error_all("lj: (input_by_atom && input_by_array)");
+  size_t type_max = 0;
+  for (size_t t : caviar_->atom_data.atom_struct_owned.type) type_max = std::max(type_max, t);
+  size_t n = 0;
+  if (input_by_atom) {
+    n = std::max(epsilon_atom.size(), sigma_atom.size());
+    epsilon_atom.resize(n, 0);
+    sigma_atom.resize(n, 0);
+    if (n < type_max + 1) {
+      n = type_max + 1;
+      epsilon_atom.resize(n, 0);
+      sigma_atom.resize(n, 0);
+    }
+    epsilon.assign(n, std::vector<double>(n, 0));
+    sigma.assign(n, std::vector<double>(n, 0));
+    for (size_t i = 0; i < n; ++i)
+      for (size_t j = 0; j < n; ++j) {
+        if (i == j) {
+          sigma[i][j] = sigma_atom[i];
+          epsilon[i][j] = epsilon_atom[i];
+        } else {
+          sigma[i][j] = 0.5 * (sigma_atom[i] + sigma_atom[j]);
+          epsilon[i][j] = std::sqrt(epsilon_atom[i] * epsilon_atom[j]);
+        }
+      }
+  } else if (input_by_array) {
+    n = std::max(epsilon.size(), sigma.size());
+    n = std::max(n, type_max + 1);
+    epsilon.resize(n);
+    sigma.resize(n);
+    for (auto &r : epsilon) r.resize(n, 0);
+    for (auto &r : sigma) r.resize(n, 0);
+  }
+  if (wca) {
+    const double coef = std::pow(2.0, 1.0 / 6.0);  // the LJ 6-12 minimum
+    cutoff_list.assign(n, std::vector<double>(n, 0));
+    for (size_t i = 0; i < n; ++i)
+      for (size_t j = 0; j < n; ++j) cutoff_list[i][j] = coef * sigma[i][j];
+  } else if (cutoff_list_activated) {
+    if (cutoff_list.size() < n) cutoff_list.resize(n);
+    for (auto &r : cutoff_list)
+      if (r.size() < n) r.resize(n, 0);
+  }
+  auto scale = [&](std::vector<std::vector<double>> &lam, std::vector<std::vector<double>> &tab) {
+    if (lam.size() <= type_max) lam.resize(type_max + 1);
+    for (auto &r : lam)
+      if (r.size() <= type_max) r.resize(type_max + 1, 1.0);
+    for (size_t i = 0; i < lam.size() && i < tab.size(); ++i)
+      for (size_t j = 0; j < lam[i].size() && j < tab[i].size(); ++j) tab[i][j] *= lam[i][j];
+  };
+  if (lambda_s_is_set) scale(lambda_s, sigma);
+  if (lambda_e_is_set) scale(lambda_e, epsilon);
 }
 void Lj::set_cutoff_list(const std::vector<std::vector<double>> &v) {
   for (auto &r : v)
@@ -167,8 +262,9 @@ Md_simulator::~Md_simulator() {
 
 void Md_simulator::initialize() {
   if (dt < 0.0) caviar_->log.error_all("expected 'dt' input");
-  if (integrator_type != Integrator_t::Velocity_verlet && integrator_type != Integrator_t::Velocity_verlet_langevin)
-    caviar_->log.error_all("integrator not on the GPU path (velocity-Verlet and Langevin are)");
+  if (integrator_type != Integrator_t::Velocity_verlet && integrator_type != Integrator_t::Velocity_verlet_langevin &&
+      integrator_type != Integrator_t::Leap_frog)
+    caviar_->log.error_all("integrator not on the GPU path (velocity-Verlet, Langevin and leap-frog are)");
   if (caviar_->forces.size() != 1) caviar_->log.error_all("the GPU path runs exactly one force_field::Lj");
   auto *lj = dynamic_cast<force_field::Lj *>(caviar_->forces[0]);
   if (!lj) caviar_->log.error_all("the GPU path runs force_field::Lj");
@@ -199,10 +295,12 @@ void Md_simulator::initialize() {
       p.cutoff_list[a * nt + b] = at(lj->cutoff_list, a, b);
     }
   p.cutoff_list_on = lj->cutoff_list_activated ? 1 : 0;
+  p.jump_tol = lj->jump_fix ? lj->jump_tol : 0.0;
   for (int t = 0; t < nt; ++t) p.mass[t] = t < (int)ad.atom_type_params.mass.size() ? ad.atom_type_params.mass[t] : 0.0;
   p.k_b = ad.k_b;
   p.dt = dt;
   p.integrator = integrator_type == Integrator_t::Velocity_verlet_langevin ? CAVGPU_VELOCITY_VERLET_LANGEVIN
+                 : integrator_type == Integrator_t::Leap_frog              ? CAVGPU_LEAP_FROG
                                                                            : CAVGPU_VELOCITY_VERLET;
   p.lang_temperature = langevin_param.temperature;
   p.lang_friction = langevin_param.friction;

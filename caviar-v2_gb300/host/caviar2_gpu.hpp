@@ -154,7 +154,10 @@ namespace force_field {
 class Lj : public Force_field {
  public:
   explicit Lj(Caviar2 *c) : Force_field(c) {}
-  void verify_settings() override {}
+  // Resolves the per-atom (Lorentz-Berthelot), WCA and lambda options into the
+  // epsilon / sigma / cutoff_list tables (src/force/lj.cpp:186-381).  As in the
+  // reference, nothing calls it on its own: a user of those options calls it.
+  void verify_settings() override;
   // The force at the current positions (list rebuilt when the half-skin test
   // asks) into atom_data.atom_struct_owned.acceleration, virial into virialForce.
   void calculate_acceleration() override;
@@ -162,10 +165,22 @@ class Lj : public Force_field {
   void set_epsilon(int t1, int t2, double v);
   void set_sigma(int t1, int t2, double v);
   void set_cutoff_list(const std::vector<std::vector<double>> &v);
+  void set_jump_tol(double v);      // enables the jump fix (r^2 floored at v inside the cutoff)
+  void enable_wca(bool flag = true);
+  void set_lambda_s(const std::vector<std::vector<double>> &v);
+  void set_lambda_e(const std::vector<std::vector<double>> &v);
+  void set_epsilon_atom(int t, double v);
+  void set_sigma_atom(int t, double v);
 
   double cutoff = 0.0;
   std::vector<std::vector<double>> epsilon, sigma, cutoff_list;
   bool cutoff_list_activated = false;
+  bool jump_fix = false, wca = false;
+  double jump_tol = 1e-6;
+  bool input_by_array = false, input_by_atom = false;
+  std::vector<double> epsilon_atom, sigma_atom;
+  std::vector<std::vector<double>> lambda_s, lambda_e;
+  bool lambda_s_is_set = false, lambda_e_is_set = false;
 };
 }  // namespace force_field
 

@@ -49,6 +49,7 @@ extern "C" {
 /* integrators (Integrator_t, inc/caviar2/md_simulator.hpp:34-41) */
 #define CAVGPU_VELOCITY_VERLET 0
 #define CAVGPU_VELOCITY_VERLET_LANGEVIN 1
+#define CAVGPU_LEAP_FROG 2             /* Md_simulator::integrate_leap_frog, src/md_simulator.cpp:871-980 */
 
 typedef struct cavgpu_params {
   double lo[3], hi[3];            /* Domain::set_lower_global / set_upper_global */
@@ -61,7 +62,7 @@ typedef struct cavgpu_params {
   double sigma[CAVGPU_MAX_TYPES * CAVGPU_MAX_TYPES];        /* Lj::set_sigma */
   double cutoff_list[CAVGPU_MAX_TYPES * CAVGPU_MAX_TYPES];  /* Lj::set_cutoff_list */
   int32_t cutoff_list_on;
-  int32_t integrator;             /* CAVGPU_VELOCITY_VERLET or ..._LANGEVIN */
+  int32_t integrator;             /* CAVGPU_VELOCITY_VERLET, ..._LANGEVIN or CAVGPU_LEAP_FROG */
   double mass[CAVGPU_MAX_TYPES];  /* Atom_data::add_type_mass */
   double k_b;                     /* Atom_data::set_k_b */
   double dt;                      /* Md_simulator::set_dt */
@@ -81,6 +82,8 @@ typedef struct cavgpu_params {
                                      graphs, every kernel launched from the host (for profilers,
                                      which cannot see the kernels of graphs with conditional nodes) */
   int32_t force_kernel;           /* CAVGPU_FORCE_*: pair-kernel variant of the mixed form */
+  double jump_tol;                /* Lj::set_jump_tol: r^2 of a pair inside the cutoff is floored at
+                                     jump_tol (src/force/lj.cpp:459-468); 0 = off (the default) */
 } cavgpu_params;
 
 /* pair-kernel variants of the mixed form (the FP64 form has one kernel); both give

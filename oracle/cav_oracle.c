@@ -417,6 +417,7 @@ static void lj_acceleration(orc_sys *s) {
         c = cl * cl;
       }
       if (dr_sq > c) continue;
+      if (dr_sq < s->p.jump_tol) dr_sq = s->p.jump_tol; /* jump_fix (:459-468); jump_tol 0 = off */
       const double eps_ij = s->p.eps[ti * nt + tj];
       if (eps_ij == 0) continue;
       const double sigma_ij = s->p.sigma[ti * nt + tj];
@@ -562,6 +563,25 @@ static int integrate_vv(orc_sys *s) {
   return ORC_OK;
 }
 
+/* integrate_leap_frog (:871-980): v += (0.5 dt) a; r += dt v; force; v += (0.5 dt) a */
+static int integrate_lf(orc_sys *s) {
+  const double dt = s->p.dt, hdt = 0.5 * dt;
+  const int32_t n = s->n;
+  if (any_nan_acc(s)) return ORC_E_NAN;
+  for (int32_t i = 0; i < n; ++i)
+    for (int d = 0; d < 3; ++d) {
+      s->vel[3 * i + d] += hdt * s->acc[3 * i + d];
+      s->pos[3 * i + d] += dt * s->vel[3 * i + d];
+    }
+  int rc = re_calculate_acc(s);
+  if (rc) return rc;
+  for (int32_t i = 0; i < n; ++i)
+    for (int d = 0; d < 3; ++d) s->vel[3 * i + d] += hdt * s->acc[3 * i + d];
+  finalize_temperature(s);
+  finalize_pressure(s);
+  return ORC_OK;
+}
+
 /* integrate_velocity_verlet_langevin (:731-869) and its coefficients (:394-416) */
 static int integrate_langevin(orc_sys *s) {
   const double dt = s->p.dt;
@@ -673,7 +693,7 @@ int32_t orc_step(orc_sys *s, int32_t nsteps) {
   }
   for (int32_t k = 0; k < nsteps; ++k) {
     s->virial = 0.0;
-    int rc = s->p.integrator == 1 ? integrate_langevin(s) : integrate_vv(s);
+    int rc = s->p.integrator == 1 ? integrate_langevin(s) : (s->p.integrator == 2 ? integrate_lf(s) : integrate_vv(s));
     if (rc) return rc;
     s->current_step++;
   }

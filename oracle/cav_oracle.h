@@ -58,10 +58,11 @@ typedef struct orc_params {
   int32_t cutoff_list_on;
   int32_t use_cell_list;        /* Neighborlist::set_make_verlet_list_from_cell_list */
   int32_t n_r_df;               /* Atom_data::set_n_r_df (0..3) */
-  int32_t integrator;           /* 0 velocity-Verlet, 1 velocity-Verlet-Langevin */
+  int32_t integrator;           /* 0 velocity-Verlet, 1 velocity-Verlet-Langevin, 2 leap-frog */
   int32_t noise_mode;           /* Langevin: 0 eta = 0, 1 Philox */
   int32_t pressure_process;     /* Atom_data::set_pressure_process */
   int32_t rebuild_test;         /* Neighborlist::set_rebuild_test: rebuild on every step */
+  double jump_tol;              /* Lj::set_jump_tol (src/force/lj.cpp:82-86); 0 = off */
 } orc_params;
 
 typedef struct orc_sys orc_sys;

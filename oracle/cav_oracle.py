@@ -26,7 +26,7 @@ class OrcParams(C.Structure):
         ("lang_kb", C.c_double), ("lang_kbt", C.c_double), ("seed", C.c_uint64),
         ("cutoff_list_on", C.c_int32), ("use_cell_list", C.c_int32), ("n_r_df", C.c_int32),
         ("integrator", C.c_int32), ("noise_mode", C.c_int32), ("pressure_process", C.c_int32),
-        ("rebuild_test", C.c_int32),
+        ("rebuild_test", C.c_int32), ("jump_tol", C.c_double),
     ]
 
 
@@ -101,6 +101,7 @@ def make_params(p, noise_mode=1):
     o.noise_mode = noise_mode
     o.pressure_process = p.get("pressure_process", 1)
     o.rebuild_test = int(p.get("rebuild_test", 0))
+    o.jump_tol = float(p.get("jump_tol", 0.0))
     return o
 
 

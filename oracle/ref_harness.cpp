@@ -7,12 +7,21 @@
 // used as the strongest pin of oracle/cav_oracle.c.  Nothing shipped links it.
 //
 // Input file (little endian), written by tests/golden/make_golden.py:
-//   int32  magic 'CAVH', N, ntypes, nsteps, integrator(0 VV,1 Langevin),
+//   int32  magic 'CAVH', N, ntypes, nsteps, integrator(0 VV,1 Langevin,2 leap-frog),
 //          use_cell_list, n_r_df, pressure_process, cutoff_list_on, pad
 //   double lo[3], hi[3], nl_cutoff, nl_coef, ghost_cutoff, lj_cutoff, k_b,
 //          dt, lang_T, lang_friction, lang_kb
 //   double eps[nt*nt], sigma[nt*nt], cutoff_list[nt*nt], mass[nt]
 //   double pos[3N], vel[3N]; int32 type[N]
+//   extension block, present per bit of the header's last word (`ext`):
+//     bit 0: double jump_tol                      -> Lj::set_jump_tol
+//     bit 1: (nothing)                            -> Lj::enable_wca
+//     bit 2: double eps_atom[nt], sigma_atom[nt]  -> Lj::set_epsilon_atom / set_sigma_atom
+//                                                    (instead of set_epsilon / set_sigma)
+//     bit 3: double lambda_s[nt*nt], lambda_e[nt*nt] -> Lj::set_lambda_s / set_lambda_e
+//   Bits 1-3 take effect in Lj::verify_settings (src/force/lj.cpp:186-381), which
+//   the library itself never calls; the harness calls it, as a user of these
+//   options must, and appends the effective tables to the output.
 // Output file: see write_* below (sections in fixed order).
 //
 // Field pinning.  Caviar2 holds Domain/Atom_data/Md_simulator by value and
@@ -20,7 +29,29 @@
 // which leaves members without initialisers undefined (the cell-list path
 // then divides by a garbage Domain::nprocs_x at src/domain.cpp:320-327).  The
 // harness constructs Caviar2 in zeroed memory and pins every such field.
+// Lj keeps its effective tables private; this test harness reads them after
+// verify_settings, so it sees the reference's headers with private members
+// exposed (the member layout GCC gives a class does not depend on access).  The
+// standard headers come first so that only the reference's own classes change.
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdint>
+#include <fstream>
+#include <functional>
+#include <iostream>
+#include <map>
+#include <memory>
+#include <random>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
+#include <vector>
+#define private public
 #include "caviar2/caviar2.hpp"
+#include "caviar2/force/lj.hpp"
+#undef private
 
 #include <cstdio>
 #include <cstdlib>
@@ -79,7 +110,7 @@ int main(int argc, char **argv) {
   double dp[15];
   if (!rd(fi, h, 10) || h[0] != 0x48564143) return 4;
   const int N = h[1], nt = h[2], nsteps = h[3], integ = h[4], cell = h[5], nrdf = h[6],
-            pproc = h[7], clon = h[8];
+            pproc = h[7], clon = h[8], ext = h[9];
   if (!rd(fi, dp, 15)) return 5;
   std::vector<double> eps(nt * nt), sig(nt * nt), cl(nt * nt), mass(nt), pos(3 * N), vel(3 * N);
   std::vector<int32_t> type(N);
@@ -87,6 +118,11 @@ int main(int argc, char **argv) {
       !rd(fi, mass.data(), mass.size()) || !rd(fi, pos.data(), pos.size()) || !rd(fi, vel.data(), vel.size()) ||
       !rd(fi, type.data(), type.size()))
     return 6;
+  double jump_tol = 0.0;
+  std::vector<double> eps_atom(nt), sig_atom(nt), lam_s(nt * nt), lam_e(nt * nt);
+  if ((ext & 1) && !rd(fi, &jump_tol, 1)) return 8;
+  if ((ext & 4) && (!rd(fi, eps_atom.data(), nt) || !rd(fi, sig_atom.data(), nt))) return 8;
+  if ((ext & 8) && (!rd(fi, lam_s.data(), lam_s.size()) || !rd(fi, lam_e.data(), lam_e.size()))) return 8;
   fclose(fi);
 
   void *mem = calloc(1, sizeof(Caviar2));
@@ -124,18 +160,35 @@ int main(int argc, char **argv) {
   // ---- force field ----
   force_field::Lj lj(&c);
   lj.set_cutoff(dp[9]);
-  for (int a = 0; a < nt; ++a)
-    for (int b = 0; b < nt; ++b) {  // both triangles: verify_settings is never called
-      lj.set_epsilon(a, b, eps[a * nt + b]);
-      lj.set_sigma(a, b, sig[a * nt + b]);
+  if (ext & 4) {
+    for (int a = 0; a < nt; ++a) {
+      lj.set_epsilon_atom(a, eps_atom[a]);
+      lj.set_sigma_atom(a, sig_atom[a]);
     }
+  } else {
+    for (int a = 0; a < nt; ++a)
+      for (int b = 0; b < nt; ++b) {  // both triangles: verify_settings is never called
+        lj.set_epsilon(a, b, eps[a * nt + b]);
+        lj.set_sigma(a, b, sig[a * nt + b]);
+      }
+  }
   if (clon) {
     std::vector<std::vector<double>> cll(nt, std::vector<double>(nt));
     for (int a = 0; a < nt; ++a)
       for (int b = 0; b < nt; ++b) cll[a][b] = cl[a * nt + b];
     lj.set_cutoff_list(cll);
   }
+  if (ext & 1) lj.set_jump_tol(jump_tol);
+  if (ext & 2) lj.enable_wca(true);
+  if (ext & 8) {
+    std::vector<std::vector<double>> ls(nt, std::vector<double>(nt)), le(nt, std::vector<double>(nt));
+    for (int a = 0; a < nt; ++a)
+      for (int b = 0; b < nt; ++b) { ls[a][b] = lam_s[a * nt + b]; le[a][b] = lam_e[a * nt + b]; }
+    lj.set_lambda_s(ls);
+    lj.set_lambda_e(le);
+  }
   c.add_force_field(&lj);
+  if (ext & 14) lj.verify_settings();
 
   // ---- Md_simulator ----
   c.md_simulator.initialized = false;
@@ -146,6 +199,8 @@ int main(int argc, char **argv) {
     c.md_simulator.langevin_friction(dp[13]);
     c.md_simulator.langevin_kb(dp[14]);
     c.md_simulator.langevin_temperature(dp[12]);
+  } else if (integ == 2) {
+    c.md_simulator.set_integrator_type(Integrator_t::Leap_frog);
   } else {
     c.md_simulator.set_integrator_type(Integrator_t::Velocity_verlet);
   }
@@ -215,6 +270,21 @@ int main(int argc, char **argv) {
       buf[3 * i] = v[i].x; buf[3 * i + 1] = v[i].y; buf[3 * i + 2] = v[i].z;
     }
     wr(fo, buf.data(), buf.size());
+  }
+  // section 5 (Lj options only): the effective tables after Lj::verify_settings
+  if (ext & 14) {
+    std::vector<double> te(nt * nt), ts(nt * nt), tc(nt * nt);
+    for (int a = 0; a < nt; ++a)
+      for (int b = 0; b < nt; ++b) {
+        te[a * nt + b] = lj.epsilon[a][b];
+        ts[a * nt + b] = lj.sigma[a][b];
+        tc[a * nt + b] = lj.cutoff_list_activated ? lj.cutoff_list[a][b] : 0.0;
+      }
+    int32_t clo = lj.cutoff_list_activated ? 1 : 0;
+    wr(fo, te.data(), te.size());
+    wr(fo, ts.data(), ts.size());
+    wr(fo, tc.data(), tc.size());
+    wr(fo, &clo, 1);
   }
   fclose(fo);
   return 0;

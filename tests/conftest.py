@@ -30,10 +30,18 @@ def load_golden(name):
 def golden_params(g):
     """Parameter dict (workloads vocabulary) of a golden case."""
     nt = int(g["ntypes"])
+    # cases with Lj options carry the tables Lj::verify_settings made of them
+    if "eff_eps" in g:
+        eps, sigma = g["eff_eps"], g["eff_sigma"]
+        cutoff_list = g["eff_cutoff_list"] if int(g["eff_cutoff_list_on"]) else None
+    else:
+        eps, sigma = g["eps"], g["sigma"]
+        cutoff_list = g["cutoff_list"] if int(g["cutoff_list_on"]) else None
     return dict(
         lo=g["lo"], hi=g["hi"], ntypes=nt, nl_cutoff=float(g["nl_cutoff"]), nl_coef=float(g["nl_coef"]),
-        ghost_cutoff=float(g["ghost_cutoff"]), lj_cutoff=float(g["lj_cutoff"]), eps=g["eps"], sigma=g["sigma"],
-        cutoff_list=g["cutoff_list"] if int(g["cutoff_list_on"]) else None, mass=g["mass"], k_b=float(g["k_b"]),
+        ghost_cutoff=float(g["ghost_cutoff"]), lj_cutoff=float(g["lj_cutoff"]), eps=eps, sigma=sigma,
+        cutoff_list=cutoff_list, jump_tol=float(g["jump_tol"]) if "jump_tol" in g else 0.0,
+        mass=g["mass"], k_b=float(g["k_b"]),
         dt=float(g["dt"]), integrator=int(g["integrator"]), lang_temperature=float(g["lang_temperature"]),
         lang_friction=float(g["lang_friction"]), lang_kb=float(g["lang_kb"]), seed=0, n_r_df=int(g["n_r_df"]),
         use_cell_list=int(g["use_cell_list"]), pressure_process=int(g["pressure_process"]),

@@ -23,13 +23,20 @@ int main(int argc, char **argv) {
   int32_t h[10];
   double dp[15];
   if (!rd(fi, h, 10) || h[0] != 0x48564143 || !rd(fi, dp, 15)) return 4;
-  const int N = h[1], nt = h[2], nsteps = h[3], integ = h[4], cell = h[5], nrdf = h[6], pproc = h[7], clon = h[8];
+  const int N = h[1], nt = h[2], nsteps = h[3], integ = h[4], cell = h[5], nrdf = h[6], pproc = h[7], clon = h[8],
+            ext = h[9];
   std::vector<double> eps(nt * nt), sig(nt * nt), cl(nt * nt), mass(nt), pos(3 * N), vel(3 * N);
   std::vector<int32_t> type(N);
   if (!rd(fi, eps.data(), eps.size()) || !rd(fi, sig.data(), sig.size()) || !rd(fi, cl.data(), cl.size()) ||
       !rd(fi, mass.data(), mass.size()) || !rd(fi, pos.data(), pos.size()) || !rd(fi, vel.data(), vel.size()) ||
       !rd(fi, type.data(), type.size()))
     return 5;
+  // extension block (oracle/ref_harness.cpp): jump_tol, WCA, per-atom eps/sigma, lambda tables
+  double jump_tol = 0.0;
+  std::vector<double> eps_atom(nt), sig_atom(nt), lam_s(nt * nt), lam_e(nt * nt);
+  if ((ext & 1) && !rd(fi, &jump_tol, 1)) return 5;
+  if ((ext & 4) && (!rd(fi, eps_atom.data(), nt) || !rd(fi, sig_atom.data(), nt))) return 5;
+  if ((ext & 8) && (!rd(fi, lam_s.data(), lam_s.size()) || !rd(fi, lam_e.data(), lam_e.size()))) return 5;
   fclose(fi);
 
   Caviar2 caviar;
@@ -59,18 +66,52 @@ int main(int argc, char **argv) {
 
   force_field::Lj lj(&caviar);
   lj.set_cutoff(dp[9]);
-  for (int a = 0; a < nt; ++a)
-    for (int b = 0; b < nt; ++b) {
-      lj.set_epsilon(a, b, eps[a * nt + b]);
-      lj.set_sigma(a, b, sig[a * nt + b]);
+  if (ext & 4) {
+    for (int a = 0; a < nt; ++a) {
+      lj.set_epsilon_atom(a, eps_atom[a]);
+      lj.set_sigma_atom(a, sig_atom[a]);
     }
+  } else {
+    for (int a = 0; a < nt; ++a)
+      for (int b = 0; b < nt; ++b) {
+        lj.set_epsilon(a, b, eps[a * nt + b]);
+        lj.set_sigma(a, b, sig[a * nt + b]);
+      }
+  }
   if (clon) {
     std::vector<std::vector<double>> cll(nt, std::vector<double>(nt));
     for (int a = 0; a < nt; ++a)
       for (int b = 0; b < nt; ++b) cll[a][b] = cl[a * nt + b];
     lj.set_cutoff_list(cll);
   }
+  if (ext & 1) lj.set_jump_tol(jump_tol);
+  if (ext & 2) lj.enable_wca(true);
+  if (ext & 8) {
+    std::vector<std::vector<double>> ls(nt, std::vector<double>(nt)), le(nt, std::vector<double>(nt));
+    for (int a = 0; a < nt; ++a)
+      for (int b = 0; b < nt; ++b) { ls[a][b] = lam_s[a * nt + b]; le[a][b] = lam_e[a * nt + b]; }
+    lj.set_lambda_s(ls);
+    lj.set_lambda_e(le);
+  }
   caviar.add_force_field(&lj);
+  if (ext & 14) lj.verify_settings();
+  if (argc > 3 && !std::strcmp(argv[3], "tables")) {  // the resolved pair tables only (no GPU needed)
+    FILE *fo = fopen(argv[2], "wb");
+    if (!fo) return 7;
+    auto at = [](const std::vector<std::vector<double>> &t, int i, int j) {
+      return (i < (int)t.size() && j < (int)t[i].size()) ? t[i][j] : 0.0;
+    };
+    for (auto *t : {&lj.epsilon, &lj.sigma, &lj.cutoff_list})
+      for (int a = 0; a < nt; ++a)
+        for (int b = 0; b < nt; ++b) {
+          const double v = at(*t, a, b);
+          wr(fo, &v, 1);
+        }
+    const int32_t clo = lj.cutoff_list_activated ? 1 : 0;
+    wr(fo, &clo, 1);
+    fclose(fo);
+    return 0;
+  }
 
   Md_simulator &md = caviar.md_simulator;
   if (integ == 1) {
@@ -78,6 +119,8 @@ int main(int argc, char **argv) {
     md.langevin_friction(dp[13]);
     md.langevin_kb(dp[14]);
     md.langevin_temperature(dp[12]);
+  } else if (integ == 2) {
+    md.set_integrator_type(Integrator_t::Leap_frog);
   } else {
     md.set_integrator_type(Integrator_t::Velocity_verlet);
   }

@@ -27,11 +27,18 @@ OUT = os.path.dirname(os.path.abspath(__file__))
 FULL_PAIRS_MAX_N = 600
 
 
+def ext_flags(p):
+    """Extension bits of the harness input: jump_tol, WCA, per-atom mixing, lambda tables."""
+    return ((1 if p.get("jump_tol") else 0) | (2 if p.get("wca") else 0) | (4 if p.get("eps_atom") is not None else 0)
+            | (8 if p.get("lambda_s") is not None else 0))
+
+
 def write_input(path, pos, vel, typ, p, nsteps):
     nt = int(p["ntypes"])
     cl = p.get("cutoff_list")
+    ext = ext_flags(p)
     hdr = np.array([0x48564143, len(pos), nt, nsteps, p["integrator"], p["use_cell_list"], p["n_r_df"],
-                    p["pressure_process"], 0 if cl is None else 1, 0], dtype=np.int32)
+                    p["pressure_process"], 0 if cl is None else 1, ext], dtype=np.int32)
     dp = np.array(list(p["lo"]) + list(p["hi"]) + [p["nl_cutoff"], p["nl_coef"], p["ghost_cutoff"],
                   p["lj_cutoff"], p["k_b"], p["dt"], p["lang_temperature"], p["lang_friction"],
                   p["lang_kb"]], dtype=np.float64)
@@ -45,6 +52,14 @@ def write_input(path, pos, vel, typ, p, nsteps):
         f.write(np.ascontiguousarray(pos, np.float64).tobytes())
         f.write(np.ascontiguousarray(vel, np.float64).tobytes())
         f.write(np.ascontiguousarray(typ, np.int32).tobytes())
+        if ext & 1:
+            f.write(np.array([p["jump_tol"]], np.float64).tobytes())
+        if ext & 4:
+            f.write(np.asarray(p["eps_atom"], np.float64).tobytes())
+            f.write(np.asarray(p["sigma_atom"], np.float64).tobytes())
+        if ext & 8:
+            f.write(np.asarray(p["lambda_s"], np.float64).reshape(nt, nt).tobytes())
+            f.write(np.asarray(p["lambda_e"], np.float64).reshape(nt, nt).tobytes())
 
 
 class Reader:
@@ -91,6 +106,23 @@ def run_case(name, pos, vel, typ, p, nsteps):
     acc_f = r.take(np.float64, 3 * n).reshape(n, 3)
     nt = int(p["ntypes"])
     cl = p.get("cutoff_list")
+    ext = ext_flags(p)
+    extra = {}
+    if ext & 14:  # the effective tables after Lj::verify_settings
+        extra["eff_eps"] = r.take(np.float64, nt * nt).reshape(nt, nt)
+        extra["eff_sigma"] = r.take(np.float64, nt * nt).reshape(nt, nt)
+        extra["eff_cutoff_list"] = r.take(np.float64, nt * nt).reshape(nt, nt)
+        (extra["eff_cutoff_list_on"],) = r.take(np.int32, 1)
+    if ext & 1:
+        extra["jump_tol"] = np.float64(p["jump_tol"])
+    if ext & 2:
+        extra["wca"] = np.int32(1)
+    if ext & 4:
+        extra["eps_atom"] = np.asarray(p["eps_atom"], np.float64)
+        extra["sigma_atom"] = np.asarray(p["sigma_atom"], np.float64)
+    if ext & 8:
+        extra["lambda_s"] = np.asarray(p["lambda_s"], np.float64).reshape(nt, nt)
+        extra["lambda_e"] = np.asarray(p["lambda_e"], np.float64).reshape(nt, nt)
     out = dict(
         # inputs
         pos=pos, vel=vel, typ=typ.astype(np.int32), nsteps=np.int32(nsteps),
@@ -105,7 +137,7 @@ def run_case(name, pos, vel, typ, p, nsteps):
         # outputs of the reference
         acc0=acc0, virial0=virial0, ke0=ke0, t0=t0, nbins=nb, bins=bins, ghost_src=gsrc, ghost_pos=gpos,
         ghost_bins=gbins, npairs=np.int64(len(pairs)), pairs_sha256=np.array(pairs_digest(pairs)),
-        thermo=thermo, pos_final=pos_f, vel_final=vel_f, acc_final=acc_f,
+        thermo=thermo, pos_final=pos_f, vel_final=vel_f, acc_final=acc_f, **extra,
     )
     if n <= FULL_PAIRS_MAX_N:
         out["pairs"] = pairs
@@ -166,13 +198,33 @@ def cases():
     vel = np.random.default_rng(1).uniform(-0.5, 0.5, pos.shape)
     vel -= vel.mean(0)
     yield "t002_grid512", pos, vel, np.zeros(len(pos), np.int32), p, 100
+    # leap-frog integrator (Md_simulator::integrate_leap_frog)
+    pos, vel, typ, p = W.lj_fluid((5, 5, 5), seed=51, integrator=2)
+    yield "fcc500_leapfrog", pos, vel, typ, p, 100
+    # Lj jump_fix: r^2 floored at jump_tol inside the cutoff; a few atoms moved close to a neighbour
+    pos, vel, typ, p = W.lj_fluid((4, 4, 4), seed=61, temperature=0.5)
+    a = (4.0 / 0.8442) ** (1.0 / 3.0)
+    for k in range(0, 40, 8):  # atom k+1 is a lattice neighbour of atom k at a / sqrt(2)
+        d = pos[k + 1] - pos[k]
+        pos[k + 1] = np.mod(pos[k] + d * (0.82 / np.linalg.norm(d)), p["hi"])
+    yield "fcc256_jumpfix", pos, vel, typ, dict(p, jump_tol=0.81), 30
+    # Lj options resolved in Lj::verify_settings: per-atom Lorentz-Berthelot mixing, WCA cutoffs,
+    # lambda scaling of sigma and epsilon (two types, 80:20)
+    pos, vel, typ, p = W.kob_andersen(n=864, seed=71, temperature=1.0)
+    p = dict(p, integrator=0, lang_friction=0.0, n_r_df=3, cutoff_list=None, wca=1,
+             eps_atom=[1.0, 0.6], sigma_atom=[1.0, 0.85],
+             lambda_s=[[1.0, 0.95], [0.95, 1.0]], lambda_e=[[1.0, 1.1], [1.1, 0.9]])
+    yield "ka864_wca_mixing_lambda", pos, vel, typ, p, 60
 
 
 def main():
+    # usage: make_golden.py [reference checkout] [case names...]  (no names: every case)
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    only = set(sys.argv[2:])
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={ref}", "-j8"], check=True)
     for c in cases():
-        run_case(*c)
+        if not only or c[0] in only:
+            run_case(*c)
 
 
 if __name__ == "__main__":

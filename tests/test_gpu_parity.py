@@ -58,16 +58,18 @@ def case(request, gpu):
 def virial_terms(g, pairs):
     """Per-pair virial terms -coef*r^2 of the canonical pair rows, with the reference's
     own expression (src/force/lj.cpp:449-489), both orders of every pair."""
-    nt = int(g["ntypes"])
+    p = golden_params(g)  # the resolved tables of cases with Lj options
     typ = g["typ"]
     L = g["hi"] - g["lo"]
     i, j = pairs[:, 0], pairs[:, 1]
     d = (g["pos"][j] + pairs[:, 2:5] * L) - g["pos"][i]
-    r2 = (d * d).sum(1)
+    r2d = (d * d).sum(1)
     ti, tj = typ[i], typ[j]
-    rc = g["cutoff_list"][ti, tj] if int(g["cutoff_list_on"]) else np.full(len(r2), float(g["lj_cutoff"]))
+    cl = p["cutoff_list"]
+    rc = cl[ti, tj] if cl is not None else np.full(len(r2d), float(g["lj_cutoff"]))
     c = rc * rc
-    eps, sig = g["eps"][ti, tj], g["sigma"][ti, tj]
+    r2 = np.maximum(r2d, p["jump_tol"])  # jump_fix floor (0 when off), after the cutoff test
+    eps, sig = p["eps"][ti, tj], p["sigma"][ti, tj]
     rcinv = 1 / c
     rc2 = sig * sig * rcinv
     rc6 = rc2 * rc2 * rc2
@@ -75,7 +77,7 @@ def virial_terms(g, pairs):
     rho2 = sig * sig * r2i
     rho6 = rho2 * rho2 * rho2
     coef = 4 * eps * (-12 * rho6 * rho6 * r2i + 6 * rho6 * r2i + 12 * rc6 * rc6 * rcinv - 6 * rc6 * rcinv)
-    keep = (r2 <= c) & (eps != 0)
+    keep = (r2d <= c) & (eps != 0)
     return (-coef * r2)[keep]
 
 
@@ -136,7 +138,7 @@ def test_trajectory(case):
     assert force_err(acc, g["acc_final"]) <= 1e-9, name
     # per-step temperature, virial and pressure
     np.testing.assert_allclose(th[:, 1], g["thermo"][:, 0], rtol=1e-9, atol=1e-14)
-    if int(g["integrator"]) == 0:
+    if int(g["integrator"]) in (0, 2):  # velocity Verlet, leap-frog: virial of the last force call
         np.testing.assert_allclose(th[:, 3], g["thermo"][:, 1], rtol=1e-9, atol=1e-12)
     np.testing.assert_allclose(th[:, 2], g["thermo"][:, 2], rtol=1e-9, atol=1e-12)
 

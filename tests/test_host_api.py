@@ -92,6 +92,28 @@ def test_host_api_mixed_precision_force_error(tmp_path):
     assert rms < 1e-4  # after 100 steps of the mixed form: trajectories drift apart slowly
 
 
+@pytest.mark.parametrize("name", [c for c in golden_cases() if "eff_eps" in load_golden(c)])
+def test_lj_option_tables_match_reference(name, tmp_path):
+    """force_field::Lj::verify_settings of the host API (per-atom mixing, WCA, lambda)
+    against the tables the reference's own verify_settings produced (CPU only)."""
+    g = load_golden(name)
+    p = golden_params(g)
+    for k in ("jump_tol", "wca", "eps_atom", "sigma_atom", "lambda_s", "lambda_e"):
+        if k in g:
+            p[k] = g[k]
+    # the inputs the reference was given, not the tables it resolved
+    p["eps"], p["sigma"] = g["eps"], g["sigma"]
+    p["cutoff_list"] = g["cutoff_list"] if int(g["cutoff_list_on"]) else None
+    fin, fout = tmp_path / "in.bin", tmp_path / "out.bin"
+    MG.write_input(str(fin), g["pos"], g["vel"], g["typ"], p, 0)
+    subprocess.run([harness(), str(fin), str(fout), "tables"], check=True, stdout=subprocess.DEVNULL)
+    r = MG.Reader(open(fout, "rb").read())
+    nt = int(g["ntypes"])
+    for key in ("eff_eps", "eff_sigma", "eff_cutoff_list"):
+        np.testing.assert_array_equal(r.take(np.float64, nt * nt).reshape(nt, nt), g[key])
+    assert int(r.take(np.int32, 1)[0]) == int(g["eff_cutoff_list_on"])
+
+
 def test_host_library_builds_and_loads():
     import ctypes
 
