@@ -19,7 +19,8 @@ MAXT = 8
 OK, E_ARG, E_CUDA, E_NAN, E_NLIST_OVERFLOW, E_STATE, E_NOMEM, E_RANGE = 0, -1, -2, -3, -4, -5, -6, -7
 FP64, MIXED = 0, 1
 FORCE_AUTO, FORCE_STRIDED, FORCE_SEGMENTS = 0, 1, 2
-VELOCITY_VERLET, VELOCITY_VERLET_LANGEVIN = 0, 1
+NVE_ENERGY_PER_DOF, NVE_ENERGY_TOT, NVE_KBT, NVE_KB_TEMPERATURE = 0, 1, 2, 3
+VELOCITY_VERLET, VELOCITY_VERLET_LANGEVIN, LEAP_FROG = 0, 1, 2
 
 
 class Params(C.Structure):
@@ -35,6 +36,8 @@ class Params(C.Structure):
         ("n_r_df", C.c_int32), ("pressure_process", C.c_int32), ("precision", C.c_int32), ("noise_off", C.c_int32),
         ("nbr_capacity", C.c_int32), ("threads_per_atom", C.c_int32), ("block_size", C.c_int32),
         ("steps_per_graph", C.c_int32), ("force_kernel", C.c_int32), ("jump_tol", C.c_double),
+        ("initial_step", C.c_int64), ("nve_step", C.c_int64), ("nve_mode", C.c_int32), ("nve_pad", C.c_int32),
+        ("nve_value", C.c_double), ("nve_kb", C.c_double),
     ]
 
 
@@ -143,6 +146,11 @@ def make_params(p, precision=FP64, noise_off=False, tpa=0, block=0, nbr_capacity
     o.nbr_capacity, o.steps_per_graph = int(nbr_capacity), int(steps_per_graph)
     o.force_kernel = int(force_kernel)
     o.jump_tol = float(p.get("jump_tol", 0.0))
+    o.initial_step = int(p.get("initial_step", 0))
+    nve = p.get("nve")  # {"step": k, "mode": CAVGPU_NVE_*, "value": x, "kb": y}
+    if nve:
+        o.nve_step, o.nve_mode = int(nve["step"]), int(nve["mode"])
+        o.nve_value, o.nve_kb = float(nve["value"]), float(nve.get("kb", 0.0))
     return o
 
 

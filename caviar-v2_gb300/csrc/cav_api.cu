@@ -53,6 +53,7 @@ struct cavgpu_ctx {
   cudaStream_t st = nullptr;
   cudaStream_t side = nullptr;  // captures the bodies of the conditional rebuild nodes
   int natoms = 0;               // atoms over all replicas
+  NveCfg nve{};                 // constraint::Nve (step 0 = off)
   bool uploaded = false, set_up = false;
   long long steps_done = 0;
   long long graph_launches = 0, kernel_launches = 0;
@@ -146,6 +147,10 @@ int enqueue_step(cavgpu_ctx *c, int k, bool thermo, int ring_slot) {
   if (c->prof && k < (int)c->ev1.size()) CK(cudaEventRecord(c->ev1[k], c->st));
   c->kernel_launches += REBUILD_KERNELS + 1;
   if (thermo) RK(enqueue_thermo_after_force(c, ring_slot));
+  if (c->nve.step > 0) {  // constraint::Nve after the temperature (src/md_simulator.cpp:681-694)
+    RK(launch_nve(c->d, c->b, c->tc, c->nve, k, thermo, ring_slot, c->st));
+    c->kernel_launches += 3;
+  }
   return CAVGPU_OK;
 }
 
@@ -186,6 +191,10 @@ int capture_step(cavgpu_ctx *c, int k, bool thermo, int ring_slot) {
   RK(launch_force(c->d, c->b, c->sc, c->lc, is_lang(c) ? 2 : 1, thermo, k, c->st));
   if (c->prof && k < (int)c->ev1.size()) CK(cudaEventRecordWithFlags(c->ev1[k], c->st, cudaEventRecordExternal));
   if (thermo) RK(enqueue_thermo_after_force(c, ring_slot));
+  if (c->nve.step > 0) {  // constraint::Nve after the temperature (src/md_simulator.cpp:681-694)
+    RK(launch_nve(c->d, c->b, c->tc, c->nve, k, thermo, ring_slot, c->st));
+    c->kernel_launches += 3;
+  }
   return CAVGPU_OK;
 }
 
@@ -387,7 +396,19 @@ int create_common(const cavgpu_params *p, int nrep, const double *lo3, const dou
   }
   sc.seed = p->seed;
   sc.noise_off = p->noise_off;
-  if (p->jump_tol < 0.0) { delete c; return CAVGPU_E_ARG; }
+  if (p->jump_tol < 0.0 || p->initial_step < 0) { delete c; return CAVGPU_E_ARG; }
+  if (p->nve_step > 0) {  // constraint::Nve: velocity Verlet or leap-frog, one system (checked at upload)
+    if (p->integrator == CAVGPU_VELOCITY_VERLET_LANGEVIN || p->nve_mode < CAVGPU_NVE_ENERGY_PER_DOF ||
+        p->nve_mode > CAVGPU_NVE_KB_TEMPERATURE || !(p->nve_value > 0.0) ||
+        (p->nve_mode == CAVGPU_NVE_KB_TEMPERATURE && !(p->nve_kb > 0.0))) {
+      delete c;
+      return CAVGPU_E_ARG;
+    }
+    c->nve.step = p->nve_step;
+    c->nve.mode = p->nve_mode;
+    c->nve.value = p->nve_value;
+    c->nve.kb = p->nve_kb;
+  }
   sc.jump_tol = p->jump_tol;  // Lj::set_jump_tol (src/force/lj.cpp:82-86); 0 = off
   sc.jump_tolf = (float)p->jump_tol;
   // launch shape
@@ -415,7 +436,8 @@ int create_common(const cavgpu_params *p, int nrep, const double *lo3, const dou
   if (!rc) rc = cuda_rc(cudaMemcpyAsync(c->d.tab, &c->tab_h, sizeof(PairTab), cudaMemcpyHostToDevice, c->st));
   if (!rc) rc = cuda_rc(cudaMemsetAsync(c->d.flags, 0, F_NWORDS * sizeof(int), c->st));
   if (!rc) rc = cuda_rc(cudaMemsetAsync(c->d.thermo, 0, 8 * sizeof(double), c->st));
-  if (!rc) rc = cuda_rc(cudaMemsetAsync(c->d.step_base, 0, sizeof(long long), c->st));
+  const long long step0 = p->initial_step;  // Md_simulator::initial_step
+  if (!rc) rc = cuda_rc(cudaMemcpyAsync(c->d.step_base, &step0, sizeof(long long), cudaMemcpyHostToDevice, c->st));
   if (!rc) rc = cuda_rc(cudaStreamSynchronize(c->st));
   if (rc) { cavgpu_destroy(c); return rc; }
   *out = c;
@@ -560,6 +582,11 @@ int upload_common(cavgpu_ctx *c, const int64_t *counts, const double *pos3, cons
   if (!rc) rc = dalloc(c, &d.partials_ev, 2 * nblk);
   if (!rc) rc = dalloc(c, &d.h3, 3 * (size_t)N);
   if (!rc) rc = dalloc(c, &d.hi3, 3 * (size_t)N);
+  if (c->nve.step > 0) {
+    if (R > 1) return CAVGPU_E_ARG;  // constraint::Nve acts on one system's kinetic energy
+    if (!rc) rc = dalloc(c, &d.nve_partials, 4 * (size_t)NVE_BLOCKS);
+    if (!rc) rc = dalloc(c, &d.nve_lambda, 1);
+  }
   RepBox *drep = nullptr;
   int *dflag = nullptr;
   if (!rc) rc = dalloc(c, &drep, R);
@@ -738,7 +765,7 @@ int cavgpu_run(cavgpu_ctx *c, int64_t nsteps, int64_t every, double *out5) {
     c->graph_launches += 1;
     // drift + condition + force per step, the thermo folds, the step counter; the
     // rebuild kernels that ran are added from the device's rebuild count below
-    c->kernel_launches += (long long)sz * 3 + 1 + nrec * (c->b.nrep > 1 && is_lang(c) ? 2 : 1);
+    c->kernel_launches += (long long)sz * (c->nve.step > 0 ? 6 : 3) + 1 + nrec * (c->b.nrep > 1 && is_lang(c) ? 2 : 1);
     if (c->prof) RK(collect_profile(c, sz));
     if (every > 0) {
       CK(cudaMemcpyAsync(out5 + THERMO_REC * rec, c->d.thermo_ring, THERMO_REC * sizeof(double) * nrec,

@@ -128,7 +128,9 @@ struct Dev {
   double *thermo;             // {KE, T, P, virialForce, PE, total mass, -, -}
   double *thermo_rep;         // batches: per replica {KE, T, P, virialForce, PE, total mass, -, -}
   double *thermo_ring;        // recorded thermo points (THERMO_REC per record)
-  long long *step_base;       // step counter read by the Langevin kernels
+  long long *step_base;       // index of the chunk's first step (Langevin noise, Nve schedule)
+  double *nve_partials;       // Nve: per-block {sum m v^2, sum m v} (4 per block, NVE_BLOCKS blocks)
+  double *nve_lambda;         // Nve: the scale factor of the current step
   PairTab *tab;
   // host-order staging for downloads
   double *h3;
@@ -255,6 +257,17 @@ int launch_thermo_final(const Dev &d, const ThermoCfg &tc, int nb_ke, int nb_ev,
 // batches: per-replica KE (ke = 1, from the current velocities) and/or virial+PE folds
 int launch_thermo_replicas(const Dev &d, const Box &b, const ThermoCfg &tc, int ke, int ev, cudaStream_t st);
 int launch_advance_step(const Dev &d, int nsteps, cudaStream_t st);
+// constraint::Nve: kinetic energy, lambda (and the thermo point of the step,
+// ring_slot >= 0 or the current one when thermo != 0), velocity scaling; every
+// kernel returns at once unless (step_base + k) % cfg.step == 0
+struct NveCfg {
+  long long step;
+  int mode;
+  double value, kb;
+};
+constexpr int NVE_BLOCKS = 1024;
+int launch_nve(const Dev &d, const Box &b, const ThermoCfg &tc, const NveCfg &cfg, int k, int thermo, int ring_slot,
+               cudaStream_t st);
 int launch_to_host_order(const Dev &d, const Box &b, int what, cudaStream_t st);
 int launch_export_pairs(const Dev &d, const Box &b, int mode, int32_t *rows, unsigned long long *counter,
                         int64_t cap, cudaStream_t st);

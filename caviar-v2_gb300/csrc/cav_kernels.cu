@@ -642,6 +642,68 @@ __global__ void __launch_bounds__(256) k_thermo_rep(Dev d, Box b, ThermoCfg tc, 
 __global__ void k_advance_step(Dev d, int nsteps) { *d.step_base += nsteps; }
 
 // ---------------------------------------------------------------------------
+// constraint::Nve (src/constraint/nve.cpp:132-184), single system: on steps whose
+// index is a multiple of `step`, lambda = sqrt(target / KE) with KE the kinetic
+// energy of Atom_data::kinetic_energy (centre-of-mass part removed for n_r_df
+// 1..3), velocities scaled by lambda, then the temperature and pressure of the
+// step follow the scaled velocities (finalize_temperature / finalize_pressure).
+// ---------------------------------------------------------------------------
+__device__ inline bool nve_applies(const Dev &d, const NveCfg &c, int k) { return (*d.step_base + k) % c.step == 0; }
+
+__global__ void __launch_bounds__(256) k_nve_ke(Dev d, int n, NveCfg c, int k) {
+  if (!nve_applies(d, c, k)) return;
+  double part[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const dbl4 v = d.vel[i];
+    const double m = d.tab->mass[d.type[i]];
+    part[0] += m * (v.x * v.x + v.y * v.y + v.z * v.z);
+    part[1] += m * v.x; part[2] += m * v.y; part[3] += m * v.z;
+  }
+  block_sum_store<4>(part, &d.nve_partials[(size_t)blockIdx.x * 4]);
+}
+
+__global__ void __launch_bounds__(256) k_nve_lambda(Dev d, ThermoCfg tc, NveCfg c, int k, int thermo, int ring_slot) {
+  if (!nve_applies(d, c, k)) return;
+  double v[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int b = threadIdx.x; b < NVE_BLOCKS; b += blockDim.x)
+    for (int q = 0; q < 4; ++q) v[q] += d.nve_partials[(size_t)b * 4 + q];
+  __shared__ double s[4];
+  block_sum_store<4>(v, s);
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  double ke2 = s[0];
+  const double msum = d.thermo[5];
+  if (tc.n_r_df >= 1 && tc.n_r_df <= 3 && msum > 0) ke2 -= (s[1] * s[1] + s[2] * s[2] + s[3] * s[3]) / msum;
+  const double ke = 0.5 * ke2;
+  const double dof = (double)(3 * tc.n - tc.n_r_df);  // Atom_data::degree_of_freedoms
+  double lambda = 1.0;
+  if (c.mode == CAVGPU_NVE_ENERGY_PER_DOF) lambda = sqrt(c.value * dof / ke);
+  else if (c.mode == CAVGPU_NVE_ENERGY_TOT) lambda = sqrt(c.value / ke);
+  else if (c.mode == CAVGPU_NVE_KBT) lambda = sqrt(dof * c.value * 0.5 / ke);
+  else lambda = sqrt(dof * c.kb * c.value * 0.5 / ke);
+  *d.nve_lambda = lambda;
+  if (thermo) {  // the thermo point of this step: KE and T of the scaled velocities, P from them
+    const double l2 = lambda * lambda;
+    double *o = d.thermo;
+    o[0] *= l2;
+    o[1] *= l2;
+    o[2] = ((double)tc.n * tc.k_b * o[1]) / tc.volume + (tc.langevin ? 0.0 : o[3]) / (3.0 * tc.volume);
+    if (ring_slot >= 0)
+      for (int q = 0; q < 3; ++q) d.thermo_ring[(size_t)ring_slot * THERMO_REC + q] = o[q];
+  }
+}
+
+__global__ void __launch_bounds__(256) k_nve_scale(Dev d, int n, NveCfg c, int k) {
+  if (!nve_applies(d, c, k)) return;
+  const double lambda = *d.nve_lambda;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    dbl4 v = d.vel[i];
+    v.x *= lambda; v.y *= lambda; v.z *= lambda;
+    d.vel[i] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // parity exports
 // ---------------------------------------------------------------------------
 // what: 0 = positions (wrapped as Domain::fix_position), 1 = velocities, 2 = accelerations
@@ -851,6 +913,16 @@ int launch_thermo_replicas(const Dev &d, const Box &b, const ThermoCfg &tc, int 
 
 int launch_advance_step(const Dev &d, int nsteps, cudaStream_t st) {
   k_advance_step<<<1, 1, 0, st>>>(d, nsteps);
+  return chk();
+}
+
+int launch_nve(const Dev &d, const Box &b, const ThermoCfg &tc, const NveCfg &cfg, int k, int thermo, int ring_slot,
+               cudaStream_t st) {
+  if (b.nrep != 1 || cfg.step <= 0) return CAVGPU_E_ARG;
+  const int n = b.nslot;
+  k_nve_ke<<<NVE_BLOCKS, 256, 0, st>>>(d, n, cfg, k);
+  k_nve_lambda<<<1, 256, 0, st>>>(d, tc, cfg, k, thermo, ring_slot);
+  k_nve_scale<<<NVE_BLOCKS, 256, 0, st>>>(d, n, cfg, k);
   return chk();
 }
 

@@ -227,6 +227,23 @@ void Lj::calculate_acceleration() {
 }
 }  // namespace force_field
 
+// ---------------------------------------------------------------- constraint::Nve
+namespace constraint {
+void Nve::verify_settings() {
+  const bool kbt_set = kbt > 0.0, temperature_set = temperature > 0.0, kb_set = kb > 0.0;
+  if ((temperature_set && kb_set) != (temperature_set || kb_set))
+    caviar_->log.error_all("kb and temperature should be set together.");
+  const bool t_set = (temperature_set && kb_set) || kbt_set;
+  const bool energy_set = energy_per_dof > 0.0 || energy_tot > 0.0;
+  if (!(energy_set || t_set)) caviar_->log.error_all("energy or temperature is not set.");
+  if (energy_set && t_set) caviar_->log.error_all("Only one of 'energy' and 'temperature' can be set.");
+  if (energy_set && energy_per_dof > 0.0 && energy_tot > 0.0)
+    caviar_->log.error_all("Only one of 'energy_per_dof' and 'energy_tot' can be set.");
+  if (t_set && kbt_set && temperature_set && kb_set)
+    caviar_->log.error_all("Only one of 'kbt' and 'temperatue kb' can be set.");
+}
+}  // namespace constraint
+
 // ---------------------------------------------------------------- Md_simulator
 void Md_simulator::check(int status, const char *what) {
   if (status == CAVGPU_OK) return;
@@ -310,6 +327,26 @@ void Md_simulator::initialize() {
   p.n_r_df = ad.get_n_r_df();
   p.pressure_process = ad.pressure_process ? 1 : 0;
   p.precision = precision;
+  p.initial_step = initial_step;
+  // constraints: the GPU path runs constraint::Nve (at most one)
+  int n_nve = 0;
+  for (Constraint *cst : caviar_->constraints) {
+    auto *nve = dynamic_cast<constraint::Nve *>(cst);
+    if (!nve) caviar_->log.error_all("the GPU path runs constraint::Nve only");
+    if (++n_nve > 1) caviar_->log.error_all("the GPU path runs one constraint::Nve");
+    if (nve->step <= 0) caviar_->log.error_all("Nve: step have to non-negative.");
+    p.nve_step = nve->step;
+    if (nve->energy_per_dof > 0.0) { p.nve_mode = CAVGPU_NVE_ENERGY_PER_DOF; p.nve_value = nve->energy_per_dof; }
+    else if (nve->energy_tot > 0.0) { p.nve_mode = CAVGPU_NVE_ENERGY_TOT; p.nve_value = nve->energy_tot; }
+    else if (nve->kbt > 0.0) { p.nve_mode = CAVGPU_NVE_KBT; p.nve_value = nve->kbt; }
+    else if (nve->temperature > 0.0 && nve->kb > 0.0) {
+      p.nve_mode = CAVGPU_NVE_KB_TEMPERATURE;
+      p.nve_value = nve->temperature;
+      p.nve_kb = nve->kb;
+    } else {
+      caviar_->log.error_all("energy or temperature is not set.");
+    }
+  }
   if (ctx_) cavgpu_destroy(ctx_);
   ctx_ = nullptr;
   check(cavgpu_create(&p, &ctx_), "cavgpu_create");

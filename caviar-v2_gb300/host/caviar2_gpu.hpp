@@ -230,6 +230,31 @@ class Md_simulator {
   bool host_dirty_ = false;
 };
 
+class Constraint {
+ public:
+  explicit Constraint(Caviar2 *c) : caviar_(c) {}
+  virtual ~Constraint() = default;
+
+ protected:
+  Caviar2 *caviar_;
+};
+
+namespace constraint {
+// constraint::Nve (inc/caviar2/constraint/nve.hpp, src/constraint/nve.cpp:132-184):
+// on steps whose index is a multiple of `step`, velocities are scaled so that the
+// kinetic energy is energy_per_dof * dof, energy_tot, dof * kbt / 2 or
+// dof * kb * temperature / 2 (the first one set).  Runs on the device, inside the
+// step; the GPU path takes at most one Nve, with velocity Verlet or leap-frog.
+class Nve : public Constraint {
+ public:
+  explicit Nve(Caviar2 *c) : Constraint(c) {}
+  void verify_settings();  // the reference's checks (src/constraint/nve.cpp:104-130)
+  double energy_per_dof = -1.0, energy_tot = -1.0;
+  double temperature = -1.0, kb = -1.0, kbt = -1.0;
+  int step = 1;
+};
+}  // namespace constraint
+
 class Caviar2 {
  public:
   Caviar2();
@@ -242,9 +267,11 @@ class Caviar2 {
   Md_simulator md_simulator;
   Neighborlist neighborlist;
   Log log;
-  std::vector<Force_field *> forces;  // non-owning (src/caviar2.cpp:40-44)
+  std::vector<Force_field *> forces;       // non-owning (src/caviar2.cpp:40-44)
+  std::vector<Constraint *> constraints;   // non-owning
 
   void add_force_field(Force_field *f) { forces.push_back(f); }
+  void add_constraint(Constraint *c) { constraints.push_back(c); }
 };
 
 }  // namespace caviar2

@@ -84,7 +84,24 @@ typedef struct cavgpu_params {
   int32_t force_kernel;           /* CAVGPU_FORCE_*: pair-kernel variant of the mixed form */
   double jump_tol;                /* Lj::set_jump_tol: r^2 of a pair inside the cutoff is floored at
                                      jump_tol (src/force/lj.cpp:459-468); 0 = off (the default) */
+  int64_t initial_step;           /* Md_simulator::set_initial_step: index of the first step (the
+                                     Philox step counter and the Nve schedule use it) */
+  /* constraint::Nve velocity rescaling (src/constraint/nve.cpp:132-184): on every step whose
+     index is a multiple of nve_step, after the closing kick and the temperature, velocities
+     are scaled by lambda so that the kinetic energy becomes the target of nve_mode.
+     Single systems with velocity Verlet or leap-frog (the Langevin integrator applies
+     thermostats mid-step); 0 = off. */
+  int64_t nve_step;
+  int32_t nve_mode;               /* CAVGPU_NVE_ENERGY_PER_DOF, _ENERGY_TOT, _KBT, _KB_TEMPERATURE */
+  int32_t nve_pad;
+  double nve_value;               /* energy_per_dof, energy_tot, kbt or temperature */
+  double nve_kb;                  /* kb of CAVGPU_NVE_KB_TEMPERATURE */
 } cavgpu_params;
+
+#define CAVGPU_NVE_ENERGY_PER_DOF 0
+#define CAVGPU_NVE_ENERGY_TOT 1
+#define CAVGPU_NVE_KBT 2
+#define CAVGPU_NVE_KB_TEMPERATURE 3
 
 /* pair-kernel variants of the mixed form (the FP64 form has one kernel); both give
  * the same results bit for bit */

@@ -512,6 +512,23 @@ static void finalize_temperature(orc_sys *s) {
   s->temperature = 2.0 * s->ke / (s->p.k_b * dof);
 }
 
+/* constraint::Nve::apply_thermostat (src/constraint/nve.cpp:132-184) on steps whose
+ * index is a multiple of nve_step, then finalize_temperature again */
+static void nve_thermostat(orc_sys *s) {
+  if (s->p.nve_step <= 0 || s->current_step % s->p.nve_step != 0) return;
+  const double energy_now = kinetic_energy(s);
+  const double dof = (double)(3 * s->n - s->p.n_r_df); /* degree_of_freedoms() */
+  double lambda = 1.0;
+  switch (s->p.nve_mode) {
+    case 0: lambda = sqrt(s->p.nve_value * dof / energy_now); break;           /* energy_per_dof */
+    case 1: lambda = sqrt(s->p.nve_value / energy_now); break;                 /* energy_tot */
+    case 2: lambda = sqrt(dof * s->p.nve_value * 0.5 / energy_now); break;     /* kbt */
+    default: lambda = sqrt(dof * s->p.nve_kb * s->p.nve_value * 0.5 / energy_now); /* kb, temperature */
+  }
+  for (int64_t k = 0; k < 3 * (int64_t)s->n; ++k) s->vel[k] *= lambda;
+  finalize_temperature(s);
+}
+
 /* finalize_pressure_mpi_domain (:238-303) */
 static void finalize_pressure(orc_sys *s) {
   if (!s->p.pressure_process) return;
@@ -559,6 +576,7 @@ static int integrate_vv(orc_sys *s) {
     for (int d = 0; d < 3; ++d)
       s->vel[3 * i + d] += (s->acc[3 * i + d] + s->acc_old[3 * i + d]) * hdt;
   finalize_temperature(s);
+  nve_thermostat(s);
   finalize_pressure(s);
   return ORC_OK;
 }
@@ -578,6 +596,7 @@ static int integrate_lf(orc_sys *s) {
   for (int32_t i = 0; i < n; ++i)
     for (int d = 0; d < 3; ++d) s->vel[3 * i + d] += hdt * s->acc[3 * i + d];
   finalize_temperature(s);
+  nve_thermostat(s);
   finalize_pressure(s);
   return ORC_OK;
 }

@@ -63,6 +63,10 @@ typedef struct orc_params {
   int32_t pressure_process;     /* Atom_data::set_pressure_process */
   int32_t rebuild_test;         /* Neighborlist::set_rebuild_test: rebuild on every step */
   double jump_tol;              /* Lj::set_jump_tol (src/force/lj.cpp:82-86); 0 = off */
+  int64_t nve_step;             /* constraint::Nve every nve_step steps; 0 = off */
+  int32_t nve_mode;             /* 0 energy_per_dof, 1 energy_tot, 2 kbt, 3 kb + temperature */
+  int32_t nve_pad;
+  double nve_value, nve_kb;
 } orc_params;
 
 typedef struct orc_sys orc_sys;

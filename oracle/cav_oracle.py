@@ -26,7 +26,8 @@ class OrcParams(C.Structure):
         ("lang_kb", C.c_double), ("lang_kbt", C.c_double), ("seed", C.c_uint64),
         ("cutoff_list_on", C.c_int32), ("use_cell_list", C.c_int32), ("n_r_df", C.c_int32),
         ("integrator", C.c_int32), ("noise_mode", C.c_int32), ("pressure_process", C.c_int32),
-        ("rebuild_test", C.c_int32), ("jump_tol", C.c_double),
+        ("rebuild_test", C.c_int32), ("jump_tol", C.c_double), ("nve_step", C.c_int64), ("nve_mode", C.c_int32),
+        ("nve_pad", C.c_int32), ("nve_value", C.c_double), ("nve_kb", C.c_double),
     ]
 
 
@@ -102,6 +103,10 @@ def make_params(p, noise_mode=1):
     o.pressure_process = p.get("pressure_process", 1)
     o.rebuild_test = int(p.get("rebuild_test", 0))
     o.jump_tol = float(p.get("jump_tol", 0.0))
+    nve = p.get("nve")
+    if nve:
+        o.nve_step, o.nve_mode = int(nve["step"]), int(nve["mode"])
+        o.nve_value, o.nve_kb = float(nve["value"]), float(nve.get("kb", 0.0))
     return o
 
 

@@ -19,6 +19,8 @@
 //     bit 2: double eps_atom[nt], sigma_atom[nt]  -> Lj::set_epsilon_atom / set_sigma_atom
 //                                                    (instead of set_epsilon / set_sigma)
 //     bit 3: double lambda_s[nt*nt], lambda_e[nt*nt] -> Lj::set_lambda_s / set_lambda_e
+//     bit 4: int64 step, int32 mode, int32 pad, double value, kb -> constraint::Nve
+//            (mode 0 energy_per_dof, 1 energy_tot, 2 kbt, 3 kb + temperature)
 //   Bits 1-3 take effect in Lj::verify_settings (src/force/lj.cpp:186-381), which
 //   the library itself never calls; the harness calls it, as a user of these
 //   options must, and appends the effective tables to the output.
@@ -50,6 +52,7 @@
 #include <vector>
 #define private public
 #include "caviar2/caviar2.hpp"
+#include "caviar2/constraint/nve.hpp"
 #include "caviar2/force/lj.hpp"
 #undef private
 
@@ -123,6 +126,10 @@ int main(int argc, char **argv) {
   if ((ext & 1) && !rd(fi, &jump_tol, 1)) return 8;
   if ((ext & 4) && (!rd(fi, eps_atom.data(), nt) || !rd(fi, sig_atom.data(), nt))) return 8;
   if ((ext & 8) && (!rd(fi, lam_s.data(), lam_s.size()) || !rd(fi, lam_e.data(), lam_e.size()))) return 8;
+  int64_t nve_step = 0;
+  int32_t nve_mode[2] = {0, 0};
+  double nve_vk[2] = {0.0, 0.0};
+  if ((ext & 16) && (!rd(fi, &nve_step, 1) || !rd(fi, nve_mode, 2) || !rd(fi, nve_vk, 2))) return 8;
   fclose(fi);
 
   void *mem = calloc(1, sizeof(Caviar2));
@@ -189,6 +196,15 @@ int main(int argc, char **argv) {
   }
   c.add_force_field(&lj);
   if (ext & 14) lj.verify_settings();
+  constraint::Nve nve(&c);
+  if (ext & 16) {
+    nve.step = (int)nve_step;
+    if (nve_mode[0] == 0) nve.energy_per_dof = nve_vk[0];
+    else if (nve_mode[0] == 1) nve.energy_tot = nve_vk[0];
+    else if (nve_mode[0] == 2) nve.kbt = nve_vk[0];
+    else { nve.temperature = nve_vk[0]; nve.kb = nve_vk[1]; }
+    c.add_constraint(&nve);
+  }
 
   // ---- Md_simulator ----
   c.md_simulator.initialized = false;

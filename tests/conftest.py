@@ -41,6 +41,8 @@ def golden_params(g):
         lo=g["lo"], hi=g["hi"], ntypes=nt, nl_cutoff=float(g["nl_cutoff"]), nl_coef=float(g["nl_coef"]),
         ghost_cutoff=float(g["ghost_cutoff"]), lj_cutoff=float(g["lj_cutoff"]), eps=eps, sigma=sigma,
         cutoff_list=cutoff_list, jump_tol=float(g["jump_tol"]) if "jump_tol" in g else 0.0,
+        nve=None if "nve" not in g else {"step": int(g["nve"][0]), "mode": int(g["nve"][1]),
+                                         "value": float(g["nve"][2]), "kb": float(g["nve"][3])},
         mass=g["mass"], k_b=float(g["k_b"]),
         dt=float(g["dt"]), integrator=int(g["integrator"]), lang_temperature=float(g["lang_temperature"]),
         lang_friction=float(g["lang_friction"]), lang_kb=float(g["lang_kb"]), seed=0, n_r_df=int(g["n_r_df"]),

@@ -37,6 +37,10 @@ int main(int argc, char **argv) {
   if ((ext & 1) && !rd(fi, &jump_tol, 1)) return 5;
   if ((ext & 4) && (!rd(fi, eps_atom.data(), nt) || !rd(fi, sig_atom.data(), nt))) return 5;
   if ((ext & 8) && (!rd(fi, lam_s.data(), lam_s.size()) || !rd(fi, lam_e.data(), lam_e.size()))) return 5;
+  int64_t nve_step = 0;
+  int32_t nve_mode[2] = {0, 0};
+  double nve_vk[2] = {0.0, 0.0};
+  if ((ext & 16) && (!rd(fi, &nve_step, 1) || !rd(fi, nve_mode, 2) || !rd(fi, nve_vk, 2))) return 5;
   fclose(fi);
 
   Caviar2 caviar;
@@ -111,6 +115,17 @@ int main(int argc, char **argv) {
     wr(fo, &clo, 1);
     fclose(fo);
     return 0;
+  }
+
+  constraint::Nve nve(&caviar);
+  if (ext & 16) {
+    nve.step = (int)nve_step;
+    if (nve_mode[0] == 0) nve.energy_per_dof = nve_vk[0];
+    else if (nve_mode[0] == 1) nve.energy_tot = nve_vk[0];
+    else if (nve_mode[0] == 2) nve.kbt = nve_vk[0];
+    else { nve.temperature = nve_vk[0]; nve.kb = nve_vk[1]; }
+    nve.verify_settings();
+    caviar.add_constraint(&nve);
   }
 
   Md_simulator &md = caviar.md_simulator;

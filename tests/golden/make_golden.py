@@ -30,7 +30,7 @@ FULL_PAIRS_MAX_N = 600
 def ext_flags(p):
     """Extension bits of the harness input: jump_tol, WCA, per-atom mixing, lambda tables."""
     return ((1 if p.get("jump_tol") else 0) | (2 if p.get("wca") else 0) | (4 if p.get("eps_atom") is not None else 0)
-            | (8 if p.get("lambda_s") is not None else 0))
+            | (8 if p.get("lambda_s") is not None else 0) | (16 if p.get("nve") else 0))
 
 
 def write_input(path, pos, vel, typ, p, nsteps):
@@ -60,6 +60,11 @@ def write_input(path, pos, vel, typ, p, nsteps):
         if ext & 8:
             f.write(np.asarray(p["lambda_s"], np.float64).reshape(nt, nt).tobytes())
             f.write(np.asarray(p["lambda_e"], np.float64).reshape(nt, nt).tobytes())
+        if ext & 16:
+            nve = p["nve"]
+            f.write(np.array([nve["step"]], np.int64).tobytes())
+            f.write(np.array([nve["mode"], 0], np.int32).tobytes())
+            f.write(np.array([nve["value"], nve.get("kb", 0.0)], np.float64).tobytes())
 
 
 class Reader:
@@ -123,6 +128,9 @@ def run_case(name, pos, vel, typ, p, nsteps):
     if ext & 8:
         extra["lambda_s"] = np.asarray(p["lambda_s"], np.float64).reshape(nt, nt)
         extra["lambda_e"] = np.asarray(p["lambda_e"], np.float64).reshape(nt, nt)
+    if ext & 16:
+        nve = p["nve"]
+        extra["nve"] = np.array([nve["step"], nve["mode"], nve["value"], nve.get("kb", 0.0)], np.float64)
     out = dict(
         # inputs
         pos=pos, vel=vel, typ=typ.astype(np.int32), nsteps=np.int32(nsteps),
@@ -215,6 +223,12 @@ def cases():
              eps_atom=[1.0, 0.6], sigma_atom=[1.0, 0.85],
              lambda_s=[[1.0, 0.95], [0.95, 1.0]], lambda_e=[[1.0, 1.1], [1.1, 0.9]])
     yield "ka864_wca_mixing_lambda", pos, vel, typ, p, 60
+    # constraint::Nve velocity rescaling: every 7 steps to k_B T = 1.1 (velocity Verlet), and every
+    # step to 1.3 energy per degree of freedom (leap-frog)
+    pos, vel, typ, p = W.lj_fluid((5, 5, 5), seed=81)
+    yield "fcc500_nve_kbt", pos, vel, typ, dict(p, nve={"step": 7, "mode": 2, "value": 1.1}), 50
+    pos, vel, typ, p = W.lj_fluid((4, 4, 4), seed=82, integrator=2)
+    yield "fcc256_leapfrog_nve_edof", pos, vel, typ, dict(p, nve={"step": 1, "mode": 0, "value": 1.3}), 40
 
 
 def main():
