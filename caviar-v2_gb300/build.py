@@ -59,10 +59,11 @@ def build_host():
     inc = ["-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(HERE, "host")]
     cxx = os.environ.get("CXX", "g++")
     steps = [
-        [cxx, "-O2", "-std=c++17", "-fPIC", "-shared", *inc, os.path.join(HERE, "host", "caviar2_gpu.cpp"),
-         "-o", HOST_LIB, "-L" + HERE, "-lcavgpu", "-Wl,-rpath,$ORIGIN"],
-        [cxx, "-O2", "-std=c++17", *inc, os.path.join(ROOT, "tests", "cpp", "host_harness.cpp"), "-o",
-         HOST_HARNESS, "-L" + HERE, "-lcaviar2_gpu", "-lcavgpu", "-Wl,-rpath," + HERE],
+        [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-pthread", "-fPIC", "-shared", *inc,
+         os.path.join(HERE, "host", "caviar2_gpu.cpp"), "-o", HOST_LIB, "-L" + HERE, "-lcavgpu", "-Wl,-rpath,$ORIGIN"],
+        [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-pthread", *inc,
+         os.path.join(ROOT, "tests", "cpp", "host_harness.cpp"), "-o", HOST_HARNESS, "-L" + HERE, "-lcaviar2_gpu",
+         "-lcavgpu", "-Wl,-rpath," + HERE],
     ]
     for cmd in steps:
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -37,7 +37,7 @@ class Params(C.Structure):
         ("nbr_capacity", C.c_int32), ("threads_per_atom", C.c_int32), ("block_size", C.c_int32),
         ("steps_per_graph", C.c_int32), ("force_kernel", C.c_int32), ("jump_tol", C.c_double),
         ("initial_step", C.c_int64), ("nve_step", C.c_int64), ("nve_mode", C.c_int32), ("nve_pad", C.c_int32),
-        ("nve_value", C.c_double), ("nve_kb", C.c_double),
+        ("nve_value", C.c_double), ("nve_kb", C.c_double), ("msd_process", C.c_int32), ("msd_pad", C.c_int32),
     ]
 
 
@@ -62,6 +62,7 @@ _SIGS = {
     "cavgpu_forces": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "cavgpu_thermo": (C.c_int, [C.c_void_p, C.c_void_p]),
     "cavgpu_download": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "cavgpu_download_images": (C.c_int, [C.c_void_p, C.c_void_p]),
     "cavgpu_export_pairs": (C.c_int64, [C.c_void_p, C.c_void_p, C.c_int64]),
     "cavgpu_export_bins": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "cavgpu_export_ghosts": (C.c_int64, [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -151,6 +152,7 @@ def make_params(p, precision=FP64, noise_off=False, tpa=0, block=0, nbr_capacity
     if nve:
         o.nve_step, o.nve_mode = int(nve["step"]), int(nve["mode"])
         o.nve_value, o.nve_kb = float(nve["value"]), float(nve.get("kb", 0.0))
+    o.msd_process = int(bool(p.get("msd_process", False)))
     return o
 
 
@@ -208,6 +210,12 @@ class System:
         p, v, a = (np.empty((self.n, 3)) for _ in range(3))
         self._check(lib().cavgpu_download(self._h, _ptr(p), _ptr(v), _ptr(a)), "download")
         return p, v, a
+
+    def images(self):
+        """Boundary crossings per atom and axis since the upload (needs msd_process)."""
+        m = np.empty((self.n, 3), np.int32)
+        self._check(lib().cavgpu_download_images(self._h, _ptr(m)), "download_images")
+        return m
 
     def pairs(self):
         n = self._check(lib().cavgpu_export_pairs(self._h, None, 0), "export_pairs")

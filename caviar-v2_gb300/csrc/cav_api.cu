@@ -116,7 +116,8 @@ int enqueue_thermo_after_force(cavgpu_ctx *c, int ring_slot) {
   const bool lang = is_lang(c);
   if (c->b.nrep == 1) {
     const int nb_ke = lang ? drift_grid_blocks(c->lc) : force_grid_blocks(c->lc);
-    RK(launch_thermo_final(c->d, c->tc, nb_ke, force_grid_blocks(c->lc), ring_slot, c->st));
+    RK(launch_thermo_final(c->d, c->tc, nb_ke, force_grid_blocks(c->lc), lang ? force_grid_blocks(c->lc) : 0,
+                           ring_slot, c->st));
   } else {
     RK(launch_thermo_replicas(c->d, c->b, c->tc, lang ? 0 : 1, 1, c->st));
   }
@@ -579,9 +580,15 @@ int upload_common(cavgpu_ctx *c, const int64_t *counts, const double *pos3, cons
   if (!rc) rc = dalloc(c, &d.cell_cursor, ncell_all);
   if (!rc) rc = dalloc(c, &d.cell_start, (size_t)ncell_all + 1);
   if (!rc) rc = dalloc(c, &d.partials_ke, 4 * std::max(nblk, nblk_d));
+  if (!rc) rc = dalloc(c, &d.partials_ke_end, 4 * nblk);
   if (!rc) rc = dalloc(c, &d.partials_ev, 2 * nblk);
   if (!rc) rc = dalloc(c, &d.h3, 3 * (size_t)N);
   if (!rc) rc = dalloc(c, &d.hi3, 3 * (size_t)N);
+  if (c->p.msd_process) {  // Atom_data::msd_process: boundary crossings per atom, zero at upload
+    if (!rc) rc = dalloc(c, &d.img, NS);
+    if (!rc) rc = dalloc(c, &d.t_img, NS);
+    if (!rc) rc = cuda_rc(cudaMemsetAsync(d.img, 0, NS * sizeof(int4), c->st));
+  }
   if (c->nve.step > 0) {
     if (R > 1) return CAVGPU_E_ARG;  // constraint::Nve acts on one system's kinetic energy
     if (!rc) rc = dalloc(c, &d.nve_partials, 4 * (size_t)NVE_BLOCKS);
@@ -640,7 +647,7 @@ int setup_common(cavgpu_ctx *c) {
   RK(launch_force(c->d, c->b, c->sc, c->lc, 0, 1, 0, c->st));
   c->kernel_launches += 1;
   if (c->b.nrep == 1) {
-    RK(launch_thermo_final(c->d, c->tc, force_grid_blocks(c->lc), force_grid_blocks(c->lc), -1, c->st));
+    RK(launch_thermo_final(c->d, c->tc, force_grid_blocks(c->lc), force_grid_blocks(c->lc), 0, -1, c->st));
   } else {
     RK(launch_thermo_replicas(c->d, c->b, c->tc, 1, 1, c->st));
   }
@@ -968,7 +975,7 @@ int cavgpu_forces(cavgpu_ctx *c, double *virial, double *pe) {
   RK(launch_force(c->d, c->b, c->sc, c->lc, 0, 1, 0, c->st));
   c->kernel_launches += 1;
   if (c->b.nrep == 1) {
-    RK(launch_thermo_final(c->d, c->tc, force_grid_blocks(c->lc), force_grid_blocks(c->lc), -1, c->st));
+    RK(launch_thermo_final(c->d, c->tc, force_grid_blocks(c->lc), force_grid_blocks(c->lc), 0, -1, c->st));
   } else {
     RK(launch_thermo_replicas(c->d, c->b, c->tc, 1, 1, c->st));
   }
@@ -1028,6 +1035,15 @@ int cavgpu_download(cavgpu_ctx *c, double *pos3, double *vel3, double *acc3) {
     CK(cudaMemcpyAsync(outs[w], c->d.h3, 3 * sizeof(double) * c->natoms, cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
   }
+  return CAVGPU_OK;
+}
+
+int cavgpu_download_images(cavgpu_ctx *c, int32_t *img3) {
+  if (!c || !img3) return CAVGPU_E_ARG;
+  if (!c->uploaded || !c->d.img) return CAVGPU_E_STATE;
+  RK(launch_images_to_host(c->d, c->b, c->st));
+  CK(cudaMemcpyAsync(img3, c->d.hi3, 3 * sizeof(int32_t) * c->natoms, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
   return CAVGPU_OK;
 }
 

@@ -109,10 +109,12 @@ struct Dev {
   int *type;
   uint32_t *id;               // host (insertion) index
   int *cell_of;               // build cell of each slot
+  int4 *img;                  // periodic-boundary crossings per axis (msd_domain_cross); null when not tracked
   // rebuild scratch
   dbl4 *t_pos, *t_vel, *t_acc, *t_acc_old;
   int *t_type;
   uint32_t *t_id;
+  int4 *t_img;
   int *atom_cell, *cell_count, *cell_start, *cell_cursor, *perm, *perm_tmp;
   // neighbour list
   uint32_t *nbr;
@@ -122,6 +124,7 @@ struct Dev {
   // status, reductions
   int *flags;
   double *partials_ke;        // per-block {sum m v^2, sum m v} (4 per block)
+  double *partials_ke_end;    // Langevin: the same sums over the velocities at the end of the step
   double *partials_ev;        // per-block {sum -coef r^2, sum V} over both pair orders (2 per block)
   int partials_blocks;        // blocks the partial arrays hold (every launch grid is checked against it)
   double2 *ev_atom;           // per-slot {-coef r^2, V} sums (batches: per-replica folds)
@@ -253,7 +256,9 @@ constexpr int REBUILD_KERNELS = 8;  // kernels launch_rebuild enqueues
 // thermo: virial/PE partials (and KE partials unless kick == 2).
 int launch_force(const Dev &d, const Box &b, const StepConsts &sc, const LaunchCfg &lc, int kick, int thermo,
                  int k_in_chunk, cudaStream_t st);
-int launch_thermo_final(const Dev &d, const ThermoCfg &tc, int nb_ke, int nb_ev, int ring_slot, cudaStream_t st);
+// nb_ke_end > 0 (Langevin): KE from partials_ke_end, the temperature from partials_ke
+int launch_thermo_final(const Dev &d, const ThermoCfg &tc, int nb_ke, int nb_ev, int nb_ke_end, int ring_slot,
+                        cudaStream_t st);
 // batches: per-replica KE (ke = 1, from the current velocities) and/or virial+PE folds
 int launch_thermo_replicas(const Dev &d, const Box &b, const ThermoCfg &tc, int ke, int ev, cudaStream_t st);
 int launch_advance_step(const Dev &d, int nsteps, cudaStream_t st);
@@ -269,6 +274,9 @@ constexpr int NVE_BLOCKS = 1024;
 int launch_nve(const Dev &d, const Box &b, const ThermoCfg &tc, const NveCfg &cfg, int k, int thermo, int ring_slot,
                cudaStream_t st);
 int launch_to_host_order(const Dev &d, const Box &b, int what, cudaStream_t st);
+// boundary crossings per atom in host order into d.hi3, counting the wrap of the
+// current position that the next list build applies
+int launch_images_to_host(const Dev &d, const Box &b, cudaStream_t st);
 int launch_export_pairs(const Dev &d, const Box &b, int mode, int32_t *rows, unsigned long long *counter,
                         int64_t cap, cudaStream_t st);
 int launch_ref_bins(const Dev &d, int n, double cutoff_inv, const int nb[3], const double lo_local[3],

@@ -152,8 +152,9 @@ __device__ inline OneType one_type(const SmemTabF &tab) {
 // KICK: 0 = store the acceleration only; 1 = velocity-Verlet closing kick
 // v += (a + a_old) * (0.5 dt) (src/md_simulator.cpp:672-679); 2 = Langevin closing
 // update v = (v a_L + eta b) + (a*0.5) dt (src/md_simulator.cpp:853-862).
-// EV: accumulate virial and potential energy (and KE unless KICK == 2); batches
-// also store them per slot for the per-replica folds.
+// EV: accumulate virial, potential energy and KE (KICK == 2: the KE of the
+// velocities at the end of the step, kept apart from the mid-step temperature's);
+// batches also store virial and PE per slot for the per-replica folds.
 template <int A, bool MIXED, int KICK, bool EV, class Tab>
 __device__ __forceinline__ void finish_atom(const Dev &d, const StepConsts &sc, const Tab &tab, bool act, int t,
                                             int i, int ti, int rep, long long step, double fx, double fy,
@@ -217,6 +218,11 @@ __device__ __forceinline__ void finish_atom(const Dev &d, const StepConsts &sc, 
     }
     d.acc[i] = an;
     d.vel[i] = v;
+    if (EV) {  // Atom_data::kinetic_energy() read after the step (the temperature was taken mid-step)
+      const double m = tab.mass[ti];
+      ke_p[0] += m * (v.x * v.x + v.y * v.y + v.z * v.z);
+      ke_p[1] += m * v.x; ke_p[2] += m * v.y; ke_p[3] += m * v.z;
+    }
   }
   if (EV) {
     ev_p[0] += vir;
@@ -229,10 +235,8 @@ template <int KICK, bool EV>
 __device__ inline void store_partials(const Dev &d, double (&ke_p)[4], double (&ev_p)[2]) {
   if (EV) {
     block_sum_store_f<2>(ev_p, &d.partials_ev[(size_t)blockIdx.x * 2]);
-    if (KICK != 2) {
-      __syncthreads();
-      block_sum_store_f<4>(ke_p, &d.partials_ke[(size_t)blockIdx.x * 4]);
-    }
+    __syncthreads();
+    block_sum_store_f<4>(ke_p, &(KICK == 2 ? d.partials_ke_end : d.partials_ke)[(size_t)blockIdx.x * 4]);
   }
 }
 

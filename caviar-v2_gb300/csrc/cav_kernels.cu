@@ -207,6 +207,13 @@ __global__ void __launch_bounds__(256) k_lang_a(Dev d, Box b, StepConsts sc, int
 // ---------------------------------------------------------------------------
 __device__ inline bool rebuild_on(const Box &b, int rep, int forced) { return forced || b.rep_flag[rep] != 0; }
 
+// Domain::fix_position's single-image test per axis (src/domain.cpp:443-493):
+// -1 below the lower face (x += L), +1 above the upper face (x -= L), else 0
+__device__ inline int3 wrap_shift(const RepBox &rb, const dbl4 &p) {
+  return make_int3(p.x < rb.lo[0] ? -1 : (p.x > rb.hi[0] ? 1 : 0), p.y < rb.lo[1] ? -1 : (p.y > rb.hi[1] ? 1 : 0),
+                   p.z < rb.lo[2] ? -1 : (p.z > rb.hi[2] ? 1 : 0));
+}
+
 __global__ void __launch_bounds__(256) k_bin(Dev d, Box b, int forced) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i == 0) d.flags[F_MAXNB] = 0;
@@ -216,11 +223,18 @@ __global__ void __launch_bounds__(256) k_bin(Dev d, Box b, int forced) {
   if (act) {
     const RepBox &rb = repbox(b, rep);
     dbl4 p = d.pos[i];
-    // single-image wrap exactly as Domain::fix_position
-    if (p.x < rb.lo[0]) p.x += rb.L[0]; else if (p.x > rb.hi[0]) p.x -= rb.L[0];
-    if (p.y < rb.lo[1]) p.y += rb.L[1]; else if (p.y > rb.hi[1]) p.y -= rb.L[1];
-    if (p.z < rb.lo[2]) p.z += rb.L[2]; else if (p.z > rb.hi[2]) p.z -= rb.L[2];
+    // single-image wrap exactly as Domain::fix_position, counting the crossings
+    // (+1 through the upper face) as exchange_owned adds them to msd_domain_cross
+    const int3 w = wrap_shift(rb, p);
+    if (w.x) p.x += w.x > 0 ? -rb.L[0] : rb.L[0];
+    if (w.y) p.y += w.y > 0 ? -rb.L[1] : rb.L[1];
+    if (w.z) p.z += w.z > 0 ? -rb.L[2] : rb.L[2];
     d.pos[i] = p;
+    if (d.img && (w.x | w.y | w.z)) {
+      int4 m = d.img[i];
+      m.x += w.x; m.y += w.y; m.z += w.z;
+      d.img[i] = m;
+    }
     int cx = (int)floor((p.x - rb.lo[0]) * rb.inv_w[0]);
     int cy = (int)floor((p.y - rb.lo[1]) * rb.inv_w[1]);
     int cz = (int)floor((p.z - rb.lo[2]) * rb.inv_w[2]);
@@ -340,6 +354,7 @@ __global__ void __launch_bounds__(256) k_copy_state(Dev d, Box b, int forced) {
   d.t_acc_old[i] = d.acc_old[i];
   d.t_type[i] = d.type[i];
   d.t_id[i] = d.id[i];
+  if (d.img) d.t_img[i] = d.img[i];
   d.perm_tmp[i] = d.atom_cell[i];  // cell of old slot i (perm_tmp is free again)
 }
 
@@ -357,6 +372,7 @@ __global__ void __launch_bounds__(256) k_gather(Dev d, Box b, int forced) {
   d.acc_old[k] = d.t_acc_old[o];
   d.type[k] = d.t_type[o];
   d.id[k] = d.t_id[o];
+  if (d.img) d.img[k] = d.t_img[o];
   d.cell_of[k] = d.perm_tmp[o];
   update_rel(d, repbox(b, rep), k, x);
   d.rel_ref[k] = d.rel[k];
@@ -573,8 +589,9 @@ __device__ inline void thermo_finish(double ke2, const double P3[3], double msum
   out[4] = 0.5 * pe2;
 }
 
-__global__ void __launch_bounds__(256) k_thermo_final(Dev d, ThermoCfg tc, int nb_ke, int nb_ev, int ring_slot) {
-  double v[6] = {0, 0, 0, 0, 0, 0};
+__global__ void __launch_bounds__(256) k_thermo_final(Dev d, ThermoCfg tc, int nb_ke, int nb_ev, int nb_ke_end,
+                                                      int ring_slot) {
+  double v[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   for (int k = threadIdx.x; k < nb_ke; k += blockDim.x)
     for (int q = 0; q < 4; ++q) v[q] += d.partials_ke[(size_t)k * 4 + q];
   const double *ev = d.partials_ev;
@@ -582,14 +599,22 @@ __global__ void __launch_bounds__(256) k_thermo_final(Dev d, ThermoCfg tc, int n
     v[4] += ev[(size_t)k * 2];
     v[5] += ev[(size_t)k * 2 + 1];
   }
-  __shared__ double out[6];
-  block_sum_store<6>(v, out);
+  for (int k = threadIdx.x; k < nb_ke_end; k += blockDim.x)
+    for (int q = 0; q < 4; ++q) v[6 + q] += d.partials_ke_end[(size_t)k * 4 + q];
+  __shared__ double out[10];
+  block_sum_store<10>(v, out);
   __syncthreads();
   if (threadIdx.x == 0) {
     double res[5];
     const double P3[3] = {out[1], out[2], out[3]};
     // total mass is fixed at upload (thermo[5])
     thermo_finish(out[0], P3, d.thermo[5], out[4], out[5], tc.n, tc.n_r_df, tc.k_b, tc.volume, tc.langevin, res);
+    if (nb_ke_end > 0) {  // KE as Atom_data::kinetic_energy() reads it after the step
+      double e[5];
+      const double Q3[3] = {out[7], out[8], out[9]};
+      thermo_finish(out[6], Q3, d.thermo[5], 0.0, 0.0, tc.n, tc.n_r_df, tc.k_b, tc.volume, tc.langevin, e);
+      res[0] = e[0];
+    }
     for (int q = 0; q < 5; ++q) d.thermo[q] = res[q];
     if (ring_slot >= 0) {
       double *r = d.thermo_ring + (size_t)ring_slot * THERMO_REC;
@@ -721,6 +746,19 @@ __global__ void __launch_bounds__(256) k_to_host_order(Dev d, Box b, int what) {
   }
   const size_t h = ((size_t)rb.id_off + d.id[k]) * 3;
   d.h3[h] = v.x; d.h3[h + 1] = v.y; d.h3[h + 2] = v.z;
+}
+
+// boundary crossings in host order: the stored counts plus the wrap the current
+// position still owes (the reference wraps every step, the device at list builds)
+__global__ void __launch_bounds__(256) k_images_to_host(Dev d, Box b) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= b.nslot) return;
+  const int rep = rep_of_slot(b, k);
+  if (rep < 0) return;
+  const int3 w = wrap_shift(repbox(b, rep), d.pos[k]);
+  const int4 m = d.img[k];
+  const size_t h = ((size_t)repbox(b, rep).id_off + d.id[k]) * 3;
+  d.hi3[h] = m.x + w.x; d.hi3[h + 1] = m.y + w.y; d.hi3[h + 2] = m.z + w.z;
 }
 
 // canonical rows (id_i, id_j, sx, sy, sz) of the current list (single system)
@@ -901,8 +939,9 @@ int launch_set_rebuild_cond(const Dev &d, cudaGraphConditionalHandle h, cudaStre
   return chk();
 }
 
-int launch_thermo_final(const Dev &d, const ThermoCfg &tc, int nb_ke, int nb_ev, int ring_slot, cudaStream_t st) {
-  k_thermo_final<<<1, 256, 0, st>>>(d, tc, nb_ke, nb_ev, ring_slot);
+int launch_thermo_final(const Dev &d, const ThermoCfg &tc, int nb_ke, int nb_ev, int nb_ke_end, int ring_slot,
+                        cudaStream_t st) {
+  k_thermo_final<<<1, 256, 0, st>>>(d, tc, nb_ke, nb_ev, nb_ke_end, ring_slot);
   return chk();
 }
 
@@ -928,6 +967,12 @@ int launch_nve(const Dev &d, const Box &b, const ThermoCfg &tc, const NveCfg &cf
 
 int launch_to_host_order(const Dev &d, const Box &b, int what, cudaStream_t st) {
   k_to_host_order<<<ceil_div(b.nslot, 256), 256, 0, st>>>(d, b, what);
+  return chk();
+}
+
+int launch_images_to_host(const Dev &d, const Box &b, cudaStream_t st) {
+  if (!d.img || !d.hi3) return CAVGPU_E_STATE;
+  k_images_to_host<<<ceil_div(b.nslot, 256), 256, 0, st>>>(d, b);
   return chk();
 }
 

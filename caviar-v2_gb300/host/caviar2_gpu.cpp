@@ -2,9 +2,15 @@
 #include "caviar2_gpu.hpp"
 
 #include <algorithm>
+#include <charconv>
 #include <cmath>
+#include <condition_variable>
 #include <cstdio>
 #include <cstdlib>
+#include <deque>
+#include <fstream>
+#include <mutex>
+#include <thread>
 #include <unordered_map>
 
 namespace caviar2 {
@@ -59,7 +65,19 @@ bool Atom_data::add_atom(size_t id, size_t type, const Vector3d<double> &pos, co
   atom_struct_owned.position.push_back(pos);
   atom_struct_owned.velocity.push_back(vel);
   atom_struct_owned.acceleration.push_back(Vector3d<double>{0, 0, 0});
+  if (msd_process) atom_struct_owned.msd_domain_cross.push_back(Vector3d<int>{0, 0, 0});
   return true;
+}
+
+void Atom_data::zero_msd_domain_cross() {
+  auto &m = atom_struct_owned.msd_domain_cross;
+  msd_base_.resize(m.size());
+  for (size_t j = 0; j < m.size(); ++j) {
+    msd_base_[j].x += m[j].x;
+    msd_base_[j].y += m[j].y;
+    msd_base_[j].z += m[j].z;
+    m[j] = Vector3d<int>{0, 0, 0};
+  }
 }
 
 bool Atom_data::add_atom(tools::Atom &a) {
@@ -347,6 +365,13 @@ void Md_simulator::initialize() {
       caviar_->log.error_all("energy or temperature is not set.");
     }
   }
+  p.msd_process = ad.msd_process ? 1 : 0;
+  if (ad.msd_process) {  // the device counts from zero: the host mirror keeps its values
+    auto &m = ad.atom_struct_owned.msd_domain_cross;
+    m.resize(ad.atom_struct_owned.position.size());
+    ad.msd_base_.assign(m.size(), Vector3d<int>{0, 0, 0});
+    for (size_t j = 0; j < m.size(); ++j) ad.msd_base_[j] = Vector3d<int>{-m[j].x, -m[j].y, -m[j].z};
+  }
   if (ctx_) cavgpu_destroy(ctx_);
   ctx_ = nullptr;
   check(cavgpu_create(&p, &ctx_), "cavgpu_create");
@@ -364,41 +389,90 @@ void Md_simulator::initialize() {
 void Md_simulator::setup() {
   check(cavgpu_setup(ctx_), "cavgpu_setup");
   time = dt * initial_step;
-  sync_host();
+  // setup takes the temperature, not the pressure (src/md_simulator.cpp:605-607)
+  Atom_data &ad = caviar_->atom_data;
+  auto &o = ad.atom_struct_owned;
+  check(cavgpu_download(ctx_, &o.position[0].x, &o.velocity[0].x, &o.acceleration[0].x), "cavgpu_download");
+  read_thermo(false);
+  if (ad.msd_process) download_images();
+  host_dirty_ = false;
+  for (Writer *w : caviar_->writers) w->write(0, 0.0);  // src/md_simulator.cpp:609-610
+}
+
+void Md_simulator::read_thermo(bool with_pressure) {
+  Atom_data &ad = caviar_->atom_data;
+  double th[6];
+  check(cavgpu_thermo(ctx_, th), "cavgpu_thermo");
+  ad.kinetic_energy_ = th[0];
+  ad.temperature_ = th[1];
+  if (with_pressure && ad.pressure_process) ad.pressure_ = th[2];  // finalize_pressure returns early without it
+  ad.virialForce = th[3];
+  ad.potential_energy_ = th[4];
+}
+
+void Md_simulator::download_images() {
+  Atom_data &ad = caviar_->atom_data;
+  auto &m = ad.atom_struct_owned.msd_domain_cross;
+  const size_t n = ad.atom_struct_owned.position.size();
+  std::vector<int32_t> img(3 * std::max<size_t>(n, 1));
+  check(cavgpu_download_images(ctx_, img.data()), "cavgpu_download_images");
+  m.resize(n);
+  ad.msd_base_.resize(n);
+  for (size_t j = 0; j < n; ++j)
+    m[j] = Vector3d<int>{img[3 * j] - ad.msd_base_[j].x, img[3 * j + 1] - ad.msd_base_[j].y,
+                         img[3 * j + 2] - ad.msd_base_[j].z};
 }
 
 void Md_simulator::sync_host() {
   Atom_data &ad = caviar_->atom_data;
   auto &o = ad.atom_struct_owned;
   check(cavgpu_download(ctx_, &o.position[0].x, &o.velocity[0].x, &o.acceleration[0].x), "cavgpu_download");
-  double th[6];
-  check(cavgpu_thermo(ctx_, th), "cavgpu_thermo");
-  ad.kinetic_energy_ = th[0];
-  ad.temperature_ = th[1];
-  ad.pressure_ = th[2];
-  ad.virialForce = th[3];
-  ad.potential_energy_ = th[4];
+  read_thermo(true);
+  if (ad.msd_process) download_images();
   host_dirty_ = false;
 }
 
+int Md_simulator::writers_want(int64_t i) const {
+  int w = 0;
+  for (const Writer *wr : caviar_->writers) w |= wr->wants(i);
+  return w;
+}
+
+void Md_simulator::write_outputs(int64_t i) {
+  const int want = writers_want(i);
+  if (!want) return;
+  Atom_data &ad = caviar_->atom_data;
+  if (want & Writer::WANT_STATE) {
+    auto &o = ad.atom_struct_owned;
+    check(cavgpu_download(ctx_, &o.position[0].x, &o.velocity[0].x, &o.acceleration[0].x), "cavgpu_download");
+    host_dirty_ = false;
+  }
+  if ((want & Writer::WANT_CROSSINGS) && ad.msd_process) download_images();
+  for (Writer *w : caviar_->writers)
+    if (w->wants(i)) w->write(i, time);
+}
+
+void Md_simulator::finish_writers() {
+  for (Writer *w : caviar_->writers) w->finish();
+}
+
+// one step of the reference's loop body (src/md_simulator.cpp:445-546): the
+// integrator, then the writers at (current_step, time), then time += dt
 void Md_simulator::step() {
   if (!initialized) {
     initialize();
     setup();
   }
   check(cavgpu_step(ctx_, 1), "cavgpu_step");
-  double th[6];
-  check(cavgpu_thermo(ctx_, th), "cavgpu_thermo");
-  Atom_data &ad = caviar_->atom_data;
-  ad.kinetic_energy_ = th[0];
-  ad.temperature_ = th[1];
-  ad.pressure_ = th[2];
-  ad.virialForce = th[3];
-  ad.potential_energy_ = th[4];
+  read_thermo(true);
   host_dirty_ = true;  // positions stay on the device until sync_host() / run() / cleanup()
+  write_outputs(current_step);
   time += dt;
 }
 
+// src/md_simulator.cpp:317-356.  The device runs uninterrupted up to the next
+// step some writer reads (CUDA graphs of many steps); the host mirror is
+// refreshed only there.
 bool Md_simulator::run() {
   if (use_time && use_step) caviar_->log.error_all("simulator md: verify_settings: cannot use both 'time' and 'step'.");
   if (!(use_time || use_step)) caviar_->log.error_all("simulator md: verify_settings: please assign 'time' or 'step' variables.");
@@ -407,16 +481,28 @@ bool Md_simulator::run() {
     initialize();
     setup();
   }
-  const int64_t n = final_step - initial_step;
-  if (n > 0) check(cavgpu_step(ctx_, n), "cavgpu_step");
-  current_step = final_step;
-  time = dt * final_step;
+  current_step = initial_step;
+  while (current_step < final_step) {
+    int64_t stop = current_step;
+    while (stop < final_step - 1 && !writers_want(stop)) ++stop;
+    const int64_t n = stop - current_step + 1;
+    check(cavgpu_step(ctx_, n), "cavgpu_step");
+    for (int64_t k = 0; k + 1 < n; ++k) time += dt;  // the reference's running sum
+    current_step = stop;
+    read_thermo(true);
+    host_dirty_ = true;
+    write_outputs(current_step);
+    time += dt;
+    ++current_step;
+  }
   sync_host();
+  finish_writers();
   caviar_->log.info("MD finished.");
   return true;
 }
 
 void Md_simulator::cleanup() {
+  finish_writers();
   if (!ctx_) return;
   if (host_dirty_) sync_host();
   cavgpu_destroy(ctx_);
@@ -465,5 +551,280 @@ void Md_simulator::export_neighborlist() {
   for (auto &r : nl.neighlist) std::sort(r.begin(), r.end());  // the O(N^2) build's order
   nl.cutoff_extra = ce;
 }
+
+// ---------------------------------------------------------------- writers
+// std::ostream prints a double with the default flags as printf("%.*g", precision);
+// std::to_chars with chars_format::general and a precision is specified as that
+// same conversion, without the locale and stream machinery.
+void append_general6(std::string &out, double v) {
+  char buf[40];
+  const auto r = std::to_chars(buf, buf + sizeof(buf), v, std::chars_format::general, 6);
+  out.append(buf, r.ptr);
+}
+
+namespace {
+template <class I>
+void append_int(std::string &out, I v) {
+  char buf[24];
+  const auto r = std::to_chars(buf, buf + sizeof(buf), v);
+  out.append(buf, r.ptr);
+}
+}  // namespace
+
+namespace writer {
+
+struct Atom_writer::Impl {
+  std::ofstream xyz, energy, temperature, pressure, msd, volume;
+
+  // an xyz frame: a copy of the host mirror, formatted by the worker thread
+  struct Frame {
+    std::vector<size_t> type, id;
+    std::vector<Vector3d<double>> pos, vel, acc;
+  };
+  std::mutex mu;
+  std::condition_variable cv;
+  std::deque<Frame> queue;
+  bool busy = false, stop = false;
+  std::thread worker;
+
+  ~Impl() {
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      stop = true;
+    }
+    cv.notify_all();
+    if (worker.joinable()) worker.join();
+  }
+
+  void push(Frame &&f) {
+    std::unique_lock<std::mutex> lk(mu);
+    if (!worker.joinable()) worker = std::thread([this] { loop(); });
+    cv.wait(lk, [this] { return queue.size() < 2; });  // at most two frames held in memory
+    queue.push_back(std::move(f));
+    cv.notify_all();
+  }
+
+  void drain() {
+    std::unique_lock<std::mutex> lk(mu);
+    cv.wait(lk, [this] { return queue.empty() && !busy; });
+  }
+
+  void loop() {
+    for (;;) {
+      Frame f;
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        cv.wait(lk, [this] { return stop || !queue.empty(); });
+        if (queue.empty()) return;  // stop, nothing left
+        f = std::move(queue.front());
+        queue.pop_front();
+        busy = true;
+      }
+      cv.notify_all();
+      write_frame(f);
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        busy = false;
+      }
+      cv.notify_all();
+    }
+  }
+
+  // rows [a, b) of dump_xyz_serial's text (src/writer/atom_writer/dump_xyz_serial.cpp:49-63);
+  // the position offset is {0, 0, 0}, and x + 0.0 turns -0.0 into 0.0 as there
+  static void rows(const Frame &f, size_t a, size_t b, std::string &out) {
+    out.clear();
+    out.reserve((b - a) * (24 + 14 * (3 + 3 * !f.vel.empty() + 3 * !f.acc.empty())));
+    for (size_t i = a; i < b; ++i) {
+      append_int(out, f.type[i]);
+      if (!f.id.empty()) { out.push_back(' '); append_int(out, f.id[i]); }
+      out.push_back(' '); append_general6(out, f.pos[i].x + 0.0);
+      out.push_back(' '); append_general6(out, f.pos[i].y + 0.0);
+      out.push_back(' '); append_general6(out, f.pos[i].z + 0.0);
+      if (!f.vel.empty()) {
+        out.push_back(' '); append_general6(out, f.vel[i].x);
+        out.push_back(' '); append_general6(out, f.vel[i].y);
+        out.push_back(' '); append_general6(out, f.vel[i].z);
+      }
+      if (!f.acc.empty()) {
+        out.push_back(' '); append_general6(out, f.acc[i].x);
+        out.push_back(' '); append_general6(out, f.acc[i].y);
+        out.push_back(' '); append_general6(out, f.acc[i].z);
+      }
+      out.push_back('\n');
+    }
+  }
+
+  void write_frame(const Frame &f) {
+    const size_t n = f.pos.size();
+    std::string head;
+    append_int(head, n);
+    head += "\nAtom\n";
+    xyz.write(head.data(), (std::streamsize)head.size());
+    const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t parts = std::max<size_t>(1, std::min<size_t>(hw, n / 16384));
+    std::vector<std::string> text(parts);
+    std::vector<std::thread> th;
+    for (size_t p = 1; p < parts; ++p) th.emplace_back(rows, std::cref(f), n * p / parts, n * (p + 1) / parts, std::ref(text[p]));
+    rows(f, 0, n / parts, text[0]);
+    for (auto &t : th) t.join();
+    for (const auto &t : text) xyz.write(t.data(), (std::streamsize)t.size());
+    xyz.flush();
+  }
+};
+
+Atom_writer::Atom_writer(Caviar2 *c) : Writer(c), impl_(new Impl) { set_caviar(c); }
+
+Atom_writer::~Atom_writer() {
+  delete impl_;  // finishes queued frames, then closes the files
+}
+
+void Atom_writer::set_caviar(Caviar2 *c) {
+  caviar_ = c;
+  atom_data = c ? &c->atom_data : nullptr;
+  domain = c ? &c->domain : nullptr;
+}
+
+void Atom_writer::set_xyz_ghost_step(int step) {
+  xyz_ghost_step = step;
+  output_xyz_ghost = step > 0;
+  if (output_xyz_ghost) caviar_->log.error_all("writer::Atom_writer: ghost xyz output is not on the GPU path");
+}
+
+void Atom_writer::set_povray_step(int step) {
+  povray_step = step;
+  output_povray = step > 0;
+  if (output_povray) caviar_->log.error_all("writer::Atom_writer: povray output is not on the GPU path");
+}
+
+void Atom_writer::initialize() {
+  initialized = true;
+  if (output_msd && !atom_data->get_msd_process())
+    caviar_->log.error_all("In order to have 'output_msd' in writer::Atom_data, 'msd_process' must be activated in atom_data::Atom_data");
+  Impl &m = *impl_;
+  if (output_xyz && !m.xyz.is_open()) m.xyz.open(file_name_xyz + ".xyz");
+  if (output_energy && !m.energy.is_open()) m.energy.open(file_name_energy + ".txt");
+  if (output_temperature && !m.temperature.is_open()) m.temperature.open(file_name_temperature + ".txt");
+  if (output_pressure && !m.pressure.is_open()) m.pressure.open(file_name_pressure + ".txt");
+  if (output_msd && !m.msd.is_open()) m.msd.open(file_name_msd + ".txt");
+  if (output_volume && !m.volume.is_open()) m.volume.open(file_name_volume + ".txt");
+}
+
+int Atom_writer::wants(int64_t i) const {
+  int w = 0;
+  if (output_xyz && i % xyz_step == 0) w |= WANT_CALL | WANT_STATE;
+  if (output_energy && i % energy_step == 0) w |= WANT_CALL | WANT_THERMO;
+  if (output_temperature && i % temperature_step == 0) w |= WANT_CALL | WANT_THERMO;
+  if (output_pressure && i % pressure_step == 0) w |= WANT_CALL | WANT_THERMO;
+  if (output_msd && i % msd_step == 0 && i >= msd_initial_step) w |= WANT_CALL | WANT_STATE | WANT_CROSSINGS;
+  if (output_volume && i % volume_step == 0) w |= WANT_CALL;
+  return w;
+}
+
+// Atom_writer::write / write_serial (src/writer/atom_writer.cpp:287-303, 427-466)
+void Atom_writer::write(int64_t i, double t) {
+  if (!initialized) initialize();
+  if (output_xyz && i % xyz_step == 0) dump_xyz_serial(i, t);
+  if (output_energy && i % energy_step == 0) dump_energy_serial(i, t);
+  if (output_temperature && i % temperature_step == 0) dump_temperature_serial(i, t);
+  if (output_pressure && i % pressure_step == 0) dump_pressure_serial(i, t);
+  if (output_msd && i % msd_step == 0) dump_msd_serial(i, t);
+  if (output_volume && i % volume_step == 0) dump_volume_serial(i, t);
+}
+
+void Atom_writer::finish() { impl_->drain(); }
+
+void Atom_writer::close_files() {
+  impl_->drain();
+  for (std::ofstream *f : {&impl_->xyz, &impl_->energy, &impl_->temperature, &impl_->pressure, &impl_->msd,
+                           &impl_->volume})
+    if (f->is_open()) f->close();
+}
+
+void Atom_writer::dump_xyz_serial(int64_t, double) {
+  const Atom_struct &o = atom_data->atom_struct_owned;
+  Impl::Frame f;
+  f.type = o.type;
+  if (xyz_output_id) f.id = o.id;
+  f.pos = o.position;
+  if (xyz_output_velocity) f.vel = o.velocity;
+  if (xyz_output_acceleration) f.acc = o.acceleration;
+  impl_->push(std::move(f));
+}
+
+namespace {
+// "i t value" and a flush (src/writer/atom_writer/dump_energy.cpp)
+void write_scalar(std::ofstream &f, int64_t i, double t, double v) {
+  std::string s;
+  append_int(s, i);
+  s.push_back(' ');
+  append_general6(s, t);
+  s.push_back(' ');
+  append_general6(s, v);
+  s.push_back('\n');
+  f.write(s.data(), (std::streamsize)s.size());
+  f.flush();
+}
+}  // namespace
+
+void Atom_writer::dump_energy_serial(int64_t i, double t) { write_scalar(impl_->energy, i, t, atom_data->kinetic_energy()); }
+void Atom_writer::dump_temperature_serial(int64_t i, double t) { write_scalar(impl_->temperature, i, t, atom_data->temperature()); }
+void Atom_writer::dump_pressure_serial(int64_t i, double t) { write_scalar(impl_->pressure, i, t, atom_data->pressure()); }
+void Atom_writer::dump_volume_serial(int64_t i, double t) { write_scalar(impl_->volume, i, t, domain->volume_global()); }
+
+// Atom_writer::dump_msd_serial (src/writer/atom_writer/dump_msd.cpp:35-101), with its
+// conventions kept: dr = initial - current + crossings * L, and the y and z crossing
+// totals accumulate the x counts.
+void Atom_writer::dump_msd_serial(int64_t i, double t) {
+  Atom_struct &o = atom_data->atom_struct_owned;
+  const auto &pos = o.position;
+  const size_t n = pos.size();
+  if (i < msd_initial_step) return;
+  std::string s;
+  if (i == msd_initial_step) {
+    msd_initial_position = pos;
+    atom_data->zero_msd_domain_cross();
+    append_int(s, i);
+    s.push_back(' ');
+    append_general6(s, t);
+    s += " 0.0\n";
+    impl_->msd.write(s.data(), (std::streamsize)s.size());
+    return;
+  }
+  if (n != msd_initial_position.size()) caviar_->log.error_all("  (pos.size != msd_initial_position.size())");
+  const auto &L = domain->size_global;
+  double sum_dr_sq = 0.0;
+  int cross[3] = {0, 0, 0};
+  int count = 0;
+  for (size_t j = 0; j < n; ++j) {
+    if (msd_type > -1 && o.type[j] != static_cast<unsigned int>(msd_type)) continue;
+    const auto &c = o.msd_domain_cross[j];
+    double dx = msd_initial_position[j].x - pos[j].x;
+    double dy = msd_initial_position[j].y - pos[j].y;
+    double dz = msd_initial_position[j].z - pos[j].z;
+    dx += c.x * L.x;
+    dy += c.y * L.y;
+    dz += c.z * L.z;
+    cross[0] += c.x;
+    cross[1] += c.x;
+    cross[2] += c.x;
+    sum_dr_sq += dx * dx + dy * dy + dz * dz;
+    ++count;
+  }
+  const double msd = count > 0 ? sum_dr_sq / count : 0.0;
+  append_int(s, i);
+  s.push_back(' ');
+  append_general6(s, t);
+  s.push_back(' ');
+  append_general6(s, msd);
+  for (int a = 0; a < 3; ++a) { s.push_back(' '); append_int(s, cross[a]); }
+  s.push_back(' ');
+  append_int(s, cross[0] + cross[1] + cross[2]);
+  s.push_back('\n');
+  impl_->msd.write(s.data(), (std::streamsize)s.size());
+  impl_->msd.flush();
+}
+
+}  // namespace writer
 
 }  // namespace caviar2

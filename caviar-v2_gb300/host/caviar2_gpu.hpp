@@ -8,7 +8,8 @@
 // objects hold the host mirror of the state in the reference's layouts; the
 // step itself runs on the GPU through include/cavgpu.h.  Members are
 // initialised (the reference leaves several uninitialised when Caviar2 is
-// default-constructed).  Out of scope here: MPI, writers, constraints, molecules.
+// default-constructed).  Constraints: Nve.  Writers: writer::Atom_writer.  Out of
+// scope here: MPI, other constraints and writers, molecules.
 #pragma once
 
 #include <cstddef>
@@ -59,6 +60,8 @@ class Domain {
 struct Atom_struct {
   std::vector<size_t> id, type;
   std::vector<Vector3d<double>> position, velocity, acceleration;
+  // periodic-boundary crossings per axis (Atom_data::msd_process), +1 through the upper face
+  std::vector<Vector3d<int>> msd_domain_cross;
 };
 
 struct Atom_type_params {
@@ -88,6 +91,16 @@ class Atom_data {
   void set_n_r_df(int v) { n_r_df = v; }
   void set_temperature_process(bool v) { temperature_process = v; }
   void set_pressure_process(bool v) { pressure_process = v; }
+  // the two overloads of the reference (src/atom_data.cpp:327-330, inc/caviar2/atom_data.hpp:695-700)
+  void set_msd_process(int flag) { msd_process = flag != 0; }
+  void set_msd_process(bool stat) {
+    msd_process = stat;
+    atom_struct_owned.msd_domain_cross.resize(atom_struct_owned.position.size());
+  }
+  bool get_msd_process() const { return msd_process; }
+  // msd_domain_cross of every atom set to zero (the writer's MSD origin); the
+  // device keeps counting, the host mirror is counted from here
+  void zero_msd_domain_cross();
   void add_type_mass(int type, double m);  // src/atom_data.cpp:368-383
   void add_type_charge(int, double) {}
   // raw add (src/atom_data.cpp:603-637): no domain check
@@ -107,7 +120,7 @@ class Atom_data {
   Atom_type_params atom_type_params;
   double ghost_cutoff = 0.0, k_b = -1.0;
   int n_r_df = -1;
-  bool temperature_process = false, pressure_process = false, stochastic_force_present = false;
+  bool temperature_process = false, pressure_process = false, stochastic_force_present = false, msd_process = false;
   double virialForce = 0.0, virialConstraint = 0.0, virialExternalForce = 0.0;
 
  private:
@@ -115,6 +128,8 @@ class Atom_data {
   friend class force_field_access;
   Caviar2 *caviar_ = nullptr;
   double temperature_ = 0.0, pressure_ = 0.0, kinetic_energy_ = 0.0, potential_energy_ = 0.0;
+  // device crossing counts at the host mirror's zero: msd_domain_cross = device - msd_base_
+  std::vector<Vector3d<int>> msd_base_;
 };
 
 class Neighborlist {
@@ -225,10 +240,142 @@ class Md_simulator {
 
  private:
   void check(int status, const char *what);
+  void read_thermo(bool with_pressure);
+  void download_images();
+  int writers_want(int64_t i) const;   // union of Writer::wants over the writers
+  void write_outputs(int64_t i);       // host mirror refreshed as the writers ask, then Writer::write
+  void finish_writers();
   Caviar2 *caviar_ = nullptr;
   cavgpu_ctx *ctx_ = nullptr;
   bool host_dirty_ = false;
 };
+
+// Writers (inc/caviar2/writer.hpp).  The GPU path adds Writer::wants(): what a
+// writer reads at step i, so that the simulator advances the device without a
+// host round trip up to the next step some writer reads.
+class Writer {
+ public:
+  enum : int { WANT_CALL = 1, WANT_THERMO = 2, WANT_STATE = 4, WANT_CROSSINGS = 8, WANT_ALL = 15 };
+  explicit Writer(Caviar2 *c = nullptr) : caviar_(c) {}
+  virtual ~Writer() = default;
+  virtual void initialize() {}
+  virtual void write(int64_t, double) {}  // time step and time
+  virtual void start_new_files() {}
+  virtual void start_new_files(std::string &) {}
+  virtual void open_files() {}
+  virtual void close_files() {}
+  virtual void generate() {}
+  virtual void set_caviar(Caviar2 *c) { caviar_ = c; }
+  // 0 when write(i, t) would do nothing, else WANT_* bits; a writer of its own
+  // (not overriding this) is called with the whole host mirror at every step
+  virtual int wants(int64_t) const { return WANT_ALL; }
+  // blocks until output handed to background threads is in its files
+  virtual void finish() {}
+
+  bool initialized = false;
+  int64_t last_timestep = 0;
+  double last_time = 0.0, dt = 0.0;
+  int my_mpi_rank = 0, mpi_world_size = 1;
+
+ protected:
+  Caviar2 *caviar_;
+};
+
+namespace writer {
+// writer::Atom_writer (inc/caviar2/writer/atom_writer.hpp, src/writer/atom_writer.cpp,
+// src/writer/atom_writer/dump_{xyz_serial,energy,msd}.cpp): xyz frames, kinetic
+// energy, temperature, pressure, volume and mean square displacement, each every
+// X steps, in the reference's text formats (std::ostream default formatting:
+// six significant digits).  xyz frames are copied and formatted on background
+// threads while the device keeps stepping.  Single process: the *_mpi_* setters
+// are kept and have no effect.  Ghost xyz and povray output are not on the GPU
+// path (the setters stop with an error).
+class Atom_writer : public Writer {
+ public:
+  explicit Atom_writer(Caviar2 *c);
+  ~Atom_writer() override;
+  Atom_writer(const Atom_writer &) = delete;
+  Atom_writer &operator=(const Atom_writer &) = delete;
+
+  void set_caviar(Caviar2 *c) override;
+  void initialize() override;  // opens the files (src/writer/atom_writer.cpp:100-166)
+  void write(int64_t i, double t) override;
+  int wants(int64_t i) const override;
+  void finish() override;
+  void close_files() override;
+
+  void set_xyz_mpi_per_process(bool) {}
+  void set_xyz_ghost_mpi_per_process(bool) {}
+  void set_energy_mpi_per_process(bool) {}
+  void set_temperature_mpi_per_process(bool) {}
+  void set_pressure_mpi_per_process(bool) {}
+  void set_povray_mpi_per_process(bool) {}
+  void set_msd_mpi_per_process(bool) {}
+  void set_volume_mpi_per_process(bool) {}
+  void set_xyz_mpi_rank0(bool) {}
+  void set_xyz_ghost_mpi_rank0(bool) {}
+  void set_energy_mpi_rank0(bool) {}
+  void set_temperature_mpi_rank0(bool) {}
+  void set_pressure_mpi_rank0(bool) {}
+  void set_povray_mpi_rank0(bool) {}
+  void set_msd_mpi_rank0(bool) {}
+  void set_volume_mpi_rank0(bool) {}
+
+  void set_xyz_step(int step) { xyz_step = step; output_xyz = step > 0; }
+  void set_xyz_ghost_step(int step);
+  void set_povray_step(int step);
+  void set_energy_step(int step) { energy_step = step; output_energy = step > 0; }
+  void set_temperature_step(int step) { temperature_step = step; output_temperature = step > 0; }
+  void set_pressure_step(int step) { pressure_step = step; output_pressure = step > 0; }
+  void set_msd_step(int step) { msd_step = step; output_msd = step > 0; }
+  void set_msd_initial_step(int step) { msd_initial_step = step; }
+  void set_volume_step(int step) { volume_step = step; output_volume = step > 0; }
+
+  void set_file_name_xyz(const std::string &fn) { file_name_xyz = fn; }
+  void set_file_name_xyz_ghost(const std::string &fn) { file_name_xyz_ghost = fn; }
+  void set_file_name_energy(const std::string &fn) { file_name_energy = fn; }
+  void set_file_name_temperature(const std::string &fn) { file_name_temperature = fn; }
+  void set_file_name_pressure(const std::string &fn) { file_name_pressure = fn; }
+  void set_file_name_povray(const std::string &fn) { file_name_povray = fn; }
+  void set_file_name_msd(const std::string &fn) { file_name_msd = fn; }
+  void set_file_name_volume(const std::string &fn) { file_name_volume = fn; }
+
+  void set_xyz_output_id(int v) { xyz_output_id = v != 0; }
+  void set_xyz_output_velocity(int v) { xyz_output_velocity = v != 0; }
+  void set_xyz_output_acceleration(int v) { xyz_output_acceleration = v != 0; }
+  void set_msd_type(int v) { msd_type = v; }
+
+  void dump_xyz_serial(int64_t i, double t);
+  void dump_energy_serial(int64_t i, double t);
+  void dump_temperature_serial(int64_t i, double t);
+  void dump_pressure_serial(int64_t i, double t);
+  void dump_volume_serial(int64_t i, double t);
+  void dump_msd_serial(int64_t i, double t);
+
+  Atom_data *atom_data = nullptr;
+  Domain *domain = nullptr;  // the reference leaves it null (MSD and volume output then crash)
+
+  bool output_energy = false, output_temperature = false, output_pressure = false, output_xyz = false,
+       output_xyz_ghost = false, output_povray = false, output_msd = false, output_volume = false;
+  bool xyz_output_velocity = false, xyz_output_acceleration = false, xyz_output_id = false;
+  int64_t energy_step = 100, temperature_step = 100, pressure_step = 100, xyz_step = 100, xyz_ghost_step = 100,
+          povray_step = 100, msd_step = 100, volume_step = 100;
+  int msd_type = -1;         // atom type of the MSD (-1: every atom)
+  int msd_initial_step = 0;  // step whose positions are the MSD origin
+  std::string file_name_xyz = "o_xyz", file_name_xyz_ghost = "o_xyz_g", file_name_energy = "o_energy",
+              file_name_temperature = "o_temperature", file_name_pressure = "o_pressure",
+              file_name_povray = "o_pov", file_name_msd = "o_msd", file_name_volume = "o_volume";
+  std::vector<Vector3d<double>> msd_initial_position;
+
+ private:
+  struct Impl;  // files and the xyz formatting thread
+  Impl *impl_ = nullptr;
+};
+}  // namespace writer
+
+// Text of a double as std::ostream prints it with the default flags and
+// precision 6 (printf "%g" of precision 6), appended to out.
+void append_general6(std::string &out, double v);
 
 class Constraint {
  public:
@@ -269,9 +416,11 @@ class Caviar2 {
   Log log;
   std::vector<Force_field *> forces;       // non-owning (src/caviar2.cpp:40-44)
   std::vector<Constraint *> constraints;   // non-owning
+  std::vector<Writer *> writers;           // non-owning (src/caviar2.cpp:51-54)
 
   void add_force_field(Force_field *f) { forces.push_back(f); }
   void add_constraint(Constraint *c) { constraints.push_back(c); }
+  void add_writer(Writer *w) { writers.push_back(w); }
 };
 
 }  // namespace caviar2

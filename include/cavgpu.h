@@ -96,6 +96,11 @@ typedef struct cavgpu_params {
   int32_t nve_pad;
   double nve_value;               /* energy_per_dof, energy_tot, kbt or temperature */
   double nve_kb;                  /* kb of CAVGPU_NVE_KB_TEMPERATURE */
+  /* Atom_data::msd_process (inc/caviar2/atom_data.hpp:690-700): count each atom's
+   * periodic-boundary crossings per axis, as exchange_owned adds them to
+   * Atom_struct::msd_domain_cross (src/atom_data/exchange_owned_single_md_domain.cpp:49-55) */
+  int32_t msd_process;
+  int32_t msd_pad;
 } cavgpu_params;
 
 #define CAVGPU_NVE_ENERGY_PER_DOF 0
@@ -155,6 +160,13 @@ int cavgpu_thermo(cavgpu_ctx *ctx, double *out6);
 /* Download in host (insertion) order; positions wrapped as Domain::fix_position
  * would (src/domain.cpp:443-493).  Any pointer may be NULL. */
 int cavgpu_download(cavgpu_ctx *ctx, double *pos3, double *vel3, double *acc3);
+
+/* Boundary crossings per atom and axis in host order (int32 x3), counted since
+ * the upload: +1 through the upper face, -1 through the lower, including the wrap
+ * Domain::fix_position would apply to the current position (src/domain.cpp:443-493).
+ * Needs params.msd_process.
+ * Replaces: reading Atom_struct::msd_domain_cross (inc/caviar2/atom_data/utility/atom_struct.hpp:86). */
+int cavgpu_download_images(cavgpu_ctx *ctx, int32_t *img3);
 
 /* Canonical pair set of the current list: rows (id_i, id_j, sx, sy, sz), the
  * image of j being pos_j + s*L; both orders of every pair.  Returns the row

@@ -47,6 +47,7 @@ struct orc_sys {
   int32_t n;
   double *pos, *vel, *acc, *acc_old, *pos_old_nl;
   int32_t *type;
+  int32_t *img;                /* Atom_struct::msd_domain_cross, x3 */
   unsigned char *in_domain;    /* Atom_struct::mpi_rank == my rank (src/atom_data.cpp:817-839) */
   /* Domain (src/domain.cpp:309-328, 495-502): single rank, nprocs = 1 */
   double size[3];              /* size_global = upper_global - lower_global */
@@ -117,22 +118,23 @@ void orc_langevin_eta(uint64_t seed, uint64_t step, uint32_t id, double eta[3]) 
 /* ------------------------------------------------------------------------ */
 /* Domain::fix_position  (src/domain.cpp:443-493)                            */
 /* ------------------------------------------------------------------------ */
-static int fix_position(const orc_sys *s, double *p) {
+static int fix_position(const orc_sys *s, double *p, int32_t *msd) {
   int wrapped = 0;
   for (int d = 0; d < 3; ++d) {
     if (s->p.bc[d] != 1) continue;
-    if (p[d] < s->p.lo[d]) { wrapped = 1; p[d] += s->size[d]; }
-    else if (p[d] > s->p.hi[d]) { wrapped = 1; p[d] -= s->size[d]; }
+    if (p[d] < s->p.lo[d]) { wrapped = 1; p[d] += s->size[d]; msd[d] -= 1; }
+    else if (p[d] > s->p.hi[d]) { wrapped = 1; p[d] -= s->size[d]; msd[d] += 1; }
   }
   return wrapped;
 }
 
 /* Atom_data::exchange_owned_single_md_domain
- * (src/atom_data/exchange_owned_single_md_domain.cpp:29-56) */
+ * (src/atom_data/exchange_owned_single_md_domain.cpp:29-56); the crossings add
+ * up in msd_domain_cross (kept whether or not msd_process is on) */
 static int exchange_owned(orc_sys *s) {
   int upd = 0;
   for (int32_t i = 0; i < s->n; ++i)
-    if (fix_position(s, &s->pos[3 * i])) upd = 1;
+    if (fix_position(s, &s->pos[3 * i], &s->img[3 * i])) upd = 1;
   return upd;
 }
 
@@ -651,7 +653,8 @@ orc_sys *orc_new(const orc_params *p, int32_t n, const double *pos3, const doubl
   s->pos_old_nl = (double *)calloc(1, b3);
   s->type = (int32_t *)malloc(((size_t)n + 1) * sizeof(int32_t));
   s->in_domain = (unsigned char *)calloc((size_t)n + 1, 1);
-  if (!s->in_domain || !s->pos || !s->vel || !s->acc || !s->acc_old || !s->pos_old_nl || !s->type) { orc_free(s); return NULL; }
+  s->img = (int32_t *)calloc(((size_t)n + 1) * 3, sizeof(int32_t));
+  if (!s->img || !s->in_domain || !s->pos || !s->vel || !s->acc || !s->acc_old || !s->pos_old_nl || !s->type) { orc_free(s); return NULL; }
   memcpy(s->pos, pos3, (size_t)n * 3 * sizeof(double));
   memcpy(s->vel, vel3, (size_t)n * 3 * sizeof(double));
   memcpy(s->type, type, (size_t)n * sizeof(int32_t));
@@ -668,6 +671,7 @@ orc_sys *orc_new(const orc_params *p, int32_t n, const double *pos3, const doubl
 void orc_free(orc_sys *s) {
   if (!s) return;
   free(s->pos); free(s->vel); free(s->acc); free(s->acc_old); free(s->pos_old_nl); free(s->type); free(s->in_domain);
+  free(s->img);
   free(s->gpos.a); free(s->gsrc.a); free(s->gshift.a); free(s->gpos_old_nl.a);
   free(s->bin_start); free(s->bin_count); free(s->bin_items); free(s->nbin_n); free(s->nbin);
   free(s->nl_start); free(s->nl_count); free(s->nl.a);
@@ -719,6 +723,10 @@ int32_t orc_step(orc_sys *s, int32_t nsteps) {
   return ORC_OK;
 }
 
+void orc_get_images(const orc_sys *s, int32_t *img3) {
+  memcpy(img3, s->img, (size_t)s->n * 3 * sizeof(int32_t));
+}
+
 void orc_get_state(const orc_sys *s, double *pos3, double *vel3, double *acc3) {
   size_t b = (size_t)s->n * 3 * sizeof(double);
   if (pos3) memcpy(pos3, s->pos, b);
@@ -726,8 +734,10 @@ void orc_get_state(const orc_sys *s, double *pos3, double *vel3, double *acc3) {
   if (acc3) memcpy(acc3, s->acc, b);
 }
 
+/* o[0] is Atom_data::kinetic_energy() of the current velocities: for Langevin the
+ * temperature was taken mid-step, the kinetic energy is read after it */
 void orc_get_thermo(const orc_sys *s, double *o) {
-  o[0] = s->ke; o[1] = s->temperature; o[2] = s->pressure; o[3] = s->virial; o[4] = s->pe;
+  o[0] = kinetic_energy(s); o[1] = s->temperature; o[2] = s->pressure; o[3] = s->virial; o[4] = s->pe;
   o[5] = (double)s->rebuilds;
 }
 

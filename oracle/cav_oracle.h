@@ -90,6 +90,8 @@ int32_t orc_step(orc_sys *s, int32_t nsteps);
 void orc_get_state(const orc_sys *s, double *pos3, double *vel3, double *acc3);
 /* out[0..5] = KE, T, P, virialForce, PE, rebuild count */
 void orc_get_thermo(const orc_sys *s, double *out6);
+/* Atom_struct::msd_domain_cross per atom, x3 (crossings since orc_new) */
+void orc_get_images(const orc_sys *s, int32_t *img3);
 int64_t orc_current_step(const orc_sys *s);
 
 /* Neighbour list, ghosts and cells of the last build. */

@@ -55,6 +55,7 @@ def lib():
         L.orc_step.restype = C.c_int32
         L.orc_get_state.argtypes = [P, D, D, D]
         L.orc_get_thermo.argtypes = [P, D]
+        L.orc_get_images.argtypes = [P, I32]
         L.orc_pair_count.argtypes = [P]
         L.orc_pair_count.restype = I64
         L.orc_get_pairs.argtypes = [P, I32, I64]
@@ -150,6 +151,12 @@ class System:
         p, v, a = (np.empty((self.n, 3)) for _ in range(3))
         lib().orc_get_state(self._h, _dp(p), _dp(v), _dp(a))
         return p, v, a
+
+    def images(self):
+        """Atom_struct::msd_domain_cross per atom (crossings since construction)."""
+        m = np.empty((self.n, 3), np.int32)
+        lib().orc_get_images(self._h, _ip(m))
+        return m
 
     def thermo(self):
         o = np.empty(6)

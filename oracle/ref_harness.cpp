@@ -21,6 +21,11 @@
 //     bit 3: double lambda_s[nt*nt], lambda_e[nt*nt] -> Lj::set_lambda_s / set_lambda_e
 //     bit 4: int64 step, int32 mode, int32 pad, double value, kb -> constraint::Nve
 //            (mode 0 energy_per_dof, 1 energy_tot, 2 kbt, 3 kb + temperature)
+//     bit 5: int64 steps of xyz, energy, temperature, pressure, msd, volume output
+//            (0 = off); int32 xyz flags (1 id, 2 velocity, 4 acceleration),
+//            msd_type, msd_initial_step, pad -> writer::Atom_writer writing
+//            <out.bin>_{xyz.xyz, energy.txt, temperature.txt, pressure.txt,
+//            msd.txt, volume.txt}; msd output turns Atom_data::msd_process on
 //   Bits 1-3 take effect in Lj::verify_settings (src/force/lj.cpp:186-381), which
 //   the library itself never calls; the harness calls it, as a user of these
 //   options must, and appends the effective tables to the output.
@@ -54,6 +59,7 @@
 #include "caviar2/caviar2.hpp"
 #include "caviar2/constraint/nve.hpp"
 #include "caviar2/force/lj.hpp"
+#include "caviar2/writer/atom_writer.hpp"
 #undef private
 
 #include <cstdio>
@@ -130,6 +136,9 @@ int main(int argc, char **argv) {
   int32_t nve_mode[2] = {0, 0};
   double nve_vk[2] = {0.0, 0.0};
   if ((ext & 16) && (!rd(fi, &nve_step, 1) || !rd(fi, nve_mode, 2) || !rd(fi, nve_vk, 2))) return 8;
+  int64_t wsteps[6] = {0, 0, 0, 0, 0, 0};
+  int32_t wopt[4] = {0, -1, 0, 0};
+  if ((ext & 32) && (!rd(fi, wsteps, 6) || !rd(fi, wopt, 4))) return 8;
   fclose(fi);
 
   void *mem = calloc(1, sizeof(Caviar2));
@@ -154,6 +163,7 @@ int main(int argc, char **argv) {
   c.atom_data.set_temperature_process(true);
   c.atom_data.set_pressure_process(pproc != 0);
   for (int t = 0; t < nt; ++t) c.atom_data.add_type_mass(t, mass[t]);
+  if (wsteps[4] > 0) c.atom_data.set_msd_process(true);  // before the atoms: add_atom extends msd_domain_cross
   for (int i = 0; i < N; ++i)
     c.atom_data.add_atom((size_t)i, (size_t)type[i], Vector3d<double>{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]},
                          Vector3d<double>{vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]});
@@ -204,6 +214,30 @@ int main(int argc, char **argv) {
     else if (nve_mode[0] == 2) nve.kbt = nve_vk[0];
     else { nve.temperature = nve_vk[0]; nve.kb = nve_vk[1]; }
     c.add_constraint(&nve);
+  }
+  // ---- writer ----
+  writer::Atom_writer aw(&c);
+  if (ext & 32) {
+    const std::string base = std::string(argv[2]) + "_";
+    aw.domain = &c.domain;  // Atom_writer::set_caviar leaves it null; MSD and volume output read it
+    aw.set_xyz_step((int)wsteps[0]);
+    aw.set_energy_step((int)wsteps[1]);
+    aw.set_temperature_step((int)wsteps[2]);
+    aw.set_pressure_step((int)wsteps[3]);
+    aw.set_msd_step((int)wsteps[4]);
+    aw.set_volume_step((int)wsteps[5]);
+    aw.set_xyz_output_id(wopt[0] & 1);
+    aw.set_xyz_output_velocity((wopt[0] >> 1) & 1);
+    aw.set_xyz_output_acceleration((wopt[0] >> 2) & 1);
+    aw.set_msd_type(wopt[1]);
+    aw.set_msd_initial_step(wopt[2]);
+    aw.set_file_name_xyz(base + "xyz");
+    aw.set_file_name_energy(base + "energy");
+    aw.set_file_name_temperature(base + "temperature");
+    aw.set_file_name_pressure(base + "pressure");
+    aw.set_file_name_msd(base + "msd");
+    aw.set_file_name_volume(base + "volume");
+    c.add_writer(&aw);
   }
 
   // ---- Md_simulator ----

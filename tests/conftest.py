@@ -37,7 +37,14 @@ def golden_params(g):
     else:
         eps, sigma = g["eps"], g["sigma"]
         cutoff_list = g["cutoff_list"] if int(g["cutoff_list_on"]) else None
+    writer = None
+    if "writer" in g:  # writer::Atom_writer settings (tests/golden/make_golden.py writer_config)
+        w = [int(v) for v in g["writer"]]
+        writer = dict(xyz=w[0], energy=w[1], temperature=w[2], pressure=w[3], msd=w[4], volume=w[5],
+                      xyz_id=w[6] & 1, xyz_velocity=(w[6] >> 1) & 1, xyz_acceleration=(w[6] >> 2) & 1,
+                      msd_type=w[7], msd_initial_step=w[8])
     return dict(
+        writer=writer, msd_process=bool(writer and writer["msd"] > 0),
         lo=g["lo"], hi=g["hi"], ntypes=nt, nl_cutoff=float(g["nl_cutoff"]), nl_coef=float(g["nl_coef"]),
         ghost_cutoff=float(g["ghost_cutoff"]), lj_cutoff=float(g["lj_cutoff"]), eps=eps, sigma=sigma,
         cutoff_list=cutoff_list, jump_tol=float(g["jump_tol"]) if "jump_tol" in g else 0.0,

@@ -2,8 +2,13 @@
 // (caviar-v2_gb300/host/caviar2_gpu.hpp) with the same set-up code a CAVIAR2
 // user writes, reading and writing the file formats of oracle/ref_harness.cpp so
 // that tests/test_host_api.py compares it with the fixtures the reference made.
+#include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <limits>
+#include <random>
+#include <sstream>
+#include <string>
 #include <vector>
 
 #include "caviar2_gpu.hpp"
@@ -13,9 +18,37 @@ using namespace caviar2;
 template <class T> static bool rd(FILE *f, T *p, size_t n) { return fread(p, sizeof(T), n, f) == n; }
 template <class T> static void wr(FILE *f, const T *p, size_t n) { fwrite(p, sizeof(T), n, f); }
 
+// The writers' number text (append_general6) against std::ostream's default
+// formatting, on values of every magnitude, sign, rounding tie region and kind.
+static int format_check() {
+  std::vector<double> v = {0.0, -0.0, 1.0, -1.0, 0.1, 1e-4, 9.99999e-5, 1e-5, 123456.0, 1234567.0, 999999.5,
+                           9999995.0, 0.0001234565, 2.5, 1e300, -1e-300, 4.9e-324, 1e16, 5e-7,
+                           std::numeric_limits<double>::infinity(), -std::numeric_limits<double>::infinity(),
+                           std::numeric_limits<double>::max(), std::numeric_limits<double>::min()};
+  std::mt19937_64 rng(12345);
+  std::uniform_real_distribution<double> u(-1.0, 1.0), e(-320.0, 308.0);
+  for (int k = 0; k < 200000; ++k) v.push_back(u(rng) * std::pow(10.0, e(rng)));
+  for (int k = 0; k < 200000; ++k) v.push_back(u(rng) * 1000.0);
+  for (int k = 0; k < 20000; ++k) v.push_back(std::round(u(rng) * 2e7) / 8.0);  // exact binary ties
+  long bad = 0;
+  for (double x : v) {
+    std::ostringstream os;
+    os << x;
+    std::string mine;
+    append_general6(mine, x);
+    if (mine != os.str()) {
+      if (bad < 5) fprintf(stderr, "format mismatch: %s vs %s\n", mine.c_str(), os.str().c_str());
+      ++bad;
+    }
+  }
+  printf("%zu values, %ld mismatches\n", v.size(), bad);
+  return bad ? 1 : 0;
+}
+
 int main(int argc, char **argv) {
+  if (argc == 2 && !std::strcmp(argv[1], "--format")) return format_check();
   if (argc < 3) {
-    fprintf(stderr, "usage: %s in.bin out.bin [mixed]\n", argv[0]);
+    fprintf(stderr, "usage: %s in.bin out.bin [mixed|tables|run] | --format\n", argv[0]);
     return 2;
   }
   FILE *fi = fopen(argv[1], "rb");
@@ -41,6 +74,9 @@ int main(int argc, char **argv) {
   int32_t nve_mode[2] = {0, 0};
   double nve_vk[2] = {0.0, 0.0};
   if ((ext & 16) && (!rd(fi, &nve_step, 1) || !rd(fi, nve_mode, 2) || !rd(fi, nve_vk, 2))) return 5;
+  int64_t wsteps[6] = {0, 0, 0, 0, 0, 0};
+  int32_t wopt[4] = {0, -1, 0, 0};
+  if ((ext & 32) && (!rd(fi, wsteps, 6) || !rd(fi, wopt, 4))) return 5;
   fclose(fi);
 
   Caviar2 caviar;
@@ -50,6 +86,7 @@ int main(int argc, char **argv) {
   caviar.domain.generate();
 
   caviar.atom_data.set_ghost_cutoff(dp[8]);
+  if (wsteps[4] > 0) caviar.atom_data.set_msd_process(true);
   for (int i = 0; i < N; ++i) {
     tools::Atom a(&caviar);
     a.set_type((size_t)type[i]);
@@ -128,6 +165,30 @@ int main(int argc, char **argv) {
     caviar.add_constraint(&nve);
   }
 
+  // writer::Atom_writer with the reference harness's settings and file names
+  writer::Atom_writer aw(&caviar);
+  if (ext & 32) {
+    const std::string base = std::string(argv[2]) + "_";
+    aw.set_xyz_step((int)wsteps[0]);
+    aw.set_energy_step((int)wsteps[1]);
+    aw.set_temperature_step((int)wsteps[2]);
+    aw.set_pressure_step((int)wsteps[3]);
+    aw.set_msd_step((int)wsteps[4]);
+    aw.set_volume_step((int)wsteps[5]);
+    aw.set_xyz_output_id(wopt[0] & 1);
+    aw.set_xyz_output_velocity((wopt[0] >> 1) & 1);
+    aw.set_xyz_output_acceleration((wopt[0] >> 2) & 1);
+    aw.set_msd_type(wopt[1]);
+    aw.set_msd_initial_step(wopt[2]);
+    aw.set_file_name_xyz(base + "xyz");
+    aw.set_file_name_energy(base + "energy");
+    aw.set_file_name_temperature(base + "temperature");
+    aw.set_file_name_pressure(base + "pressure");
+    aw.set_file_name_msd(base + "msd");
+    aw.set_file_name_volume(base + "volume");
+    caviar.add_writer(&aw);
+  }
+
   Md_simulator &md = caviar.md_simulator;
   if (integ == 1) {
     md.set_integrator_type(Integrator_t::Velocity_verlet_langevin);
@@ -195,12 +256,21 @@ int main(int argc, char **argv) {
   wr(fo, &np, 1);
   wr(fo, rows.data(), rows.size());
   wr(fo, &nsteps, 1);
-  for (int s = 0; s < nsteps; ++s) {
-    md.step((int64_t)s);
+  if (argc > 3 && !std::strcmp(argv[3], "run")) {
+    // Md_simulator::run: the device advances between the steps the writers read;
+    // only the last step's thermo exists (written for every record)
+    md.run();
     double t[3] = {caviar.atom_data.temperature(), caviar.atom_data.virialForce, caviar.atom_data.pressure()};
-    wr(fo, t, 3);
+    for (int s = 0; s < nsteps; ++s) wr(fo, t, 3);
+  } else {
+    for (int s = 0; s < nsteps; ++s) {
+      md.step((int64_t)s);
+      double t[3] = {caviar.atom_data.temperature(), caviar.atom_data.virialForce, caviar.atom_data.pressure()};
+      wr(fo, t, 3);
+    }
   }
   md.sync_host();
+  aw.finish();
   wr(fo, &o.position[0].x, 3 * (size_t)N);
   wr(fo, &o.velocity[0].x, 3 * (size_t)N);
   wr(fo, &o.acceleration[0].x, 3 * (size_t)N);

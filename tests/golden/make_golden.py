@@ -30,7 +30,20 @@ FULL_PAIRS_MAX_N = 600
 def ext_flags(p):
     """Extension bits of the harness input: jump_tol, WCA, per-atom mixing, lambda tables."""
     return ((1 if p.get("jump_tol") else 0) | (2 if p.get("wca") else 0) | (4 if p.get("eps_atom") is not None else 0)
-            | (8 if p.get("lambda_s") is not None else 0) | (16 if p.get("nve") else 0))
+            | (8 if p.get("lambda_s") is not None else 0) | (16 if p.get("nve") else 0)
+            | (32 if p.get("writer") else 0))
+
+
+WRITER_KINDS = ("xyz", "energy", "temperature", "pressure", "msd", "volume")
+WRITER_FILES = {"xyz": "_xyz.xyz", "energy": "_energy.txt", "temperature": "_temperature.txt",
+                "pressure": "_pressure.txt", "msd": "_msd.txt", "volume": "_volume.txt"}
+
+
+def writer_config(w):
+    """int64 [steps of xyz, energy, temperature, pressure, msd, volume; xyz flags; msd_type; msd_initial_step]"""
+    flags = (1 if w.get("xyz_id") else 0) | (2 if w.get("xyz_velocity") else 0) | (4 if w.get("xyz_acceleration") else 0)
+    return np.array([int(w.get(k, 0)) for k in WRITER_KINDS]
+                    + [flags, int(w.get("msd_type", -1)), int(w.get("msd_initial_step", 0))], np.int64)
 
 
 def write_input(path, pos, vel, typ, p, nsteps):
@@ -65,6 +78,10 @@ def write_input(path, pos, vel, typ, p, nsteps):
             f.write(np.array([nve["step"]], np.int64).tobytes())
             f.write(np.array([nve["mode"], 0], np.int32).tobytes())
             f.write(np.array([nve["value"], nve.get("kb", 0.0)], np.float64).tobytes())
+        if ext & 32:
+            w = writer_config(p["writer"])
+            f.write(w[:6].tobytes())
+            f.write(np.array([w[6], w[7], w[8], 0], np.int32).tobytes())
 
 
 class Reader:
@@ -94,6 +111,11 @@ def run_case(name, pos, vel, typ, p, nsteps):
         write_input(fin, pos, vel, typ, p, nsteps)
         subprocess.run([HARNESS, fin, fout], check=True, stdout=subprocess.DEVNULL)
         r = Reader(open(fout, "rb").read())
+        texts = {}
+        if p.get("writer"):  # writer::Atom_writer's files, kept byte for byte
+            for kind, suffix in WRITER_FILES.items():
+                if os.path.exists(fout + suffix):
+                    texts["w_" + kind] = np.frombuffer(open(fout + suffix, "rb").read(), np.uint8)
     n, g = r.take(np.int32, 2)
     acc0 = r.take(np.float64, 3 * n).reshape(n, 3)
     virial0, ke0, t0 = r.take(np.float64, 3)
@@ -131,6 +153,9 @@ def run_case(name, pos, vel, typ, p, nsteps):
     if ext & 16:
         nve = p["nve"]
         extra["nve"] = np.array([nve["step"], nve["mode"], nve["value"], nve.get("kb", 0.0)], np.float64)
+    if ext & 32:
+        extra["writer"] = writer_config(p["writer"])
+        extra.update(texts)
     out = dict(
         # inputs
         pos=pos, vel=vel, typ=typ.astype(np.int32), nsteps=np.int32(nsteps),
@@ -229,6 +254,20 @@ def cases():
     yield "fcc500_nve_kbt", pos, vel, typ, dict(p, nve={"step": 7, "mode": 2, "value": 1.1}), 50
     pos, vel, typ, p = W.lj_fluid((4, 4, 4), seed=82, integrator=2)
     yield "fcc256_leapfrog_nve_edof", pos, vel, typ, dict(p, nve={"step": 1, "mode": 0, "value": 1.3}), 40
+    # writer::Atom_writer: xyz frames with ids, velocities and accelerations; kinetic energy,
+    # temperature, pressure, volume; mean square displacement from step 20 with boundary crossings
+    # (lattice planes moved next to the lower x and upper y faces, so that atoms cross them)
+    pos, vel, typ, p = W.lj_fluid((4, 4, 4), seed=91)
+    pos = np.mod(pos + np.array([-0.41, 0.41, 0.0]), p["hi"])
+    wr = {"xyz": 40, "xyz_id": 1, "xyz_velocity": 1, "xyz_acceleration": 1, "energy": 10, "temperature": 10,
+          "pressure": 10, "msd": 5, "msd_initial_step": 20, "volume": 30}
+    yield "fcc256_writers", pos, vel, typ, dict(p, writer=wr), 100
+    # Langevin (friction 0) writer output: the kinetic energy is read after the step, the
+    # temperature mid-step; MSD of type 1 only, from step 0
+    pos, vel, typ, p = W.kob_andersen(n=500, seed=92, temperature=1.5)
+    pos = np.mod(pos + np.array([0.0, 0.0, -0.365]), p["hi"])
+    wr = {"xyz": 50, "energy": 5, "temperature": 5, "msd": 10, "msd_type": 1}
+    yield "ka500_langevin_writers", pos, vel, typ, dict(p, lang_friction=0.0, writer=wr), 60
 
 
 def main():

@@ -1,0 +1,121 @@
+"""writer::Atom_writer on the GPU path against the files the reference wrote.
+
+tests/cpp/host_harness.cpp sets the golden writer cases up through the
+CAVIAR2-shaped C++ API (caviar-v2_gb300/host/), steps them on the GPU (FP64) and
+lets writer::Atom_writer write its files; they must have the reference's lines and
+tokens, integers (steps, types, ids, boundary-crossing totals) identical, and
+doubles equal as text or within one unit of the sixth significant digit (the
+trajectories agree to ~1e-12, so only values next to a rounding boundary of the
+six-digit text can print differently).  The same through Md_simulator::run, which
+advances the device in CUDA graphs between the steps the writers read.
+"""
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden_cases, golden_params, load_golden
+
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+import make_golden as MG  # noqa: E402
+import writer_text as WT  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+WRITER_CASES = [c for c in golden_cases() if "writer" in load_golden(c)]
+
+
+def harness():
+    sys.path.insert(0, os.path.join(ROOT, "caviar-v2_gb300"))
+    import build as B
+
+    if not os.path.exists(B.HOST_HARNESS):
+        B.build()
+    return B.HOST_HARNESS
+
+
+def run_writers(g, tmp_path, mode=None):
+    fin, fout = tmp_path / "in.bin", tmp_path / "out.bin"
+    MG.write_input(str(fin), g["pos"], g["vel"], g["typ"], golden_params(g), int(g["nsteps"]))
+    subprocess.run([harness(), str(fin), str(fout)] + ([mode] if mode else []), check=True,
+                   stdout=subprocess.DEVNULL)
+    out = {}
+    for kind, suffix in MG.WRITER_FILES.items():
+        f = str(fout) + suffix
+        if os.path.exists(f):
+            out[kind] = open(f).read()
+    return out
+
+
+def check_files(case, mine, g):
+    ref = {k[2:]: g[k].tobytes().decode() for k in g if k.startswith("w_")}
+    assert set(mine) == set(ref), case
+    for k in ref:
+        # xyz: accelerations of ~1e-15 (cancelled forces) differ in absolute terms only
+        WT.compare_text(mine[k], ref[k], atol=1e-9 if k == "xyz" else 0.0, what=f"{case}:{k}")
+
+
+@pytest.mark.parametrize("case", WRITER_CASES)
+def test_writer_files_step_by_step(case, tmp_path):
+    g = load_golden(case)
+    check_files(case, run_writers(g, tmp_path), g)
+
+
+@pytest.mark.parametrize("case", WRITER_CASES)
+def test_writer_files_through_run(case, tmp_path):
+    g = load_golden(case)
+    check_files(case, run_writers(g, tmp_path, "run"), g)
+
+
+@pytest.mark.parametrize("case", WRITER_CASES)
+def test_boundary_crossings_match_oracle(case, oracle_lib):
+    import cavgpu
+
+    g = load_golden(case)
+    p = dict(golden_params(g), msd_process=True)
+    s = cavgpu.System(g["pos"], g["vel"], g["typ"], p, noise_off=True)
+    o = oracle_lib.System(g["pos"], g["vel"], g["typ"], p, noise_mode=0)
+    s.setup()
+    o.setup()
+    total = 0
+    for k in range(4):
+        s.step(25)
+        o.step(25)
+        np.testing.assert_array_equal(s.images(), o.images(), err_msg=f"{case} after {25 * (k + 1)} steps")
+        total = int(np.abs(o.images()).sum())
+    assert total > 0 or case.startswith("ka500"), "the case should cross the boundaries"
+
+
+def test_images_need_msd_process():
+    import cavgpu
+
+    g = load_golden(WRITER_CASES[0])
+    s = cavgpu.System(g["pos"], g["vel"], g["typ"], dict(golden_params(g), msd_process=False))
+    s.setup()
+    with pytest.raises(cavgpu.CavError):
+        s.images()
+
+
+def test_langevin_kinetic_energy_after_the_step(oracle_lib):
+    """Langevin: KE of the velocities at the end of the step, T from the mid-step velocities."""
+    import cavgpu
+
+    g = load_golden("ka500_langevin_writers")
+    p = golden_params(g)
+    s = cavgpu.System(g["pos"], g["vel"], g["typ"], p, noise_off=True)
+    o = oracle_lib.System(g["pos"], g["vel"], g["typ"], p, noise_mode=0)
+    s.setup()
+    o.setup()
+    for n in (1, 7, 30):
+        s.step(n)
+        o.step(n)
+        a, b = s.thermo(), o.thermo()
+        assert abs(a["ke"] - b["ke"]) <= 1e-10 * abs(b["ke"])
+        assert abs(a["temperature"] - b["temperature"]) <= 1e-10 * abs(b["temperature"])
+        _, vel, _ = s.state()
+        m = np.asarray(p["mass"])[np.asarray(g["typ"])]
+        ke_end = 0.5 * float((m[:, None] * vel * vel).sum())
+        assert abs(a["ke"] - ke_end) <= 1e-10 * ke_end
