@@ -303,7 +303,34 @@ def extra_workloads(cavgpu, torch, W, np, single_mixed):
                       "T_end": s.thermo()["temperature"]}
         s.close()
     res["langevin_4M"] = lang
+    res["writers_1M"] = writer_runs()
     return res
+
+
+def writer_runs(steps=2000):
+    """Md_simulator::run through the C++ API (host/lj_md.cpp) on the 1,048,576-atom fluid
+    (mixed), without writers and with writer::Atom_writer output: kinetic energy,
+    temperature and pressure every 100 steps, MSD every 100, xyz frames every 1000."""
+    import json
+    import subprocess
+    import tempfile
+
+    import build as B
+
+    out = {"workload": "LJ fluid 1,048,576 atoms (64^3 FCC cells), mixed, velocity Verlet, "
+                       f"{steps} steps through Md_simulator::run; wall time of run()"}
+    with tempfile.TemporaryDirectory() as td:
+        for name, extra in (("no_writers", []), ("writers", ["--thermo", "100", "--msd", "100", "--xyz", "1000"])):
+            cmd = [B.LJ_MD, "--cells", "64", "--steps", str(steps), "--mixed", "--out", os.path.join(td, "o")] + extra
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                out[name] = {"error": (r.stderr or r.stdout).strip()[-300:]}
+                continue
+            out[name] = json.loads([ln for ln in r.stdout.splitlines() if ln.startswith("{")][-1])
+        if "run_s" in out.get("writers", {}) and "run_s" in out.get("no_writers", {}):
+            out["writers_over_no_writers"] = out["writers"]["atom_steps_per_s"] / out["no_writers"]["atom_steps_per_s"]
+            out["xyz_bytes_per_frame"] = os.path.getsize(os.path.join(td, "o_xyz.xyz")) // 3
+    return out
 
 
 def nve_drift(cavgpu, pos, vel, typ, params, precision, steps, every=100):

@@ -52,10 +52,12 @@ def build(verbose=False):
 
 HOST_LIB = os.path.join(HERE, "libcaviar2_gpu.so")
 HOST_HARNESS = os.path.join(OBJ, "host_harness")
+LJ_MD = os.path.join(OBJ, "lj_md")
 
 
 def build_host():
-    """The CAVIAR2-shaped C++ API (host/) over libcavgpu.so, and its test harness."""
+    """The CAVIAR2-shaped C++ API (host/) over libcavgpu.so, its test harness and the
+    lj_md driver."""
     inc = ["-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(HERE, "host")]
     cxx = os.environ.get("CXX", "g++")
     steps = [
@@ -64,6 +66,8 @@ def build_host():
         [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-pthread", *inc,
          os.path.join(ROOT, "tests", "cpp", "host_harness.cpp"), "-o", HOST_HARNESS, "-L" + HERE, "-lcaviar2_gpu",
          "-lcavgpu", "-Wl,-rpath," + HERE],
+        [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-pthread", *inc, os.path.join(HERE, "host", "lj_md.cpp"),
+         "-o", LJ_MD, "-L" + HERE, "-lcaviar2_gpu", "-lcavgpu", "-Wl,-rpath," + HERE],
     ]
     for cmd in steps:
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -399,6 +399,11 @@ void Md_simulator::setup() {
   for (Writer *w : caviar_->writers) w->write(0, 0.0);  // src/md_simulator.cpp:609-610
 }
 
+void Md_simulator::autotune(int trial_steps) {
+  if (!ctx_) caviar_->log.error_all("autotune: call initialize() and setup() first");
+  check(cavgpu_autotune(ctx_, trial_steps, 0, nullptr), "cavgpu_autotune");
+}
+
 void Md_simulator::read_thermo(bool with_pressure) {
   Atom_data &ad = caviar_->atom_data;
   double th[6];
@@ -442,10 +447,14 @@ void Md_simulator::write_outputs(int64_t i) {
   const int want = writers_want(i);
   if (!want) return;
   Atom_data &ad = caviar_->atom_data;
-  if (want & Writer::WANT_STATE) {
+  const int state = want & (Writer::WANT_POSITIONS | Writer::WANT_VELOCITIES | Writer::WANT_ACCELERATIONS);
+  if (state) {  // only the arrays some writer reads
     auto &o = ad.atom_struct_owned;
-    check(cavgpu_download(ctx_, &o.position[0].x, &o.velocity[0].x, &o.acceleration[0].x), "cavgpu_download");
-    host_dirty_ = false;
+    check(cavgpu_download(ctx_, (state & Writer::WANT_POSITIONS) ? &o.position[0].x : nullptr,
+                          (state & Writer::WANT_VELOCITIES) ? &o.velocity[0].x : nullptr,
+                          (state & Writer::WANT_ACCELERATIONS) ? &o.acceleration[0].x : nullptr),
+          "cavgpu_download");
+    if (state == (Writer::WANT_POSITIONS | Writer::WANT_VELOCITIES | Writer::WANT_ACCELERATIONS)) host_dirty_ = false;
   }
   if ((want & Writer::WANT_CROSSINGS) && ad.msd_process) download_images();
   for (Writer *w : caviar_->writers)
@@ -712,11 +721,13 @@ void Atom_writer::initialize() {
 
 int Atom_writer::wants(int64_t i) const {
   int w = 0;
-  if (output_xyz && i % xyz_step == 0) w |= WANT_CALL | WANT_STATE;
+  if (output_xyz && i % xyz_step == 0)
+    w |= WANT_CALL | WANT_POSITIONS | (xyz_output_velocity ? WANT_VELOCITIES : 0) |
+         (xyz_output_acceleration ? WANT_ACCELERATIONS : 0);
   if (output_energy && i % energy_step == 0) w |= WANT_CALL | WANT_THERMO;
   if (output_temperature && i % temperature_step == 0) w |= WANT_CALL | WANT_THERMO;
   if (output_pressure && i % pressure_step == 0) w |= WANT_CALL | WANT_THERMO;
-  if (output_msd && i % msd_step == 0 && i >= msd_initial_step) w |= WANT_CALL | WANT_STATE | WANT_CROSSINGS;
+  if (output_msd && i % msd_step == 0 && i >= msd_initial_step) w |= WANT_CALL | WANT_POSITIONS | WANT_CROSSINGS;
   if (output_volume && i % volume_step == 0) w |= WANT_CALL;
   return w;
 }

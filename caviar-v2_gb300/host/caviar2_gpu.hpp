@@ -213,6 +213,9 @@ class Md_simulator {
   // GPU options (no counterpart in the reference)
   void set_precision(int p) { precision = p; }  // CAVGPU_FP64 (default) or CAVGPU_MIXED
   void set_langevin_seed(uint64_t s) { seed = s; }
+  // after setup: time the pair-kernel launch shapes on this system and keep the
+  // fastest (cavgpu_autotune; the state is restored afterwards)
+  void autotune(int trial_steps = 10);
 
   bool run();                 // src/md_simulator.cpp:317-356
   void step();                // src/md_simulator.cpp:445-546
@@ -255,7 +258,10 @@ class Md_simulator {
 // host round trip up to the next step some writer reads.
 class Writer {
  public:
-  enum : int { WANT_CALL = 1, WANT_THERMO = 2, WANT_STATE = 4, WANT_CROSSINGS = 8, WANT_ALL = 15 };
+  enum : int {
+    WANT_CALL = 1, WANT_THERMO = 2, WANT_POSITIONS = 4, WANT_VELOCITIES = 8, WANT_ACCELERATIONS = 16,
+    WANT_CROSSINGS = 32, WANT_ALL = 63
+  };
   explicit Writer(Caviar2 *c = nullptr) : caviar_(c) {}
   virtual ~Writer() = default;
   virtual void initialize() {}

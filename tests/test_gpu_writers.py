@@ -119,3 +119,26 @@ def test_langevin_kinetic_energy_after_the_step(oracle_lib):
         m = np.asarray(p["mass"])[np.asarray(g["typ"])]
         ke_end = 0.5 * float((m[:, None] * vel * vel).sum())
         assert abs(a["ke"] - ke_end) <= 1e-10 * ke_end
+
+
+def test_lj_md_driver_outputs(tmp_path):
+    """host/lj_md.cpp (the demo-style driver): Md_simulator::run with every writer kind."""
+    import json
+
+    harness()
+    import build as B
+
+    prefix = str(tmp_path / "o")
+    r = subprocess.run([B.LJ_MD, "--cells", "6", "--steps", "300", "--thermo", "20", "--msd", "25", "--xyz", "100",
+                        "--no-tune", "--out", prefix], capture_output=True, text=True, check=True)
+    rep = json.loads([ln for ln in r.stdout.splitlines() if ln.startswith("{")][-1])
+    assert rep["atoms"] == 864 and rep["steps"] == 300 and rep["atom_steps_per_s"] > 0
+    energy = open(prefix + "_energy.txt").read().splitlines()
+    # setup's step 0, then steps 0, 20, ..., 280
+    assert [int(ln.split()[0]) for ln in energy] == [0] + list(range(0, 300, 20))
+    assert [ln.split()[1] for ln in energy[1:3]] == ["0", "0.1"]
+    msd = open(prefix + "_msd.txt").read().splitlines()
+    assert [int(ln.split()[0]) for ln in msd] == [0, 0] + list(range(25, 300, 25))
+    xyz = open(prefix + "_xyz.xyz").read().splitlines()
+    assert len(xyz) == 4 * (864 + 2)  # frames at setup and steps 0, 100, 200
+    assert xyz[0] == "864" and xyz[1] == "Atom" and len(xyz[2].split()) == 4
