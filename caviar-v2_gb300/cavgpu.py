@@ -37,7 +37,8 @@ class Params(C.Structure):
         ("nbr_capacity", C.c_int32), ("threads_per_atom", C.c_int32), ("block_size", C.c_int32),
         ("steps_per_graph", C.c_int32), ("force_kernel", C.c_int32), ("jump_tol", C.c_double),
         ("initial_step", C.c_int64), ("nve_step", C.c_int64), ("nve_mode", C.c_int32), ("nve_pad", C.c_int32),
-        ("nve_value", C.c_double), ("nve_kb", C.c_double), ("msd_process", C.c_int32), ("msd_pad", C.c_int32),
+        ("nve_value", C.c_double), ("nve_kb", C.c_double), ("msd_process", C.c_int32),
+        ("ignore_intra_molecule", C.c_int32),
     ]
 
 
@@ -56,6 +57,7 @@ _SIGS = {
     "cavgpu_create": (C.c_int, [C.POINTER(Params), C.POINTER(C.c_void_p)]),
     "cavgpu_destroy": (None, [C.c_void_p]),
     "cavgpu_upload": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "cavgpu_set_molecules": (C.c_int, [C.c_void_p, C.c_void_p]),
     "cavgpu_setup": (C.c_int, [C.c_void_p]),
     "cavgpu_step": (C.c_int, [C.c_void_p, C.c_int64]),
     "cavgpu_run": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p]),
@@ -153,6 +155,7 @@ def make_params(p, precision=FP64, noise_off=False, tpa=0, block=0, nbr_capacity
         o.nve_step, o.nve_mode = int(nve["step"]), int(nve["mode"])
         o.nve_value, o.nve_kb = float(nve["value"]), float(nve.get("kb", 0.0))
     o.msd_process = int(bool(p.get("msd_process", False)))
+    o.ignore_intra_molecule = int(bool(p.get("ignore_intra_molecule", False)))
     return o
 
 
@@ -172,6 +175,9 @@ class System:
         typ = np.ascontiguousarray(typ, np.uint64)
         ids = None if ids is None else np.ascontiguousarray(ids, np.uint64)
         self._check(lib().cavgpu_upload(self._h, self.n, _ptr(pos), _ptr(vel), _ptr(typ), _ptr(ids)), "upload")
+        if params.get("molecule_index") is not None:
+            mol = np.ascontiguousarray(params["molecule_index"], np.int32)
+            self._check(lib().cavgpu_set_molecules(self._h, _ptr(mol)), "set_molecules")
 
     def _check(self, rc, what):
         if rc < 0:

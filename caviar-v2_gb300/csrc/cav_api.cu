@@ -589,6 +589,11 @@ int upload_common(cavgpu_ctx *c, const int64_t *counts, const double *pos3, cons
     if (!rc) rc = dalloc(c, &d.t_img, NS);
     if (!rc) rc = cuda_rc(cudaMemsetAsync(d.img, 0, NS * sizeof(int4), c->st));
   }
+  if (c->p.ignore_intra_molecule) {  // molecule index -1 for every atom (Atom_data::add_atom) until set
+    if (!rc) rc = dalloc(c, &d.mol, NS);
+    if (!rc) rc = dalloc(c, &d.t_mol, NS);
+    if (!rc) rc = cuda_rc(cudaMemsetAsync(d.mol, 0xff, NS * sizeof(int), c->st));
+  }
   if (c->nve.step > 0) {
     if (R > 1) return CAVGPU_E_ARG;  // constraint::Nve acts on one system's kinetic energy
     if (!rc) rc = dalloc(c, &d.nve_partials, 4 * (size_t)NVE_BLOCKS);
@@ -731,6 +736,19 @@ int cavgpu_upload_batch(cavgpu_ctx *c, const int64_t *counts, const double *pos3
   return upload_common(c, counts, pos3, vel3, type, nullptr);
 }
 
+int cavgpu_set_molecules(cavgpu_ctx *c, const int32_t *mol) {
+  if (!c || !mol) return CAVGPU_E_ARG;
+  if (!c->uploaded || c->set_up || !c->d.mol) return CAVGPU_E_STATE;
+  // slots are still in upload order: replica r's atoms from its slot offset, padding -1
+  std::vector<int> h(c->b.nslot, -1);
+  int64_t k = 0;
+  for (const RepBox &rb : c->reps)
+    for (int a = 0; a < rb.natoms; ++a) h[rb.slot_off + a] = mol[k++];
+  CK(cudaMemcpyAsync(c->d.mol, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return CAVGPU_OK;
+}
+
 int cavgpu_setup(cavgpu_ctx *c) {
   if (!c) return CAVGPU_E_ARG;
   return setup_common(c);
@@ -847,6 +865,15 @@ int cavgpu_autotune(cavgpu_ctx *c, int32_t trial_steps, int32_t flags, int64_t *
   const bool prof0 = c->prof;
   if (cudaMalloc(&snap, 4 * NS * sizeof(dbl4)) != cudaSuccess) { cudaGetLastError(); return CAVGPU_E_NOMEM; }
   if (cudaMalloc(&snap_i, 2 * NS * sizeof(int)) != cudaSuccess) { cudaFree(snap); cudaGetLastError(); return CAVGPU_E_NOMEM; }
+  // per-slot crossing counts and molecule indices move with the atoms as well
+  int4 *snap_img = nullptr;
+  int *snap_mol = nullptr;
+  if ((c->d.img && cudaMalloc(&snap_img, NS * sizeof(int4)) != cudaSuccess) ||
+      (c->d.mol && cudaMalloc(&snap_mol, NS * sizeof(int)) != cudaSuccess)) {
+    cudaGetLastError();
+    cudaFree(snap); cudaFree(snap_i); cudaFree(snap_img);
+    return CAVGPU_E_NOMEM;
+  }
   dbl4 *const src4[4] = {c->d.pos, c->d.vel, c->d.acc, c->d.acc_old};
   int rc = CAVGPU_OK;
   auto save = [&]() {
@@ -854,6 +881,10 @@ int cavgpu_autotune(cavgpu_ctx *c, int32_t trial_steps, int32_t flags, int64_t *
       rc = cuda_rc(cudaMemcpyAsync(snap + k * NS, src4[k], NS * sizeof(dbl4), cudaMemcpyDeviceToDevice, c->st));
     if (!rc) rc = cuda_rc(cudaMemcpyAsync(snap_i, c->d.type, NS * sizeof(int), cudaMemcpyDeviceToDevice, c->st));
     if (!rc) rc = cuda_rc(cudaMemcpyAsync(snap_i + NS, c->d.id, NS * sizeof(int), cudaMemcpyDeviceToDevice, c->st));
+    if (!rc && snap_img)
+      rc = cuda_rc(cudaMemcpyAsync(snap_img, c->d.img, NS * sizeof(int4), cudaMemcpyDeviceToDevice, c->st));
+    if (!rc && snap_mol)
+      rc = cuda_rc(cudaMemcpyAsync(snap_mol, c->d.mol, NS * sizeof(int), cudaMemcpyDeviceToDevice, c->st));
     if (!rc) rc = cuda_rc(cudaMemcpyAsync(&snap_step, c->d.step_base, sizeof(long long), cudaMemcpyDeviceToHost, c->st));
     if (!rc) rc = cuda_rc(cudaMemcpyAsync(snap_flags, c->d.flags, sizeof(snap_flags), cudaMemcpyDeviceToHost, c->st));
     if (!rc) rc = cuda_rc(cudaMemcpyAsync(snap_thermo, c->d.thermo, sizeof(snap_thermo), cudaMemcpyDeviceToHost, c->st));
@@ -874,6 +905,8 @@ int cavgpu_autotune(cavgpu_ctx *c, int32_t trial_steps, int32_t flags, int64_t *
       CK(cudaMemcpyAsync(src4[k], snap + k * NS, NS * sizeof(dbl4), cudaMemcpyDeviceToDevice, c->st));
     CK(cudaMemcpyAsync(c->d.type, snap_i, NS * sizeof(int), cudaMemcpyDeviceToDevice, c->st));
     CK(cudaMemcpyAsync(c->d.id, snap_i + NS, NS * sizeof(int), cudaMemcpyDeviceToDevice, c->st));
+    if (snap_img) CK(cudaMemcpyAsync(c->d.img, snap_img, NS * sizeof(int4), cudaMemcpyDeviceToDevice, c->st));
+    if (snap_mol) CK(cudaMemcpyAsync(c->d.mol, snap_mol, NS * sizeof(int), cudaMemcpyDeviceToDevice, c->st));
     CK(cudaMemcpyAsync(c->d.step_base, &snap_step, sizeof(long long), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(c->d.flags, snap_flags, sizeof(snap_flags), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(c->d.thermo, snap_thermo, sizeof(snap_thermo), cudaMemcpyHostToDevice, c->st));
@@ -952,6 +985,8 @@ int cavgpu_autotune(cavgpu_ctx *c, int32_t trial_steps, int32_t flags, int64_t *
   }
   cudaFree(snap);
   cudaFree(snap_i);
+  cudaFree(snap_img);
+  cudaFree(snap_mol);
   c->prof = prof0;
   c->steps_done = steps0;
   c->graph_launches = graphs0;

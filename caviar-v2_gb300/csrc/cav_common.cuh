@@ -110,11 +110,13 @@ struct Dev {
   uint32_t *id;               // host (insertion) index
   int *cell_of;               // build cell of each slot
   int4 *img;                  // periodic-boundary crossings per axis (msd_domain_cross); null when not tracked
+  int *mol;                   // molecule index (ignore_intra_molecule); null when off
   // rebuild scratch
   dbl4 *t_pos, *t_vel, *t_acc, *t_acc_old;
   int *t_type;
   uint32_t *t_id;
   int4 *t_img;
+  int *t_mol;
   int *atom_cell, *cell_count, *cell_start, *cell_cursor, *perm, *perm_tmp;
   // neighbour list
   uint32_t *nbr;

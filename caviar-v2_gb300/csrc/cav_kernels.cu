@@ -355,6 +355,7 @@ __global__ void __launch_bounds__(256) k_copy_state(Dev d, Box b, int forced) {
   d.t_type[i] = d.type[i];
   d.t_id[i] = d.id[i];
   if (d.img) d.t_img[i] = d.img[i];
+  if (d.mol) d.t_mol[i] = d.mol[i];
   d.perm_tmp[i] = d.atom_cell[i];  // cell of old slot i (perm_tmp is free again)
 }
 
@@ -373,6 +374,7 @@ __global__ void __launch_bounds__(256) k_gather(Dev d, Box b, int forced) {
   d.type[k] = d.t_type[o];
   d.id[k] = d.t_id[o];
   if (d.img) d.img[k] = d.t_img[o];
+  if (d.mol) d.mol[k] = d.t_mol[o];
   d.cell_of[k] = d.perm_tmp[o];
   update_rel(d, repbox(b, rep), k, x);
   d.rel_ref[k] = d.rel[k];
@@ -470,6 +472,7 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 8) k_build_warp(Dev d, Box b
       const float lo = act ? b.ce2_lo : -1.0f;  // idle lanes never hit
       const float hi = act ? b.ce2_hi : -1.0f;
       const uint32_t selfw = (uint32_t)i | (13u << CODE_SHIFT);  // home cell: stencil 13, image zero
+      const int mol_i = d.mol && act ? d.mol[i] : 0;
       uint32_t *row = d.nbr + nbr_block_base(act ? i : hs, cap, d.tpa);
       int cnt = 0;
       for (int p0 = 0; p0 < ntot; p0 += BUILD_STAGE) {
@@ -518,11 +521,14 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 8) k_build_warp(Dev d, Box b
               if (exact_pair(d, rb, b.ce2, i, (int)(w & IDX_MASK), img)) hm |= 1u << u;
             }
           }
-          // phase 2: the hits, in candidate order
+          // phase 2: the hits, in candidate order (ignore_intra_molecule: none of the
+          // atom's own molecule, as Lj::calculate_acceleration skips them, lj.cpp:446)
           while (hm) {
             const int u = __ffs(hm) - 1;
             hm &= hm - 1u;
-            if (cnt < cap) row[((cnt >> 2) << cshift) + (cnt & 3)] = __float_as_uint(stage[t0 + u].w);
+            const uint32_t w = __float_as_uint(stage[t0 + u].w);
+            if (d.mol && d.mol[w & IDX_MASK] == mol_i) continue;
+            if (cnt < cap) row[((cnt >> 2) << cshift) + (cnt & 3)] = w;
             ++cnt;
           }
         }

@@ -66,6 +66,7 @@ bool Atom_data::add_atom(size_t id, size_t type, const Vector3d<double> &pos, co
   atom_struct_owned.velocity.push_back(vel);
   atom_struct_owned.acceleration.push_back(Vector3d<double>{0, 0, 0});
   if (msd_process) atom_struct_owned.msd_domain_cross.push_back(Vector3d<int>{0, 0, 0});
+  atom_struct_owned.molecule_index.push_back(-1);
   return true;
 }
 
@@ -365,6 +366,7 @@ void Md_simulator::initialize() {
       caviar_->log.error_all("energy or temperature is not set.");
     }
   }
+  p.ignore_intra_molecule = lj->ignore_intra_molecule ? 1 : 0;
   p.msd_process = ad.msd_process ? 1 : 0;
   if (ad.msd_process) {  // the device counts from zero: the host mirror keeps its values
     auto &m = ad.atom_struct_owned.msd_domain_cross;
@@ -383,6 +385,11 @@ void Md_simulator::initialize() {
   check(cavgpu_upload(ctx_, (int64_t)o.position.size(), &o.position[0].x, &o.velocity[0].x,
                       reinterpret_cast<const uint64_t *>(o.type.data()), nullptr),
         "cavgpu_upload");
+  if (lj->ignore_intra_molecule) {
+    std::vector<int32_t> mol(o.position.size(), -1);
+    std::copy_n(o.molecule_index.begin(), std::min(mol.size(), o.molecule_index.size()), mol.begin());
+    check(cavgpu_set_molecules(ctx_, mol.data()), "cavgpu_set_molecules");
+  }
   initialized = true;
 }
 

@@ -62,6 +62,8 @@ struct Atom_struct {
   std::vector<Vector3d<double>> position, velocity, acceleration;
   // periodic-boundary crossings per axis (Atom_data::msd_process), +1 through the upper face
   std::vector<Vector3d<int>> msd_domain_cross;
+  // molecule of each atom, -1 when none (read by Lj::ignore_intra_molecule)
+  std::vector<int32_t> molecule_index;
 };
 
 struct Atom_type_params {
@@ -186,6 +188,10 @@ class Lj : public Force_field {
   void set_lambda_e(const std::vector<std::vector<double>> &v);
   void set_epsilon_atom(int t, double v);
   void set_sigma_atom(int t, double v);
+  // pairs of atoms with equal molecule_index take no force (src/force/lj.cpp:93-96, 446);
+  // atoms outside molecules share the index -1, so they exclude one another too
+  void ignore_intra_molecule_flag(bool flag = true) { ignore_intra_molecule = flag; }
+  bool ignore_intra_molecule = false;
 
   double cutoff = 0.0;
   std::vector<std::vector<double>> epsilon, sigma, cutoff_list;

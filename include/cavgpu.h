@@ -100,7 +100,11 @@ typedef struct cavgpu_params {
    * periodic-boundary crossings per axis, as exchange_owned adds them to
    * Atom_struct::msd_domain_cross (src/atom_data/exchange_owned_single_md_domain.cpp:49-55) */
   int32_t msd_process;
-  int32_t msd_pad;
+  /* force_field::Lj::ignore_intra_molecule (src/force/lj.cpp:93-96, 446): pairs of atoms
+   * with equal Atom_struct::molecule_index (cavgpu_set_molecules; -1 for every atom
+   * until then, as Atom_data::add_atom sets it) take no force.  Applied when the
+   * list is built, so cavgpu_export_pairs leaves those pairs out. */
+  int32_t ignore_intra_molecule;
 } cavgpu_params;
 
 #define CAVGPU_NVE_ENERGY_PER_DOF 0
@@ -132,6 +136,11 @@ void cavgpu_destroy(cavgpu_ctx *ctx);
  * Replaces: Atom_data::add_atom (src/atom_data.cpp:603-637). */
 int cavgpu_upload(cavgpu_ctx *ctx, int64_t n, const double *pos3, const double *vel3, const uint64_t *type,
                   const uint64_t *id);
+
+/* Per-atom molecule index in upload order (Atom_struct::molecule_index,
+ * inc/caviar2/atom_data/utility/atom_struct.hpp:93), for
+ * params.ignore_intra_molecule; after the upload, before cavgpu_setup. */
+int cavgpu_set_molecules(cavgpu_ctx *ctx, const int32_t *molecule_index);
 
 /* Initialise and set up: wrap, bin, build the list, first force, temperature.
  * Replaces: Md_simulator::initialize + setup (src/md_simulator.cpp:366-420, 565-611). */

@@ -48,6 +48,7 @@ struct orc_sys {
   double *pos, *vel, *acc, *acc_old, *pos_old_nl;
   int32_t *type;
   int32_t *img;                /* Atom_struct::msd_domain_cross, x3 */
+  int32_t *mol;                /* Atom_struct::molecule_index */
   unsigned char *in_domain;    /* Atom_struct::mpi_rank == my rank (src/atom_data.cpp:817-839) */
   /* Domain (src/domain.cpp:309-328, 495-502): single rank, nprocs = 1 */
   double size[3];              /* size_global = upper_global - lower_global */
@@ -412,6 +413,8 @@ static void lj_acceleration(orc_sys *s) {
         id_j = j;
         tj = s->type[j];
       }
+      /* ignore_intra_molecule (:446); a ghost carries its source's molecule index */
+      if (s->p.ignore_intra && s->mol[id_i] == s->mol[id_j]) continue;
       const double drx = pj[0] - pi[0], dry = pj[1] - pi[1], drz = pj[2] - pi[2];
       double dr_sq = drx * drx + dry * dry + drz * drz;
       if (s->p.cutoff_list_on) {
@@ -654,7 +657,9 @@ orc_sys *orc_new(const orc_params *p, int32_t n, const double *pos3, const doubl
   s->type = (int32_t *)malloc(((size_t)n + 1) * sizeof(int32_t));
   s->in_domain = (unsigned char *)calloc((size_t)n + 1, 1);
   s->img = (int32_t *)calloc(((size_t)n + 1) * 3, sizeof(int32_t));
-  if (!s->img || !s->in_domain || !s->pos || !s->vel || !s->acc || !s->acc_old || !s->pos_old_nl || !s->type) { orc_free(s); return NULL; }
+  s->mol = (int32_t *)malloc(((size_t)n + 1) * sizeof(int32_t));
+  if (s->mol) for (int32_t i = 0; i < n; ++i) s->mol[i] = -1;  /* Atom_data::add_atom (src/atom_data.cpp:625) */
+  if (!s->mol || !s->img || !s->in_domain || !s->pos || !s->vel || !s->acc || !s->acc_old || !s->pos_old_nl || !s->type) { orc_free(s); return NULL; }
   memcpy(s->pos, pos3, (size_t)n * 3 * sizeof(double));
   memcpy(s->vel, vel3, (size_t)n * 3 * sizeof(double));
   memcpy(s->type, type, (size_t)n * sizeof(int32_t));
@@ -671,7 +676,7 @@ orc_sys *orc_new(const orc_params *p, int32_t n, const double *pos3, const doubl
 void orc_free(orc_sys *s) {
   if (!s) return;
   free(s->pos); free(s->vel); free(s->acc); free(s->acc_old); free(s->pos_old_nl); free(s->type); free(s->in_domain);
-  free(s->img);
+  free(s->img); free(s->mol);
   free(s->gpos.a); free(s->gsrc.a); free(s->gshift.a); free(s->gpos_old_nl.a);
   free(s->bin_start); free(s->bin_count); free(s->bin_items); free(s->nbin_n); free(s->nbin);
   free(s->nl_start); free(s->nl_count); free(s->nl.a);
@@ -720,6 +725,12 @@ int32_t orc_step(orc_sys *s, int32_t nsteps) {
     if (rc) return rc;
     s->current_step++;
   }
+  return ORC_OK;
+}
+
+int32_t orc_set_molecules(orc_sys *s, const int32_t *mol) {
+  if (!s || !mol) return ORC_E_ARG;
+  memcpy(s->mol, mol, (size_t)s->n * sizeof(int32_t));
   return ORC_OK;
 }
 

@@ -65,7 +65,7 @@ typedef struct orc_params {
   double jump_tol;              /* Lj::set_jump_tol (src/force/lj.cpp:82-86); 0 = off */
   int64_t nve_step;             /* constraint::Nve every nve_step steps; 0 = off */
   int32_t nve_mode;             /* 0 energy_per_dof, 1 energy_tot, 2 kbt, 3 kb + temperature */
-  int32_t nve_pad;
+  int32_t ignore_intra;         /* Lj::ignore_intra_molecule_flag (src/force/lj.cpp:93-96, 446) */
   double nve_value, nve_kb;
 } orc_params;
 
@@ -92,6 +92,8 @@ void orc_get_state(const orc_sys *s, double *pos3, double *vel3, double *acc3);
 void orc_get_thermo(const orc_sys *s, double *out6);
 /* Atom_struct::msd_domain_cross per atom, x3 (crossings since orc_new) */
 void orc_get_images(const orc_sys *s, int32_t *img3);
+/* Atom_struct::molecule_index per atom (-1 for every atom until set, as add_atom) */
+int32_t orc_set_molecules(orc_sys *s, const int32_t *mol);
 int64_t orc_current_step(const orc_sys *s);
 
 /* Neighbour list, ghosts and cells of the last build. */

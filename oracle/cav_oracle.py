@@ -27,7 +27,7 @@ class OrcParams(C.Structure):
         ("cutoff_list_on", C.c_int32), ("use_cell_list", C.c_int32), ("n_r_df", C.c_int32),
         ("integrator", C.c_int32), ("noise_mode", C.c_int32), ("pressure_process", C.c_int32),
         ("rebuild_test", C.c_int32), ("jump_tol", C.c_double), ("nve_step", C.c_int64), ("nve_mode", C.c_int32),
-        ("nve_pad", C.c_int32), ("nve_value", C.c_double), ("nve_kb", C.c_double),
+        ("ignore_intra", C.c_int32), ("nve_value", C.c_double), ("nve_kb", C.c_double),
     ]
 
 
@@ -56,6 +56,8 @@ def lib():
         L.orc_get_state.argtypes = [P, D, D, D]
         L.orc_get_thermo.argtypes = [P, D]
         L.orc_get_images.argtypes = [P, I32]
+        L.orc_set_molecules.argtypes = [P, I32]
+        L.orc_set_molecules.restype = C.c_int32
         L.orc_pair_count.argtypes = [P]
         L.orc_pair_count.restype = I64
         L.orc_get_pairs.argtypes = [P, I32, I64]
@@ -104,6 +106,7 @@ def make_params(p, noise_mode=1):
     o.pressure_process = p.get("pressure_process", 1)
     o.rebuild_test = int(p.get("rebuild_test", 0))
     o.jump_tol = float(p.get("jump_tol", 0.0))
+    o.ignore_intra = int(bool(p.get("ignore_intra_molecule", False)))
     nve = p.get("nve")
     if nve:
         o.nve_step, o.nve_mode = int(nve["step"]), int(nve["mode"])
@@ -131,6 +134,8 @@ class System:
         self._h = lib().orc_new(C.byref(self._p), self.n, _dp(pos), _dp(vel), _ip(typ))
         if not self._h:
             raise ValueError("orc_new failed")
+        if params.get("molecule_index") is not None:
+            lib().orc_set_molecules(self._h, _ip(np.ascontiguousarray(params["molecule_index"], np.int32)))
 
     def __del__(self):
         if getattr(self, "_h", None):

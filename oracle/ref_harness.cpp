@@ -26,6 +26,8 @@
 //            msd_type, msd_initial_step, pad -> writer::Atom_writer writing
 //            <out.bin>_{xyz.xyz, energy.txt, temperature.txt, pressure.txt,
 //            msd.txt, volume.txt}; msd output turns Atom_data::msd_process on
+//     bit 6: int32 ignore flag, pad, molecule_index[N] -> Atom_struct::molecule_index
+//            and Lj::ignore_intra_molecule_flag
 //   Bits 1-3 take effect in Lj::verify_settings (src/force/lj.cpp:186-381), which
 //   the library itself never calls; the harness calls it, as a user of these
 //   options must, and appends the effective tables to the output.
@@ -139,6 +141,9 @@ int main(int argc, char **argv) {
   int64_t wsteps[6] = {0, 0, 0, 0, 0, 0};
   int32_t wopt[4] = {0, -1, 0, 0};
   if ((ext & 32) && (!rd(fi, wsteps, 6) || !rd(fi, wopt, 4))) return 8;
+  int32_t intra[2] = {0, 0};
+  std::vector<int32_t> mol(N, -1);
+  if ((ext & 64) && (!rd(fi, intra, 2) || !rd(fi, mol.data(), mol.size()))) return 8;
   fclose(fi);
 
   void *mem = calloc(1, sizeof(Caviar2));
@@ -167,6 +172,15 @@ int main(int argc, char **argv) {
   for (int i = 0; i < N; ++i)
     c.atom_data.add_atom((size_t)i, (size_t)type[i], Vector3d<double>{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]},
                          Vector3d<double>{vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]});
+
+  if (ext & 64) {
+    // molecules without bonds, angles or dihedrals (degree_of_freedoms reads
+    // molecule_struct_owned[index] for every index >= 0)
+    int32_t nmol = 0;
+    for (int i = 0; i < N; ++i) nmol = std::max(nmol, mol[i] + 1);
+    c.atom_data.molecule_struct_owned.resize((size_t)nmol);
+    for (int i = 0; i < N; ++i) c.atom_data.atom_struct_owned.molecule_index[i] = mol[i];
+  }
 
   // ---- Neighborlist ----
   c.neighborlist.set_cutoff(dp[6]);
@@ -197,6 +211,7 @@ int main(int argc, char **argv) {
   }
   if (ext & 1) lj.set_jump_tol(jump_tol);
   if (ext & 2) lj.enable_wca(true);
+  if (ext & 64) lj.ignore_intra_molecule_flag(intra[0] != 0);
   if (ext & 8) {
     std::vector<std::vector<double>> ls(nt, std::vector<double>(nt)), le(nt, std::vector<double>(nt));
     for (int a = 0; a < nt; ++a)

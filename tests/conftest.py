@@ -45,6 +45,8 @@ def golden_params(g):
                       msd_type=w[7], msd_initial_step=w[8])
     return dict(
         writer=writer, msd_process=bool(writer and writer["msd"] > 0),
+        molecule_index=g["molecule_index"] if "molecule_index" in g else None,
+        ignore_intra_molecule=int(g["ignore_intra_molecule"]) if "ignore_intra_molecule" in g else 0,
         lo=g["lo"], hi=g["hi"], ntypes=nt, nl_cutoff=float(g["nl_cutoff"]), nl_coef=float(g["nl_coef"]),
         ghost_cutoff=float(g["ghost_cutoff"]), lj_cutoff=float(g["lj_cutoff"]), eps=eps, sigma=sigma,
         cutoff_list=cutoff_list, jump_tol=float(g["jump_tol"]) if "jump_tol" in g else 0.0,
@@ -55,6 +57,17 @@ def golden_params(g):
         lang_friction=float(g["lang_friction"]), lang_kb=float(g["lang_kb"]), seed=0, n_r_df=int(g["n_r_df"]),
         use_cell_list=int(g["use_cell_list"]), pressure_process=int(g["pressure_process"]),
     )
+
+
+def reference_pairs(g):
+    """The reference's canonical pair set of a golden case as the GPU list holds it:
+    with ignore_intra_molecule, pairs inside one molecule are left out of the list
+    (the reference keeps them in its list and skips them in the force loop)."""
+    rows = g["pairs"]
+    if int(g.get("ignore_intra_molecule", 0)):
+        mol = g["molecule_index"]
+        rows = rows[mol[rows[:, 0]] != mol[rows[:, 1]]]
+    return rows
 
 
 @pytest.fixture(scope="session")

@@ -77,6 +77,9 @@ int main(int argc, char **argv) {
   int64_t wsteps[6] = {0, 0, 0, 0, 0, 0};
   int32_t wopt[4] = {0, -1, 0, 0};
   if ((ext & 32) && (!rd(fi, wsteps, 6) || !rd(fi, wopt, 4))) return 5;
+  int32_t intra[2] = {0, 0};
+  std::vector<int32_t> mol(N, -1);
+  if ((ext & 64) && (!rd(fi, intra, 2) || !rd(fi, mol.data(), mol.size()))) return 5;
   fclose(fi);
 
   Caviar2 caviar;
@@ -95,6 +98,8 @@ int main(int argc, char **argv) {
     if (!caviar.atom_data.add_atom(a)) return 6;  // outside the box
   }
   for (int t = 0; t < nt; ++t) caviar.atom_data.add_type_mass(t, mass[t]);
+  if (ext & 64)
+    for (int i = 0; i < N; ++i) caviar.atom_data.atom_struct_owned.molecule_index[i] = mol[i];
   caviar.atom_data.set_k_b(dp[10]);
   caviar.atom_data.set_n_r_df(nrdf);
   caviar.atom_data.set_temperature_process(true);
@@ -127,6 +132,7 @@ int main(int argc, char **argv) {
   }
   if (ext & 1) lj.set_jump_tol(jump_tol);
   if (ext & 2) lj.enable_wca(true);
+  if (ext & 64) lj.ignore_intra_molecule_flag(intra[0] != 0);
   if (ext & 8) {
     std::vector<std::vector<double>> ls(nt, std::vector<double>(nt)), le(nt, std::vector<double>(nt));
     for (int a = 0; a < nt; ++a)

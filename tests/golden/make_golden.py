@@ -31,7 +31,7 @@ def ext_flags(p):
     """Extension bits of the harness input: jump_tol, WCA, per-atom mixing, lambda tables."""
     return ((1 if p.get("jump_tol") else 0) | (2 if p.get("wca") else 0) | (4 if p.get("eps_atom") is not None else 0)
             | (8 if p.get("lambda_s") is not None else 0) | (16 if p.get("nve") else 0)
-            | (32 if p.get("writer") else 0))
+            | (32 if p.get("writer") else 0) | (64 if p.get("molecule_index") is not None else 0))
 
 
 WRITER_KINDS = ("xyz", "energy", "temperature", "pressure", "msd", "volume")
@@ -82,6 +82,9 @@ def write_input(path, pos, vel, typ, p, nsteps):
             w = writer_config(p["writer"])
             f.write(w[:6].tobytes())
             f.write(np.array([w[6], w[7], w[8], 0], np.int32).tobytes())
+        if ext & 64:
+            f.write(np.array([int(bool(p.get("ignore_intra_molecule"))), 0], np.int32).tobytes())
+            f.write(np.ascontiguousarray(p["molecule_index"], np.int32).tobytes())
 
 
 class Reader:
@@ -156,6 +159,9 @@ def run_case(name, pos, vel, typ, p, nsteps):
     if ext & 32:
         extra["writer"] = writer_config(p["writer"])
         extra.update(texts)
+    if ext & 64:
+        extra["molecule_index"] = np.ascontiguousarray(p["molecule_index"], np.int32)
+        extra["ignore_intra_molecule"] = np.int32(bool(p.get("ignore_intra_molecule")))
     out = dict(
         # inputs
         pos=pos, vel=vel, typ=typ.astype(np.int32), nsteps=np.int32(nsteps),
@@ -268,6 +274,12 @@ def cases():
     pos = np.mod(pos + np.array([0.0, 0.0, -0.365]), p["hi"])
     wr = {"xyz": 50, "energy": 5, "temperature": 5, "msd": 10, "msd_type": 1}
     yield "ka500_langevin_writers", pos, vel, typ, dict(p, lang_friction=0.0, writer=wr), 60
+    # Lj::ignore_intra_molecule: molecules of four consecutive atoms for the first 400 atoms; the
+    # other 100 keep add_atom's molecule index -1 and so count as one molecule among themselves
+    pos, vel, typ, p = W.lj_fluid((5, 5, 5), seed=93)
+    mol = np.full(len(pos), -1, np.int32)
+    mol[:400] = np.arange(400) // 4
+    yield "fcc500_ignore_intra", pos, vel, typ, dict(p, ignore_intra_molecule=1, molecule_index=mol), 60
 
 
 def main():

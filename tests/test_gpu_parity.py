@@ -15,7 +15,7 @@ import hashlib
 import numpy as np
 import pytest
 
-from conftest import golden_cases, golden_params, load_golden
+from conftest import golden_cases, golden_params, load_golden, reference_pairs
 
 pytestmark = pytest.mark.gpu
 
@@ -78,6 +78,8 @@ def virial_terms(g, pairs):
     rho6 = rho2 * rho2 * rho2
     coef = 4 * eps * (-12 * rho6 * rho6 * r2i + 6 * rho6 * r2i + 12 * rc6 * rc6 * rcinv - 6 * rc6 * rcinv)
     keep = (r2d <= c) & (eps != 0)
+    if p["ignore_intra_molecule"]:  # pairs inside one molecule take no force (lj.cpp:446)
+        keep &= p["molecule_index"][i] != p["molecule_index"][j]
     return (-coef * r2)[keep]
 
 
@@ -105,6 +107,10 @@ def test_setup_forces(case, oracle_lib):
 def test_pair_set_bitexact(case):
     name, g, s = case
     pairs = s.pairs()
+    if "ignore_intra_molecule" in g:  # the list leaves a molecule's own pairs out
+        np.testing.assert_array_equal(pairs, reference_pairs(g))
+        assert len(pairs) < int(g["npairs"])
+        return
     assert len(pairs) == int(g["npairs"]), name
     if "pairs" in g:
         np.testing.assert_array_equal(pairs, g["pairs"])
