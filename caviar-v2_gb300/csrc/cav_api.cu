@@ -576,6 +576,7 @@ int upload_common(cavgpu_ctx *c, const int64_t *counts, const double *pos3, cons
   for (auto pp : di) if (!rc) rc = dalloc(c, pp, NS);
   if (!rc) rc = dalloc(c, &d.id, NS);
   if (!rc) rc = dalloc(c, &d.t_id, NS);
+  if (!rc) rc = dalloc(c, &d.skey, NS);
   if (!rc) rc = dalloc(c, &d.cell_count, ncell_all);
   if (!rc) rc = dalloc(c, &d.cell_cursor, ncell_all);
   if (!rc) rc = dalloc(c, &d.cell_start, (size_t)ncell_all + 1);

@@ -118,6 +118,7 @@ struct Dev {
   int4 *t_img;
   int *t_mol;
   int *atom_cell, *cell_count, *cell_start, *cell_cursor, *perm, *perm_tmp;
+  uint64_t *skey;             // order inside a cell: Morton index of the 4x4x4 sub-cell, then id
   // neighbour list
   uint32_t *nbr;
   int *nnbr;

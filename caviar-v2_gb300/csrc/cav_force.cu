@@ -86,6 +86,16 @@ __device__ inline void load_tab(const Dev &d, Tab &tab) {
   for (int k = threadIdx.x; k < nt; k += blockDim.x) { tab.minv[k] = T.minv[k]; tab.mass[k] = T.mass[k]; }
 }
 
+// A list chunk: read once per step and larger than L1, so it is not allocated in L1
+// (which keeps the neighbour coordinates the gathers reuse).
+__device__ __forceinline__ uint4 ld_list(const uint4 *p) {
+  uint4 v;
+  asm("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
+      : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+      : "l"(p));
+  return v;
+}
+
 // Mixed-form pair loop of one lane: list chunks t, t+TPA, ... of atom i (four words
 // per 128-bit load; the next chunk's load and four neighbour coordinates in
 // flight); `gather(word)` returns the neighbour's float4 (global memory or a
@@ -95,10 +105,10 @@ __device__ __forceinline__ void mixed_pairs(const uint4 *row4, int nn, int t, co
                                             const SmemTabF &tab, const OneType c1, const float4 wf,
                                             const float4 wl, const float jtol, Gather gather, float &ax,
                                             float &ay, float &az, float &vr, float &pp) {
-  uint4 nxt = 4 * t < nn ? __ldg(row4) : make_uint4(0, 0, 0, 0);
+  uint4 nxt = 4 * t < nn ? ld_list(row4) : make_uint4(0, 0, 0, 0);
   for (int q = 0, k0 = 4 * t; k0 < nn; ++q, k0 += 4 * TPA) {
     const uint4 w4 = nxt;
-    if (k0 + 4 * TPA < nn) nxt = __ldg(row4 + (size_t)(q + 1) * 32);  // the next list chunk in flight
+    if (k0 + 4 * TPA < nn) nxt = ld_list(row4 + (size_t)(q + 1) * 32);  // the next list chunk in flight
     const uint32_t e[4] = {w4.x, w4.y, w4.z, w4.w};
     float4 rj[4];
 #pragma unroll

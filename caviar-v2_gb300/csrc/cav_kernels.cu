@@ -235,14 +235,22 @@ __global__ void __launch_bounds__(256) k_bin(Dev d, Box b, int forced) {
       m.x += w.x; m.y += w.y; m.z += w.z;
       d.img[i] = m;
     }
-    int cx = (int)floor((p.x - rb.lo[0]) * rb.inv_w[0]);
-    int cy = (int)floor((p.y - rb.lo[1]) * rb.inv_w[1]);
-    int cz = (int)floor((p.z - rb.lo[2]) * rb.inv_w[2]);
+    const double ux = (p.x - rb.lo[0]) * rb.inv_w[0], uy = (p.y - rb.lo[1]) * rb.inv_w[1],
+                 uz = (p.z - rb.lo[2]) * rb.inv_w[2];
+    int cx = (int)floor(ux), cy = (int)floor(uy), cz = (int)floor(uz);
     cx = min(max(cx, 0), rb.nc[0] - 1);
     cy = min(max(cy, 0), rb.nc[1] - 1);
     cz = min(max(cz, 0), rb.nc[2] - 1);
     c = rb.cell_off + cx + rb.nc[0] * (cy + rb.nc[1] * cz);
     d.atom_cell[i] = c;
+    // order inside the cell: the Morton index of the atom's 4x4x4 sub-cell, then its id,
+    // so that consecutive slots (a warp's lanes) sit close together and their neighbour
+    // lists run through the same candidates
+    const int sx = min(max((int)((ux - cx) * 4.0), 0), 3), sy = min(max((int)((uy - cy) * 4.0), 0), 3),
+              sz = min(max((int)((uz - cz) * 4.0), 0), 3);
+    const uint32_t morton = (sx & 1) | ((sy & 1) << 1) | ((sz & 1) << 2) | ((sx & 2) << 2) | ((sy & 2) << 3) |
+                            ((sz & 2) << 4);
+    d.skey[i] = ((uint64_t)morton << 32) | d.id[i];
   }
   // warp-aggregated counting: one atomic per distinct cell in the warp
   const unsigned m = __ballot_sync(FULL_MASK, act);
@@ -318,8 +326,9 @@ __global__ void __launch_bounds__(256) k_scatter(Dev d, Box b, int forced) {
   d.perm_tmp[d.cell_start[c] + atomicAdd(&d.cell_cursor[c], 1)] = i;
 }
 
-// one warp per cell: order the cell's atoms by host index (deterministic lists);
-// cells of up to 32 atoms rank in registers with warp shuffles
+// one warp per cell: order the cell's atoms by their sort key (sub-cell, then host
+// index: deterministic lists); cells of up to 32 atoms rank in registers with warp
+// shuffles
 __global__ void __launch_bounds__(256) k_cell_sort(Dev d, Box b, int forced) {
   const int cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (cell >= b.ncell_all) return;
@@ -328,17 +337,17 @@ __global__ void __launch_bounds__(256) k_cell_sort(Dev d, Box b, int forced) {
   const int s = d.cell_start[cell], e = d.cell_start[cell + 1], n = e - s;
   if (n <= 32) {
     const int ia = lane < n ? d.perm_tmp[s + lane] : 0;
-    const uint32_t ida = lane < n ? d.id[ia] : 0xffffffffu;
+    const uint64_t ka = lane < n ? d.skey[ia] : ~0ull;
     int rank = 0;
-    for (int q = 0; q < n; ++q) rank += __shfl_sync(FULL_MASK, ida, q) < ida;
+    for (int q = 0; q < n; ++q) rank += __shfl_sync(FULL_MASK, ka, q) < ka;
     if (lane < n) d.perm[s + rank] = ia;
     return;
   }
   for (int a = lane; a < n; a += 32) {
     const int ia = d.perm_tmp[s + a];
-    const uint32_t ida = d.id[ia];
+    const uint64_t ka = d.skey[ia];
     int rank = 0;
-    for (int q = 0; q < n; ++q) rank += d.id[d.perm_tmp[s + q]] < ida;
+    for (int q = 0; q < n; ++q) rank += d.skey[d.perm_tmp[s + q]] < ka;
     d.perm[s + rank] = ia;
   }
 }
@@ -430,10 +439,10 @@ __device__ inline StencilCell stencil_cell(const RepBox &rb, int cx, int cy, int
 // the candidates) written, in candidate order.  Hits append to the lane's own
 // row, so the list keeps the stencil order (deterministic, independent of the
 // launch shape).
-constexpr int BUILD_WARPS = 4;    // warps per block
-constexpr int BUILD_STAGE = 512;  // staged candidates per warp and pass (8 KiB)
+constexpr int BUILD_WARPS = 8;    // warps per block
+constexpr int BUILD_STAGE = 256;  // staged candidates per warp and pass (4 KiB)
 
-__global__ void __launch_bounds__(BUILD_WARPS * 32, 8) k_build_warp(Dev d, Box b, int mode, int forced) {
+__global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_warp(Dev d, Box b, int mode, int forced) {
   __shared__ float4 stage_all[BUILD_WARPS][BUILD_STAGE];
   const int lane = threadIdx.x & 31;
   float4 *stage = stage_all[threadIdx.x >> 5];
@@ -465,13 +474,15 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 8) k_build_warp(Dev d, Box b
     }
     const int ntot = __shfl_sync(FULL_MASK, kpre, 26);
     kpre -= kn;
+    const int k13 = __shfl_sync(FULL_MASK, kpre, 13);  // where the home cell's atoms start
     for (int h0 = hs; h0 < he; h0 += 32) {
       const int i = h0 + lane;
       const bool act = i < he;
       const float4 ri = act ? d.rel[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-      const float lo = act ? b.ce2_lo : -1.0f;  // idle lanes never hit
-      const float hi = act ? b.ce2_hi : -1.0f;
-      const uint32_t selfw = (uint32_t)i | (13u << CODE_SHIFT);  // home cell: stencil 13, image zero
+      const float lo = b.ce2_lo;
+      const float hi = act ? b.ce2_hi : -1.0f;  // idle lanes never hit
+      // the atom itself: stencil cell 13 (the home cell, image zero), at its rank in the cell
+      const int tself = act ? k13 + (i - hs) : -1;
       const int mol_i = d.mol && act ? d.mol[i] : 0;
       uint32_t *row = d.nbr + nbr_block_base(act ? i : hs, cap, d.tpa);
       int cnt = 0;
@@ -495,17 +506,20 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 8) k_build_warp(Dev d, Box b
         for (int t = np + lane; t < npad32; t += 32) stage[t] = make_float4(1e18f, 1e18f, 1e18f, 0.f);
         __syncwarp();
         for (int t0 = 0; t0 < npad32; t0 += 32) {
-          // phase 1: hit and band bits of 32 candidates
-          uint32_t hm = 0u, bm = 0u;
+          // phase 1: bits of the sure hits (q < ce2_lo) and of everything up to ce2_hi
+          uint32_t hm = 0u, am = 0u;
 #pragma unroll
           for (int u = 0; u < 32; ++u) {
             const float4 c = stage[t0 + u];  // broadcast
             const float fx = c.x - ri.x, fy = c.y - ri.y, fz = c.z - ri.z;
             const float q = fx * fx + fy * fy + fz * fz;
-            const bool notself = __float_as_uint(c.w) != selfw;
-            hm |= (uint32_t)((q < lo) & notself) << u;
-            bm |= (uint32_t)((q >= lo) & (q <= hi) & notself) << u;
+            if (q < lo) hm |= 1u << u;
+            if (q <= hi) am |= 1u << u;
           }
+          const int ts = tself - (p0 + t0);  // the atom itself is no candidate
+          if (ts >= 0 && ts < 32) am &= ~(1u << ts);
+          hm &= am;
+          uint32_t bm = am & ~hm;  // the band
           if (__any_sync(FULL_MASK, bm != 0u)) {  // rare: the exact FP64 predicate
             while (bm) {
               const int u = __ffs(bm) - 1;
