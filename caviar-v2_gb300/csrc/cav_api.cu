@@ -126,8 +126,17 @@ int enqueue_thermo_after_force(cavgpu_ctx *c, int ring_slot) {
 }
 
 // drift (VV) or first Langevin half; batches fold their per-replica KE right after
-// the Langevin half kick, where the reference takes the temperature
+// the Langevin half kick, where the reference takes the temperature.  Langevin
+// with constraint::Nve: the velocity half, Nve on the mid-step velocities
+// (src/md_simulator.cpp:782-793), then the temperature and the position update.
 int enqueue_drift(cavgpu_ctx *c, int k, bool thermo) {
+  if (is_lang(c) && c->nve.step > 0) {
+    RK(launch_drift(c->d, c->b, c->sc, c->lc, k, -1, c->st));
+    RK(launch_nve(c->d, c->b, c->tc, c->nve, k, 0, -1, c->st));
+    RK(launch_lang_pos(c->d, c->b, c->sc, c->lc, thermo ? 1 : 0, c->st));
+    c->kernel_launches += 5;
+    return CAVGPU_OK;
+  }
   RK(launch_drift(c->d, c->b, c->sc, c->lc, k, thermo && is_lang(c), c->st));
   c->kernel_launches += 1;
   if (thermo && is_lang(c) && c->b.nrep > 1) {
@@ -148,7 +157,7 @@ int enqueue_step(cavgpu_ctx *c, int k, bool thermo, int ring_slot) {
   if (c->prof && k < (int)c->ev1.size()) CK(cudaEventRecord(c->ev1[k], c->st));
   c->kernel_launches += REBUILD_KERNELS + 1;
   if (thermo) RK(enqueue_thermo_after_force(c, ring_slot));
-  if (c->nve.step > 0) {  // constraint::Nve after the temperature (src/md_simulator.cpp:681-694)
+  if (c->nve.step > 0 && !is_lang(c)) {  // constraint::Nve after the temperature (src/md_simulator.cpp:681-694)
     RK(launch_nve(c->d, c->b, c->tc, c->nve, k, thermo, ring_slot, c->st));
     c->kernel_launches += 3;
   }
@@ -192,7 +201,7 @@ int capture_step(cavgpu_ctx *c, int k, bool thermo, int ring_slot) {
   RK(launch_force(c->d, c->b, c->sc, c->lc, is_lang(c) ? 2 : 1, thermo, k, c->st));
   if (c->prof && k < (int)c->ev1.size()) CK(cudaEventRecordWithFlags(c->ev1[k], c->st, cudaEventRecordExternal));
   if (thermo) RK(enqueue_thermo_after_force(c, ring_slot));
-  if (c->nve.step > 0) {  // constraint::Nve after the temperature (src/md_simulator.cpp:681-694)
+  if (c->nve.step > 0 && !is_lang(c)) {  // constraint::Nve after the temperature (src/md_simulator.cpp:681-694)
     RK(launch_nve(c->d, c->b, c->tc, c->nve, k, thermo, ring_slot, c->st));
     c->kernel_launches += 3;
   }
@@ -398,9 +407,8 @@ int create_common(const cavgpu_params *p, int nrep, const double *lo3, const dou
   sc.seed = p->seed;
   sc.noise_off = p->noise_off;
   if (p->jump_tol < 0.0 || p->initial_step < 0) { delete c; return CAVGPU_E_ARG; }
-  if (p->nve_step > 0) {  // constraint::Nve: velocity Verlet or leap-frog, one system (checked at upload)
-    if (p->integrator == CAVGPU_VELOCITY_VERLET_LANGEVIN || p->nve_mode < CAVGPU_NVE_ENERGY_PER_DOF ||
-        p->nve_mode > CAVGPU_NVE_KB_TEMPERATURE || !(p->nve_value > 0.0) ||
+  if (p->nve_step > 0) {  // constraint::Nve: one system (checked at upload)
+    if (p->nve_mode < CAVGPU_NVE_ENERGY_PER_DOF || p->nve_mode > CAVGPU_NVE_KB_TEMPERATURE || !(p->nve_value > 0.0) ||
         (p->nve_mode == CAVGPU_NVE_KB_TEMPERATURE && !(p->nve_kb > 0.0))) {
       delete c;
       return CAVGPU_E_ARG;
@@ -791,7 +799,8 @@ int cavgpu_run(cavgpu_ctx *c, int64_t nsteps, int64_t every, double *out5) {
     c->graph_launches += 1;
     // drift + condition + force per step, the thermo folds, the step counter; the
     // rebuild kernels that ran are added from the device's rebuild count below
-    c->kernel_launches += (long long)sz * (c->nve.step > 0 ? 6 : 3) + 1 + nrec * (c->b.nrep > 1 && is_lang(c) ? 2 : 1);
+    c->kernel_launches += (long long)sz * (c->nve.step > 0 ? (is_lang(c) ? 7 : 6) : 3) + 1 +
+                          nrec * (c->b.nrep > 1 && is_lang(c) ? 2 : 1);
     if (c->prof) RK(collect_profile(c, sz));
     if (every > 0) {
       CK(cudaMemcpyAsync(out5 + THERMO_REC * rec, c->d.thermo_ring, THERMO_REC * sizeof(double) * nrec,

@@ -250,8 +250,11 @@ int drift_grid_blocks(const LaunchCfg &lc);
 int force_grid_blocks(const LaunchCfg &lc);
 // sets the dynamic shared-memory limit of every segment-kernel variant (call outside capture)
 int prepare_force_seg(size_t smem_bytes);
+// thermo < 0 (Langevin): the velocity half only; launch_lang_pos then moves the atoms
 int launch_drift(const Dev &d, const Box &b, const StepConsts &sc, const LaunchCfg &lc, int k_in_chunk,
                  int thermo, cudaStream_t st);
+int launch_lang_pos(const Dev &d, const Box &b, const StepConsts &sc, const LaunchCfg &lc, int thermo,
+                    cudaStream_t st);
 int launch_rebuild(const Dev &d, const Box &b, const LaunchCfg &lc, int forced, cudaStream_t st);
 int launch_set_rebuild_cond(const Dev &d, cudaGraphConditionalHandle h, cudaStream_t st);
 constexpr int REBUILD_KERNELS = 8;  // kernels launch_rebuild enqueues

@@ -150,9 +150,35 @@ __global__ void __launch_bounds__(256) k_drift_lf(Dev d, Box b, StepConsts sc) {
   else half_skin_test(d, b, rep, i, x);
 }
 
+// Langevin position update r += v*c (src/md_simulator.cpp:822-827) with the
+// half-skin tracking; with THERMO the temperature sums of the velocities first.
+template <bool MIXED, bool THERMO>
+__device__ __forceinline__ void lang_position(const Dev &d, const Box &b, const StepConsts &sc, int rep, int i, dbl4 x,
+                                              const dbl4 &v, double (&part)[4]) {
+  if (THERMO) {
+    const double m = d.tab->mass[(int)x.w];
+    part[0] = m * (v.x * v.x + v.y * v.y + v.z * v.z);
+    part[1] = m * v.x; part[2] = m * v.y; part[3] = m * v.z;
+  }
+  if (MIXED) {
+    x.x = fma(v.x, sc.lc, x.x);
+    x.y = fma(v.y, sc.lc, x.y);
+    x.z = fma(v.z, sc.lc, x.z);
+  } else {
+    x.x = __dadd_rn(x.x, __dmul_rn(v.x, sc.lc));
+    x.y = __dadd_rn(x.y, __dmul_rn(v.y, sc.lc));
+    x.z = __dadd_rn(x.z, __dmul_rn(v.z, sc.lc));
+  }
+  d.pos[i] = x;
+  if (MIXED) mixed_track(d, b, rep, i, x);
+  else half_skin_test(d, b, rep, i, x);
+}
+
 // Langevin first half (src/md_simulator.cpp:748-837):
 //   v += (a*0.5)*dt + eta*b ; [temperature here] ; r += v*c
-template <bool MIXED, bool THERMO>
+// POS false: the velocity half only; constraint::Nve then acts on the mid-step
+// velocities (:784-791) and k_lang_pos takes the temperature and moves the atoms.
+template <bool MIXED, bool THERMO, bool POS>
 __global__ void __launch_bounds__(256) k_lang_a(Dev d, Box b, StepConsts sc, int k_in_chunk) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double part[4] = {0.0, 0.0, 0.0, 0.0};
@@ -177,25 +203,18 @@ __global__ void __launch_bounds__(256) k_lang_a(Dev d, Box b, StepConsts sc, int
       v.y = __dadd_rn(v.y, __dadd_rn(__dmul_rn(__dmul_rn(a.y, 0.5), sc.dt), __dmul_rn(e1, sc.lb)));
       v.z = __dadd_rn(v.z, __dadd_rn(__dmul_rn(__dmul_rn(a.z, 0.5), sc.dt), __dmul_rn(e2, sc.lb)));
     }
-    if (THERMO) {
-      const double m = d.tab->mass[(int)x.w];
-      part[0] = m * (v.x * v.x + v.y * v.y + v.z * v.z);
-      part[1] = m * v.x; part[2] = m * v.y; part[3] = m * v.z;
-    }
-    if (MIXED) {
-      x.x = fma(v.x, sc.lc, x.x);
-      x.y = fma(v.y, sc.lc, x.y);
-      x.z = fma(v.z, sc.lc, x.z);
-    } else {
-      x.x = __dadd_rn(x.x, __dmul_rn(v.x, sc.lc));
-      x.y = __dadd_rn(x.y, __dmul_rn(v.y, sc.lc));
-      x.z = __dadd_rn(x.z, __dmul_rn(v.z, sc.lc));
-    }
-    d.pos[i] = x;
     d.vel[i] = v;
-    if (MIXED) mixed_track(d, b, rep, i, x);
-    else half_skin_test(d, b, rep, i, x);
+    if (POS) lang_position<MIXED, THERMO>(d, b, sc, rep, i, x, v, part);
   }
+  if (POS && THERMO) block_sum_store<4>(part, &d.partials_ke[(size_t)blockIdx.x * 4]);
+}
+
+template <bool MIXED, bool THERMO>
+__global__ void __launch_bounds__(256) k_lang_pos(Dev d, Box b, StepConsts sc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double part[4] = {0.0, 0.0, 0.0, 0.0};
+  const int rep = i < sc.n ? rep_of_slot(b, i) : -1;
+  if (rep >= 0) lang_position<MIXED, THERMO>(d, b, sc, rep, i, d.pos[i], d.vel[i], part);
   if (THERMO) block_sum_store<4>(part, &d.partials_ke[(size_t)blockIdx.x * 4]);
 }
 
@@ -226,14 +245,16 @@ __global__ void __launch_bounds__(256) k_bin(Dev d, Box b, int forced) {
     // single-image wrap exactly as Domain::fix_position, counting the crossings
     // (+1 through the upper face) as exchange_owned adds them to msd_domain_cross
     const int3 w = wrap_shift(rb, p);
-    if (w.x) p.x += w.x > 0 ? -rb.L[0] : rb.L[0];
-    if (w.y) p.y += w.y > 0 ? -rb.L[1] : rb.L[1];
-    if (w.z) p.z += w.z > 0 ? -rb.L[2] : rb.L[2];
-    d.pos[i] = p;
-    if (d.img && (w.x | w.y | w.z)) {
-      int4 m = d.img[i];
-      m.x += w.x; m.y += w.y; m.z += w.z;
-      d.img[i] = m;
+    if (w.x | w.y | w.z) {  // the few atoms that left the box
+      if (w.x) p.x += w.x > 0 ? -rb.L[0] : rb.L[0];
+      if (w.y) p.y += w.y > 0 ? -rb.L[1] : rb.L[1];
+      if (w.z) p.z += w.z > 0 ? -rb.L[2] : rb.L[2];
+      d.pos[i] = p;
+      if (d.img) {
+        int4 m = d.img[i];
+        m.x += w.x; m.y += w.y; m.z += w.z;
+        d.img[i] = m;
+      }
     }
     const double ux = (p.x - rb.lo[0]) * rb.inv_w[0], uy = (p.y - rb.lo[1]) * rb.inv_w[1],
                  uz = (p.z - rb.lo[2]) * rb.inv_w[2];
@@ -262,8 +283,10 @@ __global__ void __launch_bounds__(256) k_bin(Dev d, Box b, int forced) {
 
 // One block per replica: exclusive scan of its cell counts, starting at the
 // replica's first slot; the padding cell counts the replica's padding slots.
-// Tiles of 4 x 1024 counts, a warp-shuffle block scan per tile, a running carry.
-// Zeroes the counts and cursors it read.
+// Tiles of SCAN_V x 1024 counts (all of a tile's loads in flight at once), a
+// warp-shuffle block scan per tile, a running carry.  Zeroes the counts and
+// cursors it read.
+constexpr int SCAN_V = 4;
 __global__ void __launch_bounds__(1024) k_scan_rep(Dev d, Box b, int forced) {
   const int rep = blockIdx.x;
   if (!rebuild_on(b, rep, forced)) return;
@@ -274,14 +297,15 @@ __global__ void __launch_bounds__(1024) k_scan_rep(Dev d, Box b, int forced) {
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
   if (t == 0) carry_s = rb.slot_off;
   __syncthreads();
-  for (int base = 0; base < m; base += 4 * 1024) {
-    int v[4], s = 0;
+  for (int base = 0; base < m; base += SCAN_V * 1024) {
+    int v[SCAN_V], s = 0;
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int k = base + 4 * t + u;
+    for (int u = 0; u < SCAN_V; ++u) {
+      const int k = base + SCAN_V * t + u;
       v[u] = k < m ? (k == m - 1 ? rb.pad : d.cell_count[off + k]) : 0;
-      s += v[u];
     }
+#pragma unroll
+    for (int u = 0; u < SCAN_V; ++u) s += v[u];
     int inc = s;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -302,8 +326,8 @@ __global__ void __launch_bounds__(1024) k_scan_rep(Dev d, Box b, int forced) {
     __syncthreads();
     int run = carry_s + inc - s + (wid ? warp_tot[wid - 1] : 0);
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int k = base + 4 * t + u;
+    for (int u = 0; u < SCAN_V; ++u) {
+      const int k = base + SCAN_V * t + u;
       if (k < m) {
         d.cell_start[off + k] = run;
         d.cell_count[off + k] = 0;
@@ -359,7 +383,9 @@ __global__ void __launch_bounds__(256) k_copy_state(Dev d, Box b, int forced) {
   if (rep < 0 || !rebuild_on(b, rep, forced)) return;
   d.t_pos[i] = d.pos[i];
   d.t_vel[i] = d.vel[i];
-  d.t_acc[i] = d.acc[i];
+  // a rebuild inside a step sits between the drift and the pair kernel, which
+  // overwrites acc: only forced builds (set-up, restores) carry it over
+  if (forced) d.t_acc[i] = d.acc[i];
   d.t_acc_old[i] = d.acc_old[i];
   d.t_type[i] = d.type[i];
   d.t_id[i] = d.id[i];
@@ -378,7 +404,7 @@ __global__ void __launch_bounds__(256) k_gather(Dev d, Box b, int forced) {
   d.pos[k] = x;
   d.pos_ref[k] = x;
   d.vel[k] = d.t_vel[o];
-  d.acc[k] = d.t_acc[o];
+  if (forced) d.acc[k] = d.t_acc[o];
   d.acc_old[k] = d.t_acc_old[o];
   d.type[k] = d.t_type[o];
   d.id[k] = d.t_id[o];
@@ -927,14 +953,30 @@ int launch_drift(const Dev &d, const Box &b, const StepConsts &sc, const LaunchC
   } else if (lc.integrator == CAVGPU_LEAP_FROG) {
     if (mixed) k_drift_lf<true><<<g, 256, 0, st>>>(d, b, sc);
     else k_drift_lf<false><<<g, 256, 0, st>>>(d, b, sc);
+  } else if (thermo < 0) {  // the velocity half only (constraint::Nve acts next)
+    if (mixed) k_lang_a<true, false, false><<<g, 256, 0, st>>>(d, b, sc, k);
+    else k_lang_a<false, false, false><<<g, 256, 0, st>>>(d, b, sc, k);
   } else {
     if (mixed) {
-      if (thermo) k_lang_a<true, true><<<g, 256, 0, st>>>(d, b, sc, k);
-      else k_lang_a<true, false><<<g, 256, 0, st>>>(d, b, sc, k);
+      if (thermo) k_lang_a<true, true, true><<<g, 256, 0, st>>>(d, b, sc, k);
+      else k_lang_a<true, false, true><<<g, 256, 0, st>>>(d, b, sc, k);
     } else {
-      if (thermo) k_lang_a<false, true><<<g, 256, 0, st>>>(d, b, sc, k);
-      else k_lang_a<false, false><<<g, 256, 0, st>>>(d, b, sc, k);
+      if (thermo) k_lang_a<false, true, true><<<g, 256, 0, st>>>(d, b, sc, k);
+      else k_lang_a<false, false, true><<<g, 256, 0, st>>>(d, b, sc, k);
     }
+  }
+  return chk();
+}
+
+int launch_lang_pos(const Dev &d, const Box &b, const StepConsts &sc, const LaunchCfg &lc, int thermo,
+                    cudaStream_t st) {
+  const int g = drift_grid_blocks(lc);
+  if (lc.precision == CAVGPU_MIXED) {
+    if (thermo) k_lang_pos<true, true><<<g, 256, 0, st>>>(d, b, sc);
+    else k_lang_pos<true, false><<<g, 256, 0, st>>>(d, b, sc);
+  } else {
+    if (thermo) k_lang_pos<false, true><<<g, 256, 0, st>>>(d, b, sc);
+    else k_lang_pos<false, false><<<g, 256, 0, st>>>(d, b, sc);
   }
   return chk();
 }

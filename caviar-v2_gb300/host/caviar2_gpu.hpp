@@ -403,7 +403,8 @@ namespace constraint {
 // on steps whose index is a multiple of `step`, velocities are scaled so that the
 // kinetic energy is energy_per_dof * dof, energy_tot, dof * kbt / 2 or
 // dof * kb * temperature / 2 (the first one set).  Runs on the device, inside the
-// step; the GPU path takes at most one Nve, with velocity Verlet or leap-frog.
+// step where the integrator calls apply_thermostat: after the closing kick (velocity
+// Verlet, leap-frog) or on the mid-step velocities (Langevin).  At most one Nve.
 class Nve : public Constraint {
  public:
   explicit Nve(Caviar2 *c) : Constraint(c) {}

@@ -87,10 +87,10 @@ typedef struct cavgpu_params {
   int64_t initial_step;           /* Md_simulator::set_initial_step: index of the first step (the
                                      Philox step counter and the Nve schedule use it) */
   /* constraint::Nve velocity rescaling (src/constraint/nve.cpp:132-184): on every step whose
-     index is a multiple of nve_step, after the closing kick and the temperature, velocities
-     are scaled by lambda so that the kinetic energy becomes the target of nve_mode.
-     Single systems with velocity Verlet or leap-frog (the Langevin integrator applies
-     thermostats mid-step); 0 = off. */
+     index is a multiple of nve_step, velocities are scaled by lambda so that the kinetic
+     energy becomes the target of nve_mode: after the closing kick and the temperature
+     (velocity Verlet, leap-frog), or after the first half kick, before the atoms move
+     (Langevin, src/md_simulator.cpp:782-793).  Single systems; 0 = off. */
   int64_t nve_step;
   int32_t nve_mode;               /* CAVGPU_NVE_ENERGY_PER_DOF, _ENERGY_TOT, _KBT, _KB_TEMPERATURE */
   int32_t nve_pad;

@@ -629,6 +629,7 @@ static int integrate_langevin(orc_sys *s) {
     for (int d = 0; d < 3; ++d)
       s->vel[3 * i + d] += s->acc[3 * i + d] * 0.5 * dt + eta[3 * i + d] * lb;
   finalize_temperature(s);
+  nve_thermostat(s); /* constraints' apply_thermostat on the mid-step velocities (:784-791) */
   finalize_pressure(s);
   for (int32_t i = 0; i < n; ++i)
     for (int d = 0; d < 3; ++d) s->pos[3 * i + d] += s->vel[3 * i + d] * lc;

@@ -280,6 +280,10 @@ def cases():
     mol = np.full(len(pos), -1, np.int32)
     mol[:400] = np.arange(400) // 4
     yield "fcc500_ignore_intra", pos, vel, typ, dict(p, ignore_intra_molecule=1, molecule_index=mol), 60
+    # constraint::Nve with the Langevin integrator (friction 0): the rescale acts on the
+    # mid-step velocities, before the atoms move; every 4 steps to k_B T = 0.6
+    pos, vel, typ, p = W.kob_andersen(n=500, seed=94)
+    yield "ka500_langevin_nve", pos, vel, typ, dict(p, lang_friction=0.0, nve={"step": 4, "mode": 2, "value": 0.6}), 40
 
 
 def main():
