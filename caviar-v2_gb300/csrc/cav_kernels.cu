@@ -484,13 +484,17 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_warp(Dev d, Box b
     if (lc >= rb.ncell) continue;  // the padding cell
     const int hs = d.cell_start[cell], he = d.cell_start[cell + 1];
     const int cx = lc % rb.nc[0], cy = (lc / rb.nc[0]) % rb.nc[1], cz = lc / (rb.nc[0] * rb.nc[1]);
-    // lane k < 27: stencil cell k's first slot and count; exclusive scan = its
-    // position in the flattened candidate sequence
+    // lane k < 27: stencil cell k's first slot and count (exclusive scan = its
+    // position in the flattened candidate sequence), list-word code and origin offset
     int kb = 0, kn = 0;
+    uint32_t kcode = 0u;
+    float kox = 0.f, koy = 0.f, koz = 0.f;
     if (lane < 27) {
       const StencilCell s = stencil_cell(rb, cx, cy, cz, lane);
       kb = d.cell_start[s.c2];
       kn = d.cell_start[s.c2 + 1] - kb;
+      kcode = (uint32_t)(mode == 0 ? s.img : lane) << CODE_SHIFT;
+      kox = s.ox; koy = s.oy; koz = s.oz;
     }
     int kpre = kn;
 #pragma unroll
@@ -519,13 +523,14 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_warp(Dev d, Box b
           const int f0 = __shfl_sync(FULL_MASK, kpre, k), cn = __shfl_sync(FULL_MASK, kn, k);
           const int lo_t = max(f0, p0), hi_t = min(f0 + cn, p0 + np);
           if (lo_t >= hi_t) continue;
-          const StencilCell s = stencil_cell(rb, cx, cy, cz, k);
           const int jb = __shfl_sync(FULL_MASK, kb, k);
-          const uint32_t code = (uint32_t)(mode == 0 ? s.img : k) << CODE_SHIFT;
+          const uint32_t code = __shfl_sync(FULL_MASK, kcode, k);
+          const float ox = __shfl_sync(FULL_MASK, kox, k), oy = __shfl_sync(FULL_MASK, koy, k),
+                      oz = __shfl_sync(FULL_MASK, koz, k);
           for (int t = lo_t + lane; t < hi_t; t += 32) {
             const int j = jb + (t - f0);
             const float4 rj = __ldg(&d.rel[j]);
-            stage[t - p0] = make_float4(rj.x + s.ox, rj.y + s.oy, rj.z + s.oz, __uint_as_float((uint32_t)j | code));
+            stage[t - p0] = make_float4(rj.x + ox, rj.y + oy, rj.z + oz, __uint_as_float((uint32_t)j | code));
           }
         }
         const int npad32 = (np + 31) & ~31;
