@@ -455,23 +455,45 @@ __device__ inline StencilCell stencil_cell(const RepBox &rb, int cx, int cy, int
 
 // One warp per home cell, one lane per home atom (cells of more than 32 atoms
 // take several groups).  The warp first stages the 27 stencil cells' atoms, in
-// stencil order and slot order inside a cell, into its slice of shared memory as
-// {x, y, z relative to the home cell's origin, list word j | code}, padded to a
-// multiple of 32 with far-away entries; stencils of more than BUILD_STAGE
-// candidates are staged in passes.  The sweep takes 32 candidates at a time:
-// every candidate is one shared-memory broadcast tested by all home atoms, the
-// results collect in a hit and a band bit mask per lane (one warp vote per 32
-// candidates for the rare exact FP64 test), and only then are the hits (~15% of
-// the candidates) written, in candidate order.  Hits append to the lane's own
-// row, so the list keeps the stencil order (deterministic, independent of the
-// launch shape).
+// stencil order and slot order inside a cell, into its slice of shared memory,
+// candidates u and u+1 (u even) interleaved as {x_u, x_u+1, y_u, y_u+1} and
+// {z_u, z_u+1, word_u, word_u+1} (coordinates relative to the home cell's origin,
+// word = j | code), padded to a multiple of 32 with far-away entries; stencils of
+// more than BUILD_STAGE candidates are staged in passes.  The sweep takes 32
+// candidates at a time, two per packed FP32x2 distance evaluation: every pair of
+// candidates is two shared-memory broadcasts tested by all home atoms, the results
+// collect in a hit and a band bit mask per lane (one warp vote per 32 candidates
+// for the rare exact FP64 test), and only then are the hits (~15% of the
+// candidates) written, in candidate order.  Hits append to the lane's own row, so
+// the list keeps the stencil order (deterministic, independent of the launch shape).
 constexpr int BUILD_WARPS = 8;    // warps per block
 constexpr int BUILD_STAGE = 256;  // staged candidates per warp and pass (4 KiB)
+
+// q_u, q_u+1 = |c - r|^2 of two candidates with packed FP32x2 arithmetic (sm_100+):
+// (cx - rx)^2, then + (cy - ry)^2, then + (cz - rz)^2, each rounded once
+__device__ __forceinline__ void dist2_pair(const float4 &xy, const float2 &z, unsigned long long rxx,
+                                           unsigned long long ryy, unsigned long long rzz, float &q0, float &q1) {
+  asm("{\n\t.reg .b64 c, dd, q;\n\t"
+      "mov.b64 c, {%2, %3};\n\tsub.rn.f32x2 dd, c, %8;\n\tmul.rn.f32x2 q, dd, dd;\n\t"
+      "mov.b64 c, {%4, %5};\n\tsub.rn.f32x2 dd, c, %9;\n\tfma.rn.f32x2 q, dd, dd, q;\n\t"
+      "mov.b64 c, {%6, %7};\n\tsub.rn.f32x2 dd, c, %10;\n\tfma.rn.f32x2 q, dd, dd, q;\n\t"
+      "mov.b64 {%0, %1}, q;\n\t}"
+      : "=f"(q0), "=f"(q1)
+      : "f"(xy.x), "f"(xy.y), "f"(xy.z), "f"(xy.w), "f"(z.x), "f"(z.y), "l"(rxx), "l"(ryy), "l"(rzz));
+}
+
+__device__ __forceinline__ unsigned long long pack2(float v) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %1};" : "=l"(r) : "f"(v));
+  return r;
+}
 
 __global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_warp(Dev d, Box b, int mode, int forced) {
   __shared__ float4 stage_all[BUILD_WARPS][BUILD_STAGE];
   const int lane = threadIdx.x & 31;
-  float4 *stage = stage_all[threadIdx.x >> 5];
+  // pair p = candidates 2p, 2p+1: sxy[p] = {x, x', y, y'}, szw[p] = {z, z', word, word'}
+  float4 *sxy = stage_all[threadIdx.x >> 5], *szw = sxy + BUILD_STAGE / 2;
+  float *fxy = reinterpret_cast<float *>(sxy), *fzw = reinterpret_cast<float *>(szw);
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
   const int cap = d.cap;
   const int cshift = 7 - log2_pow2(d.tpa);  // chunk stride 4A words = 2^(log2 A + 2)
@@ -509,6 +531,7 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_warp(Dev d, Box b
       const int i = h0 + lane;
       const bool act = i < he;
       const float4 ri = act ? d.rel[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+      const unsigned long long rxx = pack2(ri.x), ryy = pack2(ri.y), rzz = pack2(ri.z);
       const float lo = b.ce2_lo;
       const float hi = act ? b.ce2_hi : -1.0f;  // idle lanes never hit
       // the atom itself: stencil cell 13 (the home cell, image zero), at its rank in the cell
@@ -530,22 +553,36 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_warp(Dev d, Box b
           for (int t = lo_t + lane; t < hi_t; t += 32) {
             const int j = jb + (t - f0);
             const float4 rj = __ldg(&d.rel[j]);
-            stage[t - p0] = make_float4(rj.x + ox, rj.y + oy, rj.z + oz, __uint_as_float((uint32_t)j | code));
+            const int e = ((t - p0) >> 1) * 4 + ((t - p0) & 1);
+            fxy[e] = rj.x + ox;
+            fxy[e + 2] = rj.y + oy;
+            fzw[e] = rj.z + oz;
+            fzw[e + 2] = __uint_as_float((uint32_t)j | code);
           }
         }
         const int npad32 = (np + 31) & ~31;
-        for (int t = np + lane; t < npad32; t += 32) stage[t] = make_float4(1e18f, 1e18f, 1e18f, 0.f);
+        for (int t = np + lane; t < npad32; t += 32) {
+          const int e = (t >> 1) * 4 + (t & 1);
+          fxy[e] = 1e18f;
+          fxy[e + 2] = 1e18f;
+          fzw[e] = 1e18f;
+          fzw[e + 2] = 0.f;
+        }
         __syncwarp();
         for (int t0 = 0; t0 < npad32; t0 += 32) {
           // phase 1: bits of the sure hits (q < ce2_lo) and of everything up to ce2_hi
           uint32_t hm = 0u, am = 0u;
 #pragma unroll
-          for (int u = 0; u < 32; ++u) {
-            const float4 c = stage[t0 + u];  // broadcast
-            const float fx = c.x - ri.x, fy = c.y - ri.y, fz = c.z - ri.z;
-            const float q = fx * fx + fy * fy + fz * fz;
-            if (q < lo) hm |= 1u << u;
-            if (q <= hi) am |= 1u << u;
+          for (int u = 0; u < 32; u += 2) {
+            const int pr = (t0 + u) >> 1;
+            const float4 xy = sxy[pr];                                  // broadcast
+            const float2 z = *reinterpret_cast<const float2 *>(&szw[pr]);  // broadcast
+            float q0, q1;
+            dist2_pair(xy, z, rxx, ryy, rzz, q0, q1);
+            if (q0 < lo) hm |= 1u << u;
+            if (q0 <= hi) am |= 1u << u;
+            if (q1 < lo) hm |= 2u << u;
+            if (q1 <= hi) am |= 2u << u;
           }
           const int ts = tself - (p0 + t0);  // the atom itself is no candidate
           if (ts >= 0 && ts < 32) am &= ~(1u << ts);
@@ -555,7 +592,7 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_warp(Dev d, Box b
             while (bm) {
               const int u = __ffs(bm) - 1;
               bm &= bm - 1u;
-              const uint32_t w = __float_as_uint(stage[t0 + u].w);
+              const uint32_t w = __float_as_uint(fzw[((t0 + u) >> 1) * 4 + 2 + (u & 1)]);
               const int code = (int)(w >> CODE_SHIFT);
               int img = code;
               if (mode != 0) {  // recover the image from the stencil index
@@ -571,7 +608,7 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_warp(Dev d, Box b
           while (hm) {
             const int u = __ffs(hm) - 1;
             hm &= hm - 1u;
-            const uint32_t w = __float_as_uint(stage[t0 + u].w);
+            const uint32_t w = __float_as_uint(fzw[((t0 + u) >> 1) * 4 + 2 + (u & 1)]);
             if (d.mol && d.mol[w & IDX_MASK] == mol_i) continue;
             if (cnt < cap) row[((cnt >> 2) << cshift) + (cnt & 3)] = w;
             ++cnt;
