@@ -811,24 +811,52 @@ void Atom_writer::dump_msd_serial(int64_t i, double t) {
   }
   if (n != msd_initial_position.size()) caviar_->log.error_all("  (pos.size != msd_initial_position.size())");
   const auto &L = domain->size_global;
-  double sum_dr_sq = 0.0;
-  int cross[3] = {0, 0, 0};
-  int count = 0;
-  for (size_t j = 0; j < n; ++j) {
-    if (msd_type > -1 && o.type[j] != static_cast<unsigned int>(msd_type)) continue;
-    const auto &c = o.msd_domain_cross[j];
-    double dx = msd_initial_position[j].x - pos[j].x;
-    double dy = msd_initial_position[j].y - pos[j].y;
-    double dz = msd_initial_position[j].z - pos[j].z;
-    dx += c.x * L.x;
-    dy += c.y * L.y;
-    dz += c.z * L.z;
-    cross[0] += c.x;
-    cross[1] += c.x;
-    cross[2] += c.x;
-    sum_dr_sq += dx * dx + dy * dy + dz * dz;
-    ++count;
+  // chunks of 65536 atoms summed on worker threads, then folded in chunk order (the
+  // same sum for any thread count; one chunk is the reference's sequential sum)
+  struct Part {
+    double sum = 0.0;
+    long long cross = 0;
+    long long count = 0;
+  };
+  constexpr size_t CHUNK = 65536;
+  const size_t nchunk = std::max<size_t>(1, (n + CHUNK - 1) / CHUNK);
+  std::vector<Part> part(nchunk);
+  auto run_chunk = [&](size_t ck) {
+    Part p;
+    for (size_t j = ck * CHUNK, e = std::min(n, (ck + 1) * CHUNK); j < e; ++j) {
+      if (msd_type > -1 && o.type[j] != static_cast<unsigned int>(msd_type)) continue;
+      const auto &c = o.msd_domain_cross[j];
+      double dx = msd_initial_position[j].x - pos[j].x;
+      double dy = msd_initial_position[j].y - pos[j].y;
+      double dz = msd_initial_position[j].z - pos[j].z;
+      dx += c.x * L.x;
+      dy += c.y * L.y;
+      dz += c.z * L.z;
+      p.cross += c.x;  // the reference adds the x count to all three totals
+      p.sum += dx * dx + dy * dy + dz * dz;
+      ++p.count;
+    }
+    part[ck] = p;
+  };
+  const size_t nthread = std::min<size_t>(nchunk, std::max(1u, std::thread::hardware_concurrency()));
+  if (nthread <= 1) {
+    for (size_t ck = 0; ck < nchunk; ++ck) run_chunk(ck);
+  } else {
+    std::vector<std::thread> th;
+    for (size_t w = 0; w < nthread; ++w)
+      th.emplace_back([&, w] {
+        for (size_t ck = w; ck < nchunk; ck += nthread) run_chunk(ck);
+      });
+    for (auto &x : th) x.join();
   }
+  double sum_dr_sq = 0.0;
+  long long cx = 0, count = 0;
+  for (const Part &p : part) {
+    sum_dr_sq += p.sum;
+    cx += p.cross;
+    count += p.count;
+  }
+  const int cross[3] = {(int)cx, (int)cx, (int)cx};
   const double msd = count > 0 ? sum_dr_sq / count : 0.0;
   append_int(s, i);
   s.push_back(' ');
