@@ -46,12 +46,18 @@ def build(verbose=False):
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
+    # test helper: cuRAND's Philox4x32-10 blocks (tests/test_gpu_philox.py)
+    cmd = [NVCC, *ARCH, "-O2", "-std=c++17", os.path.join(ROOT, "tests", "cpp", "philox_curand.cu"), "-o", PHILOX]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed on philox_curand.cu:\n{r.stderr}")
     build_host()
     return LIB
 
 
 HOST_LIB = os.path.join(HERE, "libcaviar2_gpu.so")
 HOST_HARNESS = os.path.join(OBJ, "host_harness")
+PHILOX = os.path.join(OBJ, "philox_curand")
 LJ_MD = os.path.join(OBJ, "lj_md")
 
 
