@@ -86,6 +86,40 @@ __device__ inline void load_tab(const Dev &d, Tab &tab) {
   for (int k = threadIdx.x; k < nt; k += blockDim.x) { tab.minv[k] = T.minv[k]; tab.mass[k] = T.mass[k]; }
 }
 
+// Two FP32 values in one 64-bit register for the packed FP32x2 arithmetic of sm_100+
+// (add/sub/mul/fma .rn.f32x2: each half rounded exactly as the scalar instruction).
+struct F2 {
+  unsigned long long v;
+};
+__device__ __forceinline__ F2 f2(float a, float b) {
+  F2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void unf2(F2 x, float &a, float &b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(x.v));
+}
+__device__ __forceinline__ F2 add2(F2 a, F2 b) {
+  F2 r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+  return r;
+}
+__device__ __forceinline__ F2 sub2(F2 a, F2 b) {
+  F2 r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+  return r;
+}
+__device__ __forceinline__ F2 mul2(F2 a, F2 b) {
+  F2 r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+  return r;
+}
+__device__ __forceinline__ F2 fma2(F2 a, F2 b, F2 c) {
+  F2 r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(a.v), "l"(b.v), "l"(c.v));
+  return r;
+}
+
 // A list chunk: read once per step and larger than L1, so it is not allocated in L1
 // (which keeps the neighbour coordinates the gathers reuse).
 __device__ __forceinline__ uint4 ld_list(const uint4 *p) {
@@ -105,6 +139,8 @@ __device__ __forceinline__ void mixed_pairs(const uint4 *row4, int nn, int t, co
                                             const SmemTabF &tab, const OneType c1, const float4 wf,
                                             const float4 wl, const float jtol, Gather gather, float &ax,
                                             float &ay, float &az, float &vr, float &pp) {
+  // single type: packed accumulators (even and odd list entries), folded at the end
+  F2 ax2 = f2(0.f, 0.f), ay2 = ax2, az2 = ax2, vr2 = ax2, pp2 = ax2;
   uint4 nxt = 4 * t < nn ? ld_list(row4) : make_uint4(0, 0, 0, 0);
   for (int q = 0, k0 = 4 * t; k0 < nn; ++q, k0 += 4 * TPA) {
     const uint4 w4 = nxt;
@@ -114,6 +150,52 @@ __device__ __forceinline__ void mixed_pairs(const uint4 *row4, int nn, int t, co
 #pragma unroll
     for (int u = 0; u < 4; ++u)  // four independent gathers in flight
       if (k0 + u < nn) rj[u] = gather(e[u]);
+      else rj[u] = make_float4(1e18f, 1e18f, 1e18f, 0.f);  // beyond every cutoff
+    if constexpr (ONE) {
+      // two pairs per packed FP32x2 evaluation; out-of-range pairs get coef = 0
+#pragma unroll
+      for (int a = 0; a < 4; a += 2) {
+        if (k0 + a >= nn) break;
+        float dd[6];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int code = e[a + h] >> CODE_SHIFT;
+          const int kz = (code * 57) >> 9, r9 = code - 9 * kz, ky = (r9 * 11) >> 5, kx = r9 - 3 * ky;
+          dd[h] = (float)(kx - 1); dd[2 + h] = (float)(ky - 1); dd[4 + h] = (float)(kz - 1);
+        }
+        const F2 ddx = f2(dd[0], dd[1]), ddy = f2(dd[2], dd[3]), ddz = f2(dd[4], dd[5]);
+        const F2 dx = fma2(ddx, f2(wl.x, wl.x), fma2(ddx, f2(wf.x, wf.x), sub2(f2(rj[a].x, rj[a + 1].x), f2(ri.x, ri.x))));
+        const F2 dy = fma2(ddy, f2(wl.y, wl.y), fma2(ddy, f2(wf.y, wf.y), sub2(f2(rj[a].y, rj[a + 1].y), f2(ri.y, ri.y))));
+        const F2 dz = fma2(ddz, f2(wl.z, wl.z), fma2(ddz, f2(wf.z, wf.z), sub2(f2(rj[a].z, rj[a + 1].z), f2(ri.z, ri.z))));
+        const F2 r2d = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+        float r2a, r2b;
+        unf2(r2d, r2a, r2b);
+        const bool ina = r2a <= c1.rc2, inb = r2b <= c1.rc2;
+        if (!(ina || inb)) continue;
+        const float r2ca = fmaxf(r2a, jtol), r2cb = fmaxf(r2b, jtol);  // Lj jump_fix floor
+        const F2 r2 = f2(r2ca, r2cb), r2i = f2(rcp_approx(r2ca), rcp_approx(r2cb));
+        const F2 s2 = mul2(f2(c1.sig2, c1.sig2), r2i);
+        const F2 s6 = mul2(mul2(s2, s2), s2);
+        const F2 w = mul2(mul2(f2(c1.eps4, c1.eps4), r2i), s6);
+        F2 coef = fma2(w, fma2(f2(-12.0f, -12.0f), s6, f2(6.0f, 6.0f)), f2(-c1.gc, -c1.gc));
+        float ca, cb;
+        unf2(coef, ca, cb);
+        ca = ina ? ca : 0.0f;
+        cb = inb ? cb : 0.0f;
+        coef = f2(ca, cb);
+        ax2 = fma2(coef, dx, ax2);
+        ay2 = fma2(coef, dy, ay2);
+        az2 = fma2(coef, dz, az2);
+        if (EV) {
+          vr2 = fma2(f2(-ca, -cb), r2, vr2);
+          const F2 pe = sub2(sub2(mul2(f2(c1.eps4, c1.eps4), sub2(mul2(s6, s6), s6)), f2(c1.uc, c1.uc)),
+                             mul2(f2(0.5f * c1.gc, 0.5f * c1.gc), sub2(r2, f2(c1.rc2, c1.rc2))));
+          float pa, pb;
+          unf2(pe, pa, pb);
+          pp2 = add2(pp2, f2(ina ? pa : 0.0f, inb ? pb : 0.0f));
+        }
+      }
+    } else {
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       if (k0 + u >= nn) break;
@@ -149,6 +231,17 @@ __device__ __forceinline__ void mixed_pairs(const uint4 *row4, int nn, int t, co
           pp += eps4 * (s6 * s6 - s6) - uc - 0.5f * gc * (r2 - rc2);
         }
       }
+    }
+    }
+  }
+  if constexpr (ONE) {
+    float lo, hi;
+    unf2(ax2, lo, hi); ax += lo + hi;
+    unf2(ay2, lo, hi); ay += lo + hi;
+    unf2(az2, lo, hi); az += lo + hi;
+    if (EV) {
+      unf2(vr2, lo, hi); vr += lo + hi;
+      unf2(pp2, lo, hi); pp += lo + hi;
     }
   }
 }
