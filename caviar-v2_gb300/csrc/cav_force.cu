@@ -133,13 +133,22 @@ __device__ __forceinline__ uint4 ld_list(const uint4 *p) {
 // Mixed-form pair loop of one lane: list chunks t, t+TPA, ... of atom i (four words
 // per 128-bit load; the next chunk's load and four neighbour coordinates in
 // flight); `gather(word)` returns the neighbour's float4 (global memory or a
-// shared-memory stage).  ONE: single-type system, pair constants in registers.
+// shared-memory stage).  Two pairs go through each packed FP32x2 evaluation (even
+// and odd list entries, with their own accumulators, folded at the end); a pair
+// beyond its cutoff gets coef = 0.  ONE: single-type system, pair constants in
+// registers; otherwise from the shared-memory table.
+//
+// ((r_j - r_i) + d wf) + d wlo, each sum rounded once (d wf and d wlo are exact
+// products): rounding is symmetric under negation and i seen from j has offset -d,
+// so d_ji = -d_ij bit for bit and the FP32 pair forces obey Newton's third law
+// exactly (each half of a packed operation rounds as the scalar one).  d comes from
+// the stencil index k = (dx+1) + 3 (dy+1) + 9 (dz+1) by integer arithmetic (a table
+// in shared memory would load the L1 pipe that the neighbour gathers saturate).
 template <int TPA, bool EV, bool ONE, class Gather>
 __device__ __forceinline__ void mixed_pairs(const uint4 *row4, int nn, int t, const float4 ri, int ti, int nt,
                                             const SmemTabF &tab, const OneType c1, const float4 wf,
                                             const float4 wl, const float jtol, Gather gather, float &ax,
                                             float &ay, float &az, float &vr, float &pp) {
-  // single type: packed accumulators (even and odd list entries), folded at the end
   F2 ax2 = f2(0.f, 0.f), ay2 = ax2, az2 = ax2, vr2 = ax2, pp2 = ax2;
   uint4 nxt = 4 * t < nn ? ld_list(row4) : make_uint4(0, 0, 0, 0);
   for (int q = 0, k0 = 4 * t; k0 < nn; ++q, k0 += 4 * TPA) {
@@ -150,99 +159,66 @@ __device__ __forceinline__ void mixed_pairs(const uint4 *row4, int nn, int t, co
 #pragma unroll
     for (int u = 0; u < 4; ++u)  // four independent gathers in flight
       if (k0 + u < nn) rj[u] = gather(e[u]);
-      else rj[u] = make_float4(1e18f, 1e18f, 1e18f, 0.f);  // beyond every cutoff
-    if constexpr (ONE) {
-      // two pairs per packed FP32x2 evaluation; out-of-range pairs get coef = 0
+      else rj[u] = make_float4(1e18f, 1e18f, 1e18f, __int_as_float(ti));  // beyond every cutoff
 #pragma unroll
-      for (int a = 0; a < 4; a += 2) {
-        if (k0 + a >= nn) break;
-        float dd[6];
+    for (int a = 0; a < 4; a += 2) {
+      if (k0 + a >= nn) break;
+      float dd[6];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const int code = e[a + h] >> CODE_SHIFT;
-          const int kz = (code * 57) >> 9, r9 = code - 9 * kz, ky = (r9 * 11) >> 5, kx = r9 - 3 * ky;
-          dd[h] = (float)(kx - 1); dd[2 + h] = (float)(ky - 1); dd[4 + h] = (float)(kz - 1);
-        }
-        const F2 ddx = f2(dd[0], dd[1]), ddy = f2(dd[2], dd[3]), ddz = f2(dd[4], dd[5]);
-        const F2 dx = fma2(ddx, f2(wl.x, wl.x), fma2(ddx, f2(wf.x, wf.x), sub2(f2(rj[a].x, rj[a + 1].x), f2(ri.x, ri.x))));
-        const F2 dy = fma2(ddy, f2(wl.y, wl.y), fma2(ddy, f2(wf.y, wf.y), sub2(f2(rj[a].y, rj[a + 1].y), f2(ri.y, ri.y))));
-        const F2 dz = fma2(ddz, f2(wl.z, wl.z), fma2(ddz, f2(wf.z, wf.z), sub2(f2(rj[a].z, rj[a + 1].z), f2(ri.z, ri.z))));
-        const F2 r2d = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
-        float r2a, r2b;
-        unf2(r2d, r2a, r2b);
-        const bool ina = r2a <= c1.rc2, inb = r2b <= c1.rc2;
-        if (!(ina || inb)) continue;
-        const float r2ca = fmaxf(r2a, jtol), r2cb = fmaxf(r2b, jtol);  // Lj jump_fix floor
-        const F2 r2 = f2(r2ca, r2cb), r2i = f2(rcp_approx(r2ca), rcp_approx(r2cb));
-        const F2 s2 = mul2(f2(c1.sig2, c1.sig2), r2i);
-        const F2 s6 = mul2(mul2(s2, s2), s2);
-        const F2 w = mul2(mul2(f2(c1.eps4, c1.eps4), r2i), s6);
-        F2 coef = fma2(w, fma2(f2(-12.0f, -12.0f), s6, f2(6.0f, 6.0f)), f2(-c1.gc, -c1.gc));
-        float ca, cb;
-        unf2(coef, ca, cb);
-        ca = ina ? ca : 0.0f;
-        cb = inb ? cb : 0.0f;
-        coef = f2(ca, cb);
-        ax2 = fma2(coef, dx, ax2);
-        ay2 = fma2(coef, dy, ay2);
-        az2 = fma2(coef, dz, az2);
-        if (EV) {
-          vr2 = fma2(f2(-ca, -cb), r2, vr2);
-          const F2 pe = sub2(sub2(mul2(f2(c1.eps4, c1.eps4), sub2(mul2(s6, s6), s6)), f2(c1.uc, c1.uc)),
-                             mul2(f2(0.5f * c1.gc, 0.5f * c1.gc), sub2(r2, f2(c1.rc2, c1.rc2))));
-          float pa, pb;
-          unf2(pe, pa, pb);
-          pp2 = add2(pp2, f2(ina ? pa : 0.0f, inb ? pb : 0.0f));
-        }
+      for (int h = 0; h < 2; ++h) {
+        const int code = e[a + h] >> CODE_SHIFT;
+        const int kz = (code * 57) >> 9, r9 = code - 9 * kz, ky = (r9 * 11) >> 5, kx = r9 - 3 * ky;  // k/9, k/3
+        dd[h] = (float)(kx - 1); dd[2 + h] = (float)(ky - 1); dd[4 + h] = (float)(kz - 1);
       }
-    } else {
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      if (k0 + u >= nn) break;
-      // ((r_j - r_i) + d wf) + d wlo, each sum rounded once (d wf and d wlo are exact
-      // products): rounding is symmetric under negation and i seen from j has offset
-      // -d, so d_ji = -d_ij bit for bit and the FP32 pair forces obey Newton's third
-      // law exactly.  d comes from the stencil index k = (dx+1) + 3 (dy+1) + 9 (dz+1)
-      // by integer arithmetic (a table in shared memory would load the L1 pipe that
-      // the neighbour gathers saturate).
-      const int code = e[u] >> CODE_SHIFT;
-      const int kz = (code * 57) >> 9, r9 = code - 9 * kz, ky = (r9 * 11) >> 5, kx = r9 - 3 * ky;  // k/9, k/3
-      const float ddx = (float)(kx - 1), ddy = (float)(ky - 1), ddz = (float)(kz - 1);
-      const float dx = fmaf(ddx, wl.x, fmaf(ddx, wf.x, rj[u].x - ri.x));
-      const float dy = fmaf(ddy, wl.y, fmaf(ddy, wf.y, rj[u].y - ri.y));
-      const float dz = fmaf(ddz, wl.z, fmaf(ddz, wf.z, rj[u].z - ri.z));
-      const float r2d = dx * dx + dy * dy + dz * dz;
-      float rc2, sig2, eps4, gc, uc;
+      const F2 ddx = f2(dd[0], dd[1]), ddy = f2(dd[2], dd[3]), ddz = f2(dd[4], dd[5]);
+      const F2 dx = fma2(ddx, f2(wl.x, wl.x), fma2(ddx, f2(wf.x, wf.x), sub2(f2(rj[a].x, rj[a + 1].x), f2(ri.x, ri.x))));
+      const F2 dy = fma2(ddy, f2(wl.y, wl.y), fma2(ddy, f2(wf.y, wf.y), sub2(f2(rj[a].y, rj[a + 1].y), f2(ri.y, ri.y))));
+      const F2 dz = fma2(ddz, f2(wl.z, wl.z), fma2(ddz, f2(wf.z, wf.z), sub2(f2(rj[a].z, rj[a + 1].z), f2(ri.z, ri.z))));
+      const F2 r2d = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+      float r2a, r2b;
+      unf2(r2d, r2a, r2b);
+      float rc2a, rc2b, sg2a, sg2b, e4a, e4b, gca, gcb, uca, ucb;
       if (ONE) {
-        rc2 = c1.rc2; sig2 = c1.sig2; eps4 = c1.eps4; gc = c1.gc; uc = c1.uc;
+        rc2a = rc2b = c1.rc2; sg2a = sg2b = c1.sig2; e4a = e4b = c1.eps4; gca = gcb = c1.gc; uca = ucb = c1.uc;
       } else {
-        const int tt = ti * nt + __float_as_int(rj[u].w);
-        rc2 = tab.rc2[tt]; sig2 = tab.sig2[tt]; eps4 = tab.eps4[tt]; gc = tab.gc[tt]; uc = tab.uc[tt];
+        const int ta = ti * nt + __float_as_int(rj[a].w), tb = ti * nt + __float_as_int(rj[a + 1].w);
+        rc2a = tab.rc2[ta]; sg2a = tab.sig2[ta]; e4a = tab.eps4[ta]; gca = tab.gc[ta]; uca = tab.uc[ta];
+        rc2b = tab.rc2[tb]; sg2b = tab.sig2[tb]; e4b = tab.eps4[tb]; gcb = tab.gc[tb]; ucb = tab.uc[tb];
       }
-      if (r2d <= rc2) {
-        const float r2 = fmaxf(r2d, jtol);  // Lj jump_fix floor (0 when off)
-        const float r2i = rcp_approx(r2);
-        const float s2 = sig2 * r2i;
-        const float s6 = s2 * s2 * s2;
-        const float coef = eps4 * r2i * s6 * (6.0f - 12.0f * s6) - gc;
-        ax += coef * dx; ay += coef * dy; az += coef * dz;
-        if (EV) {
-          vr -= coef * r2;
-          pp += eps4 * (s6 * s6 - s6) - uc - 0.5f * gc * (r2 - rc2);
-        }
+      const bool ina = r2a <= rc2a, inb = r2b <= rc2b;
+      if (!(ina || inb)) continue;
+      const float r2ca = fmaxf(r2a, jtol), r2cb = fmaxf(r2b, jtol);  // Lj jump_fix floor (0 when off)
+      const F2 r2 = f2(r2ca, r2cb), r2i = f2(rcp_approx(r2ca), rcp_approx(r2cb));
+      const F2 eps4 = f2(e4a, e4b);
+      const F2 s2 = mul2(f2(sg2a, sg2b), r2i);
+      const F2 s6 = mul2(mul2(s2, s2), s2);
+      const F2 w = mul2(mul2(eps4, r2i), s6);
+      F2 coef = fma2(w, fma2(f2(-12.0f, -12.0f), s6, f2(6.0f, 6.0f)), f2(-gca, -gcb));
+      float ca, cb;
+      unf2(coef, ca, cb);
+      ca = ina ? ca : 0.0f;
+      cb = inb ? cb : 0.0f;
+      coef = f2(ca, cb);
+      ax2 = fma2(coef, dx, ax2);
+      ay2 = fma2(coef, dy, ay2);
+      az2 = fma2(coef, dz, az2);
+      if (EV) {
+        vr2 = fma2(f2(-ca, -cb), r2, vr2);
+        const F2 pe = sub2(sub2(mul2(eps4, sub2(mul2(s6, s6), s6)), f2(uca, ucb)),
+                           mul2(f2(0.5f * gca, 0.5f * gcb), sub2(r2, f2(rc2a, rc2b))));
+        float pa, pb;
+        unf2(pe, pa, pb);
+        pp2 = add2(pp2, f2(ina ? pa : 0.0f, inb ? pb : 0.0f));
       }
-    }
     }
   }
-  if constexpr (ONE) {
-    float lo, hi;
-    unf2(ax2, lo, hi); ax += lo + hi;
-    unf2(ay2, lo, hi); ay += lo + hi;
-    unf2(az2, lo, hi); az += lo + hi;
-    if (EV) {
-      unf2(vr2, lo, hi); vr += lo + hi;
-      unf2(pp2, lo, hi); pp += lo + hi;
-    }
+  float lo, hi;
+  unf2(ax2, lo, hi); ax += lo + hi;
+  unf2(ay2, lo, hi); ay += lo + hi;
+  unf2(az2, lo, hi); az += lo + hi;
+  if (EV) {
+    unf2(vr2, lo, hi); vr += lo + hi;
+    unf2(pp2, lo, hi); pp += lo + hi;
   }
 }
 
