@@ -283,61 +283,54 @@ __global__ void __launch_bounds__(256) k_bin(Dev d, Box b, int forced) {
 
 // One block per replica: exclusive scan of its cell counts, starting at the
 // replica's first slot; the padding cell counts the replica's padding slots.
-// Tiles of SCAN_V x 1024 counts (all of a tile's loads in flight at once), a
-// warp-shuffle block scan per tile, a running carry.  Zeroes the counts and
-// cursors it read.
-constexpr int SCAN_V = 4;
+// Warp w owns the contiguous run [w*seg, (w+1)*seg) of the m counts and walks it
+// 32 counts at a time with coalesced loads: a first pass sums the run, one scan of
+// the 32 warp sums gives every run its start, and a second pass scans the run
+// (warp shuffles, carry from lane 31) and writes the starts.  Zeroes the counts
+// and cursors it read.
 __global__ void __launch_bounds__(1024) k_scan_rep(Dev d, Box b, int forced) {
   const int rep = blockIdx.x;
   if (!rebuild_on(b, rep, forced)) return;
   const RepBox &rb = repbox(b, rep);
   const int m = rb.ncell + 1, off = rb.cell_off;
   __shared__ int warp_tot[32];
-  __shared__ int carry_s;
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-  if (t == 0) carry_s = rb.slot_off;
+  const int seg = ((m + 31) / 32 + 31) & ~31;  // counts per warp, a multiple of 32
+  const int k0 = min(m, wid * seg), k1 = min(m, k0 + seg);
+  auto count = [&](int k) { return k < k1 ? (k == m - 1 ? rb.pad : d.cell_count[off + k]) : 0; };
+  int s = 0;
+#pragma unroll 4
+  for (int k = k0 + lane; k < k1; k += 32) s += count(k);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL_MASK, s, o);
+  if (lane == 0) warp_tot[wid] = s;
   __syncthreads();
-  for (int base = 0; base < m; base += SCAN_V * 1024) {
-    int v[SCAN_V], s = 0;
+  if (wid == 0) {
+    int wv = warp_tot[lane];
 #pragma unroll
-    for (int u = 0; u < SCAN_V; ++u) {
-      const int k = base + SCAN_V * t + u;
-      v[u] = k < m ? (k == m - 1 ? rb.pad : d.cell_count[off + k]) : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(FULL_MASK, wv, o);
+      if (lane >= o) wv += y;
     }
-#pragma unroll
-    for (int u = 0; u < SCAN_V; ++u) s += v[u];
-    int inc = s;
+    warp_tot[lane] = wv;  // inclusive
+  }
+  __syncthreads();
+  int carry = rb.slot_off + (wid ? warp_tot[wid - 1] : 0);
+  for (int base = k0; base < k1; base += 32) {
+    const int k = base + lane;
+    const int v = count(k);
+    int inc = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const int y = __shfl_up_sync(FULL_MASK, inc, o);
       if (lane >= o) inc += y;
     }
-    if (lane == 31) warp_tot[wid] = inc;
-    __syncthreads();
-    if (wid == 0) {
-      int wv = warp_tot[lane];
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(FULL_MASK, wv, o);
-        if (lane >= o) wv += y;
-      }
-      warp_tot[lane] = wv;
+    if (k < k1) {
+      d.cell_start[off + k] = carry + inc - v;
+      d.cell_count[off + k] = 0;
+      d.cell_cursor[off + k] = 0;
     }
-    __syncthreads();
-    int run = carry_s + inc - s + (wid ? warp_tot[wid - 1] : 0);
-#pragma unroll
-    for (int u = 0; u < SCAN_V; ++u) {
-      const int k = base + SCAN_V * t + u;
-      if (k < m) {
-        d.cell_start[off + k] = run;
-        d.cell_count[off + k] = 0;
-        d.cell_cursor[off + k] = 0;
-      }
-      run += v[u];
-    }
-    __syncthreads();  // every thread has read carry_s and warp_tot
-    if (t == 1023) carry_s = run;
-    __syncthreads();
+    carry += __shfl_sync(FULL_MASK, inc, 31);
   }
 }
 
