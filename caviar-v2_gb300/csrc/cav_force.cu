@@ -163,14 +163,20 @@ __device__ __forceinline__ void mixed_pairs(const uint4 *row4, int nn, int t, co
 #pragma unroll
     for (int a = 0; a < 4; a += 2) {
       if (k0 + a >= nn) break;
+      // d = k - 1 for k in {0, 1, 2} without an int-to-float conversion: the float
+      // with bits 0x4B400000 | k is 12582912 + k exactly, and 12582913 is subtracted
       float dd[6];
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int code = e[a + h] >> CODE_SHIFT;
         const int kz = (code * 57) >> 9, r9 = code - 9 * kz, ky = (r9 * 11) >> 5, kx = r9 - 3 * ky;  // k/9, k/3
-        dd[h] = (float)(kx - 1); dd[2 + h] = (float)(ky - 1); dd[4 + h] = (float)(kz - 1);
+        dd[h] = __int_as_float(0x4B400000 | kx);
+        dd[2 + h] = __int_as_float(0x4B400000 | ky);
+        dd[4 + h] = __int_as_float(0x4B400000 | kz);
       }
-      const F2 ddx = f2(dd[0], dd[1]), ddy = f2(dd[2], dd[3]), ddz = f2(dd[4], dd[5]);
+      const F2 magic = f2(12582913.0f, 12582913.0f);
+      const F2 ddx = sub2(f2(dd[0], dd[1]), magic), ddy = sub2(f2(dd[2], dd[3]), magic),
+               ddz = sub2(f2(dd[4], dd[5]), magic);
       const F2 dx = fma2(ddx, f2(wl.x, wl.x), fma2(ddx, f2(wf.x, wf.x), sub2(f2(rj[a].x, rj[a + 1].x), f2(ri.x, ri.x))));
       const F2 dy = fma2(ddy, f2(wl.y, wl.y), fma2(ddy, f2(wf.y, wf.y), sub2(f2(rj[a].y, rj[a + 1].y), f2(ri.y, ri.y))));
       const F2 dz = fma2(ddz, f2(wl.z, wl.z), fma2(ddz, f2(wf.z, wf.z), sub2(f2(rj[a].z, rj[a + 1].z), f2(ri.z, ri.z))));
