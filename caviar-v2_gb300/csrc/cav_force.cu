@@ -8,6 +8,8 @@
 //   MIXED : FP32 pair arithmetic on coordinates relative to each atom's build cell
 //           (float4 x,y,z,type; cell offsets decoded from the stencil index), FP64
 //           accumulation across lanes, FP64 acceleration/velocity/reductions.
+#include <type_traits>
+
 #include "cav_common.cuh"
 
 namespace cav {
@@ -39,6 +41,7 @@ struct SmemTabD {
   double minv[MAXT], mass[MAXT];
 };
 struct SmemTabF {
+  float4 c4[MAXT * MAXT];  // {rc2, sig2, eps4, gc} of a type pair: one 128-bit load per pair
   float rc2[MAXT * MAXT], sig2[MAXT * MAXT], eps4[MAXT * MAXT], gc[MAXT * MAXT], uc[MAXT * MAXT];
   double minv[MAXT], mass[MAXT];
 };
@@ -82,6 +85,8 @@ __device__ inline void load_tab(const Dev &d, Tab &tab) {
   for (int k = threadIdx.x; k < nt * nt; k += blockDim.x) {
     tab.rc2[k] = T.rc2[k]; tab.sig2[k] = T.sig2[k]; tab.eps4[k] = T.eps4[k]; tab.gc[k] = T.gc[k];
     tab.uc[k] = T.uc[k];
+    if constexpr (std::is_same<Tab, SmemTabF>::value)
+      tab.c4[k] = make_float4(tab.rc2[k], tab.sig2[k], tab.eps4[k], tab.gc[k]);
   }
   for (int k = threadIdx.x; k < nt; k += blockDim.x) { tab.minv[k] = T.minv[k]; tab.mass[k] = T.mass[k]; }
 }
@@ -188,8 +193,11 @@ __device__ __forceinline__ void mixed_pairs(const uint4 *row4, int nn, int t, co
         rc2a = rc2b = c1.rc2; sg2a = sg2b = c1.sig2; e4a = e4b = c1.eps4; gca = gcb = c1.gc; uca = ucb = c1.uc;
       } else {
         const int ta = ti * nt + __float_as_int(rj[a].w), tb = ti * nt + __float_as_int(rj[a + 1].w);
-        rc2a = tab.rc2[ta]; sg2a = tab.sig2[ta]; e4a = tab.eps4[ta]; gca = tab.gc[ta]; uca = tab.uc[ta];
-        rc2b = tab.rc2[tb]; sg2b = tab.sig2[tb]; e4b = tab.eps4[tb]; gcb = tab.gc[tb]; ucb = tab.uc[tb];
+        const float4 pa = tab.c4[ta], pb = tab.c4[tb];
+        rc2a = pa.x; sg2a = pa.y; e4a = pa.z; gca = pa.w;
+        rc2b = pb.x; sg2b = pb.y; e4b = pb.z; gcb = pb.w;
+        uca = EV ? tab.uc[ta] : 0.0f;
+        ucb = EV ? tab.uc[tb] : 0.0f;
       }
       const bool ina = r2a <= rc2a, inb = r2b <= rc2b;
       if (!(ina || inb)) continue;
