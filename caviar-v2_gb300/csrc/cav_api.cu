@@ -576,7 +576,7 @@ int upload_common(cavgpu_ctx *c, const int64_t *counts, const double *pos3, cons
   const size_t nblk_d = (size_t)std::max((NS + 255) / 256, 1);
   d.partials_blocks = (int)nblk;
   int rc = CAVGPU_OK;
-  dbl4 **d4[] = {&d.pos, &d.vel, &d.acc, &d.acc_old, &d.pos_ref, &d.t_pos, &d.t_vel, &d.t_acc, &d.t_acc_old};
+  dbl4 **d4[] = {&d.pos, &d.vel, &d.acc, &d.pos_ref, &d.t_pos, &d.t_vel, &d.t_acc};
   for (auto pp : d4) if (!rc) rc = dalloc(c, pp, NS);
   if (!rc) rc = dalloc(c, &d.rel, NS);
   if (!rc) rc = dalloc(c, &d.rel_ref, NS);
@@ -640,7 +640,6 @@ int upload_common(cavgpu_ctx *c, const int64_t *counts, const double *pos3, cons
   CK(cudaMemcpyAsync(d.pos, hp.data(), NS * sizeof(dbl4), cudaMemcpyHostToDevice, c->st));
   CK(cudaMemcpyAsync(d.vel, hv.data(), NS * sizeof(dbl4), cudaMemcpyHostToDevice, c->st));
   CK(cudaMemsetAsync(d.acc, 0, NS * sizeof(dbl4), c->st));
-  CK(cudaMemsetAsync(d.acc_old, 0, NS * sizeof(dbl4), c->st));
   CK(cudaMemsetAsync(d.nnbr, 0, NS * sizeof(int), c->st));
   CK(cudaMemcpyAsync(d.type, ht.data(), NS * sizeof(int), cudaMemcpyHostToDevice, c->st));
   CK(cudaMemcpyAsync(d.id, hid.data(), NS * sizeof(uint32_t), cudaMemcpyHostToDevice, c->st));
@@ -873,7 +872,7 @@ int cavgpu_autotune(cavgpu_ctx *c, int32_t trial_steps, int32_t flags, int64_t *
   std::vector<double> snap_rep(c->d.thermo_rep ? 8 * (size_t)c->b.nrep : 0);
   const long long steps0 = c->steps_done, graphs0 = c->graph_launches, kern0 = c->kernel_launches;
   const bool prof0 = c->prof;
-  if (cudaMalloc(&snap, 4 * NS * sizeof(dbl4)) != cudaSuccess) { cudaGetLastError(); return CAVGPU_E_NOMEM; }
+  if (cudaMalloc(&snap, 3 * NS * sizeof(dbl4)) != cudaSuccess) { cudaGetLastError(); return CAVGPU_E_NOMEM; }
   if (cudaMalloc(&snap_i, 2 * NS * sizeof(int)) != cudaSuccess) { cudaFree(snap); cudaGetLastError(); return CAVGPU_E_NOMEM; }
   // per-slot crossing counts and molecule indices move with the atoms as well
   int4 *snap_img = nullptr;
@@ -884,10 +883,10 @@ int cavgpu_autotune(cavgpu_ctx *c, int32_t trial_steps, int32_t flags, int64_t *
     cudaFree(snap); cudaFree(snap_i); cudaFree(snap_img);
     return CAVGPU_E_NOMEM;
   }
-  dbl4 *const src4[4] = {c->d.pos, c->d.vel, c->d.acc, c->d.acc_old};
+  dbl4 *const src4[3] = {c->d.pos, c->d.vel, c->d.acc};
   int rc = CAVGPU_OK;
   auto save = [&]() {
-    for (int k = 0; k < 4 && !rc; ++k)
+    for (int k = 0; k < 3 && !rc; ++k)
       rc = cuda_rc(cudaMemcpyAsync(snap + k * NS, src4[k], NS * sizeof(dbl4), cudaMemcpyDeviceToDevice, c->st));
     if (!rc) rc = cuda_rc(cudaMemcpyAsync(snap_i, c->d.type, NS * sizeof(int), cudaMemcpyDeviceToDevice, c->st));
     if (!rc) rc = cuda_rc(cudaMemcpyAsync(snap_i + NS, c->d.id, NS * sizeof(int), cudaMemcpyDeviceToDevice, c->st));
@@ -911,7 +910,7 @@ int cavgpu_autotune(cavgpu_ctx *c, int32_t trial_steps, int32_t flags, int64_t *
     c->lc.use_seg = seg;
     c->d.tpa = tpa;
     RK(alloc_nbr(c, c->d.cap));
-    for (int k = 0; k < 4; ++k)
+    for (int k = 0; k < 3; ++k)
       CK(cudaMemcpyAsync(src4[k], snap + k * NS, NS * sizeof(dbl4), cudaMemcpyDeviceToDevice, c->st));
     CK(cudaMemcpyAsync(c->d.type, snap_i, NS * sizeof(int), cudaMemcpyDeviceToDevice, c->st));
     CK(cudaMemcpyAsync(c->d.id, snap_i + NS, NS * sizeof(int), cudaMemcpyDeviceToDevice, c->st));

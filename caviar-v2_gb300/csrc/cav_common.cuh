@@ -103,7 +103,9 @@ struct StepConsts {
 
 // Device arrays, in cell-sorted slot order.
 struct Dev {
-  dbl4 *pos, *vel, *acc, *acc_old, *pos_ref;
+  // acc holds a(t) from the pair kernel until the next pair kernel replaces it, so
+  // the velocity-Verlet kick reads it as a_old (leap-frog's drift zeroes it)
+  dbl4 *pos, *vel, *acc, *pos_ref;
   float4 *rel;                // position relative to the build cell's origin; w = type bits
   float4 *rel_ref;            // rel at the last build (mixed form: rel = rel_ref + (x - pos_ref))
   int *type;
@@ -112,7 +114,7 @@ struct Dev {
   int4 *img;                  // periodic-boundary crossings per axis (msd_domain_cross); null when not tracked
   int *mol;                   // molecule index (ignore_intra_molecule); null when off
   // rebuild scratch
-  dbl4 *t_pos, *t_vel, *t_acc, *t_acc_old;
+  dbl4 *t_pos, *t_vel, *t_acc;
   int *t_type;
   uint32_t *t_id;
   int4 *t_img;

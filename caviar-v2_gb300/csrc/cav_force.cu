@@ -276,7 +276,7 @@ __device__ __forceinline__ void finish_atom(const Dev &d, const StepConsts &sc, 
     }
   } else if (KICK == 1) {
     dbl4 v = d.vel[i];
-    const dbl4 ao = d.acc_old[i];
+    const dbl4 ao = d.acc[i];  // a(t), still in place until the store below
     if (MIXED) {
       v.x = fma(an.x + ao.x, sc.hdt, v.x);
       v.y = fma(an.y + ao.y, sc.hdt, v.y);

@@ -114,8 +114,7 @@ __global__ void __launch_bounds__(256) k_drift_vv(Dev d, Box b, StepConsts sc) {
     x.y = __dadd_rn(x.y, __dadd_rn(__dmul_rn(v.y, sc.dt), __dmul_rn(__dmul_rn(__dmul_rn(a.y, 0.5), sc.dt), sc.dt)));
     x.z = __dadd_rn(x.z, __dadd_rn(__dmul_rn(v.z, sc.dt), __dmul_rn(__dmul_rn(__dmul_rn(a.z, 0.5), sc.dt), sc.dt)));
   }
-  d.pos[i] = x;
-  d.acc_old[i] = a;
+  d.pos[i] = x;  // acc stays: the pair kernel's kick reads it as a_old
   if (MIXED) mixed_track(d, b, rep, i, x);
   else half_skin_test(d, b, rep, i, x);
 }
@@ -145,7 +144,7 @@ __global__ void __launch_bounds__(256) k_drift_lf(Dev d, Box b, StepConsts sc) {
   }
   d.pos[i] = x;
   d.vel[i] = v;
-  d.acc_old[i] = make_dbl4(0.0, 0.0, 0.0, 0.0);
+  d.acc[i] = make_dbl4(0.0, 0.0, 0.0, 0.0);  // a_old = 0 for the kick
   if (MIXED) mixed_track(d, b, rep, i, x);
   else half_skin_test(d, b, rep, i, x);
 }
@@ -376,10 +375,7 @@ __global__ void __launch_bounds__(256) k_copy_state(Dev d, Box b, int forced) {
   if (rep < 0 || !rebuild_on(b, rep, forced)) return;
   d.t_pos[i] = d.pos[i];
   d.t_vel[i] = d.vel[i];
-  // a rebuild inside a step sits between the drift and the pair kernel, which
-  // overwrites acc: only forced builds (set-up, restores) carry it over
-  if (forced) d.t_acc[i] = d.acc[i];
-  d.t_acc_old[i] = d.acc_old[i];
+  d.t_acc[i] = d.acc[i];  // a(t): the next kick reads it as a_old
   d.t_type[i] = d.type[i];
   d.t_id[i] = d.id[i];
   if (d.img) d.t_img[i] = d.img[i];
@@ -397,8 +393,7 @@ __global__ void __launch_bounds__(256) k_gather(Dev d, Box b, int forced) {
   d.pos[k] = x;
   d.pos_ref[k] = x;
   d.vel[k] = d.t_vel[o];
-  if (forced) d.acc[k] = d.t_acc[o];
-  d.acc_old[k] = d.t_acc_old[o];
+  d.acc[k] = d.t_acc[o];
   d.type[k] = d.t_type[o];
   d.id[k] = d.t_id[o];
   if (d.img) d.img[k] = d.t_img[o];
