@@ -467,7 +467,7 @@ def main():
     e2e_rate = ws * n * args.steps / max_over_ranks(ws, n * args.steps / e2e_rate)
 
     # roofline of the dominant kernel (mixed force kernel): algorithmic bytes per launch
-    #   per atom: 4 * nbar list words + rel_i 16 + nnbr 4 + vel r/w 64 + acc_old r 32 + acc w 32
+    #   per atom: 4 * nbar list words + rel_i 16 + nnbr 4 + vel r/w 64 + acc r 32 (a_old) + acc w 32
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs")
     peak_note = "measured" if hbm else "fallback"

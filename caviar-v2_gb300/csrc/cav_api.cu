@@ -442,6 +442,9 @@ int create_common(const cavgpu_params *p, int nrep, const double *lo3, const dou
   if (!rc) rc = dalloc(c, &c->d.thermo, 8);
   if (!rc) rc = dalloc(c, &c->d.step_base, 1);
   if (!rc) rc = dalloc(c, &c->d.thermo_ring, THERMO_REC * (size_t)MAX_GRAPH_STEPS);
+  if (!rc) rc = dalloc(c, &c->d.fold, 10 * (size_t)THERMO_FOLD_BLOCKS);
+  if (!rc) rc = dalloc(c, &c->d.fold_ticket, 1);
+  if (!rc) rc = cuda_rc(cudaMemsetAsync(c->d.fold_ticket, 0, sizeof(unsigned int), c->st));
   if (!rc) rc = cuda_rc(cudaMemcpyAsync(c->d.tab, &c->tab_h, sizeof(PairTab), cudaMemcpyHostToDevice, c->st));
   if (!rc) rc = cuda_rc(cudaMemsetAsync(c->d.flags, 0, F_NWORDS * sizeof(int), c->st));
   if (!rc) rc = cuda_rc(cudaMemsetAsync(c->d.thermo, 0, 8 * sizeof(double), c->st));

@@ -138,6 +138,8 @@ struct Dev {
   double *thermo_ring;        // recorded thermo points (THERMO_REC per record)
   long long *step_base;       // index of the chunk's first step (Langevin noise, Nve schedule)
   double *nve_partials;       // Nve: per-block {sum m v^2, sum m v} (4 per block, NVE_BLOCKS blocks)
+  double *fold;               // thermo fold: per-block sums of the first level (THERMO_FOLD_BLOCKS x 10)
+  unsigned int *fold_ticket;  // thermo fold: blocks done (the last one folds and resets it to 0)
   double *nve_lambda;         // Nve: the scale factor of the current step
   PairTab *tab;
   // host-order staging for downloads
@@ -264,7 +266,10 @@ constexpr int REBUILD_KERNELS = 8;  // kernels launch_rebuild enqueues
 // thermo: virial/PE partials (and KE partials unless kick == 2).
 int launch_force(const Dev &d, const Box &b, const StepConsts &sc, const LaunchCfg &lc, int kick, int thermo,
                  int k_in_chunk, cudaStream_t st);
-// nb_ke_end > 0 (Langevin): KE from partials_ke_end, the temperature from partials_ke
+// nb_ke_end > 0 (Langevin): KE from partials_ke_end, the temperature from partials_ke.
+// Two levels in a fixed order: THERMO_FOLD_BLOCKS blocks fold strided subsets of the
+// partials, the last block to finish folds their sums (deterministic).
+constexpr int THERMO_FOLD_BLOCKS = 32;
 int launch_thermo_final(const Dev &d, const ThermoCfg &tc, int nb_ke, int nb_ev, int nb_ke_end, int ring_slot,
                         cudaStream_t st);
 // batches: per-replica KE (ke = 1, from the current velocities) and/or virial+PE folds

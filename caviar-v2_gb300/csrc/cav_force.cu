@@ -349,8 +349,12 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 1) k_force(Dev d, Box b, Step
   const int n = sc.n, cap = d.cap;
   const int warps_total = (gridDim.x * blockDim.x) >> 5;
   const int ntask = (n + A - 1) / A;
-  double ke_p[4] = {0.0, 0.0, 0.0, 0.0};
-  double ev_p[2] = {0.0, 0.0};
+  // EV: each thread's KE / virial / PE sums live in shared memory between tasks;
+  // six doubles held in registers across the pair loop spill at 64 registers
+  __shared__ double s_sum[EV ? 6 * 256 : 1];
+  if (EV)
+#pragma unroll
+    for (int q = 0; q < 6; ++q) s_sum[q * 256 + threadIdx.x] = 0.0;
   long long step = 0;
   if (KICK == 2) step = *d.step_base + k_in_chunk;
   int img_rep = -1;
@@ -424,7 +428,21 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 1) k_force(Dev d, Box b, Step
         }
       }
     }
-    finish_atom<A, MIXED, KICK, EV>(d, sc, tab, act, t, i, ti, rep, step, fx, fy, fz, vir, pe, ke_p, ev_p);
+    double ke_t[4] = {0.0, 0.0, 0.0, 0.0}, ev_t[2] = {0.0, 0.0};
+    finish_atom<A, MIXED, KICK, EV>(d, sc, tab, act, t, i, ti, rep, step, fx, fy, fz, vir, pe, ke_t, ev_t);
+    if (EV) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) s_sum[q * 256 + threadIdx.x] += ke_t[q];
+#pragma unroll
+      for (int q = 0; q < 2; ++q) s_sum[(4 + q) * 256 + threadIdx.x] += ev_t[q];
+    }
+  }
+  double ke_p[4] = {0.0, 0.0, 0.0, 0.0}, ev_p[2] = {0.0, 0.0};
+  if (EV) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) ke_p[q] = s_sum[q * 256 + threadIdx.x];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) ev_p[q] = s_sum[(4 + q) * 256 + threadIdx.x];
   }
   store_partials<KICK, EV>(d, ke_p, ev_p);
 }

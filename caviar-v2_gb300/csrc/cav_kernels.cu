@@ -667,20 +667,41 @@ __device__ inline void thermo_finish(double ke2, const double P3[3], double msum
 
 __global__ void __launch_bounds__(256) k_thermo_final(Dev d, ThermoCfg tc, int nb_ke, int nb_ev, int nb_ke_end,
                                                       int ring_slot) {
+  // level 1: block g folds partials g*256 + tid, stepping by the grid's threads (one
+  // round of independent loads for up to 8192 partials)
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
   double v[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-  for (int k = threadIdx.x; k < nb_ke; k += blockDim.x)
+  for (int k = gt; k < nb_ke; k += gs)
     for (int q = 0; q < 4; ++q) v[q] += d.partials_ke[(size_t)k * 4 + q];
   const double *ev = d.partials_ev;
-  for (int k = threadIdx.x; k < nb_ev; k += blockDim.x) {
+  for (int k = gt; k < nb_ev; k += gs) {
     v[4] += ev[(size_t)k * 2];
     v[5] += ev[(size_t)k * 2 + 1];
   }
-  for (int k = threadIdx.x; k < nb_ke_end; k += blockDim.x)
+  for (int k = gt; k < nb_ke_end; k += gs)
     for (int q = 0; q < 4; ++q) v[6 + q] += d.partials_ke_end[(size_t)k * 4 + q];
   __shared__ double out[10];
+  __shared__ bool last;
   block_sum_store<10>(v, out);
   __syncthreads();
   if (threadIdx.x == 0) {
+    for (int q = 0; q < 10; ++q) d.fold[blockIdx.x * 10 + q] = out[q];
+    __threadfence();
+    last = atomicAdd(d.fold_ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  // level 2, in the last block: the blocks' sums in block order
+  if (threadIdx.x < 10) {
+    __threadfence();
+    const volatile double *f = d.fold;
+    double s = 0.0;
+    for (int g = 0; g < (int)gridDim.x; ++g) s += f[g * 10 + threadIdx.x];
+    out[threadIdx.x] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    *d.fold_ticket = 0u;
     double res[5];
     const double P3[3] = {out[1], out[2], out[3]};
     // total mass is fixed at upload (thermo[5])
@@ -1033,7 +1054,7 @@ int launch_set_rebuild_cond(const Dev &d, cudaGraphConditionalHandle h, cudaStre
 
 int launch_thermo_final(const Dev &d, const ThermoCfg &tc, int nb_ke, int nb_ev, int nb_ke_end, int ring_slot,
                         cudaStream_t st) {
-  k_thermo_final<<<1, 256, 0, st>>>(d, tc, nb_ke, nb_ev, nb_ke_end, ring_slot);
+  k_thermo_final<<<THERMO_FOLD_BLOCKS, 256, 0, st>>>(d, tc, nb_ke, nb_ev, nb_ke_end, ring_slot);
   return chk();
 }
 
