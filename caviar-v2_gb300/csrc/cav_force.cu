@@ -42,7 +42,8 @@ struct SmemTabD {
 };
 struct SmemTabF {
   float4 c4[MAXT * MAXT];  // {rc2, sig2, eps4, gc} of a type pair: one 128-bit load per pair
-  float rc2[MAXT * MAXT], sig2[MAXT * MAXT], eps4[MAXT * MAXT], gc[MAXT * MAXT], uc[MAXT * MAXT];
+  float rc2[MAXT * MAXT], sig2[MAXT * MAXT], eps4[MAXT * MAXT], gc[MAXT * MAXT];
+  float pk[MAXT * MAXT];   // 0.5 gc rc2 - uc, rounded once from FP64: V = eps4 s6 (s6 - 1) - 0.5 gc r2 + pk
   double minv[MAXT], mass[MAXT];
 };
 // per warp: the 27 image shifts s*L (FP64) or the cell widths (mixed) of the
@@ -61,7 +62,7 @@ struct WarpImages<true> {
 
 // Single-type systems keep the pair constants in registers (no table lookups).
 struct OneType {
-  float rc2, sig2, eps4, gc, uc;
+  float rc2, sig2, eps4, gc, pk;
 };
 
 // FP32 reciprocal from the hardware approximation (PTX rcp.approx.ftz.f32): one
@@ -84,9 +85,12 @@ __device__ inline void load_tab(const Dev &d, Tab &tab) {
   const int nt = T.nt;
   for (int k = threadIdx.x; k < nt * nt; k += blockDim.x) {
     tab.rc2[k] = T.rc2[k]; tab.sig2[k] = T.sig2[k]; tab.eps4[k] = T.eps4[k]; tab.gc[k] = T.gc[k];
-    tab.uc[k] = T.uc[k];
-    if constexpr (std::is_same<Tab, SmemTabF>::value)
+    if constexpr (std::is_same<Tab, SmemTabF>::value) {
       tab.c4[k] = make_float4(tab.rc2[k], tab.sig2[k], tab.eps4[k], tab.gc[k]);
+      tab.pk[k] = (float)(0.5 * T.gc[k] * T.rc2[k] - T.uc[k]);
+    } else {
+      tab.uc[k] = T.uc[k];
+    }
   }
   for (int k = threadIdx.x; k < nt; k += blockDim.x) { tab.minv[k] = T.minv[k]; tab.mass[k] = T.mass[k]; }
 }
@@ -154,7 +158,7 @@ __device__ __forceinline__ void mixed_pairs(const uint4 *row4, int nn, int t, co
                                             const SmemTabF &tab, const OneType c1, const float4 wf,
                                             const float4 wl, const float jtol, Gather gather, float &ax,
                                             float &ay, float &az, float &vr, float &pp) {
-  F2 ax2 = f2(0.f, 0.f), ay2 = ax2, az2 = ax2, vr2 = ax2, pp2 = ax2;
+  F2 ax2 = f2(0.f, 0.f), ay2 = ax2, az2 = ax2, vr2 = ax2, pp2 = ax2;  // vr2: sum of +coef r^2
   uint4 nxt = 4 * t < nn ? ld_list(row4) : make_uint4(0, 0, 0, 0);
   for (int q = 0, k0 = 4 * t; k0 < nn; ++q, k0 += 4 * TPA) {
     const uint4 w4 = nxt;
@@ -188,16 +192,16 @@ __device__ __forceinline__ void mixed_pairs(const uint4 *row4, int nn, int t, co
       const F2 r2d = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
       float r2a, r2b;
       unf2(r2d, r2a, r2b);
-      float rc2a, rc2b, sg2a, sg2b, e4a, e4b, gca, gcb, uca, ucb;
+      float rc2a, rc2b, sg2a, sg2b, e4a, e4b, gca, gcb, pka, pkb;
       if (ONE) {
-        rc2a = rc2b = c1.rc2; sg2a = sg2b = c1.sig2; e4a = e4b = c1.eps4; gca = gcb = c1.gc; uca = ucb = c1.uc;
+        rc2a = rc2b = c1.rc2; sg2a = sg2b = c1.sig2; e4a = e4b = c1.eps4; gca = gcb = c1.gc; pka = pkb = c1.pk;
       } else {
         const int ta = ti * nt + __float_as_int(rj[a].w), tb = ti * nt + __float_as_int(rj[a + 1].w);
         const float4 pa = tab.c4[ta], pb = tab.c4[tb];
         rc2a = pa.x; sg2a = pa.y; e4a = pa.z; gca = pa.w;
         rc2b = pb.x; sg2b = pb.y; e4b = pb.z; gcb = pb.w;
-        uca = EV ? tab.uc[ta] : 0.0f;
-        ucb = EV ? tab.uc[tb] : 0.0f;
+        pka = EV ? tab.pk[ta] : 0.0f;
+        pkb = EV ? tab.pk[tb] : 0.0f;
       }
       const bool ina = r2a <= rc2a, inb = r2b <= rc2b;
       if (!(ina || inb)) continue;
@@ -217,9 +221,9 @@ __device__ __forceinline__ void mixed_pairs(const uint4 *row4, int nn, int t, co
       ay2 = fma2(coef, dy, ay2);
       az2 = fma2(coef, dz, az2);
       if (EV) {
-        vr2 = fma2(f2(-ca, -cb), r2, vr2);
-        const F2 pe = sub2(sub2(mul2(eps4, sub2(mul2(s6, s6), s6)), f2(uca, ucb)),
-                           mul2(f2(0.5f * gca, 0.5f * gcb), sub2(r2, f2(rc2a, rc2b))));
+        vr2 = fma2(coef, r2, vr2);
+        const F2 pe = fma2(mul2(eps4, s6), sub2(s6, f2(1.0f, 1.0f)),
+                           fma2(f2(-0.5f * gca, -0.5f * gcb), r2, f2(pka, pkb)));
         float pa, pb;
         unf2(pe, pa, pb);
         pp2 = add2(pp2, f2(ina ? pa : 0.0f, inb ? pb : 0.0f));
@@ -231,13 +235,13 @@ __device__ __forceinline__ void mixed_pairs(const uint4 *row4, int nn, int t, co
   unf2(ay2, lo, hi); ay += lo + hi;
   unf2(az2, lo, hi); az += lo + hi;
   if (EV) {
-    unf2(vr2, lo, hi); vr += lo + hi;
+    unf2(vr2, lo, hi); vr -= lo + hi;
     unf2(pp2, lo, hi); pp += lo + hi;
   }
 }
 
 __device__ inline OneType one_type(const SmemTabF &tab) {
-  return OneType{tab.rc2[0], tab.sig2[0], tab.eps4[0], tab.gc[0], tab.uc[0]};
+  return OneType{tab.rc2[0], tab.sig2[0], tab.eps4[0], tab.gc[0], tab.pk[0]};
 }
 
 // Folds the TPA lanes of each atom (lanes a, a+A, a+2A, ...; every lane of the warp
