@@ -155,7 +155,7 @@ int enqueue_step(cavgpu_ctx *c, int k, bool thermo, int ring_slot) {
   if (c->prof && k < (int)c->ev0.size()) CK(cudaEventRecord(c->ev0[k], c->st));
   RK(launch_force(c->d, c->b, c->sc, c->lc, is_lang(c) ? 2 : 1, thermo, k, c->st));
   if (c->prof && k < (int)c->ev1.size()) CK(cudaEventRecord(c->ev1[k], c->st));
-  c->kernel_launches += REBUILD_KERNELS + 1;
+  c->kernel_launches += rebuild_kernels(c->b) + 1;
   if (thermo) RK(enqueue_thermo_after_force(c, ring_slot));
   if (c->nve.step > 0 && !is_lang(c)) {  // constraint::Nve after the temperature (src/md_simulator.cpp:681-694)
     RK(launch_nve(c->d, c->b, c->tc, c->nve, k, thermo, ring_slot, c->st));
@@ -167,7 +167,7 @@ int enqueue_step(cavgpu_ctx *c, int k, bool thermo, int ring_slot) {
 // One MD step recorded into the graph being captured on c->st.  The rebuild
 // kernels sit in the body of an IF conditional node whose value the step's
 // half-skin flags set on the device, so steps without a rebuild launch three
-// kernels (drift, condition, force) instead of eleven.
+// kernels (drift, condition, force) instead of all the rebuild kernels as well.
 int capture_step(cavgpu_ctx *c, int k, bool thermo, int ring_slot) {
   RK(enqueue_drift(c, k, thermo));
   cudaStreamCaptureStatus cs;
@@ -306,7 +306,7 @@ int forced_build(cavgpu_ctx *c) {
     zero[F_PASSES] = f[F_PASSES];
     CK(cudaMemcpyAsync(c->d.flags, zero, sizeof(zero), cudaMemcpyHostToDevice, c->st));
     RK(launch_rebuild(c->d, c->b, c->lc, 1, c->st));
-    c->kernel_launches += REBUILD_KERNELS;
+    c->kernel_launches += rebuild_kernels(c->b);
     RK(read_flags(c, f));
     c->max_nb = f[F_MAXNB];
     if (!f[F_OVERFLOW]) return CAVGPU_OK;
@@ -443,6 +443,7 @@ int create_common(const cavgpu_params *p, int nrep, const double *lo3, const dou
   if (!rc) rc = dalloc(c, &c->d.step_base, 1);
   if (!rc) rc = dalloc(c, &c->d.thermo_ring, THERMO_REC * (size_t)MAX_GRAPH_STEPS);
   if (!rc) rc = dalloc(c, &c->d.fold, 10 * (size_t)THERMO_FOLD_BLOCKS);
+  if (!rc) rc = dalloc(c, &c->d.scan_part, (size_t)SCAN_SLICES);
   if (!rc) rc = dalloc(c, &c->d.fold_ticket, 1);
   if (!rc) rc = cuda_rc(cudaMemsetAsync(c->d.fold_ticket, 0, sizeof(unsigned int), c->st));
   if (!rc) rc = cuda_rc(cudaMemcpyAsync(c->d.tab, &c->tab_h, sizeof(PairTab), cudaMemcpyHostToDevice, c->st));
@@ -821,7 +822,7 @@ int cavgpu_run(cavgpu_ctx *c, int64_t nsteps, int64_t every, double *out5) {
   auto count_graph_rebuilds = [&]() -> int {
     int f[F_NWORDS];
     RK(read_flags(c, f));
-    if (f[F_PASSES] > rebuilds_at_start) c->kernel_launches += (long long)REBUILD_KERNELS * (f[F_PASSES] - rebuilds_at_start);
+    if (f[F_PASSES] > rebuilds_at_start) c->kernel_launches += (long long)rebuild_kernels(c->b) * (f[F_PASSES] - rebuilds_at_start);
     return CAVGPU_OK;
   };
   if (done < nsteps) RK(count_graph_rebuilds());

@@ -138,6 +138,7 @@ struct Dev {
   double *thermo_ring;        // recorded thermo points (THERMO_REC per record)
   long long *step_base;       // index of the chunk's first step (Langevin noise, Nve schedule)
   double *nve_partials;       // Nve: per-block {sum m v^2, sum m v} (4 per block, NVE_BLOCKS blocks)
+  int *scan_part;             // single system: counts per scan slice (SCAN_SLICES)
   double *fold;               // thermo fold: per-block sums of the first level (THERMO_FOLD_BLOCKS x 10)
   unsigned int *fold_ticket;  // thermo fold: blocks done (the last one folds and resets it to 0)
   double *nve_lambda;         // Nve: the scale factor of the current step
@@ -261,7 +262,11 @@ int launch_lang_pos(const Dev &d, const Box &b, const StepConsts &sc, const Laun
                     cudaStream_t st);
 int launch_rebuild(const Dev &d, const Box &b, const LaunchCfg &lc, int forced, cudaStream_t st);
 int launch_set_rebuild_cond(const Dev &d, cudaGraphConditionalHandle h, cudaStream_t st);
-constexpr int REBUILD_KERNELS = 8;  // kernels launch_rebuild enqueues
+// a single system scans its cell counts in SCAN_SLICES slices (one more kernel)
+constexpr int SCAN_SLICES = 64;
+inline int scan_slices(const Box &b) { return b.nrep == 1 ? SCAN_SLICES : 1; }
+// kernels launch_rebuild enqueues
+inline int rebuild_kernels(const Box &b) { return 8 + (scan_slices(b) > 1 ? 1 : 0); }
 // kick: 0 = force only, 1 = VV closing kick, 2 = Langevin closing update.
 // thermo: virial/PE partials (and KE partials unless kick == 2).
 int launch_force(const Dev &d, const Box &b, const StepConsts &sc, const LaunchCfg &lc, int kick, int thermo,

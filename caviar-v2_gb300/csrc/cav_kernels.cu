@@ -280,23 +280,66 @@ __global__ void __launch_bounds__(256) k_bin(Dev d, Box b, int forced) {
   }
 }
 
-// One block per replica: exclusive scan of its cell counts, starting at the
-// replica's first slot; the padding cell counts the replica's padding slots.
-// Warp w owns the contiguous run [w*seg, (w+1)*seg) of the m counts and walks it
-// 32 counts at a time with coalesced loads: a first pass sums the run, one scan of
-// the 32 warp sums gives every run its start, and a second pass scans the run
-// (warp shuffles, carry from lane 31) and writes the starts.  Zeroes the counts
-// and cursors it read.
-__global__ void __launch_bounds__(1024) k_scan_rep(Dev d, Box b, int forced) {
-  const int rep = blockIdx.x;
+// Exclusive scan of each replica's cell counts, starting at the replica's first
+// slot; the padding cell counts the replica's padding slots.  Block rep*P + p owns
+// slice p of the replica's m counts (scan_slice(m, P, p); P > 1 only for a single
+// system, whose slices start from the sums k_scan_part left in scan_part).
+// Warp w owns the contiguous run [w*seg, (w+1)*seg) of its slice and walks it 32
+// counts at a time with coalesced loads: a first pass sums the run, one scan of the
+// 32 warp sums gives every run its start, and a second pass scans the run (warp
+// shuffles, carry from lane 31) and writes the starts.  Zeroes the counts and
+// cursors it read.
+__device__ inline int2 scan_slice(int m, int P, int p) {
+  const int len = ((m + P - 1) / P + 31) & ~31;
+  const int s0 = min(m, p * len);
+  return make_int2(s0, min(m, s0 + len));
+}
+
+__device__ inline int scan_count(const Dev &d, const RepBox &rb, int m, int k) {
+  return k == m - 1 ? rb.pad : d.cell_count[rb.cell_off + k];
+}
+
+// single system: the sum of each slice's counts (first level of the scan)
+__global__ void __launch_bounds__(1024) k_scan_part(Dev d, Box b, int forced) {
+  if (!rebuild_on(b, 0, forced)) return;
+  const RepBox &rb = repbox(b, 0);
+  const int m = rb.ncell + 1;
+  const int2 sl = scan_slice(m, gridDim.x, blockIdx.x);
+  int v = 0;
+  for (int k = sl.x + (int)threadIdx.x; k < sl.y; k += blockDim.x) v += scan_count(d, rb, m, k);
+  __shared__ int warp_tot[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL_MASK, v, o);
+  if (lane == 0) warp_tot[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    v = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL_MASK, v, o);
+    if (lane == 0) d.scan_part[blockIdx.x] = v;
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_scan_rep(Dev d, Box b, int forced, int P) {
+  const int rep = blockIdx.x / P, p = blockIdx.x - rep * P;
   if (!rebuild_on(b, rep, forced)) return;
   const RepBox &rb = repbox(b, rep);
   const int m = rb.ncell + 1, off = rb.cell_off;
+  const int2 sl = scan_slice(m, P, p);
   __shared__ int warp_tot[32];
+  __shared__ int slice_base;
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-  const int seg = ((m + 31) / 32 + 31) & ~31;  // counts per warp, a multiple of 32
-  const int k0 = min(m, wid * seg), k1 = min(m, k0 + seg);
-  auto count = [&](int k) { return k < k1 ? (k == m - 1 ? rb.pad : d.cell_count[off + k]) : 0; };
+  if (wid == 0) {  // counts before this slice: the first-level sums of slices 0 .. p-1
+    int v = 0;
+    for (int q = lane; q < p; q += 32) v += d.scan_part[q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL_MASK, v, o);
+    if (lane == 0) slice_base = v;
+  }
+  const int seg = ((sl.y - sl.x + 31) / 32 + 31) & ~31;  // counts per warp, a multiple of 32
+  const int k0 = min(sl.y, sl.x + wid * seg), k1 = min(sl.y, k0 + seg);
+  auto count = [&](int k) { return k < k1 ? scan_count(d, rb, m, k) : 0; };
   int s = 0;
 #pragma unroll 4
   for (int k = k0 + lane; k < k1; k += 32) s += count(k);
@@ -314,7 +357,7 @@ __global__ void __launch_bounds__(1024) k_scan_rep(Dev d, Box b, int forced) {
     warp_tot[lane] = wv;  // inclusive
   }
   __syncthreads();
-  int carry = rb.slot_off + (wid ? warp_tot[wid - 1] : 0);
+  int carry = rb.slot_off + slice_base + (wid ? warp_tot[wid - 1] : 0);
   for (int base = k0; base < k1; base += 32) {
     const int k = base + lane;
     const int v = count(k);
@@ -1035,7 +1078,9 @@ int launch_lang_pos(const Dev &d, const Box &b, const StepConsts &sc, const Laun
 int launch_rebuild(const Dev &d, const Box &b, const LaunchCfg &lc, int forced, cudaStream_t st) {
   const int g = ceil_div(b.nslot, 256);
   k_bin<<<g, 256, 0, st>>>(d, b, forced);
-  k_scan_rep<<<b.nrep, 1024, 0, st>>>(d, b, forced);
+  const int P = scan_slices(b);
+  if (P > 1) k_scan_part<<<P, 1024, 0, st>>>(d, b, forced);
+  k_scan_rep<<<b.nrep * P, 1024, 0, st>>>(d, b, forced, P);
   k_scatter<<<g, 256, 0, st>>>(d, b, forced);
   k_cell_sort<<<ceil_div((long long)b.ncell_all * 32, 256), 256, 0, st>>>(d, b, forced);
   k_copy_state<<<g, 256, 0, st>>>(d, b, forced);
