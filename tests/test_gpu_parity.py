@@ -164,6 +164,38 @@ def test_potential_energy_matches_oracle(gpu, oracle_lib):
     s.close()
 
 
+def test_thermo_fold_with_many_block_partials(gpu, oracle_lib):
+    """500,000 atoms with 32-thread pair-kernel blocks: 15,625 block partials, so each
+    thread of the fold's first level (32 blocks x 256) sums two of them and the last
+    block folds 32 real sums.  PE and virial against the oracle; the KE recorded at
+    every step against the host sum over the downloaded velocities (n_r_df = 3: the
+    centre-of-mass part removed).
+
+    The oracle adds the ~13M pair terms of the lattice in one sequential double
+    accumulator; the terms of a shell are equal, so its rounding errors share a sign
+    and grow as n_pairs * eps (measured 2.3e-10 of the PE): the PE and virial bars
+    are that bound.  A partial lost or counted twice by the fold moves the sums by
+    ~1/15625 = 6e-5."""
+    import workloads as W
+
+    pos, vel, typ, p = W.lj_fluid((50, 50, 50), seed=11)
+    o = oracle_lib.System(pos, vel, typ, p, noise_mode=0)
+    o.setup()
+    t = o.thermo()
+    s = gpu.System(pos, vel, typ, p, tpa=1, block=32)
+    s.setup()
+    vir, pe = s.forces()
+    assert rel(pe, t["pe"]) <= 2e-9
+    assert rel(vir, t["virial"]) <= 1e-8
+    th = s.run(4, 1)
+    v = s.state()[1]
+    m = p["mass"][typ][:, None]
+    mv = (m * v).sum(0)
+    ke = 0.5 * ((m * v * v).sum() - float(mv @ mv) / m.sum())
+    assert rel(th[-1, 0], ke) <= 1e-12
+    s.close()
+
+
 def test_langevin_noise_matches_oracle(gpu, oracle_lib):
     """Philox noise keyed by (seed, id, step): GPU and oracle draw the same eta."""
     import workloads as W
