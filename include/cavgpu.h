@@ -153,7 +153,9 @@ int cavgpu_setup(cavgpu_ctx *ctx);
 int cavgpu_step(cavgpu_ctx *ctx, int64_t nsteps);
 
 /* Same as cavgpu_step, recording thermo every `every` steps into
- * out5[k*5 + {0..4}] = {KE, T, P, virialForce, PE} for k < nsteps/every. */
+ * out5[k*5 + {0..4}] = {KE, T, P, virialForce, PE} for k < nsteps/every.
+ * Both calls return once the steps and the copies into out5 have completed
+ * (they end by reading the device status word: NaN, list overflow). */
 int cavgpu_run(cavgpu_ctx *ctx, int64_t nsteps, int64_t every, double *out5);
 
 /* Recompute the force at the current positions (list rebuilt if the half-skin
