@@ -45,10 +45,39 @@ static int format_check() {
   return bad ? 1 : 0;
 }
 
+// One invalid setting per call, made through the public setters (no GPU is
+// touched).  Returns what the reference does: Log::error_all exits with status 1
+// after printing "[ERR] <message>"; a setter that throws std::runtime_error is
+// reported here as status 2 with "[EXC] <message>"; 0 = nothing was raised.
+static int error_case(const std::string &n) {
+  Caviar2 c;
+  Md_simulator &md = c.md_simulator;
+  try {
+    if (n == "nl_cutoff") c.neighborlist.set_cutoff(0.0);
+    else if (n == "nl_coef") c.neighborlist.set_cutoff_extra_coef(0.5);
+    else if (n == "lj_cutoff") { force_field::Lj lj(&c); lj.set_cutoff(-1.0); }
+    else if (n == "lang_temperature") md.langevin_temperature(-1.0);
+    else if (n == "lang_friction") md.langevin_friction(-1.0);
+    else if (n == "integrator") md.set_integrator_type(Integrator_t::Unknown);
+    else if (n == "time_and_step") { md.use_time = true; md.set_final_step(10); md.run(); }
+    else if (n == "no_time_no_step") md.run();
+    else if (n == "nve_kb_alone") { constraint::Nve v(&c); v.kb = 1.0; v.temperature = -1.0; v.verify_settings(); }
+    else if (n == "nve_unset") { constraint::Nve v(&c); v.verify_settings(); }
+    else if (n == "nve_energy_and_kbt") { constraint::Nve v(&c); v.energy_tot = 1.0; v.kbt = 1.0; v.verify_settings(); }
+    else if (n == "valid") { c.neighborlist.set_cutoff(2.5); c.neighborlist.set_cutoff_extra_coef(1.1); }
+    else { fprintf(stderr, "unknown error case %s\n", n.c_str()); return 3; }
+  } catch (const std::runtime_error &e) {
+    fprintf(stderr, "[EXC] %s\n", e.what());
+    return 2;
+  }
+  return 0;
+}
+
 int main(int argc, char **argv) {
   if (argc == 2 && !std::strcmp(argv[1], "--format")) return format_check();
+  if (argc == 3 && !std::strcmp(argv[1], "--error")) return error_case(argv[2]);
   if (argc < 3) {
-    fprintf(stderr, "usage: %s in.bin out.bin [mixed|tables|run] | --format\n", argv[0]);
+    fprintf(stderr, "usage: %s in.bin out.bin [mixed|tables|run] | --format | --error <case>\n", argv[0]);
     return 2;
   }
   FILE *fi = fopen(argv[1], "rb");

@@ -125,3 +125,34 @@ def test_host_library_builds_and_loads():
     import build as B
 
     ctypes.CDLL(B.HOST_LIB)
+
+
+# (case, status, message, reference site).  Status 1: Log::error_all printed the
+# message and exited with 1 (src/log.cpp:193); 2: the setter threw std::runtime_error.
+SETTER_ERRORS = [
+    ("nl_cutoff", 1, "cutoff have to non-negative.", "src/neighborlist.cpp:206"),
+    ("nl_coef", 1, "cutoff_extra_coef must be larger than 1.0", "src/neighborlist.cpp:214"),
+    ("lj_cutoff", 2, "Force field cutoff must be non-negative.", "src/force/lj.cpp:77"),
+    ("lang_temperature", 1, "Temperature have to non-negative.", "src/md_simulator.cpp:102"),
+    ("lang_friction", 1, "friction have to non-negative.", "src/md_simulator.cpp:108"),
+    ("integrator", 1, "invalid or non-implemented integrator", "src/md_simulator.cpp:131"),
+    ("time_and_step", 1, "cannot use both 'time' and 'step'.", "src/md_simulator.cpp:361"),
+    ("no_time_no_step", 1, "please assign 'time' or 'step' variables.", "src/md_simulator.cpp:363"),
+    ("nve_kb_alone", 1, "kb and temperature should be set together.", "src/constraint/nve.cpp:109"),
+    ("nve_unset", 1, "energy or temperature is not set.", "src/constraint/nve.cpp:116"),
+    ("nve_energy_and_kbt", 1, "Only one of 'energy' and 'temperature' can be set.", "src/constraint/nve.cpp:119"),
+]
+
+
+@pytest.mark.parametrize("case,status,message,site", SETTER_ERRORS, ids=[c[0] for c in SETTER_ERRORS])
+def test_setter_validation_matches_reference(case, status, message, site):
+    """The host API rejects each invalid setting the way the reference does (same
+    message; exit through Log::error_all or a thrown std::runtime_error).  CPU only."""
+    r = subprocess.run([harness(), "--error", case], capture_output=True, text=True, timeout=60)
+    assert r.returncode == status, (site, r.stderr)
+    assert message in r.stderr, site
+
+
+def test_valid_settings_raise_nothing():
+    r = subprocess.run([harness(), "--error", "valid"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "[ERR]" not in r.stderr
