@@ -393,9 +393,18 @@ void Md_simulator::initialize() {
   initialized = true;
 }
 
+void Md_simulator::steps_from_time() {
+  if (!use_time) return;
+  initial_step = (int64_t)((int)initial_time / dt);
+  final_step = (int64_t)((int)final_time / dt);
+}
+
 void Md_simulator::setup() {
-  check(cavgpu_setup(ctx_), "cavgpu_setup");
+  // Md_simulator::step's first call: time from the step index, then setup's
+  // time-mode conversion (src/md_simulator.cpp:458, 569-573)
   time = dt * initial_step;
+  steps_from_time();
+  check(cavgpu_setup(ctx_), "cavgpu_setup");
   // setup takes the temperature, not the pressure (src/md_simulator.cpp:605-607)
   Atom_data &ad = caviar_->atom_data;
   auto &o = ad.atom_struct_owned;

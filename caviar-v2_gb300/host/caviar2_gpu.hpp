@@ -211,6 +211,11 @@ class Md_simulator {
   void set_integrator_type(Integrator_t t);
   void set_initial_step(size_t i) { initial_step = (int64_t)i; use_step = true; }
   void set_final_step(size_t i) { final_step = (int64_t)i; use_step = true; }
+  void set_initial_time(double t) { initial_time = t; use_time = true; }
+  void set_final_time(double t) { final_time = t; use_time = true; }
+  // setup()'s time mode (src/md_simulator.cpp:569-573): step = (int)time / dt, the
+  // time truncated to an integer before the division, then truncated again
+  void steps_from_time();
   void set_dt(double v) { dt = v; }
   void langevin_temperature(double v);
   void langevin_friction(double v);
@@ -235,6 +240,7 @@ class Md_simulator {
   ~Md_simulator();
 
   double time = 0.0, dt = -1.0;
+  double initial_time = 0.0, final_time = 0.0;
   int64_t current_step = 0, initial_step = 0, final_step = 0;
   bool use_time = false, use_step = false, initialized = false;
   Integrator_t integrator_type = Integrator_t::Velocity_verlet;

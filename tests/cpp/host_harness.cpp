@@ -3,6 +3,7 @@
 // user writes, reading and writing the file formats of oracle/ref_harness.cpp so
 // that tests/test_host_api.py compares it with the fixtures the reference made.
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <limits>
@@ -76,8 +77,18 @@ static int error_case(const std::string &n) {
 int main(int argc, char **argv) {
   if (argc == 2 && !std::strcmp(argv[1], "--format")) return format_check();
   if (argc == 3 && !std::strcmp(argv[1], "--error")) return error_case(argv[2]);
+  if (argc == 5 && !std::strcmp(argv[1], "--time-steps")) {  // setup()'s time-mode conversion only
+    Caviar2 c;
+    Md_simulator &md = c.md_simulator;
+    md.set_dt(std::atof(argv[4]));
+    md.set_initial_time(std::atof(argv[2]));
+    md.set_final_time(std::atof(argv[3]));
+    md.steps_from_time();
+    printf("%lld %lld\n", (long long)md.initial_step, (long long)md.final_step);
+    return 0;
+  }
   if (argc < 3) {
-    fprintf(stderr, "usage: %s in.bin out.bin [mixed|tables|run] | --format | --error <case>\n", argv[0]);
+    fprintf(stderr, "usage: %s in.bin out.bin [mixed|tables|run] | --format | --error <case> | --time-steps t0 t1 dt\n", argv[0]);
     return 2;
   }
   FILE *fi = fopen(argv[1], "rb");

@@ -156,3 +156,14 @@ def test_setter_validation_matches_reference(case, status, message, site):
 def test_valid_settings_raise_nothing():
     r = subprocess.run([harness(), "--error", "valid"], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0 and "[ERR]" not in r.stderr
+
+
+@pytest.mark.parametrize("t0,t1,dt", [(0.0, 1.5, 0.5), (2.9, 10.2, 0.003), (0.0, 1.0, 0.005), (3.0, 7.99, 0.01)])
+def test_time_mode_steps_match_reference(t0, t1, dt):
+    """Md_simulator::set_initial_time/set_final_time: setup() turns the times into
+    steps with the reference's expression (int)time / dt (src/md_simulator.cpp:569-573),
+    the time truncated before the division: a final time of 1.5 at dt 0.5 gives 2 steps."""
+    r = subprocess.run([harness(), "--time-steps", repr(t0), repr(t1), repr(dt)], capture_output=True, text=True,
+                       timeout=60, check=True)
+    first, last = (int(x) for x in r.stdout.split())
+    assert (first, last) == (int(int(t0) / dt), int(int(t1) / dt))
