@@ -498,10 +498,14 @@ void Md_simulator::step() {
 // src/md_simulator.cpp:317-356.  The device runs uninterrupted up to the next
 // step some writer reads (CUDA graphs of many steps); the host mirror is
 // refreshed only there.
-bool Md_simulator::run() {
+void Md_simulator::verify_settings() {
   if (use_time && use_step) caviar_->log.error_all("simulator md: verify_settings: cannot use both 'time' and 'step'.");
   if (!(use_time || use_step)) caviar_->log.error_all("simulator md: verify_settings: please assign 'time' or 'step' variables.");
+}
+
+bool Md_simulator::run() {
   caviar_->log.info("MD started.");
+  verify_settings();
   if (!initialized) {
     initialize();
     setup();

@@ -213,6 +213,9 @@ class Md_simulator {
   void set_final_step(size_t i) { final_step = (int64_t)i; use_step = true; }
   void set_initial_time(double t) { initial_time = t; use_time = true; }
   void set_final_time(double t) { final_time = t; use_time = true; }
+  // continue a finished run for i more steps (src/md_simulator.cpp:92-97)
+  void set_final_add(size_t i) { final_step += (int64_t)i; initial_step = current_step; }
+  void verify_settings();  // time or step, not both (src/md_simulator.cpp:358-364)
   // setup()'s time mode (src/md_simulator.cpp:569-573): step = (int)time / dt, the
   // time truncated to an integer before the division, then truncated again
   void steps_from_time();

@@ -77,6 +77,15 @@ static int error_case(const std::string &n) {
 int main(int argc, char **argv) {
   if (argc == 2 && !std::strcmp(argv[1], "--format")) return format_check();
   if (argc == 3 && !std::strcmp(argv[1], "--error")) return error_case(argv[2]);
+  if (argc == 5 && !std::strcmp(argv[1], "--final-add")) {  // set_final_add after a run ended at `current`
+    Caviar2 c;
+    Md_simulator &md = c.md_simulator;
+    md.set_final_step((size_t)std::atoll(argv[2]));
+    md.current_step = std::atoll(argv[3]);
+    md.set_final_add((size_t)std::atoll(argv[4]));
+    printf("%lld %lld\n", (long long)md.initial_step, (long long)md.final_step);
+    return 0;
+  }
   if (argc == 5 && !std::strcmp(argv[1], "--time-steps")) {  // setup()'s time-mode conversion only
     Caviar2 c;
     Md_simulator &md = c.md_simulator;
@@ -88,7 +97,7 @@ int main(int argc, char **argv) {
     return 0;
   }
   if (argc < 3) {
-    fprintf(stderr, "usage: %s in.bin out.bin [mixed|tables|run] | --format | --error <case> | --time-steps t0 t1 dt\n", argv[0]);
+    fprintf(stderr, "usage: %s in.bin out.bin [mixed|tables|run] | --format | --error <case> | --time-steps t0 t1 dt | --final-add final current add\n", argv[0]);
     return 2;
   }
   FILE *fi = fopen(argv[1], "rb");

@@ -167,3 +167,11 @@ def test_time_mode_steps_match_reference(t0, t1, dt):
                        timeout=60, check=True)
     first, last = (int(x) for x in r.stdout.split())
     assert (first, last) == (int(int(t0) / dt), int(int(t1) / dt))
+
+
+def test_final_add_continues_from_current_step():
+    """Md_simulator::set_final_add (src/md_simulator.cpp:92-97): after a run that ended
+    at step 100 of 100, 50 more steps run from 100 to 150."""
+    r = subprocess.run([harness(), "--final-add", "100", "100", "50"], capture_output=True, text=True, timeout=60,
+                       check=True)
+    assert r.stdout.split() == ["100", "150"]
