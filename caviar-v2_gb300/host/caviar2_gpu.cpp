@@ -94,6 +94,8 @@ void Atom_data::reset_owned_acceleration() {
   for (auto &v : atom_struct_owned.acceleration) v = Vector3d<double>{0, 0, 0};
 }
 
+int Atom_data::degree_of_freedoms() { return (int)(3 * atom_struct_owned.position.size()) - get_n_r_df(); }
+
 int Atom_data::get_n_r_df() {
   if (n_r_df == -1) {
     if (stochastic_force_present) {

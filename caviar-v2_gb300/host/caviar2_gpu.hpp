@@ -100,6 +100,14 @@ class Atom_data {
     atom_struct_owned.msd_domain_cross.resize(atom_struct_owned.position.size());
   }
   bool get_msd_process() const { return msd_process; }
+  bool get_temperature_process() const { return temperature_process; }
+  bool get_pressure_process() const { return pressure_process; }
+  long get_num_of_atoms_local() const { return (long)atom_struct_owned.id.size(); }  // src/atom_data.cpp:480-483
+  // one rank: the local count (src/atom_data.cpp:484-497)
+  long get_num_of_atoms_global() const { return (long)atom_struct_owned.id.size(); }
+  // 3N - n_r_df (src/atom_data/kinetic_energy.cpp:642-673; molecules here carry no
+  // bonds, angles or dihedrals, so those terms are zero)
+  int degree_of_freedoms();
   // msd_domain_cross of every atom set to zero (the writer's MSD origin); the
   // device keeps counting, the host mirror is counted from here
   void zero_msd_domain_cross();

@@ -77,6 +77,17 @@ static int error_case(const std::string &n) {
 int main(int argc, char **argv) {
   if (argc == 2 && !std::strcmp(argv[1], "--format")) return format_check();
   if (argc == 3 && !std::strcmp(argv[1], "--error")) return error_case(argv[2]);
+  if (argc == 4 && !std::strcmp(argv[1], "--counts")) {  // Atom_data counts and flags for n atoms
+    Caviar2 c;
+    const int n = std::atoi(argv[2]);
+    for (int i = 0; i < n; ++i) c.atom_data.add_atom((size_t)i, 0, Vector3d<double>{0.5 * i, 0.0, 0.0});
+    c.atom_data.set_n_r_df(std::atoi(argv[3]));
+    c.atom_data.set_pressure_process(true);
+    printf("%ld %ld %d %d %d\n", c.atom_data.get_num_of_atoms_local(), c.atom_data.get_num_of_atoms_global(),
+           c.atom_data.degree_of_freedoms(), (int)c.atom_data.get_temperature_process(),
+           (int)c.atom_data.get_pressure_process());
+    return 0;
+  }
   if (argc == 5 && !std::strcmp(argv[1], "--final-add")) {  // set_final_add after a run ended at `current`
     Caviar2 c;
     Md_simulator &md = c.md_simulator;
@@ -97,7 +108,7 @@ int main(int argc, char **argv) {
     return 0;
   }
   if (argc < 3) {
-    fprintf(stderr, "usage: %s in.bin out.bin [mixed|tables|run] | --format | --error <case> | --time-steps t0 t1 dt | --final-add final current add\n", argv[0]);
+    fprintf(stderr, "usage: %s in.bin out.bin [mixed|tables|run] | --format | --error <case> | --time-steps t0 t1 dt | --final-add final current add | --counts n n_r_df\n", argv[0]);
     return 2;
   }
   FILE *fi = fopen(argv[1], "rb");

@@ -175,3 +175,13 @@ def test_final_add_continues_from_current_step():
     r = subprocess.run([harness(), "--final-add", "100", "100", "50"], capture_output=True, text=True, timeout=60,
                        check=True)
     assert r.stdout.split() == ["100", "150"]
+
+
+@pytest.mark.parametrize("n,nrdf", [(7, 3), (10, 0), (1, 6)])
+def test_atom_counts_and_degrees_of_freedom(n, nrdf):
+    """Atom_data::get_num_of_atoms_local/global (one rank: both the owned count,
+    src/atom_data.cpp:480-497), degree_of_freedoms() = 3N - n_r_df for bondless
+    atoms (src/atom_data/kinetic_energy.cpp:642-673) and the process flags."""
+    r = subprocess.run([harness(), "--counts", str(n), str(nrdf)], capture_output=True, text=True, timeout=60,
+                       check=True)
+    assert [int(x) for x in r.stdout.split()] == [n, n, 3 * n - nrdf, 0, 1]
