@@ -49,11 +49,27 @@ class Domain {
   void set_boundary_condition(const Vector3d<int> &v) { boundary_condition = v; }
   void generate();  // single rank: local = global (src/domain.cpp:295-328)
   double volume_global() const { return size_global.x * size_global.y * size_global.z; }
+  double volume_local() const { return size_local.x * size_local.y * size_local.z; }  // src/domain.cpp:433-436
+  // a distance component on a periodic axis shifted once by the box edge when it
+  // is beyond half of it (src/domain.cpp:330-398)
+  double fix_distance_x(double d) const { return fix_axis(d, boundary_condition.x, half_edge.x); }
+  double fix_distance_y(double d) const { return fix_axis(d, boundary_condition.y, half_edge.y); }
+  double fix_distance_z(double d) const { return fix_axis(d, boundary_condition.z, half_edge.z); }
+  Vector3d<double> fix_distance(const Vector3d<double> &v) const {
+    return Vector3d<double>{fix_distance_x(v.x), fix_distance_y(v.y), fix_distance_z(v.z)};
+  }
 
   Vector3d<int> boundary_condition{0, 0, 0};
   Vector3d<double> lower_global, upper_global, lower_local, upper_local, size_local, size_global, half_edge;
 
  private:
+  static double fix_axis(double d, int periodic, double h) {
+    if (periodic == 1) {
+      if (d > +h) d -= h * 2.0;
+      if (d < -h) d += h * 2.0;
+    }
+    return d;
+  }
   Caviar2 *caviar_ = nullptr;
 };
 

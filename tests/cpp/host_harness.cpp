@@ -77,6 +77,17 @@ static int error_case(const std::string &n) {
 int main(int argc, char **argv) {
   if (argc == 2 && !std::strcmp(argv[1], "--format")) return format_check();
   if (argc == 3 && !std::strcmp(argv[1], "--error")) return error_case(argv[2]);
+  if (argc == 3 && !std::strcmp(argv[1], "--fix-distance")) {  // box [0,10)x[0,4)x[0,6), periodic x and z
+    Caviar2 c;
+    c.domain.set_lower_global(Vector3d<double>{0.0, 0.0, 0.0});
+    c.domain.set_upper_global(Vector3d<double>{10.0, 4.0, 6.0});
+    c.domain.set_boundary_condition(Vector3d<int>{1, 0, 1});
+    c.domain.generate();
+    const double d = std::atof(argv[2]);
+    const Vector3d<double> v = c.domain.fix_distance(Vector3d<double>{d, d, d});
+    printf("%.17g %.17g %.17g %.17g %.17g\n", v.x, v.y, v.z, c.domain.volume_local(), c.domain.volume_global());
+    return 0;
+  }
   if (argc == 4 && !std::strcmp(argv[1], "--counts")) {  // Atom_data counts and flags for n atoms
     Caviar2 c;
     const int n = std::atoi(argv[2]);
@@ -108,7 +119,7 @@ int main(int argc, char **argv) {
     return 0;
   }
   if (argc < 3) {
-    fprintf(stderr, "usage: %s in.bin out.bin [mixed|tables|run] | --format | --error <case> | --time-steps t0 t1 dt | --final-add final current add | --counts n n_r_df\n", argv[0]);
+    fprintf(stderr, "usage: %s in.bin out.bin [mixed|tables|run] | --format | --error <case> | --time-steps t0 t1 dt | --final-add final current add | --counts n n_r_df | --fix-distance d\n", argv[0]);
     return 2;
   }
   FILE *fi = fopen(argv[1], "rb");

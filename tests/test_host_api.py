@@ -185,3 +185,24 @@ def test_atom_counts_and_degrees_of_freedom(n, nrdf):
     r = subprocess.run([harness(), "--counts", str(n), str(nrdf)], capture_output=True, text=True, timeout=60,
                        check=True)
     assert [int(x) for x in r.stdout.split()] == [n, n, 3 * n - nrdf, 0, 1]
+
+
+@pytest.mark.parametrize("d", [0.0, 4.9, 5.1, -5.1, 7.0, -7.0, 2.9, 3.1, 12.0])
+def test_domain_fix_distance_matches_reference(d):
+    """Domain::fix_distance_{x,y,z} (src/domain.cpp:330-398): on a periodic axis one
+    shift by the edge when |d| exceeds half of it (12 on a 6-wide axis stays 6);
+    non-periodic axes unchanged.  Box 10 x 4 x 6, periodic in x and z."""
+    r = subprocess.run([harness(), "--fix-distance", repr(d)], capture_output=True, text=True, timeout=60,
+                       check=True)
+    x, y, z, vl, vg = (float(v) for v in r.stdout.split())
+
+    def fix(v, edge):
+        h = 0.5 * edge
+        if v > h:
+            v -= h * 2.0
+        if v < -h:
+            v += h * 2.0
+        return v
+
+    assert (x, y, z) == (fix(d, 10.0), d, fix(d, 6.0))
+    assert vl == vg == 240.0
