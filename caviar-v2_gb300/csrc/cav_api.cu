@@ -6,6 +6,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <deque>
+#include <map>
 #include <mutex>
 #include <new>
 #include <utility>
@@ -19,9 +21,28 @@ namespace {
 
 constexpr int MAX_GRAPH_STEPS = 1000;  // steps captured per graph, and thermo records per chunk
 
+// A chunk of S steps launched as one unit (one captured graph, or directly).
+// fuse[k]: step k's pair kernel also does step k + 1's drift (Fuse), so that a step is
+// one launch; steps that begin a chunk, or follow a step that did not drift them,
+// launch their drift kernel.  The fused steps of a chunk are made even in number,
+// so that the gathered coordinates (FP64 positions or mixed rel), which alternate
+// between two buffers at every fused step, end the chunk in the buffer they began.
+struct ChunkPlan {
+  int S = 0, ev = 0;          // steps; record period (thermo at step k iff ev > 0 and (k + 1) % ev == 0)
+  std::vector<uint8_t> fuse;  // [S]
+  bool thermo(int k) const { return ev > 0 && (k + 1) % ev == 0; }
+  int fused_before(int k) const {
+    int n = 0;
+    for (int j = 0; j < k; ++j) n += fuse[j];
+    return n;
+  }
+};
+
 struct GraphEntry {
   int S, every, prof;
   cudaGraphExec_t exec;
+  long long launches;  // kernels one replay launches outside the conditional rebuild bodies
+  ChunkPlan plan;
 };
 
 // autotuner results, per process: a system of the same kind and size on the same
@@ -58,7 +79,11 @@ struct cavgpu_ctx {
   long long steps_done = 0;
   long long graph_launches = 0, kernel_launches = 0;
   int max_nb = 0;
-  std::vector<GraphEntry> graphs;
+  std::deque<GraphEntry> graphs;                      // stable references (chunks in flight hold them)
+  std::map<std::pair<int, int>, ChunkPlan> eager_plans;  // chunks launched from the host
+  // status words of the last chunks, read back without a full synchronisation
+  int *h_status = nullptr;   // pinned, 2 x F_NWORDS
+  cudaEvent_t ev_status[2] = {nullptr, nullptr};
   // reference binning (Neighborlist::init, src/neighborlist.cpp:334-342), single system
   double cutoff_extra = 0.0, cutoff_inv = 0.0, lo_local[3] = {0, 0, 0};
   int ref_nb[3] = {0, 0, 0};
@@ -112,7 +137,7 @@ void free_graphs(cavgpu_ctx *c) {
 bool is_lang(const cavgpu_ctx *c) { return c->p.integrator == CAVGPU_VELOCITY_VERLET_LANGEVIN; }
 
 // thermo folds after the force kernel of a thermo step
-int enqueue_thermo_after_force(cavgpu_ctx *c, int ring_slot) {
+int enqueue_thermo_after_force(cavgpu_ctx *c, int ring_slot, long long *nl) {
   const bool lang = is_lang(c);
   if (c->b.nrep == 1) {
     const int nb_ke = lang ? drift_grid_blocks(c->lc) : force_grid_blocks(c->lc);
@@ -121,7 +146,7 @@ int enqueue_thermo_after_force(cavgpu_ctx *c, int ring_slot) {
   } else {
     RK(launch_thermo_replicas(c->d, c->b, c->tc, lang ? 0 : 1, 1, c->st));
   }
-  c->kernel_launches += 1;
+  *nl += 1;
   return CAVGPU_OK;
 }
 
@@ -129,82 +154,135 @@ int enqueue_thermo_after_force(cavgpu_ctx *c, int ring_slot) {
 // the Langevin half kick, where the reference takes the temperature.  Langevin
 // with constraint::Nve: the velocity half, Nve on the mid-step velocities
 // (src/md_simulator.cpp:782-793), then the temperature and the position update.
-int enqueue_drift(cavgpu_ctx *c, int k, bool thermo) {
+// `view` holds the buffers current at this step.
+int enqueue_drift(cavgpu_ctx *c, const Dev &view, int k, bool thermo, long long *nl) {
   if (is_lang(c) && c->nve.step > 0) {
-    RK(launch_drift(c->d, c->b, c->sc, c->lc, k, -1, c->st));
-    RK(launch_nve(c->d, c->b, c->tc, c->nve, k, 0, -1, c->st));
-    RK(launch_lang_pos(c->d, c->b, c->sc, c->lc, thermo ? 1 : 0, c->st));
-    c->kernel_launches += 5;
+    RK(launch_drift(view, c->b, c->sc, c->lc, k, -1, c->st));
+    RK(launch_nve(view, c->b, c->tc, c->nve, k, 0, -1, c->st));
+    RK(launch_lang_pos(view, c->b, c->sc, c->lc, thermo ? 1 : 0, c->st));
+    *nl += 5;
     return CAVGPU_OK;
   }
-  RK(launch_drift(c->d, c->b, c->sc, c->lc, k, thermo && is_lang(c), c->st));
-  c->kernel_launches += 1;
+  RK(launch_drift(view, c->b, c->sc, c->lc, k, thermo && is_lang(c), c->st));
+  *nl += 1;
   if (thermo && is_lang(c) && c->b.nrep > 1) {
-    RK(launch_thermo_replicas(c->d, c->b, c->tc, 1, 0, c->st));
-    c->kernel_launches += 1;
+    RK(launch_thermo_replicas(view, c->b, c->tc, 1, 0, c->st));
+    *nl += 1;
   }
   return CAVGPU_OK;
 }
 
-// one MD step on the stream, launched directly; the rebuild kernels return at
-// once unless a replica's half-skin flag is set.  k = step index inside the chunk.
-int enqueue_step(cavgpu_ctx *c, int k, bool thermo, int ring_slot) {
-  RK(enqueue_drift(c, k, thermo));
-  RK(launch_rebuild(c->d, c->b, c->lc, 0, c->st));
-  // launched directly, not captured: plain event records
-  if (c->prof && k < (int)c->ev0.size()) CK(cudaEventRecord(c->ev0[k], c->st));
-  RK(launch_force(c->d, c->b, c->sc, c->lc, is_lang(c) ? 2 : 1, thermo, k, c->st));
-  if (c->prof && k < (int)c->ev1.size()) CK(cudaEventRecord(c->ev1[k], c->st));
-  c->kernel_launches += rebuild_kernels(c->b) + 1;
-  if (thermo) RK(enqueue_thermo_after_force(c, ring_slot));
-  if (c->nve.step > 0 && !is_lang(c)) {  // constraint::Nve after the temperature (src/md_simulator.cpp:681-694)
-    RK(launch_nve(c->d, c->b, c->tc, c->nve, k, thermo, ring_slot, c->st));
-    c->kernel_launches += 3;
-  }
-  return CAVGPU_OK;
+int fuse_mode(const cavgpu_ctx *c) {
+  if (c->p.integrator == CAVGPU_VELOCITY_VERLET) return FUSE_VV;
+  if (c->p.integrator == CAVGPU_LEAP_FROG) return FUSE_LF;
+  return FUSE_LANG;
 }
 
-// One MD step recorded into the graph being captured on c->st.  The rebuild
-// kernels sit in the body of an IF conditional node whose value the step's
-// half-skin flags set on the device, so steps without a rebuild launch three
-// kernels (drift, condition, force) instead of all the rebuild kernels as well.
-int capture_step(cavgpu_ctx *c, int k, bool thermo, int ring_slot) {
-  RK(enqueue_drift(c, k, thermo));
-  cudaStreamCaptureStatus cs;
-  cudaGraph_t g = nullptr;
-  CK(cudaStreamGetCaptureInfo(c->st, &cs, nullptr, &g, nullptr, nullptr, nullptr));
-  cudaGraphConditionalHandle h;
-  CK(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
-  RK(launch_set_rebuild_cond(c->d, h, c->st));
-  const cudaGraphNode_t *deps = nullptr;
-  size_t nd = 0;
-  CK(cudaStreamGetCaptureInfo(c->st, &cs, nullptr, &g, &deps, nullptr, &nd));
-  // the params struct holds a union without a default constructor: zeroed storage
-  alignas(cudaGraphNodeParams) unsigned char cp_raw[sizeof(cudaGraphNodeParams)];
-  std::memset(cp_raw, 0, sizeof(cp_raw));
-  cudaGraphNodeParams &cp = *reinterpret_cast<cudaGraphNodeParams *>(cp_raw);
-  cp.type = cudaGraphNodeTypeConditional;
-  cp.conditional.handle = h;
-  cp.conditional.type = cudaGraphCondTypeIf;
-  cp.conditional.size = 1;
-  cudaGraphNode_t cond = nullptr;
-  CK(cudaGraphAddNode(&cond, g, deps, nullptr, nd, &cp));
-  CK(cudaStreamBeginCaptureToGraph(c->side, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
-                                   cudaStreamCaptureModeThreadLocal));
-  const int brc = launch_rebuild(c->d, c->b, c->lc, 0, c->side);
-  cudaGraph_t body = nullptr;
-  const cudaError_t be = cudaStreamEndCapture(c->side, &body);
-  RK(brc);
-  CK(be);
-  CK(cudaStreamUpdateCaptureDependencies(c->st, &cond, nullptr, 1, cudaStreamSetCaptureDependencies));
-  if (c->prof && k < (int)c->ev0.size()) CK(cudaEventRecordWithFlags(c->ev0[k], c->st, cudaEventRecordExternal));
-  RK(launch_force(c->d, c->b, c->sc, c->lc, is_lang(c) ? 2 : 1, thermo, k, c->st));
-  if (c->prof && k < (int)c->ev1.size()) CK(cudaEventRecordWithFlags(c->ev1[k], c->st, cudaEventRecordExternal));
-  if (thermo) RK(enqueue_thermo_after_force(c, ring_slot));
-  if (c->nve.step > 0 && !is_lang(c)) {  // constraint::Nve after the temperature (src/md_simulator.cpp:681-694)
-    RK(launch_nve(c->d, c->b, c->tc, c->nve, k, thermo, ring_slot, c->st));
-    c->kernel_launches += 3;
+// Which steps of a chunk drift the next one.  Not with constraint::Nve (it rescales
+// the velocities between the kick and the next drift); Langevin: not into a step
+// whose temperature is recorded (the mid-step sums come from the drift kernel);
+// leap-frog: not out of a recorded step (the closing velocities are read after it).
+ChunkPlan make_plan(const cavgpu_ctx *c, int S, int ev) {
+  ChunkPlan pl;
+  pl.S = S;
+  pl.ev = ev;
+  pl.fuse.assign(S, 0);
+  if (c->nve.step > 0) return pl;
+  int nf = 0, last = -1;
+  for (int k = 0; k + 1 < S; ++k) {
+    if (is_lang(c) && pl.thermo(k + 1)) continue;
+    if (c->p.integrator == CAVGPU_LEAP_FROG && pl.thermo(k)) continue;
+    pl.fuse[k] = 1;
+    ++nf;
+    last = k;
   }
+  if (nf & 1) pl.fuse[last] = 0;  // an even number: the buffers end where they began
+  return pl;
+}
+
+// The steps of a chunk, captured into the graph being recorded on c->st (capture)
+// or launched directly.  A step: [drift kernel] -> rebuild kernels, behind a
+// conditional node in a graph (they return at once without a half-skin trigger when
+// launched directly) -> pair kernel with the closing update [and the next drift] ->
+// [thermo fold] -> [constraint::Nve].  The conditional value comes from the
+// condition kernel after a drift kernel, else from the previous pair kernel.
+int enqueue_chunk(cavgpu_ctx *c, const ChunkPlan &pl, bool capture, long long *launches) {
+  Dev view = c->d;
+  const bool mixed = c->p.precision == CAVGPU_MIXED;
+  long long nl = 0;
+  cudaGraphConditionalHandle hnext = 0;
+  for (int k = 0; k < pl.S; ++k) {
+    const bool th = pl.thermo(k);
+    const int ring_slot = th ? (k + 1) / pl.ev - 1 : -1;
+    const bool separate = k == 0 || !pl.fuse[k - 1];
+    if (separate) RK(enqueue_drift(c, view, k, th, &nl));
+    if (capture) {
+      cudaStreamCaptureStatus cs;
+      cudaGraph_t g = nullptr;
+      CK(cudaStreamGetCaptureInfo(c->st, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+      cudaGraphConditionalHandle h = hnext;
+      if (separate) {
+        CK(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
+        RK(launch_set_rebuild_cond(view, h, c->st));
+        nl += 1;
+      }
+      const cudaGraphNode_t *deps = nullptr;
+      size_t nd = 0;
+      CK(cudaStreamGetCaptureInfo(c->st, &cs, nullptr, &g, &deps, nullptr, &nd));
+      // the params struct holds a union without a default constructor: zeroed storage
+      alignas(cudaGraphNodeParams) unsigned char cp_raw[sizeof(cudaGraphNodeParams)];
+      std::memset(cp_raw, 0, sizeof(cp_raw));
+      cudaGraphNodeParams &cp = *reinterpret_cast<cudaGraphNodeParams *>(cp_raw);
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = h;
+      cp.conditional.type = cudaGraphCondTypeIf;
+      cp.conditional.size = 1;
+      cudaGraphNode_t cond = nullptr;
+      CK(cudaGraphAddNode(&cond, g, deps, nullptr, nd, &cp));
+      CK(cudaStreamBeginCaptureToGraph(c->side, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                       cudaStreamCaptureModeThreadLocal));
+      const int brc = launch_rebuild(view, c->b, c->lc, 0, c->side);
+      cudaGraph_t body = nullptr;
+      const cudaError_t be = cudaStreamEndCapture(c->side, &body);
+      RK(brc);
+      CK(be);
+      CK(cudaStreamUpdateCaptureDependencies(c->st, &cond, nullptr, 1, cudaStreamSetCaptureDependencies));
+    } else {
+      if (separate) {
+        RK(launch_halt_check(view, c->st));
+        nl += 1;
+      }
+      RK(launch_rebuild(view, c->b, c->lc, 0, c->st));
+      nl += rebuild_kernels(c->b);
+    }
+    const int fuse = pl.fuse[k] ? fuse_mode(c) : FUSE_NONE;
+    int set_cond = 0;
+    hnext = 0;
+    if (fuse && capture) {
+      cudaStreamCaptureStatus cs;
+      cudaGraph_t g = nullptr;
+      CK(cudaStreamGetCaptureInfo(c->st, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+      CK(cudaGraphConditionalHandleCreate(&hnext, g, 0, cudaGraphCondAssignDefault));
+      set_cond = 1;
+    }
+    if (c->prof && k < (int)c->ev0.size())
+      CK(capture ? cudaEventRecordWithFlags(c->ev0[k], c->st, cudaEventRecordExternal) : cudaEventRecord(c->ev0[k], c->st));
+    RK(launch_force(view, c->b, c->sc, c->lc, is_lang(c) ? 2 : 1, th, k, fuse, set_cond, hnext, c->st));
+    if (c->prof && k < (int)c->ev1.size())
+      CK(capture ? cudaEventRecordWithFlags(c->ev1[k], c->st, cudaEventRecordExternal) : cudaEventRecord(c->ev1[k], c->st));
+    nl += 1;
+    if (fuse) {  // the next step gathers the coordinates this launch wrote
+      if (mixed) std::swap(view.rel, view.rel_alt);
+      else std::swap(view.pos, view.pos_alt);
+    }
+    if (th) RK(enqueue_thermo_after_force(c, ring_slot, &nl));
+    if (c->nve.step > 0 && !is_lang(c)) {  // constraint::Nve after the temperature (src/md_simulator.cpp:681-694)
+      RK(launch_nve(view, c->b, c->tc, c->nve, k, th, ring_slot, c->st));
+      nl += 3;
+    }
+  }
+  RK(launch_advance_step(view, c->st));
+  *launches = nl + 1;
   return CAVGPU_OK;
 }
 
@@ -235,28 +313,21 @@ GraphEntry *get_graph(cavgpu_ctx *c, int S, int every, int *rc) {
     if (g.S == S && g.every == every && g.prof == (int)c->prof) return &g;
   *rc = CAVGPU_OK;
   if (c->prof && (*rc = ensure_events(c, S))) return nullptr;
+  GraphEntry ge{S, every, (int)c->prof, nullptr, 0, make_plan(c, S, every)};
   cudaGraph_t graph = nullptr;
   if ((*rc = cuda_rc(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal)))) return nullptr;
-  const long long kl = c->kernel_launches;
-  int erc = CAVGPU_OK;
-  for (int k = 0; k < S && !erc; ++k) {
-    const bool th = every > 0 && ((k + 1) % every == 0);
-    erc = capture_step(c, k, th, th ? (k + 1) / every - 1 : -1);
-  }
-  if (!erc) erc = launch_advance_step(c->d, S, c->st);
+  const int erc = enqueue_chunk(c, ge.plan, true, &ge.launches);
   cudaError_t e = cudaStreamEndCapture(c->st, &graph);
-  c->kernel_launches = kl;  // capture launches nothing; replays are counted in cavgpu_run
   if (erc || e != cudaSuccess) {
     if (graph) cudaGraphDestroy(graph);
     cudaGetLastError();
     *rc = erc ? erc : CAVGPU_E_CUDA;
     return nullptr;
   }
-  cudaGraphExec_t exec = nullptr;
-  e = cudaGraphInstantiate(&exec, graph, 0);
+  e = cudaGraphInstantiate(&ge.exec, graph, 0);
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) { *rc = CAVGPU_E_CUDA; return nullptr; }
-  c->graphs.push_back({S, every, (int)c->prof, exec});
+  c->graphs.push_back(std::move(ge));
   return &c->graphs.back();
 }
 
@@ -296,8 +367,13 @@ int alloc_nbr(cavgpu_ctx *c, int cap) {
   return CAVGPU_OK;
 }
 
-// forced list build of every replica; grows the capacity until the build fits
-int forced_build(cavgpu_ctx *c) {
+// forced list build of every replica; grows the capacity until the build fits.
+// Clears every status word but the rebuild counts; with count = false those stay
+// as they were (a build that completes a step whose own rebuild overflowed, or
+// that restarts from a snapshot, is not a rebuild of the trajectory).
+int forced_build(cavgpu_ctx *c, bool count = true) {
+  int f0[F_NWORDS];
+  RK(read_flags(c, f0));
   for (int attempt = 0; attempt < 4; ++attempt) {
     int zero[F_NWORDS] = {0};
     int f[F_NWORDS];
@@ -309,7 +385,15 @@ int forced_build(cavgpu_ctx *c) {
     c->kernel_launches += rebuild_kernels(c->b);
     RK(read_flags(c, f));
     c->max_nb = f[F_MAXNB];
-    if (!f[F_OVERFLOW]) return CAVGPU_OK;
+    if (!f[F_OVERFLOW]) {
+      if (!count) {
+        f[F_REBUILDS] = f0[F_REBUILDS];
+        f[F_PASSES] = f0[F_PASSES];
+        CK(cudaMemcpyAsync(c->d.flags, f, sizeof(f), cudaMemcpyHostToDevice, c->st));
+        CK(cudaStreamSynchronize(c->st));
+      }
+      return CAVGPU_OK;
+    }
     RK(alloc_nbr(c, (int)(f[F_OVERFLOW] * 1.25) + 32));
   }
   return CAVGPU_E_NLIST_OVERFLOW;
@@ -446,6 +530,8 @@ int create_common(const cavgpu_params *p, int nrep, const double *lo3, const dou
   if (!rc) rc = dalloc(c, &c->d.scan_part, (size_t)SCAN_SLICES);
   if (!rc) rc = dalloc(c, &c->d.fold_ticket, 1);
   if (!rc) rc = cuda_rc(cudaMemsetAsync(c->d.fold_ticket, 0, sizeof(unsigned int), c->st));
+  if (!rc) rc = dalloc(c, &c->d.force_ticket, 1);
+  if (!rc) rc = cuda_rc(cudaMemsetAsync(c->d.force_ticket, 0, sizeof(unsigned int), c->st));
   if (!rc) rc = cuda_rc(cudaMemcpyAsync(c->d.tab, &c->tab_h, sizeof(PairTab), cudaMemcpyHostToDevice, c->st));
   if (!rc) rc = cuda_rc(cudaMemsetAsync(c->d.flags, 0, F_NWORDS * sizeof(int), c->st));
   if (!rc) rc = cuda_rc(cudaMemsetAsync(c->d.thermo, 0, 8 * sizeof(double), c->st));
@@ -584,6 +670,12 @@ int upload_common(cavgpu_ctx *c, const int64_t *counts, const double *pos3, cons
   for (auto pp : d4) if (!rc) rc = dalloc(c, pp, NS);
   if (!rc) rc = dalloc(c, &d.rel, NS);
   if (!rc) rc = dalloc(c, &d.rel_ref, NS);
+  // the second buffer of the coordinates a pair kernel gathers (it drifts into it)
+  if (c->p.precision == CAVGPU_MIXED) {
+    if (!rc) rc = dalloc(c, &d.rel_alt, NS);
+  } else {
+    if (!rc) rc = dalloc(c, &d.pos_alt, NS);
+  }
   int **di[] = {&d.type, &d.cell_of, &d.t_type, &d.atom_cell, &d.perm, &d.perm_tmp, &d.nnbr};
   for (auto pp : di) if (!rc) rc = dalloc(c, pp, NS);
   if (!rc) rc = dalloc(c, &d.id, NS);
@@ -661,7 +753,7 @@ int upload_common(cavgpu_ctx *c, const int64_t *counts, const double *pos3, cons
 int setup_common(cavgpu_ctx *c) {
   if (!c->uploaded) return CAVGPU_E_STATE;
   RK(forced_build(c));
-  RK(launch_force(c->d, c->b, c->sc, c->lc, 0, 1, 0, c->st));
+  RK(launch_force(c->d, c->b, c->sc, c->lc, 0, 1, 0, FUSE_NONE, 0, 0, c->st));
   c->kernel_launches += 1;
   if (c->b.nrep == 1) {
     RK(launch_thermo_final(c->d, c->tc, force_grid_blocks(c->lc), force_grid_blocks(c->lc), 0, -1, c->st));
@@ -671,6 +763,153 @@ int setup_common(cavgpu_ctx *c) {
   c->kernel_launches += 1;
   RK(check_status(c));
   c->set_up = true;
+  return CAVGPU_OK;
+}
+
+int ensure_status(cavgpu_ctx *c) {
+  if (c->h_status) return CAVGPU_OK;
+  int *h = nullptr;
+  CK(cudaMallocHost(&h, 2 * F_NWORDS * sizeof(int)));
+  c->h_status = h;
+  for (auto &e : c->ev_status) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  return CAVGPU_OK;
+}
+
+// The chunk with plan `pl` halted after completing k of its steps because step k's
+// list build overflowed (the rebuild ran, its rows were cut at `cap`; the pair
+// kernel did not).  Bring the gathered coordinates back to their canonical buffer,
+// grow the list, build it again from the same positions -- the same cells, slot
+// order and rows as an uninterrupted run with a larger list -- and complete step k:
+// its pair kernel with the closing update, its thermo record, constraint::Nve.
+// `g` = the step's index in the call (for the thermo record).
+int complete_overflowed_step(cavgpu_ctx *c, const ChunkPlan &pl, int k, int64_t g, int64_t nsteps, int64_t every,
+                             double *out5, int need) {
+  if (pl.fused_before(k) & 1) {
+    if (c->p.precision == CAVGPU_MIXED)
+      CK(cudaMemcpyAsync(c->d.rel, c->d.rel_alt, (size_t)c->b.nslot * sizeof(float4), cudaMemcpyDeviceToDevice, c->st));
+    else
+      CK(cudaMemcpyAsync(c->d.pos, c->d.pos_alt, (size_t)c->b.nslot * sizeof(dbl4), cudaMemcpyDeviceToDevice, c->st));
+  }
+  RK(alloc_nbr(c, (int)(need * 1.25) + 32));
+  RK(forced_build(c, false));
+  const bool th = (every > 0 && (g + 1) % every == 0) || (every == 0 && g == nsteps - 1);
+  const int ring_slot = (th && every > 0) ? 0 : -1;
+  long long nl = 0;
+  RK(launch_force(c->d, c->b, c->sc, c->lc, is_lang(c) ? 2 : 1, th, 0, FUSE_NONE, 0, 0, c->st));
+  nl += 1;
+  if (th) RK(enqueue_thermo_after_force(c, ring_slot, &nl));
+  if (c->nve.step > 0 && !is_lang(c)) {
+    RK(launch_nve(c->d, c->b, c->tc, c->nve, 0, th, ring_slot, c->st));
+    nl += 3;
+  }
+  RK(launch_advance_step(c->d, c->st));
+  c->kernel_launches += nl + 1;
+  if (ring_slot >= 0)
+    CK(cudaMemcpyAsync(out5 + THERMO_REC * ((g + 1) / every - 1), c->d.thermo_ring, THERMO_REC * sizeof(double),
+                       cudaMemcpyDeviceToHost, c->st));
+  return CAVGPU_OK;
+}
+
+// Steps of cavgpu_run: chunks of up to S steps (one captured graph each, cached per
+// size and record period; or launched directly when steps_per_graph < 0).  Each
+// chunk ends with a copy of the status words into pinned host memory; while the
+// device runs chunk g the host reads the status of chunk g - 1, so a NaN or a list
+// overflow is seen one chunk later at most, and the steps after it did nothing (the
+// halt).  A NaN ends the call (CAVGPU_E_NAN, the state at the failing step, as the
+// reference's run ends there, src/md_simulator.cpp:646-652); an overflow grows the
+// list and completes the step, and the run goes on.  Without records, the call's
+// last chunk computes the thermo of its final step, so that the state after the
+// call carries a fresh temperature (finalize_temperature runs every step).
+int run_steps(cavgpu_ctx *c, int64_t nsteps, int64_t every, double *out5) {
+  int S = c->p.steps_per_graph > 0 ? std::min(c->p.steps_per_graph, MAX_GRAPH_STEPS) : 50;
+  if (every > 0) S = (int)std::max<int64_t>(every, (S / every) * every);
+  const bool eager = c->p.steps_per_graph < 0;
+  RK(ensure_status(c));
+  int f[F_NWORDS];
+  RK(read_flags(c, f));
+  if (f[F_NAN]) return CAVGPU_E_NAN;  // a context that met a NaN does not step again
+  const int passes0 = f[F_PASSES];
+  struct InFlight {
+    int64_t start;
+    int sz, slot;
+    const ChunkPlan *plan;
+  };
+  std::deque<InFlight> q;
+  int64_t done = 0, launched = 0;
+  int slot = 0;
+  const size_t depth = c->prof ? 1 : 2;  // profiling reads its events chunk by chunk
+  while (done < nsteps) {
+    while (launched < nsteps && q.size() < depth) {
+      const int64_t left = nsteps - launched;
+      int sz = (int)std::min<int64_t>(left, S), ev;
+      if (every == 0) ev = (left == sz) ? sz : 0;
+      else if (sz % every == 0) ev = (int)every;
+      else {  // a tail that holds no whole record period: one step at a time
+        sz = 1;
+        ev = ((launched + 1) % every == 0) ? 1 : 0;
+      }
+      const ChunkPlan *plan;
+      if (!eager) {
+        int rc = CAVGPU_OK;
+        GraphEntry *g = get_graph(c, sz, ev, &rc);
+        if (!g) return rc;
+        CK(cudaGraphLaunch(g->exec, c->st));
+        c->graph_launches += 1;
+        c->kernel_launches += g->launches;
+        plan = &g->plan;
+      } else {
+        auto it = c->eager_plans.find({sz, ev});
+        if (it == c->eager_plans.end()) it = c->eager_plans.emplace(std::make_pair(sz, ev), make_plan(c, sz, ev)).first;
+        plan = &it->second;
+        if (c->prof) RK(ensure_events(c, sz));
+        long long nl = 0;
+        RK(enqueue_chunk(c, *plan, false, &nl));
+        c->kernel_launches += nl;
+      }
+      const int nrec = ev > 0 ? sz / ev : 0;
+      if (every > 0 && nrec > 0)
+        CK(cudaMemcpyAsync(out5 + THERMO_REC * ((launched + ev) / every - 1), c->d.thermo_ring,
+                           THERMO_REC * sizeof(double) * nrec, cudaMemcpyDeviceToHost, c->st));
+      CK(cudaMemcpyAsync(c->h_status + slot * F_NWORDS, c->d.flags, F_NWORDS * sizeof(int), cudaMemcpyDeviceToHost,
+                         c->st));
+      CK(cudaEventRecord(c->ev_status[slot], c->st));
+      q.push_back({launched, sz, slot, plan});
+      slot ^= 1;
+      launched += sz;
+    }
+    const InFlight p = q.front();
+    q.pop_front();
+    CK(cudaEventSynchronize(c->ev_status[p.slot]));
+    const int *hf = c->h_status + p.slot * F_NWORDS;
+    c->max_nb = std::max(c->max_nb, hf[F_MAXNB]);
+    if (c->prof) RK(collect_profile(c, p.sz));
+    if (!hf[F_HALT]) {
+      done = p.start + p.sz;
+      c->steps_done += p.sz;
+      continue;
+    }
+    // halted inside chunk p; the chunk after it, if launched, did nothing
+    CK(cudaStreamSynchronize(c->st));
+    q.clear();
+    RK(read_flags(c, f));
+    const int k = f[F_HALT_STEP];
+    done = p.start + k;
+    c->steps_done += k;
+    if (f[F_NAN] || !f[F_OVERFLOW]) return CAVGPU_E_NAN;
+    const ChunkPlan plan = *p.plan;  // growing the list frees the graphs that hold it
+    RK(complete_overflowed_step(c, plan, k, done, nsteps, every, out5, f[F_OVERFLOW]));
+    RK(read_flags(c, f));
+    if (f[F_HALT]) return f[F_NAN] ? CAVGPU_E_NAN : CAVGPU_E_NLIST_OVERFLOW;
+    done += 1;
+    c->steps_done += 1;
+    launched = done;
+  }
+  RK(check_status(c));
+  // rebuild kernels launched by the graphs' conditional nodes
+  if (!eager) {
+    RK(read_flags(c, f));
+    if (f[F_PASSES] > passes0) c->kernel_launches += (long long)rebuild_kernels(c->b) * (f[F_PASSES] - passes0);
+  }
   return CAVGPU_OK;
 }
 
@@ -730,6 +969,8 @@ void cavgpu_destroy(cavgpu_ctx *c) {
   free_graphs(c);
   for (auto e : c->ev0) cudaEventDestroy(e);
   for (auto e : c->ev1) cudaEventDestroy(e);
+  for (auto e : c->ev_status) if (e) cudaEventDestroy(e);
+  if (c->h_status) cudaFreeHost(c->h_status);
   for (void *q : c->allocs) cudaFree(q);
   if (c->st) cudaStreamDestroy(c->st);
   if (c->side) cudaStreamDestroy(c->side);
@@ -771,82 +1012,7 @@ int cavgpu_run(cavgpu_ctx *c, int64_t nsteps, int64_t every, double *out5) {
   if (every > 0 && c->b.nrep > 1) return CAVGPU_E_ARG;  // batches: cavgpu_thermo_batch after the call
   if (!c->set_up) return CAVGPU_E_STATE;
   if (nsteps == 0) return CAVGPU_OK;
-  int S = c->p.steps_per_graph > 0 ? std::min(c->p.steps_per_graph, MAX_GRAPH_STEPS) : 50;
-  if (every > 0) S = (int)std::max<int64_t>(every, (S / every) * every);
-  int64_t done = 0, rec = 0, eager_steps = 0;
-  int rc = CAVGPU_OK;
-  int chunks_since_check = 0;
-  int rebuilds_at_start = 0;
-  {
-    int f[F_NWORDS];
-    RK(read_flags(c, f));
-    rebuilds_at_start = f[F_PASSES];
-  }
-  // chunks of up to S steps, each one captured CUDA graph (cached per size).  Without
-  // recording, the last chunk computes the thermo of its final step, so that the state
-  // after the call carries a fresh temperature (finalize_temperature runs every step).
-  // steps_per_graph < 0: no graphs, every step launched from the host (profilers
-  // cannot see the kernels of graphs that hold conditional nodes).
-  const bool eager = c->p.steps_per_graph < 0;
-  while (!eager && done < nsteps) {
-    const int64_t left = nsteps - done;
-    const int sz = (int)std::min<int64_t>(left, S);
-    int ev;
-    if (every == 0) ev = (left == sz) ? sz : 0;
-    else if (sz % every == 0) ev = (int)every;
-    else break;  // a tail that does not hold whole recording periods runs eagerly below
-    GraphEntry *g = get_graph(c, sz, ev, &rc);
-    if (!g) return rc;
-    CK(cudaGraphLaunch(g->exec, c->st));
-    const int nrec = ev > 0 ? sz / ev : 0;
-    c->graph_launches += 1;
-    // drift + condition + force per step, the thermo folds, the step counter; the
-    // rebuild kernels that ran are added from the device's rebuild count below
-    c->kernel_launches += (long long)sz * (c->nve.step > 0 ? (is_lang(c) ? 7 : 6) : 3) + 1 +
-                          nrec * (c->b.nrep > 1 && is_lang(c) ? 2 : 1);
-    if (c->prof) RK(collect_profile(c, sz));
-    if (every > 0) {
-      CK(cudaMemcpyAsync(out5 + THERMO_REC * rec, c->d.thermo_ring, THERMO_REC * sizeof(double) * nrec,
-                         cudaMemcpyDeviceToHost, c->st));
-      rec += nrec;
-    }
-    done += sz;
-    c->steps_done += sz;
-    // status (NaN, list overflow) is read back every 20 chunks and at the end
-    if (++chunks_since_check == 20) {
-      RK(check_status(c));
-      chunks_since_check = 0;
-    }
-  }
-  // rebuild kernels launched by the graphs' conditional nodes
-  auto count_graph_rebuilds = [&]() -> int {
-    int f[F_NWORDS];
-    RK(read_flags(c, f));
-    if (f[F_PASSES] > rebuilds_at_start) c->kernel_launches += (long long)rebuild_kernels(c->b) * (f[F_PASSES] - rebuilds_at_start);
-    return CAVGPU_OK;
-  };
-  if (done < nsteps) RK(count_graph_rebuilds());
-  // remaining steps eagerly (they count their own rebuild launches)
-  while (done < nsteps) {
-    const bool last = done == nsteps - 1;
-    const bool th = (every > 0 && (done + 1) % every == 0) || (every == 0 && last);
-    if (c->prof) RK(ensure_events(c, 1));
-    RK(enqueue_step(c, 0, th, (every > 0 && th) ? 0 : -1));
-    RK(launch_advance_step(c->d, 1, c->st));
-    c->kernel_launches += 1;
-    if (c->prof) RK(collect_profile(c, 1));
-    if (every > 0 && th) {
-      CK(cudaMemcpyAsync(out5 + THERMO_REC * rec, c->d.thermo_ring, THERMO_REC * sizeof(double),
-                         cudaMemcpyDeviceToHost, c->st));
-      rec += 1;
-    }
-    ++done;
-    ++eager_steps;
-    c->steps_done += 1;
-  }
-  RK(check_status(c));
-  if (eager_steps == 0) RK(count_graph_rebuilds());
-  return CAVGPU_OK;
+  return run_steps(c, nsteps, every, out5);
 }
 
 int cavgpu_step(cavgpu_ctx *c, int64_t nsteps) { return cavgpu_run(c, nsteps, 0, nullptr); }
@@ -1020,7 +1186,7 @@ int cavgpu_forces(cavgpu_ctx *c, double *virial, double *pe) {
   if (!c) return CAVGPU_E_ARG;
   if (!c->set_up) return CAVGPU_E_STATE;
   RK(forced_build(c));
-  RK(launch_force(c->d, c->b, c->sc, c->lc, 0, 1, 0, c->st));
+  RK(launch_force(c->d, c->b, c->sc, c->lc, 0, 1, 0, FUSE_NONE, 0, 0, c->st));
   c->kernel_launches += 1;
   if (c->b.nrep == 1) {
     RK(launch_thermo_final(c->d, c->tc, force_grid_blocks(c->lc), force_grid_blocks(c->lc), 0, -1, c->st));

@@ -40,15 +40,26 @@ constexpr int SLOT_ALIGN = 32;                     // replica slot ranges start 
 
 // device flag words
 enum Flag : int {
-  F_REBUILD = 0,   // some replica must rebuild its list before the next force (half-skin test fired)
-  F_MAXNB = 1,     // largest neighbour count seen by the last build
-  F_OVERFLOW = 2,  // a build wanted more than `cap` slots
-  F_NAN = 3,       // NaN acceleration seen
-  F_NAN_ATOM = 4,  // host index of one NaN atom
-  F_REBUILDS = 5,  // replica list builds (a single system: its rebuild count)
-  F_PASSES = 6,    // rebuild passes that built at least one replica
-  F_NWORDS = 8
+  F_REBUILD = 0,    // some replica must rebuild its list before the next force (half-skin test fired)
+  F_MAXNB = 1,      // largest neighbour count seen by the last build
+  F_OVERFLOW = 2,   // a build wanted more than `cap` slots
+  F_NAN = 3,        // NaN acceleration seen
+  F_NAN_ATOM = 4,   // host index of one NaN atom
+  F_REBUILDS = 5,   // replica list builds (a single system: its rebuild count)
+  F_PASSES = 6,     // rebuild passes that built at least one replica
+  // Halt: raised after a list overflow or a NaN, only by single points of a step
+  // (the condition kernel, the pair kernel's last block, the end of a rebuild), so
+  // that it is constant while any kernel runs; every step kernel that starts with
+  // it raised returns at once, and the rest of the chunk does nothing.
+  F_HALT = 7,
+  F_STEPS_OK = 8,   // steps of the current chunk whose pair kernel ran (the step counter adds them)
+  F_HALT_STEP = 9,  // steps of the halted chunk that completed before the halt
+  F_NWORDS = 12
 };
+
+// what the pair kernel does after the closing update of its step: nothing, or the
+// first half of the next step (its drift), so that one launch serves one step
+enum Fuse : int { FUSE_NONE = 0, FUSE_VV = 1, FUSE_LF = 2, FUSE_LANG = 3 };
 
 // Per type-pair constants of the shifted-force LJ (force_field::Lj,
 // src/force/lj.cpp:470-484).  For r^2 <= rc2:
@@ -108,6 +119,12 @@ struct Dev {
   dbl4 *pos, *vel, *acc, *pos_ref;
   float4 *rel;                // position relative to the build cell's origin; w = type bits
   float4 *rel_ref;            // rel at the last build (mixed form: rel = rel_ref + (x - pos_ref))
+  // the coordinates a pair kernel gathers from its neighbours, for the next step: a pair
+  // kernel that also drifts its atoms writes them here (FP64 form: positions; mixed
+  // form: rel), while other atoms still read the current ones, and the two swap
+  dbl4 *pos_alt;
+  float4 *rel_alt;
+  unsigned int *force_ticket; // pair kernel: blocks done (the last one ends the step and resets it)
   int *type;
   uint32_t *id;               // host (insertion) index
   int *cell_of;               // build cell of each slot
@@ -230,6 +247,102 @@ __device__ inline void langevin_eta_f(uint64_t seed, long long step, uint32_t id
   e2 = (double)(r1 * cospif(2.0f * u3));
 }
 
+// ---- integrator arithmetic shared by the drift kernels and the pair kernel ----
+// FP64 form: the reference's expression orders (src/md_simulator.cpp:654, 898-899,
+// 765, 822-827), no contraction, so that equal forces give equal trajectories.
+// Mixed form: FMAs (the FP64 pipe of these updates is their scarcest resource).
+
+// velocity Verlet: pos += vel*dt + ((acc*0.5)*dt)*dt
+template <bool MIXED>
+__device__ __forceinline__ void drift_vv(dbl4 &x, const dbl4 &v, const dbl4 &a, const StepConsts &sc) {
+  if (MIXED) {
+    x.x = fma(a.x, sc.hdt2, fma(v.x, sc.dt, x.x));
+    x.y = fma(a.y, sc.hdt2, fma(v.y, sc.dt, x.y));
+    x.z = fma(a.z, sc.hdt2, fma(v.z, sc.dt, x.z));
+  } else {
+    x.x = __dadd_rn(x.x, __dadd_rn(__dmul_rn(v.x, sc.dt), __dmul_rn(__dmul_rn(__dmul_rn(a.x, 0.5), sc.dt), sc.dt)));
+    x.y = __dadd_rn(x.y, __dadd_rn(__dmul_rn(v.y, sc.dt), __dmul_rn(__dmul_rn(__dmul_rn(a.y, 0.5), sc.dt), sc.dt)));
+    x.z = __dadd_rn(x.z, __dadd_rn(__dmul_rn(v.z, sc.dt), __dmul_rn(__dmul_rn(__dmul_rn(a.z, 0.5), sc.dt), sc.dt)));
+  }
+}
+
+// leap-frog first half: v += (0.5 dt) a ; r += dt v
+template <bool MIXED>
+__device__ __forceinline__ void drift_lf(dbl4 &x, dbl4 &v, const dbl4 &a, const StepConsts &sc) {
+  if (MIXED) {
+    v.x = fma(a.x, sc.hdt, v.x); v.y = fma(a.y, sc.hdt, v.y); v.z = fma(a.z, sc.hdt, v.z);
+    x.x = fma(v.x, sc.dt, x.x); x.y = fma(v.y, sc.dt, x.y); x.z = fma(v.z, sc.dt, x.z);
+  } else {
+    v.x = __dadd_rn(v.x, __dmul_rn(sc.hdt, a.x));
+    v.y = __dadd_rn(v.y, __dmul_rn(sc.hdt, a.y));
+    v.z = __dadd_rn(v.z, __dmul_rn(sc.hdt, a.z));
+    x.x = __dadd_rn(x.x, __dmul_rn(sc.dt, v.x));
+    x.y = __dadd_rn(x.y, __dmul_rn(sc.dt, v.y));
+    x.z = __dadd_rn(x.z, __dmul_rn(sc.dt, v.z));
+  }
+}
+
+// Langevin first half, velocity part: v += (a*0.5)*dt + eta*b
+template <bool MIXED>
+__device__ __forceinline__ void lang_half(dbl4 &v, const dbl4 &a, double e0, double e1, double e2,
+                                          const StepConsts &sc) {
+  if (MIXED) {
+    v.x = fma(a.x, sc.hdt, fma(e0, sc.lb, v.x));
+    v.y = fma(a.y, sc.hdt, fma(e1, sc.lb, v.y));
+    v.z = fma(a.z, sc.hdt, fma(e2, sc.lb, v.z));
+  } else {
+    v.x = __dadd_rn(v.x, __dadd_rn(__dmul_rn(__dmul_rn(a.x, 0.5), sc.dt), __dmul_rn(e0, sc.lb)));
+    v.y = __dadd_rn(v.y, __dadd_rn(__dmul_rn(__dmul_rn(a.y, 0.5), sc.dt), __dmul_rn(e1, sc.lb)));
+    v.z = __dadd_rn(v.z, __dadd_rn(__dmul_rn(__dmul_rn(a.z, 0.5), sc.dt), __dmul_rn(e2, sc.lb)));
+  }
+}
+
+// Langevin position update r += v*c
+template <bool MIXED>
+__device__ __forceinline__ void lang_move(dbl4 &x, const dbl4 &v, const StepConsts &sc) {
+  if (MIXED) {
+    x.x = fma(v.x, sc.lc, x.x); x.y = fma(v.y, sc.lc, x.y); x.z = fma(v.z, sc.lc, x.z);
+  } else {
+    x.x = __dadd_rn(x.x, __dmul_rn(v.x, sc.lc));
+    x.y = __dadd_rn(x.y, __dmul_rn(v.y, sc.lc));
+    x.z = __dadd_rn(x.z, __dmul_rn(v.z, sc.lc));
+  }
+}
+
+__device__ inline void request_rebuild(const Dev &d, const Box &b, int rep) {
+  b.rep_flag[rep] = 1;
+  d.flags[F_REBUILD] = 1;
+}
+
+// Half-skin test of the reference (src/neighborlist.cpp:134-143), FP64 form.
+__device__ inline void half_skin_test(const Dev &d, const Box &b, int rep, int i, const dbl4 &x) {
+  const dbl4 r = d.pos_ref[i];
+  const double dx = x.x - r.x, dy = x.y - r.y, dz = x.z - r.z;
+  if (dx * dx + dy * dy + dz * dz > b.thr2) request_rebuild(d, b, rep);
+}
+
+// Mixed form: the displacement since the build is taken once in FP64 (3
+// subtractions) and serves both the half-skin test (in FP32 against a threshold
+// shrunk by 1e-6, so it can only fire early) and the FP32 cell-relative
+// coordinates, rel = rel_at_build + (float)(x - x_at_build), written to rel_out.
+__device__ inline void mixed_track(const Dev &d, const Box &b, int rep, int i, const dbl4 &x, float4 *rel_out) {
+  const dbl4 r = d.pos_ref[i];
+  const float fx = (float)(x.x - r.x), fy = (float)(x.y - r.y), fz = (float)(x.z - r.z);
+  if (fx * fx + fy * fy + fz * fz > b.thr2f) request_rebuild(d, b, rep);
+  const float4 q = d.rel_ref[i];
+  rel_out[i] = make_float4(q.x + fx, q.y + fy, q.z + fz, q.w);
+}
+
+__device__ inline void nan_check(const Dev &d, int i, const dbl4 &a) {
+  if (isnan(a.x) || isnan(a.y) || isnan(a.z)) {
+    d.flags[F_NAN] = 1;
+    d.flags[F_NAN_ATOM] = (int)d.id[i];
+  }
+}
+
+// the halt word as every thread of a kernel sees it (constant while kernels run)
+__device__ inline bool halted(const Dev &d) { return *(volatile const int *)&d.flags[F_HALT] != 0; }
+
 // ---- host-side launch helpers ----------------------------------------------
 struct LaunchCfg {
   int precision;   // CAVGPU_FP64 / CAVGPU_MIXED
@@ -262,6 +375,8 @@ int launch_lang_pos(const Dev &d, const Box &b, const StepConsts &sc, const Laun
                     cudaStream_t st);
 int launch_rebuild(const Dev &d, const Box &b, const LaunchCfg &lc, int forced, cudaStream_t st);
 int launch_set_rebuild_cond(const Dev &d, cudaGraphConditionalHandle h, cudaStream_t st);
+// steps launched from the host: a NaN the drift saw halts the chunk
+int launch_halt_check(const Dev &d, cudaStream_t st);
 // a single system scans its cell counts in SCAN_SLICES slices (one more kernel)
 constexpr int SCAN_SLICES = 64;
 inline int scan_slices(const Box &b) { return b.nrep == 1 ? SCAN_SLICES : 1; }
@@ -269,8 +384,13 @@ inline int scan_slices(const Box &b) { return b.nrep == 1 ? SCAN_SLICES : 1; }
 inline int rebuild_kernels(const Box &b) { return 8 + (scan_slices(b) > 1 ? 1 : 0); }
 // kick: 0 = force only, 1 = VV closing kick, 2 = Langevin closing update.
 // thermo: virial/PE partials (and KE partials unless kick == 2).
+// fuse (Fuse): the next step's drift in the same launch, written to d.pos_alt (FP64)
+// or d.rel_alt (mixed); the caller swaps them with d.pos / d.rel afterwards.
+// cond: when set_cond, the last block sets the conditional node of the next step's
+// rebuild to the half-skin flag (unless halted).  The last block also counts the
+// step (F_STEPS_OK) and raises the halt on a NaN.
 int launch_force(const Dev &d, const Box &b, const StepConsts &sc, const LaunchCfg &lc, int kick, int thermo,
-                 int k_in_chunk, cudaStream_t st);
+                 int k_in_chunk, int fuse, int set_cond, cudaGraphConditionalHandle cond, cudaStream_t st);
 // nb_ke_end > 0 (Langevin): KE from partials_ke_end, the temperature from partials_ke.
 // Two levels in a fixed order: THERMO_FOLD_BLOCKS blocks fold strided subsets of the
 // partials, the last block to finish folds their sums (deterministic).
@@ -279,7 +399,7 @@ int launch_thermo_final(const Dev &d, const ThermoCfg &tc, int nb_ke, int nb_ev,
                         cudaStream_t st);
 // batches: per-replica KE (ke = 1, from the current velocities) and/or virial+PE folds
 int launch_thermo_replicas(const Dev &d, const Box &b, const ThermoCfg &tc, int ke, int ev, cudaStream_t st);
-int launch_advance_step(const Dev &d, int nsteps, cudaStream_t st);
+int launch_advance_step(const Dev &d, cudaStream_t st);
 // constraint::Nve: kinetic energy, lambda (and the thermo point of the step,
 // ring_slot >= 0 or the current one when thermo != 0), velocity scaling; every
 // kernel returns at once unless (step_base + k) % cfg.step == 0

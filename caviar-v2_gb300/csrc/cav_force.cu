@@ -38,6 +38,7 @@ __device__ inline void block_sum_store_f(double (&v)[NV], double *out) {
 
 struct SmemTabD {
   double rc2[MAXT * MAXT], sig2[MAXT * MAXT], eps4[MAXT * MAXT], gc[MAXT * MAXT], uc[MAXT * MAXT];
+  double e6[MAXT * MAXT], e12[MAXT * MAXT];  // 6 eps4 and 12 eps4 (exact: products by 6 and 12)
   double minv[MAXT], mass[MAXT];
 };
 struct SmemTabF {
@@ -65,6 +66,21 @@ struct OneType {
   float rc2, sig2, eps4, gc, pk;
 };
 
+// FP64 reciprocal by Newton-Raphson refinement of the hardware approximation
+// (PTX rcp.approx.ftz.f64): each step y <- y + y (1 - x y) with two FMAs roughly
+// doubles the correct bits (Markstein, "IA-64 and Elementary Functions", 2000), so
+// two steps take the approximation to within an ulp or two of 1/x -- far inside the
+// 1e-12 force tolerance -- at four FP64-pipe operations, the pipe this kernel is
+// bound by.  Both orders of a pair see the same r^2, hence the same value.
+__device__ __forceinline__ double rcp_nr(double x) {
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  double e = fma(-x, y, 1.0);
+  y = fma(y, e, y);
+  e = fma(-x, y, 1.0);
+  return fma(y, e, y);
+}
+
 // FP32 reciprocal from the hardware approximation (PTX rcp.approx.ftz.f32): one
 // instruction instead of the correctly rounded sequence; it is a function of r^2
 // alone, so both orders of a pair still see the same value.
@@ -90,6 +106,8 @@ __device__ inline void load_tab(const Dev &d, Tab &tab) {
       tab.pk[k] = (float)(0.5 * T.gc[k] * T.rc2[k] - T.uc[k]);
     } else {
       tab.uc[k] = T.uc[k];
+      tab.e6[k] = 6.0 * T.eps4[k];
+      tab.e12[k] = 12.0 * T.eps4[k];
     }
   }
   for (int k = threadIdx.x; k < nt; k += blockDim.x) { tab.minv[k] = T.minv[k]; tab.mass[k] = T.mass[k]; }
@@ -252,11 +270,17 @@ __device__ inline OneType one_type(const SmemTabF &tab) {
 // EV: accumulate virial, potential energy and KE (KICK == 2: the KE of the
 // velocities at the end of the step, kept apart from the mid-step temperature's);
 // batches also store virial and PE per slot for the per-replica folds.
+// fuse: then the first half of the next step, with the arithmetic of the drift
+// kernels (k_drift_vv, k_drift_lf, k_lang_a): the NaN check of the new acceleration,
+// the drift, the half-skin test; the new coordinates go to the alternate buffer
+// (FP64: pos_alt, which the neighbours of this step no longer read; mixed: rel_alt,
+// the FP64 positions being this atom's alone).  Leap-frog keeps a_old = 0 for the
+// next kick, as its drift kernel does.
 template <int A, bool MIXED, int KICK, bool EV, class Tab>
-__device__ __forceinline__ void finish_atom(const Dev &d, const StepConsts &sc, const Tab &tab, bool act, int t,
-                                            int i, int ti, int rep, long long step, double fx, double fy,
-                                            double fz, double vir, double pe, double (&ke_p)[4],
-                                            double (&ev_p)[2]) {
+__device__ __forceinline__ void finish_atom(const Dev &d, const Box &b, const StepConsts &sc, const Tab &tab,
+                                            bool act, int t, int i, int ti, int rep, long long step, int fuse,
+                                            double fx, double fy, double fz, double vir, double pe,
+                                            double (&ke_p)[4], double (&ev_p)[2]) {
 #pragma unroll
   for (int o = A; o < 32; o <<= 1) {
     fx += __shfl_xor_sync(FULL_MASK, fx, o);
@@ -270,16 +294,17 @@ __device__ __forceinline__ void finish_atom(const Dev &d, const StepConsts &sc, 
   if (!(act && t == 0)) return;
   const double mi = tab.minv[ti];
   dbl4 an = make_dbl4(fx * mi, fy * mi, fz * mi, 0.0);
+  dbl4 v;
   if (KICK == 0) {
     d.acc[i] = an;
     if (EV) {
-      const dbl4 v = d.vel[i];
+      v = d.vel[i];
       const double m = tab.mass[ti];
       ke_p[0] += m * (v.x * v.x + v.y * v.y + v.z * v.z);
       ke_p[1] += m * v.x; ke_p[2] += m * v.y; ke_p[3] += m * v.z;
     }
   } else if (KICK == 1) {
-    dbl4 v = d.vel[i];
+    v = d.vel[i];
     const dbl4 ao = d.acc[i];  // a(t), still in place until the store below
     if (MIXED) {
       v.x = fma(an.x + ao.x, sc.hdt, v.x);
@@ -290,15 +315,13 @@ __device__ __forceinline__ void finish_atom(const Dev &d, const StepConsts &sc, 
       v.y = __dadd_rn(v.y, __dmul_rn(__dadd_rn(an.y, ao.y), sc.hdt));
       v.z = __dadd_rn(v.z, __dmul_rn(__dadd_rn(an.z, ao.z), sc.hdt));
     }
-    d.acc[i] = an;
-    d.vel[i] = v;
     if (EV) {
       const double m = tab.mass[ti];
       ke_p[0] += m * (v.x * v.x + v.y * v.y + v.z * v.z);
       ke_p[1] += m * v.x; ke_p[2] += m * v.y; ke_p[3] += m * v.z;
     }
   } else {
-    dbl4 v = d.vel[i];
+    v = d.vel[i];
     double e0 = 0.0, e1 = 0.0, e2 = 0.0;
     if (!sc.noise_off) {  // replica r draws the noise stream of seed + r with its local ids
       if (MIXED) langevin_eta_f(sc.seed + rep, step, d.id[i], e0, e1, e2);
@@ -313,12 +336,43 @@ __device__ __forceinline__ void finish_atom(const Dev &d, const StepConsts &sc, 
       v.y = __dadd_rn(__dadd_rn(__dmul_rn(v.y, sc.la), __dmul_rn(e1, sc.lb)), __dmul_rn(__dmul_rn(an.y, 0.5), sc.dt));
       v.z = __dadd_rn(__dadd_rn(__dmul_rn(v.z, sc.la), __dmul_rn(e2, sc.lb)), __dmul_rn(__dmul_rn(an.z, 0.5), sc.dt));
     }
-    d.acc[i] = an;
-    d.vel[i] = v;
     if (EV) {  // Atom_data::kinetic_energy() read after the step (the temperature was taken mid-step)
       const double m = tab.mass[ti];
       ke_p[0] += m * (v.x * v.x + v.y * v.y + v.z * v.z);
       ke_p[1] += m * v.x; ke_p[2] += m * v.y; ke_p[3] += m * v.z;
+    }
+  }
+  if (KICK != 0) {
+    if (fuse != FUSE_NONE) {  // the next step's first half (its drift kernel's arithmetic)
+      nan_check(d, i, an);
+      dbl4 x = d.pos[i];
+      dbl4 ao = an;
+      if (fuse == FUSE_VV) {
+        drift_vv<MIXED>(x, v, an, sc);
+      } else if (fuse == FUSE_LF) {
+        drift_lf<MIXED>(x, v, an, sc);
+        ao = make_dbl4(0.0, 0.0, 0.0, 0.0);  // a_old = 0 for the next kick
+      } else {
+        double e0 = 0.0, e1 = 0.0, e2 = 0.0;
+        if (!sc.noise_off) {
+          if (MIXED) langevin_eta_f(sc.seed + rep, step + 1, d.id[i], e0, e1, e2);
+          else langevin_eta(sc.seed + rep, step + 1, d.id[i], e0, e1, e2);
+        }
+        lang_half<MIXED>(v, an, e0, e1, e2, sc);
+        lang_move<MIXED>(x, v, sc);
+      }
+      d.acc[i] = ao;
+      d.vel[i] = v;
+      if (MIXED) {
+        d.pos[i] = x;
+        mixed_track(d, b, rep, i, x, d.rel_alt);
+      } else {
+        d.pos_alt[i] = x;
+        half_skin_test(d, b, rep, i, x);
+      }
+    } else {
+      d.acc[i] = an;
+      d.vel[i] = v;
     }
   }
   if (EV) {
@@ -327,6 +381,35 @@ __device__ __forceinline__ void finish_atom(const Dev &d, const StepConsts &sc, 
     if (d.ev_atom) d.ev_atom[i] = make_double2(vir, pe);
   }
 }
+
+// End of a pair-kernel launch, every block: the last block to finish counts the
+// step, turns a NaN seen by the fused drift into a halt, and -- inside a graph --
+// sets the conditional node of the next step's rebuild.  The flag stores of this
+// launch are ordered before the ticket by the fence.
+__device__ __forceinline__ void end_of_step(const Dev &d, bool was_halted, int set_cond,
+                                            cudaGraphConditionalHandle cond) {
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  __threadfence();
+  const unsigned int t = atomicAdd(d.force_ticket, 1u);
+  if (t != gridDim.x - 1) return;
+  __threadfence();
+  volatile int *f = d.flags;
+  if (!was_halted) {
+    f[F_STEPS_OK] = f[F_STEPS_OK] + 1;
+    if (f[F_NAN]) f[F_HALT] = 1;
+  }
+  if (set_cond) cudaGraphSetConditional(cond, (f[F_REBUILD] != 0 && f[F_HALT] == 0) ? 1u : 0u);
+  *d.force_ticket = 0u;
+}
+
+// per-launch arguments of the pair kernels
+struct ForceArgs {
+  int k_in_chunk;                   // step index inside the chunk (Langevin noise counter)
+  int fuse;                         // Fuse: the next step's drift in this launch
+  int set_cond;                     // set `cond` at the end (inside a captured graph)
+  cudaGraphConditionalHandle cond;  // the next step's rebuild node
+};
 
 template <int KICK, bool EV>
 __device__ inline void store_partials(const Dev &d, double (&ke_p)[4], double (&ev_p)[2]) {
@@ -341,18 +424,21 @@ __device__ inline void store_partials(const Dev &d, double (&ke_p)[4], double (&
 // warp-sized tasks of A consecutive slots, neighbour coordinates gathered from
 // global memory.
 template <int TPA, bool MIXED, int KICK, bool EV, bool ONE>
-__global__ void __launch_bounds__(256, MIXED ? 4 : 1) k_force(Dev d, Box b, StepConsts sc, int k_in_chunk) {
+__global__ void __launch_bounds__(256, MIXED ? 4 : 1) k_force(Dev d, Box b, StepConsts sc, ForceArgs fa) {
   constexpr int A = 32 / TPA;
   __shared__ typename std::conditional<MIXED, SmemTabF, SmemTabD>::type tab;
   __shared__ WarpImages<MIXED> wimg[8];
+  __shared__ int s_halt;
+  if (threadIdx.x == 0) s_halt = halted(d);
   load_tab(d, tab);
   __syncthreads();
+  const bool was_halted = s_halt != 0;  // a step after a halt does nothing
   const int nt = d.tab->nt;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int a = lane % A, t = lane / A;
   const int n = sc.n, cap = d.cap;
   const int warps_total = (gridDim.x * blockDim.x) >> 5;
-  const int ntask = (n + A - 1) / A;
+  const int ntask = was_halted ? 0 : (n + A - 1) / A;
   // EV: each thread's KE / virial / PE sums live in shared memory between tasks;
   // six doubles held in registers across the pair loop spill at 64 registers
   __shared__ double s_sum[EV ? 6 * 256 : 1];
@@ -360,7 +446,7 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 1) k_force(Dev d, Box b, Step
 #pragma unroll
     for (int q = 0; q < 6; ++q) s_sum[q * 256 + threadIdx.x] = 0.0;
   long long step = 0;
-  if (KICK == 2) step = *d.step_base + k_in_chunk;
+  if (KICK == 2) step = *d.step_base + fa.k_in_chunk;
   int img_rep = -1;
 
   for (int task = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; task < ntask; task += warps_total) {
@@ -400,6 +486,7 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 1) k_force(Dev d, Box b, Step
       } else {
         const dbl4 xi = d.pos[i];
         ti = (int)xi.w;
+        const bool jump = sc.jump_tol > 0.0;
         for (int q = 0, k0 = 4 * t; k0 < nn; ++q, k0 += 4 * TPA) {
           const uint4 w4 = __ldg(row4 + (size_t)q * 32);
           const uint32_t e[4] = {w4.x, w4.y, w4.z, w4.w};
@@ -410,19 +497,28 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 1) k_force(Dev d, Box b, Step
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
             if (k0 + u >= nn) break;
-            const double3 s = wimg[wid].v[e[u] >> CODE_SHIFT];
-            const double dx = (xj[u].x + s.x) - xi.x, dy = (xj[u].y + s.y) - xi.y, dz = (xj[u].z + s.z) - xi.z;
+            // image x_j + s L (the reference's ghost coordinate); s = 0 for most
+            // entries, where x_j + 0 is x_j exactly and the three adds are skipped
+            const int code = (int)(e[u] >> CODE_SHIFT);
+            double jx = xj[u].x, jy = xj[u].y, jz = xj[u].z;
+            if (code != CODE_ZERO) {
+              const double3 s = wimg[wid].v[code];
+              jx += s.x; jy += s.y; jz += s.z;
+            }
+            const double dx = jx - xi.x, dy = jy - xi.y, dz = jz - xi.z;
             const double r2d = dx * dx + dy * dy + dz * dz;
             const int tt = ti * nt + (int)xj[u].w;
             if (r2d <= tab.rc2[tt]) {
               // Lj jump_fix (src/force/lj.cpp:459-468): r^2 floored at jump_tol after the
               // cutoff test (jump_tol = 0 when off); the direction stays dx, dy, dz
-              const double r2 = r2d < sc.jump_tol ? sc.jump_tol : r2d;
-              const double r2i = __drcp_rn(r2);
+              double r2 = r2d;
+              if (jump) r2 = r2d < sc.jump_tol ? sc.jump_tol : r2d;
+              const double r2i = rcp_nr(r2);
               const double s2 = tab.sig2[tt] * r2i;
               const double s6 = s2 * s2 * s2;
-              const double coef = tab.eps4[tt] * r2i * s6 * (6.0 - 12.0 * s6) - tab.gc[tt];
-              fx += coef * dx; fy += coef * dy; fz += coef * dz;
+              // eps4 s6 (6 - 12 s6) / r^2 - g(rc) as (s6 (e6 - e12 s6)) r2i - gc
+              const double coef = fma(s6 * fma(-tab.e12[tt], s6, tab.e6[tt]), r2i, -tab.gc[tt]);
+              fx = fma(coef, dx, fx); fy = fma(coef, dy, fy); fz = fma(coef, dz, fz);
               if (EV) {
                 vir -= coef * r2;
                 pe += tab.eps4[tt] * (s6 * s6 - s6) - tab.uc[tt] - 0.5 * tab.gc[tt] * (r2 - tab.rc2[tt]);
@@ -433,7 +529,8 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 1) k_force(Dev d, Box b, Step
       }
     }
     double ke_t[4] = {0.0, 0.0, 0.0, 0.0}, ev_t[2] = {0.0, 0.0};
-    finish_atom<A, MIXED, KICK, EV>(d, sc, tab, act, t, i, ti, rep, step, fx, fy, fz, vir, pe, ke_t, ev_t);
+    finish_atom<A, MIXED, KICK, EV>(d, b, sc, tab, act, t, i, ti, rep, step, fa.fuse, fx, fy, fz, vir, pe, ke_t,
+                                    ev_t);
     if (EV) {
 #pragma unroll
       for (int q = 0; q < 4; ++q) s_sum[q * 256 + threadIdx.x] += ke_t[q];
@@ -448,7 +545,8 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 1) k_force(Dev d, Box b, Step
 #pragma unroll
     for (int q = 0; q < 2; ++q) ev_p[q] = s_sum[(4 + q) * 256 + threadIdx.x];
   }
-  store_partials<KICK, EV>(d, ke_p, ev_p);
+  if (!was_halted) store_partials<KICK, EV>(d, ke_p, ev_p);
+  if (KICK != 0) end_of_step(d, was_halted, fa.set_cond, fa.cond);
 }
 
 // Mixed-form pair kernel over row segments.  A block takes a segment -- up to
@@ -463,7 +561,7 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 1) k_force(Dev d, Box b, Step
 // global gathers.  Warps take the segment's A-slot tasks; lanes whose atom lies
 // outside the segment idle (their atoms belong to the adjacent segment).
 template <int TPA, int KICK, bool EV, bool ONE>
-__global__ void __launch_bounds__(256) k_force_seg(Dev d, Box b, StepConsts sc, int k_in_chunk) {
+__global__ void __launch_bounds__(256) k_force_seg(Dev d, Box b, StepConsts sc, ForceArgs fa) {
   constexpr int A = 32 / TPA;
   constexpr int AS = 5 - (TPA == 1 ? 0 : TPA == 2 ? 1 : TPA == 4 ? 2 : TPA == 8 ? 3 : 4);  // log2(A)
   __shared__ SmemTabF tab;
@@ -473,7 +571,11 @@ __global__ void __launch_bounds__(256) k_force_seg(Dev d, Box b, StepConsts sc, 
   const int umax = d.seg_umax;
   int *const toff = reinterpret_cast<int *>(stage + d.stage_cap);  // [9 * umax] stage offset - first slot
   int *const tcnt = toff + 9 * umax;                                 // [9 * umax] atoms, then exclusive scan
+  __shared__ int s_halt;
+  if (threadIdx.x == 0) s_halt = halted(d);
   load_tab(d, tab);
+  __syncthreads();
+  const bool was_halted = s_halt != 0;  // a step after a halt does nothing
   const int nt = d.tab->nt;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   const int a = lane % A, t = lane / A;
@@ -481,10 +583,11 @@ __global__ void __launch_bounds__(256) k_force_seg(Dev d, Box b, StepConsts sc, 
   double ke_p[4] = {0.0, 0.0, 0.0, 0.0};
   double ev_p[2] = {0.0, 0.0};
   long long step = 0;
-  if (KICK == 2) step = *d.step_base + k_in_chunk;
+  if (KICK == 2) step = *d.step_base + fa.k_in_chunk;
   int img_rep = -1;
+  const int nseg = was_halted ? 0 : d.nseg;
 
-  for (int sgi = blockIdx.x; sgi < d.nseg; sgi += gridDim.x) {
+  for (int sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
     const int4 sg = d.seg[sgi];
     const int rep = sg.x, cy = sg.y & 0xffff, cz = sg.y >> 16, x0 = sg.z, len = sg.w;
     const RepBox &rb = repbox(b, rep);
@@ -572,42 +675,44 @@ __global__ void __launch_bounds__(256) k_force_seg(Dev d, Box b, StepConsts sc, 
           }
           fx = ax; fy = ay; fz = az; vir = vr; pe = pp;
         }
-        finish_atom<A, true, KICK, EV>(d, sc, tab, act, t, i, ti, rep, step, fx, fy, fz, vir, pe, ke_p, ev_p);
+        finish_atom<A, true, KICK, EV>(d, b, sc, tab, act, t, i, ti, rep, step, fa.fuse, fx, fy, fz, vir, pe, ke_p,
+                                       ev_p);
       }
     }
   }
-  store_partials<KICK, EV>(d, ke_p, ev_p);
+  if (!was_halted) store_partials<KICK, EV>(d, ke_p, ev_p);
+  if (KICK != 0) end_of_step(d, was_halted, fa.set_cond, fa.cond);
 }
 
 template <int TPA, bool MIXED, int KICK>
 static void launch_ev(bool ev, bool one, int grid, int block, const Dev &d, const Box &b, const StepConsts &sc,
-                      int k, cudaStream_t st) {
+                      const ForceArgs &fa, cudaStream_t st) {
   if (MIXED && one) {  // single-type systems: constants in registers (mixed form)
-    if (ev) k_force<TPA, MIXED, KICK, true, MIXED><<<grid, block, 0, st>>>(d, b, sc, k);
-    else k_force<TPA, MIXED, KICK, false, MIXED><<<grid, block, 0, st>>>(d, b, sc, k);
+    if (ev) k_force<TPA, MIXED, KICK, true, MIXED><<<grid, block, 0, st>>>(d, b, sc, fa);
+    else k_force<TPA, MIXED, KICK, false, MIXED><<<grid, block, 0, st>>>(d, b, sc, fa);
     return;
   }
-  if (ev) k_force<TPA, MIXED, KICK, true, false><<<grid, block, 0, st>>>(d, b, sc, k);
-  else k_force<TPA, MIXED, KICK, false, false><<<grid, block, 0, st>>>(d, b, sc, k);
+  if (ev) k_force<TPA, MIXED, KICK, true, false><<<grid, block, 0, st>>>(d, b, sc, fa);
+  else k_force<TPA, MIXED, KICK, false, false><<<grid, block, 0, st>>>(d, b, sc, fa);
 }
 
 template <int TPA, bool MIXED>
 static void launch_kick(int kick, bool ev, bool one, int grid, int block, const Dev &d, const Box &b,
-                        const StepConsts &sc, int k, cudaStream_t st) {
-  if (kick == 0) launch_ev<TPA, MIXED, 0>(ev, one, grid, block, d, b, sc, k, st);
-  else if (kick == 1) launch_ev<TPA, MIXED, 1>(ev, one, grid, block, d, b, sc, k, st);
-  else launch_ev<TPA, MIXED, 2>(ev, one, grid, block, d, b, sc, k, st);
+                        const StepConsts &sc, const ForceArgs &fa, cudaStream_t st) {
+  if (kick == 0) launch_ev<TPA, MIXED, 0>(ev, one, grid, block, d, b, sc, fa, st);
+  else if (kick == 1) launch_ev<TPA, MIXED, 1>(ev, one, grid, block, d, b, sc, fa, st);
+  else launch_ev<TPA, MIXED, 2>(ev, one, grid, block, d, b, sc, fa, st);
 }
 
 template <bool MIXED>
 static int launch_tpa(int tpa, int kick, bool ev, bool one, int grid, int block, const Dev &d, const Box &b,
-                      const StepConsts &sc, int k, cudaStream_t st) {
+                      const StepConsts &sc, const ForceArgs &fa, cudaStream_t st) {
   switch (tpa) {
-    case 1: launch_kick<1, MIXED>(kick, ev, one, grid, block, d, b, sc, k, st); break;
-    case 2: launch_kick<2, MIXED>(kick, ev, one, grid, block, d, b, sc, k, st); break;
-    case 4: launch_kick<4, MIXED>(kick, ev, one, grid, block, d, b, sc, k, st); break;
-    case 8: launch_kick<8, MIXED>(kick, ev, one, grid, block, d, b, sc, k, st); break;
-    case 16: launch_kick<16, MIXED>(kick, ev, one, grid, block, d, b, sc, k, st); break;
+    case 1: launch_kick<1, MIXED>(kick, ev, one, grid, block, d, b, sc, fa, st); break;
+    case 2: launch_kick<2, MIXED>(kick, ev, one, grid, block, d, b, sc, fa, st); break;
+    case 4: launch_kick<4, MIXED>(kick, ev, one, grid, block, d, b, sc, fa, st); break;
+    case 8: launch_kick<8, MIXED>(kick, ev, one, grid, block, d, b, sc, fa, st); break;
+    case 16: launch_kick<16, MIXED>(kick, ev, one, grid, block, d, b, sc, fa, st); break;
     default: return CAVGPU_E_ARG;
   }
   return CAVGPU_OK;
@@ -616,7 +721,7 @@ static int launch_tpa(int tpa, int kick, bool ev, bool one, int grid, int block,
 // the segment kernel's variants, for launching and for their shared-memory attribute
 template <int TPA, int KICK, bool EV>
 static int seg_variant(bool launch, bool one, int grid, int block, size_t smem, const Dev &d, const Box &b,
-                       const StepConsts &sc, int k, cudaStream_t st) {
+                       const StepConsts &sc, const ForceArgs &fa, cudaStream_t st) {
   if (!launch) {
     if (cudaFuncSetAttribute(k_force_seg<TPA, KICK, EV, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem) != cudaSuccess ||
@@ -625,28 +730,28 @@ static int seg_variant(bool launch, bool one, int grid, int block, size_t smem, 
       return CAVGPU_E_CUDA;
     return CAVGPU_OK;
   }
-  if (one) k_force_seg<TPA, KICK, EV, true><<<grid, block, smem, st>>>(d, b, sc, k);
-  else k_force_seg<TPA, KICK, EV, false><<<grid, block, smem, st>>>(d, b, sc, k);
+  if (one) k_force_seg<TPA, KICK, EV, true><<<grid, block, smem, st>>>(d, b, sc, fa);
+  else k_force_seg<TPA, KICK, EV, false><<<grid, block, smem, st>>>(d, b, sc, fa);
   return CAVGPU_OK;
 }
 template <int TPA>
 static int seg_kick(bool launch, int kick, bool ev, bool one, int grid, int block, size_t smem, const Dev &d,
-                    const Box &b, const StepConsts &sc, int k, cudaStream_t st) {
-  if (kick == 0) return ev ? seg_variant<TPA, 0, true>(launch, one, grid, block, smem, d, b, sc, k, st)
-                           : seg_variant<TPA, 0, false>(launch, one, grid, block, smem, d, b, sc, k, st);
-  if (kick == 1) return ev ? seg_variant<TPA, 1, true>(launch, one, grid, block, smem, d, b, sc, k, st)
-                           : seg_variant<TPA, 1, false>(launch, one, grid, block, smem, d, b, sc, k, st);
-  return ev ? seg_variant<TPA, 2, true>(launch, one, grid, block, smem, d, b, sc, k, st)
-            : seg_variant<TPA, 2, false>(launch, one, grid, block, smem, d, b, sc, k, st);
+                    const Box &b, const StepConsts &sc, const ForceArgs &fa, cudaStream_t st) {
+  if (kick == 0) return ev ? seg_variant<TPA, 0, true>(launch, one, grid, block, smem, d, b, sc, fa, st)
+                           : seg_variant<TPA, 0, false>(launch, one, grid, block, smem, d, b, sc, fa, st);
+  if (kick == 1) return ev ? seg_variant<TPA, 1, true>(launch, one, grid, block, smem, d, b, sc, fa, st)
+                           : seg_variant<TPA, 1, false>(launch, one, grid, block, smem, d, b, sc, fa, st);
+  return ev ? seg_variant<TPA, 2, true>(launch, one, grid, block, smem, d, b, sc, fa, st)
+            : seg_variant<TPA, 2, false>(launch, one, grid, block, smem, d, b, sc, fa, st);
 }
 static int seg_tpa(bool launch, int tpa, int kick, bool ev, bool one, int grid, int block, size_t smem,
-                   const Dev &d, const Box &b, const StepConsts &sc, int k, cudaStream_t st) {
+                   const Dev &d, const Box &b, const StepConsts &sc, const ForceArgs &fa, cudaStream_t st) {
   switch (tpa) {
-    case 1: return seg_kick<1>(launch, kick, ev, one, grid, block, smem, d, b, sc, k, st);
-    case 2: return seg_kick<2>(launch, kick, ev, one, grid, block, smem, d, b, sc, k, st);
-    case 4: return seg_kick<4>(launch, kick, ev, one, grid, block, smem, d, b, sc, k, st);
-    case 8: return seg_kick<8>(launch, kick, ev, one, grid, block, smem, d, b, sc, k, st);
-    case 16: return seg_kick<16>(launch, kick, ev, one, grid, block, smem, d, b, sc, k, st);
+    case 1: return seg_kick<1>(launch, kick, ev, one, grid, block, smem, d, b, sc, fa, st);
+    case 2: return seg_kick<2>(launch, kick, ev, one, grid, block, smem, d, b, sc, fa, st);
+    case 4: return seg_kick<4>(launch, kick, ev, one, grid, block, smem, d, b, sc, fa, st);
+    case 8: return seg_kick<8>(launch, kick, ev, one, grid, block, smem, d, b, sc, fa, st);
+    case 16: return seg_kick<16>(launch, kick, ev, one, grid, block, smem, d, b, sc, fa, st);
     default: return CAVGPU_E_ARG;
   }
 }
@@ -658,7 +763,7 @@ int prepare_force_seg(size_t smem_bytes) {
   for (int tpa = 1; tpa <= 16; tpa *= 2)
     for (int kick = 0; kick < 3; ++kick)
       for (int ev = 0; ev < 2; ++ev) {
-        const int rc = seg_tpa(false, tpa, kick, ev != 0, false, 0, 0, smem_bytes, d, b, sc, 0, nullptr);
+        const int rc = seg_tpa(false, tpa, kick, ev != 0, false, 0, 0, smem_bytes, d, b, sc, ForceArgs{}, nullptr);
         if (rc) return rc;
       }
   return CAVGPU_OK;
@@ -686,19 +791,21 @@ int force_grid_blocks(const LaunchCfg &lc) {
 }
 
 int launch_force(const Dev &d, const Box &b, const StepConsts &sc, const LaunchCfg &lc, int kick, int thermo,
-                 int k, cudaStream_t st) {
+                 int k, int fuse, int set_cond, cudaGraphConditionalHandle cond, cudaStream_t st) {
   const int grid = force_grid_blocks(lc);
   if (grid > d.partials_blocks) return CAVGPU_E_ARG;  // each block writes its own partial sums
+  if (kick == 0 && (fuse || set_cond)) return CAVGPU_E_ARG;
+  const ForceArgs fa{k, fuse, set_cond, cond};
   int rc;
   if (lc.precision == CAVGPU_MIXED && lc.use_seg && lc.nseg > 0) {
     if (!d.seg || d.nseg != lc.nseg) return CAVGPU_E_ARG;
     rc = seg_tpa(true, lc.tpa, kick, thermo != 0, lc.ntypes == 1, grid, lc.block,
-                 seg_smem_bytes(d.stage_cap, d.seg_umax), d, b, sc, k, st);
+                 seg_smem_bytes(d.stage_cap, d.seg_umax), d, b, sc, fa, st);
   } else {
     const bool one = lc.ntypes == 1;
     rc = lc.precision == CAVGPU_MIXED
-             ? launch_tpa<true>(lc.tpa, kick, thermo != 0, one, grid, lc.block, d, b, sc, k, st)
-             : launch_tpa<false>(lc.tpa, kick, thermo != 0, one, grid, lc.block, d, b, sc, k, st);
+             ? launch_tpa<true>(lc.tpa, kick, thermo != 0, one, grid, lc.block, d, b, sc, fa, st)
+             : launch_tpa<false>(lc.tpa, kick, thermo != 0, one, grid, lc.block, d, b, sc, fa, st);
   }
   if (rc) return rc;
   return cudaPeekAtLastError() == cudaSuccess ? CAVGPU_OK : CAVGPU_E_CUDA;

@@ -62,60 +62,21 @@ __device__ inline void update_rel(const Dev &d, const RepBox &rb, int i, const d
   d.rel[i] = r;
 }
 
-__device__ inline void request_rebuild(const Dev &d, const Box &b, int rep) {
-  b.rep_flag[rep] = 1;
-  d.flags[F_REBUILD] = 1;
-}
-
-__device__ inline void half_skin_test(const Dev &d, const Box &b, int rep, int i, const dbl4 &x) {
-  const dbl4 r = d.pos_ref[i];
-  const double dx = x.x - r.x, dy = x.y - r.y, dz = x.z - r.z;
-  if (dx * dx + dy * dy + dz * dz > b.thr2) request_rebuild(d, b, rep);
-}
-
-// Mixed form: the displacement since the build is taken once in FP64 (3
-// subtractions) and serves both the half-skin test (in FP32 against a threshold
-// shrunk by 1e-6, so it can only fire early) and the FP32 cell-relative
-// coordinates, rel = rel_at_build + (float)(x - x_at_build).
-__device__ inline void mixed_track(const Dev &d, const Box &b, int rep, int i, const dbl4 &x) {
-  const dbl4 r = d.pos_ref[i];
-  const float fx = (float)(x.x - r.x), fy = (float)(x.y - r.y), fz = (float)(x.z - r.z);
-  if (fx * fx + fy * fy + fz * fz > b.thr2f) request_rebuild(d, b, rep);
-  const float4 q = d.rel_ref[i];
-  d.rel[i] = make_float4(q.x + fx, q.y + fy, q.z + fz, q.w);
-}
-
-__device__ inline void nan_check(const Dev &d, int i, const dbl4 &a) {
-  if (isnan(a.x) || isnan(a.y) || isnan(a.z)) {
-    d.flags[F_NAN] = 1;
-    d.flags[F_NAN_ATOM] = (int)d.id[i];
-  }
-}
-
-// FP64 form: pos += vel*dt + ((acc*0.5)*dt)*dt, unfused, in the reference's order
-// (src/md_simulator.cpp:654), so that equal forces give equal trajectories.
-// Mixed form: the same update with two FMAs per component (the FP64 pipe of
-// this part is its scarcest resource).
+// Velocity-Verlet drift (src/md_simulator.cpp:640-656) with the NaN check of the
+// acceleration and the half-skin test; the pair kernel fuses the same update into
+// the step before when it can (FUSE_VV), so this kernel runs at the start of a chunk.
 template <bool MIXED>
 __global__ void __launch_bounds__(256) k_drift_vv(Dev d, Box b, StepConsts sc) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= sc.n) return;
+  if (i >= sc.n || halted(d)) return;
   const int rep = rep_of_slot(b, i);
   if (rep < 0) return;  // padding slot
   dbl4 x = d.pos[i];
   const dbl4 v = d.vel[i], a = d.acc[i];
   nan_check(d, i, a);
-  if (MIXED) {
-    x.x = fma(a.x, sc.hdt2, fma(v.x, sc.dt, x.x));
-    x.y = fma(a.y, sc.hdt2, fma(v.y, sc.dt, x.y));
-    x.z = fma(a.z, sc.hdt2, fma(v.z, sc.dt, x.z));
-  } else {
-    x.x = __dadd_rn(x.x, __dadd_rn(__dmul_rn(v.x, sc.dt), __dmul_rn(__dmul_rn(__dmul_rn(a.x, 0.5), sc.dt), sc.dt)));
-    x.y = __dadd_rn(x.y, __dadd_rn(__dmul_rn(v.y, sc.dt), __dmul_rn(__dmul_rn(__dmul_rn(a.y, 0.5), sc.dt), sc.dt)));
-    x.z = __dadd_rn(x.z, __dadd_rn(__dmul_rn(v.z, sc.dt), __dmul_rn(__dmul_rn(__dmul_rn(a.z, 0.5), sc.dt), sc.dt)));
-  }
+  drift_vv<MIXED>(x, v, a, sc);
   d.pos[i] = x;  // acc stays: the pair kernel's kick reads it as a_old
-  if (MIXED) mixed_track(d, b, rep, i, x);
+  if (MIXED) mixed_track(d, b, rep, i, x, d.rel);
   else half_skin_test(d, b, rep, i, x);
 }
 
@@ -125,27 +86,17 @@ __global__ void __launch_bounds__(256) k_drift_vv(Dev d, Box b, StepConsts sc) {
 template <bool MIXED>
 __global__ void __launch_bounds__(256) k_drift_lf(Dev d, Box b, StepConsts sc) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= sc.n) return;
+  if (i >= sc.n || halted(d)) return;
   const int rep = rep_of_slot(b, i);
   if (rep < 0) return;  // padding slot
   dbl4 x = d.pos[i], v = d.vel[i];
   const dbl4 a = d.acc[i];
   nan_check(d, i, a);
-  if (MIXED) {
-    v.x = fma(a.x, sc.hdt, v.x); v.y = fma(a.y, sc.hdt, v.y); v.z = fma(a.z, sc.hdt, v.z);
-    x.x = fma(v.x, sc.dt, x.x); x.y = fma(v.y, sc.dt, x.y); x.z = fma(v.z, sc.dt, x.z);
-  } else {
-    v.x = __dadd_rn(v.x, __dmul_rn(sc.hdt, a.x));
-    v.y = __dadd_rn(v.y, __dmul_rn(sc.hdt, a.y));
-    v.z = __dadd_rn(v.z, __dmul_rn(sc.hdt, a.z));
-    x.x = __dadd_rn(x.x, __dmul_rn(sc.dt, v.x));
-    x.y = __dadd_rn(x.y, __dmul_rn(sc.dt, v.y));
-    x.z = __dadd_rn(x.z, __dmul_rn(sc.dt, v.z));
-  }
+  drift_lf<MIXED>(x, v, a, sc);
   d.pos[i] = x;
   d.vel[i] = v;
   d.acc[i] = make_dbl4(0.0, 0.0, 0.0, 0.0);  // a_old = 0 for the kick
-  if (MIXED) mixed_track(d, b, rep, i, x);
+  if (MIXED) mixed_track(d, b, rep, i, x, d.rel);
   else half_skin_test(d, b, rep, i, x);
 }
 
@@ -159,17 +110,9 @@ __device__ __forceinline__ void lang_position(const Dev &d, const Box &b, const 
     part[0] = m * (v.x * v.x + v.y * v.y + v.z * v.z);
     part[1] = m * v.x; part[2] = m * v.y; part[3] = m * v.z;
   }
-  if (MIXED) {
-    x.x = fma(v.x, sc.lc, x.x);
-    x.y = fma(v.y, sc.lc, x.y);
-    x.z = fma(v.z, sc.lc, x.z);
-  } else {
-    x.x = __dadd_rn(x.x, __dmul_rn(v.x, sc.lc));
-    x.y = __dadd_rn(x.y, __dmul_rn(v.y, sc.lc));
-    x.z = __dadd_rn(x.z, __dmul_rn(v.z, sc.lc));
-  }
+  lang_move<MIXED>(x, v, sc);
   d.pos[i] = x;
-  if (MIXED) mixed_track(d, b, rep, i, x);
+  if (MIXED) mixed_track(d, b, rep, i, x, d.rel);
   else half_skin_test(d, b, rep, i, x);
 }
 
@@ -179,6 +122,7 @@ __device__ __forceinline__ void lang_position(const Dev &d, const Box &b, const 
 // velocities (:784-791) and k_lang_pos takes the temperature and moves the atoms.
 template <bool MIXED, bool THERMO, bool POS>
 __global__ void __launch_bounds__(256) k_lang_a(Dev d, Box b, StepConsts sc, int k_in_chunk) {
+  if (halted(d)) return;  // the same value for every block: no block reaches the reduction alone
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double part[4] = {0.0, 0.0, 0.0, 0.0};
   const int rep = i < sc.n ? rep_of_slot(b, i) : -1;
@@ -193,15 +137,7 @@ __global__ void __launch_bounds__(256) k_lang_a(Dev d, Box b, StepConsts sc, int
       if (MIXED) langevin_eta_f(sc.seed + rep, step, d.id[i], e0, e1, e2);
       else langevin_eta(sc.seed + rep, step, d.id[i], e0, e1, e2);
     }
-    if (MIXED) {
-      v.x = fma(a.x, sc.hdt, fma(e0, sc.lb, v.x));
-      v.y = fma(a.y, sc.hdt, fma(e1, sc.lb, v.y));
-      v.z = fma(a.z, sc.hdt, fma(e2, sc.lb, v.z));
-    } else {
-      v.x = __dadd_rn(v.x, __dadd_rn(__dmul_rn(__dmul_rn(a.x, 0.5), sc.dt), __dmul_rn(e0, sc.lb)));
-      v.y = __dadd_rn(v.y, __dadd_rn(__dmul_rn(__dmul_rn(a.y, 0.5), sc.dt), __dmul_rn(e1, sc.lb)));
-      v.z = __dadd_rn(v.z, __dadd_rn(__dmul_rn(__dmul_rn(a.z, 0.5), sc.dt), __dmul_rn(e2, sc.lb)));
-    }
+    lang_half<MIXED>(v, a, e0, e1, e2, sc);
     d.vel[i] = v;
     if (POS) lang_position<MIXED, THERMO>(d, b, sc, rep, i, x, v, part);
   }
@@ -210,6 +146,7 @@ __global__ void __launch_bounds__(256) k_lang_a(Dev d, Box b, StepConsts sc, int
 
 template <bool MIXED, bool THERMO>
 __global__ void __launch_bounds__(256) k_lang_pos(Dev d, Box b, StepConsts sc) {
+  if (halted(d)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double part[4] = {0.0, 0.0, 0.0, 0.0};
   const int rep = i < sc.n ? rep_of_slot(b, i) : -1;
@@ -223,7 +160,11 @@ __global__ void __launch_bounds__(256) k_lang_pos(Dev d, Box b, StepConsts sc) {
 // (Neighborlist::update_cell_list + update_verlet_list_from_cell_list,
 //  src/neighborlist.cpp:422-455, 496-553; Domain::fix_position, src/domain.cpp:443-493)
 // ---------------------------------------------------------------------------
-__device__ inline bool rebuild_on(const Box &b, int rep, int forced) { return forced || b.rep_flag[rep] != 0; }
+// a rebuild pass builds the replicas whose half-skin test fired (all when forced);
+// nothing after a halt
+__device__ inline bool rebuild_on(const Dev &d, const Box &b, int rep, int forced) {
+  return !halted(d) && (forced || b.rep_flag[rep] != 0);
+}
 
 // Domain::fix_position's single-image test per axis (src/domain.cpp:443-493):
 // -1 below the lower face (x += L), +1 above the upper face (x -= L), else 0
@@ -236,7 +177,7 @@ __global__ void __launch_bounds__(256) k_bin(Dev d, Box b, int forced) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i == 0) d.flags[F_MAXNB] = 0;
   int rep = i < b.nslot ? rep_of_slot(b, i) : -1;
-  const bool act = rep >= 0 && rebuild_on(b, rep, forced);
+  const bool act = rep >= 0 && rebuild_on(d, b, rep, forced);
   int c = 0;
   if (act) {
     const RepBox &rb = repbox(b, rep);
@@ -301,7 +242,7 @@ __device__ inline int scan_count(const Dev &d, const RepBox &rb, int m, int k) {
 
 // single system: the sum of each slice's counts (first level of the scan)
 __global__ void __launch_bounds__(1024) k_scan_part(Dev d, Box b, int forced) {
-  if (!rebuild_on(b, 0, forced)) return;
+  if (!rebuild_on(d, b, 0, forced)) return;
   const RepBox &rb = repbox(b, 0);
   const int m = rb.ncell + 1;
   const int2 sl = scan_slice(m, gridDim.x, blockIdx.x);
@@ -323,7 +264,7 @@ __global__ void __launch_bounds__(1024) k_scan_part(Dev d, Box b, int forced) {
 
 __global__ void __launch_bounds__(1024) k_scan_rep(Dev d, Box b, int forced, int P) {
   const int rep = blockIdx.x / P, p = blockIdx.x - rep * P;
-  if (!rebuild_on(b, rep, forced)) return;
+  if (!rebuild_on(d, b, rep, forced)) return;
   const RepBox &rb = repbox(b, rep);
   const int m = rb.ncell + 1, off = rb.cell_off;
   const int2 sl = scan_slice(m, P, p);
@@ -380,7 +321,7 @@ __global__ void __launch_bounds__(256) k_scatter(Dev d, Box b, int forced) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.nslot) return;
   const int rep = rep_of_slot(b, i);
-  if (rep < 0 || !rebuild_on(b, rep, forced)) return;
+  if (rep < 0 || !rebuild_on(d, b, rep, forced)) return;
   const int c = d.atom_cell[i];
   d.perm_tmp[d.cell_start[c] + atomicAdd(&d.cell_cursor[c], 1)] = i;
 }
@@ -392,7 +333,7 @@ __global__ void __launch_bounds__(256) k_cell_sort(Dev d, Box b, int forced) {
   const int cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (cell >= b.ncell_all) return;
   const int rep = rep_of_cell(b, cell);
-  if (rep < 0 || !rebuild_on(b, rep, forced)) return;
+  if (rep < 0 || !rebuild_on(d, b, rep, forced)) return;
   const int s = d.cell_start[cell], e = d.cell_start[cell + 1], n = e - s;
   if (n <= 32) {
     const int ia = lane < n ? d.perm_tmp[s + lane] : 0;
@@ -415,7 +356,7 @@ __global__ void __launch_bounds__(256) k_copy_state(Dev d, Box b, int forced) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.nslot) return;
   const int rep = rep_of_slot(b, i);
-  if (rep < 0 || !rebuild_on(b, rep, forced)) return;
+  if (rep < 0 || !rebuild_on(d, b, rep, forced)) return;
   d.t_pos[i] = d.pos[i];
   d.t_vel[i] = d.vel[i];
   d.t_acc[i] = d.acc[i];  // a(t): the next kick reads it as a_old
@@ -430,7 +371,7 @@ __global__ void __launch_bounds__(256) k_gather(Dev d, Box b, int forced) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= b.nslot) return;
   const int rep = rep_of_slot(b, k);
-  if (rep < 0 || !rebuild_on(b, rep, forced)) return;
+  if (rep < 0 || !rebuild_on(d, b, rep, forced)) return;
   const int o = d.perm[k];
   const dbl4 x = d.t_pos[o];
   d.pos[k] = x;
@@ -463,42 +404,31 @@ __device__ __noinline__ bool exact_pair(const Dev &d, const RepBox &rb, double c
   return r2 < ce2;
 }
 
-// Stencil cell k of home cell (cx, cy, cz): its global index, its periodic image
-// code and the offset of its origin from the home cell's origin.
-struct StencilCell {
-  int c2, img;
-  float ox, oy, oz;
-};
-__device__ inline StencilCell stencil_cell(const RepBox &rb, int cx, int cy, int cz, int k) {
-  const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
-  int nx = cx + dx, ny = cy + dy, nz = cz + dz, sx = 0, sy = 0, sz = 0;
-  if (nx < 0) { nx += rb.nc[0]; sx = -1; } else if (nx >= rb.nc[0]) { nx -= rb.nc[0]; sx = 1; }
-  if (ny < 0) { ny += rb.nc[1]; sy = -1; } else if (ny >= rb.nc[1]) { ny -= rb.nc[1]; sy = 1; }
-  if (nz < 0) { nz += rb.nc[2]; sz = -1; } else if (nz >= rb.nc[2]) { nz -= rb.nc[2]; sz = 1; }
-  StencilCell s;
-  s.c2 = rb.cell_off + nx + rb.nc[0] * (ny + rb.nc[1] * nz);
-  s.img = image_code(sx, sy, sz);
-  s.ox = dx * rb.wf[0];
-  s.oy = dy * rb.wf[1];
-  s.oz = dz * rb.wf[2];
-  return s;
-}
-
-// One warp per home cell, one lane per home atom (cells of more than 32 atoms
-// take several groups).  The warp first stages the 27 stencil cells' atoms, in
-// stencil order and slot order inside a cell, into its slice of shared memory,
-// candidates u and u+1 (u even) interleaved as {x_u, x_u+1, y_u, y_u+1} and
-// {z_u, z_u+1, word_u, word_u+1} (coordinates relative to the home cell's origin,
-// word = j | code), padded to a multiple of 32 with far-away entries; stencils of
-// more than BUILD_STAGE candidates are staged in passes.  The sweep takes 32
-// candidates at a time, two per packed FP32x2 distance evaluation: every pair of
-// candidates is two shared-memory broadcasts tested by all home atoms, the results
-// collect in a hit and a band bit mask per lane (one warp vote per 32 candidates
-// for the rare exact FP64 test), and only then are the hits (~15% of the
-// candidates) written, in candidate order.  Hits append to the lane's own row, so
-// the list keeps the stencil order (deterministic, independent of the launch shape).
+// Home groups.  A warp takes a window of 32 consecutive slots; the window's atoms
+// that lie in one x-row of search cells, within GROUP_SPAN + 1 consecutive cells of
+// it, form a group (a window that crosses the end of a row, or a sparse row, takes
+// two or more groups in turn).  Slots are sorted by cell, so a group is 32 (or
+// fewer) atoms from 1-3 neighbouring cells.  Its candidates are the atoms of the
+// cells cx_first - 1 .. cx_last + 1 of the 3 x 3 neighbouring rows, taken row by row
+// (dz, then dy, then x, slot order inside a cell), and of those only the ones within
+// the list cutoff (plus the FP32 band) of the group's bounding box are staged: ~540
+// staged candidates per 32 atoms of the 1M-atom fluid, against 27 cells x 19 atoms
+// = 516 per 19-atom cell when a warp took one cell.  Every atom's row keeps the
+// stencil order k = (dx+1) + 3(dy+1) + 9(dz+1), slot order inside a cell, so the
+// lists do not depend on how slots fall into windows.
+//
+// Staging: candidates u and u+1 (u even) interleaved as {x_u, x_u+1, y_u, y_u+1}
+// and {z_u, z_u+1, word_u, word_u+1} in the warp's slice of shared memory
+// (coordinates relative to the origin of the group's first cell, word = j | image
+// code), plus one byte per candidate: its cell's x index in the group's window of
+// cells and its row (dy, dz).  The sweep takes 32 candidates at a time, two per
+// packed FP32x2 distance evaluation: every pair of candidates is two shared-memory
+// broadcasts tested by all group atoms, the results collect in a hit and a band bit
+// mask per lane (one warp vote per 32 candidates for the rare exact FP64 test), and
+// only then are the hits (~15% of the staged candidates) written, in candidate order.
 constexpr int BUILD_WARPS = 8;    // warps per block
-constexpr int BUILD_STAGE = 256;  // staged candidates per warp and pass (4 KiB)
+constexpr int BUILD_STAGE = 256;  // staged candidates per warp and pass (4 KiB + 256 B)
+constexpr int GROUP_SPAN = 5;     // a group spans at most 6 cells: x index + 8 row < 256
 
 // q_u, q_u+1 = |c - r|^2 of two candidates with packed FP32x2 arithmetic (sm_100+):
 // (cx - rx)^2, then + (cy - ry)^2, then + (cz - rz)^2, each rounded once
@@ -519,137 +449,253 @@ __device__ __forceinline__ unsigned long long pack2(float v) {
   return r;
 }
 
-__global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_warp(Dev d, Box b, int mode, int forced) {
+// The lane's side of a group: its atom, where it sits in the group, its row.
+struct BuildLane {
+  int i;              // slot (valid when `me`)
+  bool me;            // member of the current group
+  int ci;             // x cell index within the group (0 .. span)
+  int cx, cy, cz;     // cell of the atom
+  int mol;            // molecule index (ignore_intra_molecule)
+  unsigned long long rxx, ryy, rzz;  // the atom's coordinates in the group frame, packed twice
+  float hi;           // upper end of the FP32 band (-1 for non-members: they never hit)
+  uint32_t *row;      // the atom's list row
+  int cnt;            // list words the atom has so far
+  const int *selfpos; // shared: per lane, where its own atom sits in the current stage (-1: not in it)
+};
+
+// Sweep of nst staged candidates against every member of the group (see above).
+// Staged words carry j and a code: the image code (mode 0), or (mode 1) the cell's
+// x index in the group's window of cells plus 3 x its row, from which a member
+// subtracts its own x index to get the stencil index of j's cell relative to its own.
+__device__ __forceinline__ void build_sweep(const Dev &d, const Box &b, const RepBox &rb, int mode, int nst,
+                                            const float4 *sxy, const float4 *szw, const uint8_t *su, BuildLane &L,
+                                            int cshift) {
+  const int lane = threadIdx.x & 31;
+  const float *fzw = reinterpret_cast<const float *>(szw);
+  float *pxy = const_cast<float *>(reinterpret_cast<const float *>(sxy));
+  float *pzw = const_cast<float *>(fzw);
+  const int npad32 = (nst + 31) & ~31;
+  for (int t = nst + lane; t < npad32; t += 32) {  // far-away padding up to a whole 32
+    const int e = (t >> 1) * 4 + (t & 1);
+    pxy[e] = 1e18f;
+    pxy[e + 2] = 1e18f;
+    pzw[e] = 1e18f;
+    pzw[e + 2] = 0.f;
+  }
+  __syncwarp();
+  const float lo = b.ce2_lo;
+  const int cap = d.cap;
+  const int self = L.selfpos[lane];
+  const uint32_t ci_code = (uint32_t)L.ci << CODE_SHIFT;
+  for (int t0 = 0; t0 < npad32; t0 += 32) {
+    // phase 1: bits of the sure hits (q < ce2_lo) and of everything up to ce2_hi
+    uint32_t hm = 0u, am = 0u;
+#pragma unroll
+    for (int u = 0; u < 32; u += 2) {
+      const int pr = (t0 + u) >> 1;
+      const float4 xy = sxy[pr];                                     // broadcast
+      const float2 z = *reinterpret_cast<const float2 *>(&szw[pr]);  // broadcast
+      float q0, q1;
+      dist2_pair(xy, z, L.rxx, L.ryy, L.rzz, q0, q1);
+      if (q0 < lo) hm |= 1u << u;
+      if (q0 <= L.hi) am |= 1u << u;
+      if (q1 < lo) hm |= 2u << u;
+      if (q1 <= L.hi) am |= 2u << u;
+    }
+    const int ts = self - t0;  // the atom itself is no candidate
+    if (ts >= 0 && ts < 32) am &= ~(1u << ts);
+    hm &= am;
+    uint32_t bm = am & ~hm;  // the band
+    if (__any_sync(FULL_MASK, bm != 0u)) {  // rare: the exact FP64 predicate
+      while (bm) {
+        const int u = __ffs(bm) - 1;
+        bm &= bm - 1u;
+        const int t = t0 + u;
+        const uint32_t w = __float_as_uint(fzw[(t >> 1) * 4 + 2 + (t & 1)]);
+        const int j = (int)(w & IDX_MASK);
+        int img = (int)(w >> CODE_SHIFT);
+        if (mode != 0) {  // the image from the candidate cell's unwrapped index
+          const int s = su[t], r = s >> 3;
+          const int nx = L.cx + (s & 7) - 1 - L.ci, ny = L.cy + r % 3 - 1, nz = L.cz + r / 3 - 1;
+          img = image_code(nx < 0 ? -1 : (nx >= rb.nc[0] ? 1 : 0), ny < 0 ? -1 : (ny >= rb.nc[1] ? 1 : 0),
+                           nz < 0 ? -1 : (nz >= rb.nc[2] ? 1 : 0));
+        }
+        if (exact_pair(d, rb, b.ce2, L.i, j, img)) hm |= 1u << u;
+      }
+    }
+    // phase 2: the hits, in candidate order (with ignore_intra_molecule none of the
+    // atom's own molecule, as Lj::calculate_acceleration skips them, src/force/lj.cpp:446)
+    while (hm) {
+      const int u = __ffs(hm) - 1;
+      hm &= hm - 1u;
+      const int t = t0 + u;
+      uint32_t w = __float_as_uint(fzw[(t >> 1) * 4 + 2 + (t & 1)]);
+      if (d.mol && d.mol[w & IDX_MASK] == L.mol) continue;
+      if (mode != 0) w -= ci_code;  // stencil index of j's cell relative to the atom's
+      if (L.cnt < cap) L.row[((L.cnt >> 2) << cshift) + (L.cnt & 3)] = w;
+      ++L.cnt;
+    }
+  }
+  __syncwarp();  // the stage is refilled next
+}
+
+__device__ inline float warp_minf(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(FULL_MASK, v, o));
+  return v;
+}
+__device__ inline float warp_maxf(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(FULL_MASK, v, o));
+  return v;
+}
+
+__global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_group(Dev d, Box b, int mode, int forced) {
   __shared__ float4 stage_all[BUILD_WARPS][BUILD_STAGE];
+  __shared__ uint8_t su_all[BUILD_WARPS][BUILD_STAGE];
+  __shared__ int selfpos_all[BUILD_WARPS][32];
   const int lane = threadIdx.x & 31;
   // pair p = candidates 2p, 2p+1: sxy[p] = {x, x', y, y'}, szw[p] = {z, z', word, word'}
   float4 *sxy = stage_all[threadIdx.x >> 5], *szw = sxy + BUILD_STAGE / 2;
   float *fxy = reinterpret_cast<float *>(sxy), *fzw = reinterpret_cast<float *>(szw);
+  uint8_t *su = su_all[threadIdx.x >> 5];
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-  const int cap = d.cap;
   const int cshift = 7 - log2_pow2(d.tpa);  // chunk stride 4A words = 2^(log2 A + 2)
+  const unsigned lt_mask = (1u << lane) - 1u;
+  const int nwin = (b.nslot + 31) >> 5;
   int wmax = 0;
-  for (int cell = gw; cell < b.ncell_all; cell += nw) {
-    const int rep = rep_of_cell(b, cell);
-    if (rep < 0 || !rebuild_on(b, rep, forced)) continue;
-    const RepBox &rb = repbox(b, rep);
-    const int lc = cell - rb.cell_off;
-    if (lc >= rb.ncell) continue;  // the padding cell
-    const int hs = d.cell_start[cell], he = d.cell_start[cell + 1];
-    const int cx = lc % rb.nc[0], cy = (lc / rb.nc[0]) % rb.nc[1], cz = lc / (rb.nc[0] * rb.nc[1]);
-    // lane k < 27: stencil cell k's first slot and count (exclusive scan = its
-    // position in the flattened candidate sequence), list-word code and origin offset
-    int kb = 0, kn = 0;
-    uint32_t kcode = 0u;
-    float kox = 0.f, koy = 0.f, koz = 0.f;
-    if (lane < 27) {
-      const StencilCell s = stencil_cell(rb, cx, cy, cz, lane);
-      kb = d.cell_start[s.c2];
-      kn = d.cell_start[s.c2 + 1] - kb;
-      kcode = (uint32_t)(mode == 0 ? s.img : lane) << CODE_SHIFT;
-      kox = s.ox; koy = s.oy; koz = s.oz;
+  for (int win = gw; win < nwin; win += nw) {
+    BuildLane L;
+    L.i = (win << 5) + lane;
+    const int rep = L.i < b.nslot ? rep_of_slot(b, L.i) : -1;
+    const bool act = rep >= 0 && rebuild_on(d, b, rep, forced);
+    int rowkey = -1;  // global index of the first cell of the atom's row: one value per (replica, row)
+    float4 ri = make_float4(0.f, 0.f, 0.f, 0.f);
+    L.cx = L.cy = L.cz = 0;
+    L.mol = 0;
+    if (act) {
+      const RepBox &rb = repbox(b, rep);
+      const int c = d.cell_of[L.i], lc = c - rb.cell_off;
+      L.cx = lc % rb.nc[0];
+      L.cy = (lc / rb.nc[0]) % rb.nc[1];
+      L.cz = lc / (rb.nc[0] * rb.nc[1]);
+      rowkey = c - L.cx;
+      ri = d.rel[L.i];
+      if (d.mol) L.mol = d.mol[L.i];
     }
-    int kpre = kn;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(FULL_MASK, kpre, o);
-      if (lane >= o) kpre += y;
-    }
-    const int ntot = __shfl_sync(FULL_MASK, kpre, 26);
-    kpre -= kn;
-    const int k13 = __shfl_sync(FULL_MASK, kpre, 13);  // where the home cell's atoms start
-    for (int h0 = hs; h0 < he; h0 += 32) {
-      const int i = h0 + lane;
-      const bool act = i < he;
-      const float4 ri = act ? d.rel[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-      const unsigned long long rxx = pack2(ri.x), ryy = pack2(ri.y), rzz = pack2(ri.z);
-      const float lo = b.ce2_lo;
-      const float hi = act ? b.ce2_hi : -1.0f;  // idle lanes never hit
-      // the atom itself: stencil cell 13 (the home cell, image zero), at its rank in the cell
-      const int tself = act ? k13 + (i - hs) : -1;
-      const int mol_i = d.mol && act ? d.mol[i] : 0;
-      uint32_t *row = d.nbr + nbr_block_base(act ? i : hs, cap, d.tpa);
-      int cnt = 0;
-      for (int p0 = 0; p0 < ntot; p0 += BUILD_STAGE) {
-        const int np = min(BUILD_STAGE, ntot - p0);
-        __syncwarp();
-        for (int k = 0; k < 27; ++k) {
-          const int f0 = __shfl_sync(FULL_MASK, kpre, k), cn = __shfl_sync(FULL_MASK, kn, k);
-          const int lo_t = max(f0, p0), hi_t = min(f0 + cn, p0 + np);
-          if (lo_t >= hi_t) continue;
+    L.row = d.nbr + nbr_block_base(act ? L.i : 0, d.cap, d.tpa);
+    int *selfpos = selfpos_all[threadIdx.x >> 5];
+    L.selfpos = selfpos;
+    const int win0 = win << 5;
+    unsigned pending = __ballot_sync(FULL_MASK, act);
+    while (pending) {
+      const int leader = __ffs(pending) - 1;
+      const int rk = __shfl_sync(FULL_MASK, rowkey, leader);
+      const int cx0 = __shfl_sync(FULL_MASK, L.cx, leader);  // slots sort by cell: the leader's is the lowest
+      const int grep = __shfl_sync(FULL_MASK, rep, leader);
+      const unsigned mem = __ballot_sync(FULL_MASK, ((pending >> lane) & 1u) && rowkey == rk && L.cx - cx0 <= GROUP_SPAN);
+      pending &= ~mem;
+      L.me = (mem >> lane) & 1u;
+      const RepBox &rb = repbox(b, grep);
+      const int span = __reduce_max_sync(FULL_MASK, L.me ? L.cx - cx0 : 0);
+      L.ci = L.me ? L.cx - cx0 : 0;
+      const int cy = __shfl_sync(FULL_MASK, L.cy, leader), cz = __shfl_sync(FULL_MASK, L.cz, leader);
+      // the atom in the group frame (origin: the group's first cell), and the group's box
+      const float gx = ri.x + (float)L.ci * rb.wf[0], gy = ri.y, gz = ri.z;
+      const float bxl = warp_minf(L.me ? gx : 1e30f), bxh = warp_maxf(L.me ? gx : -1e30f);
+      const float byl = warp_minf(L.me ? gy : 1e30f), byh = warp_maxf(L.me ? gy : -1e30f);
+      const float bzl = warp_minf(L.me ? gz : 1e30f), bzh = warp_maxf(L.me ? gz : -1e30f);
+      L.rxx = pack2(gx);
+      L.ryy = pack2(gy);
+      L.rzz = pack2(gz);
+      L.hi = L.me ? b.ce2_hi : -1.0f;
+      L.cnt = 0;
+      // candidate cells q = r * nu + u: row r = (dy+1) + 3 (dz+1), x cell cx0 - 1 + u
+      const int nu = span + 3, ncand = 9 * nu;
+      int nst = 0;
+      selfpos[lane] = -1;
+      __syncwarp();
+      for (int q0 = 0; q0 < ncand; q0 += 32) {
+        // lane q - q0: the candidate cell's first slot, count, image code, origin offset
+        int kb = 0, kn = 0, ks = 0, kimg = 0;
+        uint32_t kcode = 0u;
+        float kox = 0.f, koy = 0.f, koz = 0.f;
+        const int q = q0 + lane;
+        if (q < ncand) {
+          const int r = q / nu, u = q - r * nu;
+          const int dy = r % 3 - 1, dz = r / 3 - 1;
+          int nx = cx0 - 1 + u, ny = cy + dy, nz = cz + dz, sx = 0, sy = 0, sz = 0;
+          if (nx < 0) { nx += rb.nc[0]; sx = -1; } else if (nx >= rb.nc[0]) { nx -= rb.nc[0]; sx = 1; }
+          if (ny < 0) { ny += rb.nc[1]; sy = -1; } else if (ny >= rb.nc[1]) { ny -= rb.nc[1]; sy = 1; }
+          if (nz < 0) { nz += rb.nc[2]; sz = -1; } else if (nz >= rb.nc[2]) { nz -= rb.nc[2]; sz = 1; }
+          const int c2 = rb.cell_off + nx + rb.nc[0] * (ny + rb.nc[1] * nz);
+          kb = d.cell_start[c2];
+          kn = d.cell_start[c2 + 1] - kb;
+          // mode 0: the image code; mode 1: x index + 3 x row (<= 7 + 24), from which a
+          // member's stencil index follows by subtracting its own x index
+          kimg = image_code(sx, sy, sz);
+          kcode = (uint32_t)(mode == 0 ? kimg : u + 3 * r) << CODE_SHIFT;
+          ks = u | (r << 3);
+          kox = (float)(u - 1) * rb.wf[0];
+          koy = (float)dy * rb.wf[1];
+          koz = (float)dz * rb.wf[2];
+        }
+        const int kend = min(32, ncand - q0);
+        for (int k = 0; k < kend; ++k) {
+          const int cn = __shfl_sync(FULL_MASK, kn, k);
+          if (cn == 0) continue;
           const int jb = __shfl_sync(FULL_MASK, kb, k);
           const uint32_t code = __shfl_sync(FULL_MASK, kcode, k);
+          const uint8_t sbyte = (uint8_t)__shfl_sync(FULL_MASK, ks, k);
+          const bool zero_img = __shfl_sync(FULL_MASK, kimg, k) == CODE_ZERO;
           const float ox = __shfl_sync(FULL_MASK, kox, k), oy = __shfl_sync(FULL_MASK, koy, k),
                       oz = __shfl_sync(FULL_MASK, koz, k);
-          for (int t = lo_t + lane; t < hi_t; t += 32) {
-            const int j = jb + (t - f0);
-            const float4 rj = __ldg(&d.rel[j]);
-            const int e = ((t - p0) >> 1) * 4 + ((t - p0) & 1);
-            fxy[e] = rj.x + ox;
-            fxy[e + 2] = rj.y + oy;
-            fzw[e] = rj.z + oz;
-            fzw[e + 2] = __uint_as_float((uint32_t)j | code);
-          }
-        }
-        const int npad32 = (np + 31) & ~31;
-        for (int t = np + lane; t < npad32; t += 32) {
-          const int e = (t >> 1) * 4 + (t & 1);
-          fxy[e] = 1e18f;
-          fxy[e + 2] = 1e18f;
-          fzw[e] = 1e18f;
-          fzw[e + 2] = 0.f;
-        }
-        __syncwarp();
-        for (int t0 = 0; t0 < npad32; t0 += 32) {
-          // phase 1: bits of the sure hits (q < ce2_lo) and of everything up to ce2_hi
-          uint32_t hm = 0u, am = 0u;
-#pragma unroll
-          for (int u = 0; u < 32; u += 2) {
-            const int pr = (t0 + u) >> 1;
-            const float4 xy = sxy[pr];                                  // broadcast
-            const float2 z = *reinterpret_cast<const float2 *>(&szw[pr]);  // broadcast
-            float q0, q1;
-            dist2_pair(xy, z, rxx, ryy, rzz, q0, q1);
-            if (q0 < lo) hm |= 1u << u;
-            if (q0 <= hi) am |= 1u << u;
-            if (q1 < lo) hm |= 2u << u;
-            if (q1 <= hi) am |= 2u << u;
-          }
-          const int ts = tself - (p0 + t0);  // the atom itself is no candidate
-          if (ts >= 0 && ts < 32) am &= ~(1u << ts);
-          hm &= am;
-          uint32_t bm = am & ~hm;  // the band
-          if (__any_sync(FULL_MASK, bm != 0u)) {  // rare: the exact FP64 predicate
-            while (bm) {
-              const int u = __ffs(bm) - 1;
-              bm &= bm - 1u;
-              const uint32_t w = __float_as_uint(fzw[((t0 + u) >> 1) * 4 + 2 + (u & 1)]);
-              const int code = (int)(w >> CODE_SHIFT);
-              int img = code;
-              if (mode != 0) {  // recover the image from the stencil index
-                const int nx = cx + code % 3 - 1, ny = cy + (code / 3) % 3 - 1, nz = cz + code / 9 - 1;
-                img = image_code(nx < 0 ? -1 : (nx >= rb.nc[0] ? 1 : 0), ny < 0 ? -1 : (ny >= rb.nc[1] ? 1 : 0),
-                                 nz < 0 ? -1 : (nz >= rb.nc[2] ? 1 : 0));
-              }
-              if (exact_pair(d, rb, b.ce2, i, (int)(w & IDX_MASK), img)) hm |= 1u << u;
+          for (int t0 = 0; t0 < cn; t0 += 32) {
+            const int t = t0 + lane;
+            bool keep = false;
+            float X = 0.f, Y = 0.f, Z = 0.f;
+            if (t < cn) {
+              const float4 rj = __ldg(&d.rel[jb + t]);
+              X = rj.x + ox;
+              Y = rj.y + oy;
+              Z = rj.z + oz;
+              // squared distance to the group's box; within the band's upper end: staged
+              const float ex = fmaxf(fmaxf(bxl - X, X - bxh), 0.f), ey = fmaxf(fmaxf(byl - Y, Y - byh), 0.f),
+                          ez = fmaxf(fmaxf(bzl - Z, Z - bzh), 0.f);
+              keep = fmaf(ez, ez, fmaf(ey, ey, ex * ex)) <= b.ce2_hi;
             }
-          }
-          // phase 2: the hits, in candidate order (ignore_intra_molecule: none of the
-          // atom's own molecule, as Lj::calculate_acceleration skips them, lj.cpp:446)
-          while (hm) {
-            const int u = __ffs(hm) - 1;
-            hm &= hm - 1u;
-            const uint32_t w = __float_as_uint(fzw[((t0 + u) >> 1) * 4 + 2 + (u & 1)]);
-            if (d.mol && d.mol[w & IDX_MASK] == mol_i) continue;
-            if (cnt < cap) row[((cnt >> 2) << cshift) + (cnt & 3)] = w;
-            ++cnt;
+            const unsigned km = __ballot_sync(FULL_MASK, keep);
+            if (keep) {
+              const int s = nst + __popc(km & lt_mask);
+              const int e = (s >> 1) * 4 + (s & 1);
+              fxy[e] = X;
+              fxy[e + 2] = Y;
+              fzw[e] = Z;
+              fzw[e + 2] = __uint_as_float((uint32_t)(jb + t) | code);
+              su[s] = sbyte;
+              // a window atom at its own cell and zero image: that lane's self position
+              const unsigned l = (unsigned)(jb + t - win0);
+              if (zero_img && l < 32u) selfpos[l] = s;
+            }
+            nst += __popc(km);
+            if (nst > BUILD_STAGE - 32) {
+              __syncwarp();
+              build_sweep(d, b, rb, mode, nst, sxy, szw, su, L, cshift);
+              selfpos[lane] = -1;
+              __syncwarp();
+              nst = 0;
+            }
           }
         }
       }
-      if (act) {
-        d.nnbr[i] = min(cnt, cap);
-        if (cnt > cap) atomicMax(&d.flags[F_OVERFLOW], cnt);
-        wmax = max(wmax, cnt);
+      if (nst > 0) {
+        __syncwarp();
+        build_sweep(d, b, rb, mode, nst, sxy, szw, su, L, cshift);
+      }
+      if (L.me) {
+        d.nnbr[L.i] = min(L.cnt, d.cap);
+        if (L.cnt > d.cap) atomicMax(&d.flags[F_OVERFLOW], L.cnt);
+        wmax = max(wmax, L.cnt);
       }
     }
   }
@@ -659,14 +705,17 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_warp(Dev d, Box b
   if (lane == 0 && wmax > 0) atomicMax(&d.flags[F_MAXNB], wmax);
 }
 
-// after the build: count the rebuilt replicas, clear their flags and the global one
+// after the build: count the rebuilt replicas, clear their flags and the global one;
+// a build that overflowed its rows halts the chunk (the host grows the list and
+// completes the step)
 __global__ void __launch_bounds__(256) k_finish_rebuild(Dev d, Box b, int forced) {
+  if (halted(d)) return;
   __shared__ int total;
   if (threadIdx.x == 0) total = 0;
   __syncthreads();
   int n = 0;
   for (int r = threadIdx.x; r < b.nrep; r += blockDim.x) {
-    n += rebuild_on(b, r, forced) ? 1 : 0;
+    n += (forced || b.rep_flag[r] != 0) ? 1 : 0;
     b.rep_flag[r] = 0;
   }
 #pragma unroll
@@ -679,13 +728,22 @@ __global__ void __launch_bounds__(256) k_finish_rebuild(Dev d, Box b, int forced
       d.flags[F_PASSES] += 1;
     }
     d.flags[F_REBUILD] = 0;
+    if (d.flags[F_OVERFLOW]) d.flags[F_HALT] = 1;
   }
 }
 
-// Inside a captured step: the half-skin flag becomes the value of the graph's
-// conditional node that wraps the rebuild kernels.
+// Inside a captured step that starts with a drift kernel: a NaN the drift saw halts
+// the chunk, and the half-skin flag becomes the value of the graph's conditional
+// node that wraps the rebuild kernels (when the pair kernel drifted the step, its
+// last block does both).
 __global__ void k_set_rebuild_cond(Dev d, cudaGraphConditionalHandle h) {
-  cudaGraphSetConditional(h, d.flags[F_REBUILD] != 0 ? 1u : 0u);
+  if (d.flags[F_NAN]) d.flags[F_HALT] = 1;
+  cudaGraphSetConditional(h, (d.flags[F_REBUILD] != 0 && d.flags[F_HALT] == 0) ? 1u : 0u);
+}
+
+// the same NaN check for steps launched from the host (no conditional node)
+__global__ void k_halt_check(Dev d) {
+  if (d.flags[F_NAN]) d.flags[F_HALT] = 1;
 }
 
 // ---------------------------------------------------------------------------
@@ -710,6 +768,7 @@ __device__ inline void thermo_finish(double ke2, const double P3[3], double msum
 
 __global__ void __launch_bounds__(256) k_thermo_final(Dev d, ThermoCfg tc, int nb_ke, int nb_ev, int nb_ke_end,
                                                       int ring_slot) {
+  if (halted(d)) return;  // every block alike: the ticket is not taken
   // level 1: block g folds partials g*256 + tid, stepping by the grid's threads (one
   // round of independent loads for up to 8192 partials)
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
@@ -767,6 +826,7 @@ __global__ void __launch_bounds__(256) k_thermo_final(Dev d, ThermoCfg tc, int n
 // from the current velocities; ev: virial and PE from the per-slot sums the
 // force kernel wrote (VV: P gets the virial term).  thermo_rep[r*8 + 0..5].
 __global__ void __launch_bounds__(256) k_thermo_rep(Dev d, Box b, ThermoCfg tc, int ke, int ev) {
+  if (halted(d)) return;
   const int rep = blockIdx.x;
   const RepBox &rb = repbox(b, rep);
   double v[7] = {0, 0, 0, 0, 0, 0, 0};
@@ -804,7 +864,14 @@ __global__ void __launch_bounds__(256) k_thermo_rep(Dev d, Box b, ThermoCfg tc, 
   }
 }
 
-__global__ void k_advance_step(Dev d, int nsteps) { *d.step_base += nsteps; }
+// end of a chunk: the step counter advances by the steps whose pair kernel ran; a
+// halted chunk records how many that were (the host completes the failed step)
+__global__ void k_advance_step(Dev d) {
+  const int ok = d.flags[F_STEPS_OK];
+  *d.step_base += ok;
+  if (d.flags[F_HALT]) d.flags[F_HALT_STEP] += ok;
+  d.flags[F_STEPS_OK] = 0;
+}
 
 // ---------------------------------------------------------------------------
 // constraint::Nve (src/constraint/nve.cpp:132-184), single system: on steps whose
@@ -813,7 +880,9 @@ __global__ void k_advance_step(Dev d, int nsteps) { *d.step_base += nsteps; }
 // 1..3), velocities scaled by lambda, then the temperature and pressure of the
 // step follow the scaled velocities (finalize_temperature / finalize_pressure).
 // ---------------------------------------------------------------------------
-__device__ inline bool nve_applies(const Dev &d, const NveCfg &c, int k) { return (*d.step_base + k) % c.step == 0; }
+__device__ inline bool nve_applies(const Dev &d, const NveCfg &c, int k) {
+  return !halted(d) && (*d.step_base + k) % c.step == 0;
+}
 
 __global__ void __launch_bounds__(256) k_nve_ke(Dev d, int n, NveCfg c, int k) {
   if (!nve_applies(d, c, k)) return;
@@ -1086,14 +1155,19 @@ int launch_rebuild(const Dev &d, const Box &b, const LaunchCfg &lc, int forced, 
   k_copy_state<<<g, 256, 0, st>>>(d, b, forced);
   k_gather<<<g, 256, 0, st>>>(d, b, forced);
   const int mode = lc.precision == CAVGPU_MIXED ? 1 : 0;
-  const int build_grid = std::min(ceil_div(b.ncell_all, BUILD_WARPS), num_sms() * 8);
-  k_build_warp<<<build_grid, BUILD_WARPS * 32, 0, st>>>(d, b, mode, forced);
+  const int build_grid = std::min(ceil_div(ceil_div(b.nslot, 32), BUILD_WARPS), num_sms() * 8);
+  k_build_group<<<build_grid, BUILD_WARPS * 32, 0, st>>>(d, b, mode, forced);
   k_finish_rebuild<<<1, 256, 0, st>>>(d, b, forced);
   return chk();
 }
 
 int launch_set_rebuild_cond(const Dev &d, cudaGraphConditionalHandle h, cudaStream_t st) {
   k_set_rebuild_cond<<<1, 1, 0, st>>>(d, h);
+  return chk();
+}
+
+int launch_halt_check(const Dev &d, cudaStream_t st) {
+  k_halt_check<<<1, 1, 0, st>>>(d);
   return chk();
 }
 
@@ -1108,8 +1182,8 @@ int launch_thermo_replicas(const Dev &d, const Box &b, const ThermoCfg &tc, int 
   return chk();
 }
 
-int launch_advance_step(const Dev &d, int nsteps, cudaStream_t st) {
-  k_advance_step<<<1, 1, 0, st>>>(d, nsteps);
+int launch_advance_step(const Dev &d, cudaStream_t st) {
+  k_advance_step<<<1, 1, 0, st>>>(d);
   return chk();
 }
 
