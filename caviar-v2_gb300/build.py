@@ -46,32 +46,21 @@ def build(verbose=False):
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
-    # test helper: cuRAND's Philox4x32-10 blocks (tests/test_gpu_philox.py)
-    cmd = [NVCC, *ARCH, "-O2", "-std=c++17", os.path.join(ROOT, "tests", "cpp", "philox_curand.cu"), "-o", PHILOX]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"nvcc failed on philox_curand.cu:\n{r.stderr}")
     build_host()
     return LIB
 
 
 HOST_LIB = os.path.join(HERE, "libcaviar2_gpu.so")
-HOST_HARNESS = os.path.join(OBJ, "host_harness")
-PHILOX = os.path.join(OBJ, "philox_curand")
 LJ_MD = os.path.join(OBJ, "lj_md")
 
 
 def build_host():
-    """The CAVIAR2-shaped C++ API (host/) over libcavgpu.so, its test harness and the
-    lj_md driver."""
+    """The CAVIAR2-shaped C++ API (host/) over libcavgpu.so and the lj_md driver."""
     inc = ["-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(HERE, "host")]
     cxx = os.environ.get("CXX", "g++")
     steps = [
         [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-pthread", "-fPIC", "-shared", *inc,
          os.path.join(HERE, "host", "caviar2_gpu.cpp"), "-o", HOST_LIB, "-L" + HERE, "-lcavgpu", "-Wl,-rpath,$ORIGIN"],
-        [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-pthread", *inc,
-         os.path.join(ROOT, "tests", "cpp", "host_harness.cpp"), "-o", HOST_HARNESS, "-L" + HERE, "-lcaviar2_gpu",
-         "-lcavgpu", "-Wl,-rpath," + HERE],
         [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-pthread", *inc, os.path.join(HERE, "host", "lj_md.cpp"),
          "-o", LJ_MD, "-L" + HERE, "-lcaviar2_gpu", "-lcavgpu", "-Wl,-rpath," + HERE],
     ]

@@ -310,6 +310,20 @@ void Md_simulator::initialize() {
   Domain &dom = caviar_->domain;
   Neighborlist &nl = caviar_->neighborlist;
   if (ad.k_b < 0) caviar_->log.error_all("k_b is not set.");
+  // Atom_data::add_atom(id, type, pos, vel) takes an atom outside the domain, which
+  // the reference then treats as another rank's for the whole run (left out of the
+  // kinetic energy and temperature); the GPU path takes only atoms inside it, as
+  // Atom_data::add_atom(tools::Atom &) does (src/atom_data/add_unique_atom_molecule.cpp:29-38)
+  {
+    const auto &o = ad.atom_struct_owned;
+    for (size_t j = 0; j < o.position.size(); ++j) {
+      const auto &x = o.position[j];
+      if (x.x < dom.lower_global.x || x.x >= dom.upper_global.x || x.y < dom.lower_global.y ||
+          x.y >= dom.upper_global.y || x.z < dom.lower_global.z || x.z >= dom.upper_global.z)
+        caviar_->log.error_all("Md_simulator::initialize: the atom with id " + std::to_string(o.id[j]) +
+                               " starts outside the domain; the GPU path takes atoms inside it only.");
+    }
+  }
 
   cavgpu_params p;
   cavgpu_default_params(&p);
@@ -402,10 +416,14 @@ void Md_simulator::steps_from_time() {
 }
 
 void Md_simulator::setup() {
-  // Md_simulator::step's first call: time from the step index, then setup's
-  // time-mode conversion (src/md_simulator.cpp:458, 569-573)
-  time = dt * initial_step;
+  // setup's time-mode conversion (src/md_simulator.cpp:569-573), then the time of the
+  // first step from its index, as Md_simulator::step's first call sets it
+  // (src/md_simulator.cpp:458).  The reference sets the time before the conversion,
+  // from the index its run() loop then does not use (its run() reads the loop bounds
+  // before setup and runs no step in time mode); run() here sets up first and runs
+  // from the converted index, so the writers see (step i, time i * dt).
   steps_from_time();
+  time = dt * initial_step;
   check(cavgpu_setup(ctx_), "cavgpu_setup");
   // setup takes the temperature, not the pressure (src/md_simulator.cpp:605-607)
   Atom_data &ad = caviar_->atom_data;

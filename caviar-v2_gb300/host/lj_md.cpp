@@ -4,10 +4,12 @@
 // on an FCC lattice at density 0.8442 and temperature 1.44 (rc 2.5, skin 0.3,
 // dt 0.005, velocity Verlet).  Prints one JSON line with the wall time of run().
 //
-//   lj_md [--cells C] [--steps K] [--xyz X] [--thermo T] [--msd M] [--mixed]
-//         [--no-tune] [--out PREFIX]
-//   C^3 FCC cells (4 C^3 atoms); xyz frames every X steps, kinetic energy,
-//   temperature and pressure every T steps, MSD every M steps (0 = off).
+//   lj_md [--cells C] [--steps K | --time T0 T1] [--xyz X] [--thermo T] [--msd M]
+//         [--mixed] [--no-tune] [--out PREFIX]
+//   C^3 FCC cells (4 C^3 atoms); K steps, or the steps of the time span [T0, T1)
+//   (Md_simulator::set_initial_time / set_final_time); xyz frames every X steps,
+//   kinetic energy, temperature and pressure every T steps, MSD every M steps
+//   (0 = off).
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -22,6 +24,7 @@ using namespace caviar2;
 
 int main(int argc, char **argv) {
   int cells = 64, steps = 2000, xyz = 0, thermo = 0, msd = 0;
+  double time0 = -1.0, time1 = -1.0;
   bool mixed = false, tune = true;
   std::string out = "lj_md";
   for (int a = 1; a < argc; ++a) {
@@ -37,6 +40,10 @@ int main(int argc, char **argv) {
     else if (!std::strcmp(argv[a], "--mixed")) mixed = true;
     else if (!std::strcmp(argv[a], "--no-tune")) tune = false;
     else if (!std::strcmp(argv[a], "--out") && a + 1 < argc) out = argv[++a];
+    else if (!std::strcmp(argv[a], "--time") && a + 2 < argc) {
+      time0 = std::atof(argv[++a]);
+      time1 = std::atof(argv[++a]);
+    }
     else { std::fprintf(stderr, "unknown option %s\n", argv[a]); return 2; }
   }
   const double rho = 0.8442, temp = 1.44, rc = 2.5, skin = 0.3, dt = 0.005;
@@ -111,12 +118,18 @@ int main(int argc, char **argv) {
   md.set_integrator_type(Integrator_t::Velocity_verlet);
   md.set_precision(mixed ? CAVGPU_MIXED : CAVGPU_FP64);
   md.set_dt(dt);
-  md.set_initial_step(0);
-  md.set_final_step(steps);
+  if (time0 >= 0.0) {
+    md.set_initial_time(time0);
+    md.set_final_time(time1);
+  } else {
+    md.set_initial_step(0);
+    md.set_final_step(steps);
+  }
   using clk = std::chrono::steady_clock;
   const auto t0 = clk::now();
   md.initialize();
   md.setup();
+  steps = (int)(md.final_step - md.initial_step);
   if (tune) md.autotune(10);
   const auto t1 = clk::now();
   md.run();
@@ -125,9 +138,9 @@ int main(int argc, char **argv) {
   const double run_s = std::chrono::duration<double>(t2 - t1).count();
   std::printf("{\"atoms\": %zu, \"steps\": %d, \"precision\": \"%s\", \"xyz_every\": %d, \"thermo_every\": %d, "
               "\"msd_every\": %d, \"setup_s\": %.4f, \"run_s\": %.4f, \"atom_steps_per_s\": %.6g, "
-              "\"T_end\": %.6g}\n",
+              "\"T_end\": %.6g, \"initial_step\": %lld, \"final_step\": %lld, \"current_step\": %lld}\n",
               n, steps, mixed ? "mixed" : "fp64", xyz, thermo, msd, setup_s, run_s, (double)n * steps / run_s,
-              ad.temperature());
+              ad.temperature(), (long long)md.initial_step, (long long)md.final_step, (long long)md.current_step);
   md.cleanup();
   return 0;
 }

@@ -12,6 +12,32 @@ for p in (PKG, os.path.join(ROOT, "oracle"), ROOT):
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 
 
+def host_harness():
+    """tests/cpp/host_harness.cpp -- a test driver of the CAVIAR2-shaped C++ API --
+    compiled against the built libraries into tests/cpp/_build/ (when missing or older
+    than its inputs)."""
+    import subprocess
+
+    if PKG not in sys.path:
+        sys.path.insert(0, PKG)
+    import build as B
+
+    if not (os.path.exists(B.LIB) and os.path.exists(B.HOST_LIB)):
+        B.build()
+    src = os.path.join(ROOT, "tests", "cpp", "host_harness.cpp")
+    out_dir = os.path.join(ROOT, "tests", "cpp", "_build")
+    exe = os.path.join(out_dir, "host_harness")
+    inputs = [src, B.LIB, B.HOST_LIB, os.path.join(PKG, "host", "caviar2_gpu.hpp")]
+    if not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(f) for f in inputs):
+        os.makedirs(out_dir, exist_ok=True)
+        cxx = os.environ.get("CXX", "g++")
+        cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-pthread", "-I" + os.path.join(ROOT, "include"),
+               "-I" + os.path.join(PKG, "host"), src, "-o", exe, "-L" + PKG, "-lcaviar2_gpu", "-lcavgpu",
+               "-Wl,-rpath," + PKG]
+        subprocess.run(cmd, check=True, capture_output=True, text=True)
+    return exe
+
+
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 

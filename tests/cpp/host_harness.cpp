@@ -65,6 +65,20 @@ static int error_case(const std::string &n) {
     else if (n == "nve_kb_alone") { constraint::Nve v(&c); v.kb = 1.0; v.temperature = -1.0; v.verify_settings(); }
     else if (n == "nve_unset") { constraint::Nve v(&c); v.verify_settings(); }
     else if (n == "nve_energy_and_kbt") { constraint::Nve v(&c); v.energy_tot = 1.0; v.kbt = 1.0; v.verify_settings(); }
+    else if (n == "outside_start") {  // an atom placed outside the domain before the run (no GPU is reached)
+      c.domain.set_lower_global(Vector3d<double>{0.0, 0.0, 0.0});
+      c.domain.set_upper_global(Vector3d<double>{6.0, 6.0, 6.0});
+      c.domain.set_boundary_condition(Vector3d<int>{1, 1, 1});
+      c.atom_data.add_type_mass(0, 1.0);
+      c.atom_data.set_k_b(1.0);
+      c.atom_data.add_atom((size_t)0, 0, Vector3d<double>{1.0, 1.0, 1.0});
+      c.atom_data.add_atom((size_t)1, 0, Vector3d<double>{3.0, 4.0, 6.2});
+      force_field::Lj lj(&c);
+      c.add_force_field(&lj);
+      md.set_dt(0.001);
+      md.set_integrator_type(Integrator_t::Velocity_verlet);
+      md.initialize();
+    }
     else if (n == "valid") { c.neighborlist.set_cutoff(2.5); c.neighborlist.set_cutoff_extra_coef(1.1); }
     else { fprintf(stderr, "unknown error case %s\n", n.c_str()); return 3; }
   } catch (const std::runtime_error &e) {

@@ -287,8 +287,10 @@ def cases():
 
 
 def main():
-    # usage: make_golden.py [reference checkout] [case names...]  (no names: every case)
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    # usage: make_golden.py [reference checkout] [case names...]  (no names: every case);
+    # the checkout defaults to $CAVIAR2_REF, then to `reference` beside the repository
+    default = os.environ.get("CAVIAR2_REF") or os.path.join(os.path.dirname(ROOT), "reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else default
     only = set(sys.argv[2:])
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={ref}", "-j8"], check=True)
     for c in cases():

@@ -118,6 +118,24 @@ def test_pair_set_bitexact(case):
     assert digest == str(g["pairs_sha256"])
 
 
+def test_outside_start_refused_by_upload(gpu):
+    """The reference's quirk_outside_start fixture (an atom placed outside the domain,
+    which the reference keeps as another rank's): cavgpu_upload refuses it with
+    CAVGPU_E_ARG, as Atom_data::add_atom(tools::Atom &) refuses such an atom
+    (src/atom_data/add_unique_atom_molecule.cpp:29-38)."""
+    g = load_golden("quirk_outside_start")
+    p = golden_params(g)
+    outside = ~((g["pos"] >= p["lo"]) & (g["pos"] < p["hi"])).all(1)
+    assert outside.sum() == 1
+    with pytest.raises(gpu.CavError) as e:
+        gpu.System(g["pos"], g["vel"], g["typ"], p, precision=gpu.FP64)
+    assert e.value.status == gpu.E_ARG
+    inside = ~outside
+    s = gpu.System(g["pos"][inside], g["vel"][inside], g["typ"][inside], p, precision=gpu.FP64)
+    s.setup()
+    s.close()
+
+
 def test_cells_and_ghosts_bitexact(case):
     name, g, s = case
     if not int(g["use_cell_list"]):

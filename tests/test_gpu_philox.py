@@ -10,7 +10,6 @@ so this ties the GPU path's noise to NVIDIA's generator too.
 """
 import os
 import subprocess
-import sys
 
 import pytest
 
@@ -19,13 +18,19 @@ from conftest import ROOT
 pytestmark = pytest.mark.gpu
 
 
-def test_oracle_philox_equals_curand(oracle_lib):
-    sys.path.insert(0, os.path.join(ROOT, "caviar-v2_gb300"))
-    import build as B
+@pytest.fixture(scope="module")
+def philox_curand(tmp_path_factory):
+    """tests/cpp/philox_curand.cu (a test helper that calls cuRAND's device API),
+    compiled for sm_103a into a temporary directory."""
+    exe = str(tmp_path_factory.mktemp("philox") / "philox_curand")
+    nvcc = os.environ.get("NVCC", "nvcc")
+    subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O2", "-std=c++17",
+                    os.path.join(ROOT, "tests", "cpp", "philox_curand.cu"), "-o", exe], check=True)
+    return exe
 
-    if not os.path.exists(B.PHILOX):
-        B.build()
-    out = subprocess.run([B.PHILOX], capture_output=True, text=True, check=True).stdout.split("\n")
+
+def test_oracle_philox_equals_curand(oracle_lib, philox_curand):
+    out = subprocess.run([philox_curand], capture_output=True, text=True, check=True).stdout.split("\n")
     rows = [ln.split() for ln in out if ln.strip()]
     assert len(rows) == 64
     for r in rows:

@@ -16,7 +16,7 @@ import sys
 import numpy as np
 import pytest
 
-from conftest import ROOT, golden_cases, golden_params, load_golden
+from conftest import ROOT, golden_cases, golden_params, host_harness, load_golden
 
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
@@ -29,12 +29,7 @@ WRITER_CASES = [c for c in golden_cases() if "writer" in load_golden(c)]
 
 
 def harness():
-    sys.path.insert(0, os.path.join(ROOT, "caviar-v2_gb300"))
-    import build as B
-
-    if not os.path.exists(B.HOST_HARNESS):
-        B.build()
-    return B.HOST_HARNESS
+    return host_harness()
 
 
 def run_writers(g, tmp_path, mode=None):
@@ -142,3 +137,29 @@ def test_lj_md_driver_outputs(tmp_path):
     xyz = open(prefix + "_xyz.xyz").read().splitlines()
     assert len(xyz) == 4 * (864 + 2)  # frames at setup and steps 0, 100, 200
     assert xyz[0] == "864" and xyz[1] == "Atom" and len(xyz[2].split()) == 4
+
+
+def test_time_mode_run_writes_step_times(tmp_path):
+    """Md_simulator::set_initial_time / set_final_time through run(): setup() turns
+    [1.0, 2.0) at dt 0.005 into steps 200 .. 400 with the reference's (int)time / dt
+    (src/md_simulator.cpp:569-573), run() takes exactly those 200 steps, and every row
+    the writers emit carries (step i, time i dt) -- setup's own row stays (0, 0), as
+    the reference's setup writes it (src/md_simulator.cpp:609-610)."""
+    import json
+
+    harness()
+    import build as B
+
+    prefix = str(tmp_path / "t")
+    r = subprocess.run([B.LJ_MD, "--cells", "4", "--time", "1.0", "2.0", "--thermo", "20", "--no-tune", "--out",
+                        prefix], capture_output=True, text=True, check=True)
+    rep = json.loads([ln for ln in r.stdout.splitlines() if ln.startswith("{")][-1])
+    assert (rep["initial_step"], rep["final_step"], rep["steps"]) == (200, 400, 200)
+    assert rep["current_step"] == 400
+    rows = [ln.split() for ln in open(prefix + "_energy.txt").read().splitlines()]
+    assert rows[0][:2] == ["0", "0"]
+    steps = [int(r[0]) for r in rows[1:]]
+    assert steps == list(range(200, 400, 20))
+    for r in rows[1:]:
+        assert abs(float(r[1]) - int(r[0]) * 0.005) <= 1e-5 * int(r[0]) * 0.005, r
+

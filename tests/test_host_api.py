@@ -13,7 +13,7 @@ import sys
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, ROOT, golden_cases, golden_params, load_golden, reference_pairs
+from conftest import GOLDEN, ROOT, golden_cases, golden_params, host_harness, load_golden, reference_pairs
 
 sys.path.insert(0, GOLDEN)
 import make_golden as MG  # noqa: E402  (input writer / output reader of the harness format)
@@ -22,12 +22,7 @@ CASES = [c for c in golden_cases() if not c.startswith("quirk_")]
 
 
 def harness():
-    sys.path.insert(0, os.path.join(ROOT, "caviar-v2_gb300"))
-    import build as B
-
-    if not os.path.exists(B.HOST_HARNESS):
-        B.build()
-    return B.HOST_HARNESS
+    return host_harness()
 
 
 def run_host(g, tmp_path, mixed=False):
@@ -151,6 +146,18 @@ def test_setter_validation_matches_reference(case, status, message, site):
     r = subprocess.run([harness(), "--error", case], capture_output=True, text=True, timeout=60)
     assert r.returncode == status, (site, r.stderr)
     assert message in r.stderr, site
+
+
+def test_atom_outside_the_domain_is_refused():
+    """Deliberate difference: the reference's Atom_data::add_atom(id, type, pos, vel)
+    keeps an atom that starts outside the domain and leaves it out of the kinetic
+    energy and temperature for the whole run (the quirk_outside_start fixture); the GPU
+    path takes atoms inside the domain only, as Atom_data::add_atom(tools::Atom &)
+    does (src/atom_data/add_unique_atom_molecule.cpp:29-38).  Md_simulator::initialize
+    stops through Log::error_all before any GPU call.  CPU only."""
+    r = subprocess.run([harness(), "--error", "outside_start"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1, r.stderr
+    assert "the atom with id 1 starts outside the domain" in r.stderr
 
 
 def test_valid_settings_raise_nothing():

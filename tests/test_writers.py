@@ -14,7 +14,7 @@ import sys
 import numpy as np
 import pytest
 
-from conftest import ROOT, golden_cases, golden_params, load_golden
+from conftest import ROOT, golden_cases, golden_params, host_harness, load_golden
 
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import writer_text as WT  # noqa: E402
@@ -35,12 +35,7 @@ def test_writer_cases_present():
 
 def test_number_text_matches_ostream():
     """append_general6 (the writers' double-to-text) equals std::ostream's default output."""
-    sys.path.insert(0, os.path.join(ROOT, "caviar-v2_gb300"))
-    import build as B
-
-    if not os.path.exists(B.HOST_HARNESS):
-        B.build_host()
-    r = subprocess.run([B.HOST_HARNESS, "--format"], capture_output=True, text=True)
+    r = subprocess.run([host_harness(), "--format"], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     assert " 0 mismatches" in r.stdout
 
