@@ -79,6 +79,33 @@ def dist_setup():
     return ws, rank, local
 
 
+def relaunch_under_torchrun(argv, n):
+    """`--gpus N` (N > 1) without a launcher: start N ranks of this script through
+    torch.distributed.run on this node (127.0.0.1) and return their exit status."""
+    port = 29500 + os.getpid() % 2000
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", str(n),
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__)] + list(argv)
+    return subprocess.call(cmd)
+
+
+def replica_share(n_rep, ws, rank):
+    """Replicas of a batch that rank `rank` of `ws` runs: r = rank, rank + ws, ...
+    (round robin: every rank's share holds the same spread of sizes).  The replicas
+    are independent systems, so the shares need no communication."""
+    return list(range(rank, n_rep, ws))
+
+
+def sum_over_ranks(ws, x):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def barrier(ws):
     if ws > 1:
         import torch.distributed as dist
@@ -180,6 +207,20 @@ def cpu_reference_rate(pos, vel, typ, params, steps, warmup):
     return len(pos) * steps / dt, dt
 
 
+def cpu_model():
+    """The host CPU's model name (lscpu), for the CPU baseline's record."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+
+    return platform.machine()
+
+
 def read_profile_traffic(name):
     """dram bytes per launch recorded in a committed ncu summary, or None."""
     path = os.path.join(ROOT, "profiles", name)
@@ -230,9 +271,11 @@ def time_device(cavgpu, torch, pos, vel, typ, params, precision, steps, warmup, 
     return s, out
 
 
-def time_batch(cavgpu, torch, systems, params, precision, steps, warmup, trial_steps):
-    """A batch of replicas, device-resident: autotune, warm-up, K timed steps.
-    Returns throughput over all replicas and the per-replica thermo after the run."""
+def time_batch(cavgpu, torch, systems, params, precision, steps, warmup, trial_steps, ws=1):
+    """A batch of replicas, device-resident: autotune, warm-up, K timed steps.  With
+    ws > 1 ranks, each runs its own share of the replicas; the timed region is
+    bracketed by barriers and its time is the max over ranks.  Returns throughput
+    over all replicas of all ranks and this rank's per-replica thermo after the run."""
     b = cavgpu.Batch(systems, params, precision=precision, **LAUNCH)
     b.setup()
     choice = b.autotune(trial_steps=trial_steps)
@@ -242,48 +285,56 @@ def time_batch(cavgpu, torch, systems, params, precision, steps, warmup, trial_s
     st0 = b.stats()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
+    barrier(ws)
     e0.record(stream)
     b.step(steps)
     e1.record(stream)
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
+    barrier(ws)
+    ms = max_over_ranks(ws, e0.elapsed_time(e1))
+    atoms = sum_over_ranks(ws, b.n)
+    reps = sum_over_ranks(ws, b.nrep)
     st1 = b.stats()
     nl, fms = b.read_profile()
     th = b.thermo_batch()
-    out = dict(value=b.n * steps / (ms * 1e-3), ms_per_step=ms / steps, steps=steps, warmup=warmup,
-               atoms=b.n, replicas=b.nrep, force_ms_per_launch=fms / max(nl, 1),
+    out = dict(value=atoms * steps / (ms * 1e-3), ms_per_step=ms / steps, steps=steps, warmup=warmup,
+               atoms=int(atoms), replicas=int(reps), ranks=ws, force_ms_per_launch=fms / max(nl, 1),
                replica_rebuilds=st1["rebuilds"] - st0["rebuilds"],
                gpu_launches=st1["kernel_launches"] - st0["kernel_launches"], autotune=choice)
     b.close()
     return out, th
 
 
-def extra_workloads(cavgpu, torch, W, np, single_mixed):
+def extra_workloads(cavgpu, torch, W, np, single_mixed, ws=1, rank=0):
     """The other benchmark configurations, each timed on this GPU beside the headline:
-    4096 uneven replicas (mixed and FP64), 64 Kob-Andersen replicas (mixed Langevin)
-    and the 4,194,304-atom Langevin fluid (mixed and FP64)."""
+    4096 uneven replicas (mixed and FP64), 64 Kob-Andersen replicas (mixed Langevin),
+    split over the ranks (replica_share), then -- on rank 0 -- the 4,194,304-atom
+    Langevin fluid (mixed and FP64) and the writer runs."""
     res = {}
     sets = W.replica_set(4096)
-    systems = [(p, v, np.zeros(len(p), np.int32), np.zeros(3), b) for p, v, b, _, _ in sets]
+    mine = replica_share(len(sets), ws, rank)
+    systems = [(p, v, np.zeros(len(p), np.int32), np.zeros(3), b) for p, v, b, _, _ in (sets[r] for r in mine)]
     params = W.lj_params(systems[0][4])
-    m, _ = time_batch(cavgpu, torch, systems, params, cavgpu.MIXED, 200, 20, 10)
-    f, _ = time_batch(cavgpu, torch, systems, params, cavgpu.FP64, 20, 3, 4)
+    m, _ = time_batch(cavgpu, torch, systems, params, cavgpu.MIXED, 200, 20, 10, ws)
+    f, _ = time_batch(cavgpu, torch, systems, params, cavgpu.FP64, 20, 3, 4, ws)
     res["replicas_4096"] = {
         "workload": "4096 periodic LJ replicas, N_r ~ U[256, 8192], rho_r ~ U[0.6, 1.0], T_r ~ U[0.7, 2.0], "
                     "random FCC fill + N(0, 0.05) displacement, rc 2.5, skin 0.3, dt 0.005, NVE",
-        "mixed": m, "fp64": f, "mixed_over_single_system_mixed": m["value"] / single_mixed}
+        "mixed": m, "fp64": f, "mixed_over_single_system_mixed": m["value"] / ws / single_mixed}
     del systems, sets
     systems = []
-    for r in range(64):
+    for r in replica_share(64, ws, rank):
         pos, vel, typ, p = W.kob_andersen(n=32768, seed=1005 + r)
         systems.append((pos, vel, typ, np.zeros(3), p["hi"]))
     params = W.kob_andersen(n=32768, seed=1005)[3]
-    k, th = time_batch(cavgpu, torch, systems, params, cavgpu.MIXED, 400, 20, 20)
-    k["mean_T_over_replicas"] = float(th[:, 1].mean())
+    k, th = time_batch(cavgpu, torch, systems, params, cavgpu.MIXED, 400, 20, 20, ws)
+    k["mean_T_over_replicas"] = sum_over_ranks(ws, float(th[:, 1].sum())) / 64
     res["kob_andersen_64x32768"] = {
         "workload": "64 replicas x 32768 atoms, Kob-Andersen 80:20, rho 1.2, Langevin T 0.45 gamma 1, dt 0.003",
         "mixed": k}
     del systems
+    if rank != 0:
+        return res
     pos, vel, typ, params = W.config_langevin()
     lang = {"workload": "Langevin LJ fluid, 4,194,304 atoms (128x128x64 FCC cells), T 1.0, gamma 1, skin 0.4"}
     for prec, name, steps in ((cavgpu.MIXED, "mixed", 400), (cavgpu.FP64, "fp64", 40)):
@@ -352,8 +403,10 @@ def nve_drift(cavgpu, pos, vel, typ, params, precision, steps, every=100):
 
 
 def time_e2e(cavgpu, torch, pos, vel, typ, params, precision, steps, **launch):
-    """Through the C ABI with host buffers: pinned host arrays -> upload -> set-up ->
-    K steps (thermo of every step read back) -> download of the final state."""
+    """Through the C ABI with host buffers: pinned host arrays -> context + upload ->
+    set-up -> K steps (thermo of every step read back) -> download of the final state,
+    all timed.  Returns the rate, the bytes copied per step each way, and the wall
+    time of each phase (the per-call fixed cost is everything but `steps_ms`)."""
     import numpy as np
 
     n = len(pos)
@@ -366,26 +419,35 @@ def time_e2e(cavgpu, torch, pos, vel, typ, params, precision, steps, **launch):
     op = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
     ov = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
     oa = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    thermo = np.zeros((steps, 5))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     s = cavgpu.System(hp, hv, ht.view(np.uint64), params, precision=precision, **launch)
+    t1 = time.perf_counter()
     s.setup()
-    thermo = np.zeros((steps, 5))
+    t2 = time.perf_counter()
     rc = cavgpu.lib().cavgpu_run(s._h, steps, 1, cavgpu._ptr(thermo))
     if rc:
         raise cavgpu.CavError(rc, "run")
+    t3 = time.perf_counter()
     cavgpu.lib().cavgpu_download(s._h, cavgpu._ptr(op), cavgpu._ptr(ov), cavgpu._ptr(oa))
-    dt = time.perf_counter() - t0
+    t4 = time.perf_counter()
     s.close()
     h2d = n * (3 * 8 + 3 * 8 + 8)
     d2h = steps * 5 * 8 + n * 3 * 3 * 8
-    return n * steps / dt, h2d / steps, d2h / steps
+    phases = {"create_upload_ms": 1e3 * (t1 - t0), "setup_ms": 1e3 * (t2 - t1), "steps_ms": 1e3 * (t3 - t2),
+              "download_ms": 1e3 * (t4 - t3)}
+    return n * steps / (t4 - t0), h2d / steps, d2h / steps, phases
 
 
 # ---------------------------------------------------------------------------
 def main():
     args = parse()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(relaunch_under_torchrun(sys.argv[1:], args.gpus))
     ws, rank, local = dist_setup()
+    if ws != args.gpus and rank == 0:
+        print(f"bench.py: --gpus {args.gpus} but WORLD_SIZE {ws}; measuring {ws} ranks", file=sys.stderr)
     import numpy as np
 
     import workloads as W
@@ -401,11 +463,14 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        steps = max(1, min(args.steps, 3))
-        warm = min(args.warmup, 1)
+        # the K and W of this call, each step a full step of the 1,048,576-atom system
+        # (~0.55 s on one core); beyond 200 timed steps the window is cut at 200
+        steps = max(1, min(args.steps, 200))
+        warm = min(args.warmup, 20)
         rate, secs = cpu_reference_rate(pos, vel, typ, params, steps, warm)
-        sample = (f"{n} atoms, set-up + {warm} warm-up step untimed, {steps} timed steps ({secs:.1f} s); "
-                  "cell-list Verlet build, rebuild checks as the reference")
+        sample = (f"{n} atoms, set-up + {warm} warm-up steps untimed, {steps} timed steps ({secs:.1f} s) of the "
+                  "reference's serial cell-list path (oracle/cav_oracle.c); 1 core, 1 process, 1 MPI rank, "
+                  f"{cpu_model()}")
         line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
                 "steps": steps, "warmup": warm, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
@@ -462,9 +527,13 @@ def main():
     kern = {"segments": cavgpu.FORCE_SEGMENTS, "strided": cavgpu.FORCE_STRIDED}.get(tuned.get("force_kernel"),
                                                                                       cavgpu.FORCE_AUTO)
     spg = LAUNCH.get("steps_per_graph", tuned.get("steps_per_graph", 0))
-    e2e_rate, h2d, d2h = time_e2e(cavgpu, torch, pos, vel, typ, params, cavgpu.MIXED, args.steps,
-                                  tpa=rm["tpa"], block=rm["block"], steps_per_graph=spg, force_kernel=kern)
+    e2e_rate, h2d, d2h, phases = time_e2e(cavgpu, torch, pos, vel, typ, params, cavgpu.MIXED, args.steps,
+                                          tpa=rm["tpa"], block=rm["block"], steps_per_graph=spg, force_kernel=kern)
     e2e_rate = ws * n * args.steps / max_over_ranks(ws, n * args.steps / e2e_rate)
+    # the same call shape over a long window: the per-call fixed cost amortised
+    long_steps = max(args.steps, 2000)
+    e2e_long, _, _, phases_long = time_e2e(cavgpu, torch, pos, vel, typ, params, cavgpu.MIXED, long_steps,
+                                           tpa=rm["tpa"], block=rm["block"], steps_per_graph=spg, force_kernel=kern)
 
     # roofline of the dominant kernel (mixed force kernel): algorithmic bytes per launch
     #   per atom: 4 * nbar list words + rel_i 16 + nnbr 4 + vel r/w 64 + acc r 32 (a_old) + acc w 32
@@ -484,15 +553,16 @@ def main():
     fp64_achieved = flops_atom * n / (l64 * 1e-3) / 1e12
 
     extra = None
-    if rank == 0 and not args.no_extra:
-        extra = extra_workloads(cavgpu, torch, W, np, value / ws)
+    if not args.no_extra:
+        extra = extra_workloads(cavgpu, torch, W, np, value / ws, ws, rank)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        rate, secs = cpu_reference_rate(pos, vel, typ, params, 3, 0)
+        rate, secs = cpu_reference_rate(pos, vel, typ, params, 20, 5)
         cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"{n} atoms, set-up untimed, 3 timed steps ({secs:.1f} s) of the reference's serial "
-                         "cell-list path restated in oracle/cav_oracle.c"}
+               "sample": f"{n} atoms, set-up + 5 warm-up steps untimed, 20 timed steps ({secs:.1f} s) of the "
+                         "reference's serial cell-list path restated in oracle/cav_oracle.c; 1 core, 1 process, "
+                         f"1 MPI rank, {cpu_model()}"}
 
     if rank != 0:
         return
@@ -523,7 +593,11 @@ def main():
                                     "least-squares slope of KE+PE sampled every 100 steps, per 1e6 steps, "
                                     "relative to the mean |E|"},
         "cpu_baseline": cpu,
-        "e2e": {"value": e2e_rate, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": e2e_rate, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "phases_ms": phases,
+                "fixed_ms": phases["create_upload_ms"] + phases["setup_ms"] + phases["download_ms"],
+                "steady_value": n * args.steps / (phases["steps_ms"] * 1e-3),
+                "long_window": {"steps": long_steps, "value": e2e_long, "phases_ms": phases_long}},
         "gpu_launches": rm["kernel_launches"],
         "clocks": rm["clocks"],
         "peaks": {"fp64_tflops": fp64_peak, "fp32_tflops": fp32_peak},
