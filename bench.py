@@ -44,6 +44,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cells", type=int, default=64, help="FCC cells per edge (64 -> 1,048,576 atoms)")
     ap.add_argument("--drift-steps", type=int, default=20000)
+    ap.add_argument("--drift-only", action="store_true",
+                    help="measure only the NVE energy drift: mixed and FP64 from one equilibrated state, "
+                         "--drift-steps steps each, energy sampled every 1000 steps; prints one JSON line")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-extra", action="store_true", help="skip the batched and Langevin configurations")
     ap.add_argument("--eager", action="store_true",
@@ -205,6 +208,22 @@ def cpu_reference_rate(pos, vel, typ, params, steps, warmup):
     s.step(steps)
     dt = time.perf_counter() - t0
     return len(pos) * steps / dt, dt
+
+
+def fused_fraction(steps, tuned, spg_default=50):
+    """Share of the timed pair-kernel launches that also drift the next step: in
+    each chunk of S steps (one CUDA graph) every step but the last drifts the next,
+    made even in number (cav_api.cu, make_plan), velocity Verlet without records."""
+    spg = (tuned or {}).get("steps_per_graph") or spg_default
+    spg = LAUNCH.get("steps_per_graph", spg)
+    if spg <= 0:
+        spg = spg_default
+    fused, left = 0, steps
+    while left > 0:
+        sz = min(left, spg)
+        fused += (sz - 1) - ((sz - 1) % 2)
+        left -= sz
+    return fused / max(steps, 1)
 
 
 def cpu_model():
@@ -384,14 +403,15 @@ def writer_runs(steps=2000):
     return out
 
 
-def nve_drift(cavgpu, pos, vel, typ, params, precision, steps, every=100):
+def nve_drift(cavgpu, pos, vel, typ, params, precision, steps, every=100, series=False):
     """NVE energy drift: least-squares slope of E = KE + PE sampled every `every`
     steps over `steps` steps, per 1e6 steps and relative to the mean |E|; and the
-    largest |E - E_first| / |E| seen.  None when steps is 0."""
+    largest |E - E_first| / |E| seen (with series, also the sampled E).  None when
+    steps is 0."""
     import numpy as np
 
     if steps <= 0:
-        return None, None
+        return (None, None, None) if series else (None, None)
     s = cavgpu.System(pos, vel, typ, params, precision=precision, **LAUNCH)
     s.setup()
     th = s.run(steps, every)
@@ -399,7 +419,30 @@ def nve_drift(cavgpu, pos, vel, typ, params, precision, steps, every=100):
     e = th[:, 0] + th[:, 4]
     t = (1 + np.arange(len(e))) * every
     slope = np.polyfit(t, e, 1)[0]
-    return float(slope * 1e6 / abs(e.mean())), float(np.abs(e - e[0]).max() / abs(e.mean()))
+    out = (float(slope * 1e6 / abs(e.mean())), float(np.abs(e - e[0]).max() / abs(e.mean())))
+    return out + (e,) if series else out
+
+
+def drift_only(args, cavgpu, W, np):
+    """The NVE energy drift of the 1,048,576-atom fluid over --drift-steps steps, mixed
+    and FP64 from one state (the lattice melted by 5000 mixed steps), E = KE + PE
+    sampled every 1000 steps.  One JSON line."""
+    pos, vel, typ, params = W.lj_fluid((args.cells,) * 3, seed=1002)
+    eq = cavgpu.System(pos, vel, typ, params, precision=cavgpu.MIXED, **LAUNCH)
+    eq.setup()
+    eq.step(5000)
+    p_eq, v_eq, _ = eq.state()
+    eq.close()
+    out = {"workload": f"lj_fluid_{len(pos)}_atoms_nve", "start": "FCC lattice melted by 5000 mixed steps",
+           "steps": args.drift_steps, "every": 1000,
+           "definition": "least-squares slope of E = KE + PE, per 1e6 steps, relative to the mean |E|"}
+    for prec, name in ((cavgpu.MIXED, "mixed"), (cavgpu.FP64, "fp64")):
+        t0 = time.perf_counter()
+        slope, dmax, e = nve_drift(cavgpu, p_eq, v_eq, typ, params, prec, args.drift_steps, every=1000, series=True)
+        out[name] = {"drift_per_1e6_steps": slope, "max_rel_dE": dmax, "E_first": float(e[0]),
+                     "E_last": float(e[-1]), "wall_s": time.perf_counter() - t0,
+                     "E_every_10000": [float(x) for x in e[9::10]]}
+    print(json.dumps(out), flush=True)
 
 
 def time_e2e(cavgpu, torch, pos, vel, typ, params, precision, steps, **launch):
@@ -485,6 +528,10 @@ def main():
 
     torch.cuda.set_device(local)
     sid = gpu_uuid()
+    if args.drift_only:
+        if rank == 0:
+            drift_only(args, cavgpu, W, np)
+        return
 
     # mixed precision (headline) and all-FP64, state resident in HBM
     tune = not args.no_tune
@@ -536,12 +583,15 @@ def main():
                                            tpa=rm["tpa"], block=rm["block"], steps_per_graph=spg, force_kernel=kern)
 
     # roofline of the dominant kernel (mixed force kernel): algorithmic bytes per launch
-    #   per atom: 4 * nbar list words + rel_i 16 + nnbr 4 + vel r/w 64 + acc r 32 (a_old) + acc w 32
+    #   per atom: 4 * nbar list words + rel_i 16 + nnbr 4 + vel r/w 64 + acc r 32 (a_old) + acc w 32,
+    #   and on the launches that also drift the next step: pos r/w 64 + pos_ref 32 + rel_ref 16
+    #   + the next rel 16 = 128 more
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs")
     peak_note = "measured" if hbm else "fallback"
     hbm = hbm or 6800.0
-    bytes_per_atom = 4.0 * rm["nbar"] + 148.0
+    fused = fused_fraction(args.steps, rm["autotune"])
+    bytes_per_atom = 4.0 * rm["nbar"] + 148.0 + 128.0 * fused
     launch_ms = rm["force_ms"] / max(rm["force_launches"], 1)
     achieved = bytes_per_atom * n / (launch_ms * 1e-3) / 1e9
     traffic = read_profile_traffic("lj_force_mixed_1M.md")
@@ -577,7 +627,7 @@ def main():
         "data": "synthetic seeded FCC LJ fluid (no dataset exists for this path)", "config": config,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "kernel": "k_force<mixed>", "peak_source": peak_note,
-                     "bytes_per_atom": bytes_per_atom, "launch_ms": launch_ms},
+                     "bytes_per_atom": bytes_per_atom, "launch_ms": launch_ms, "fused_launch_share": fused},
         "fp64": {"value": value64, "ms_per_step": ms_fp64 / k64, "kernel": "k_force<fp64>",
                  "roofline": {"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                               "frac": fp64_achieved / fp64_peak, "flops_per_atom": flops_atom, "launch_ms": l64,

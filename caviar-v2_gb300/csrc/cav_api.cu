@@ -10,6 +10,7 @@
 #include <map>
 #include <mutex>
 #include <new>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -605,13 +606,28 @@ int upload_common(cavgpu_ctx *c, const int64_t *counts, const double *pos3, cons
   }
   if (nslot > MAX_ATOMS || ncell_all > (1ll << 30)) return CAVGPU_E_RANGE;
   const int N = (int)total, NS = (int)nslot;
-  std::vector<dbl4> hp(NS, make_dbl4(0, 0, 0, 0)), hv(NS, make_dbl4(0, 0, 0, 0));
-  std::vector<int> ht(NS, 0), rep_of(NS, -1), cell_rep(ncell_all, -1);
-  std::vector<uint32_t> hid(NS, 0);
-  std::vector<char> seen(id ? N : 0, 0);
-  std::vector<double> msum(R, 0.0);
+  // a single system goes to the device as the caller's arrays are and is converted
+  // and checked there (k_upload_single); batches are laid out here
+  const bool on_device = R == 1;
+  std::vector<dbl4> hp, hv;
+  std::vector<int> ht, rep_of, cell_rep;
+  std::vector<uint32_t> hid;
+  std::vector<char> seen;
+  // atoms per type and replica: the total mass is sum_t mass_t n_t, in type order (exact
+  // counts, the same value however the atoms are ordered or counted)
+  std::vector<int64_t> ntype((size_t)R * CAVGPU_MAX_TYPES, 0);
+  c->reps[0].id_off = 0;
   int64_t h = 0;
-  for (int r = 0; r < R; ++r) {
+  if (!on_device) {
+    hp.assign(NS, make_dbl4(0, 0, 0, 0));
+    hv.assign(NS, make_dbl4(0, 0, 0, 0));
+    ht.assign(NS, 0);
+    rep_of.assign(NS, -1);
+    cell_rep.assign(ncell_all, -1);
+    hid.assign(NS, 0);
+    seen.assign(id ? N : 0, 0);
+  }
+  for (int r = 0; r < R && !on_device; ++r) {
     RepBox &rb = c->reps[r];
     rb.id_off = (int)h;
     for (int k = 0; k < rb.natoms; ++k, ++h) {
@@ -624,12 +640,12 @@ int upload_common(cavgpu_ctx *c, const int64_t *counts, const double *pos3, cons
       if (type[h] >= (uint64_t)c->p.ntypes) return CAVGPU_E_ARG;
       const uint64_t ii = id ? id[h] : (uint64_t)k;  // batches: ids local to the replica
       if (ii >= (uint64_t)N || (id && seen[ii]++)) return CAVGPU_E_ARG;  // ids: a permutation of 0..n-1
-      hp[s] = make_dbl4(pos3[3 * h], pos3[3 * h + 1], pos3[3 * h + 2], (double)type[h]);
+      hp[s] = make_dbl4(pos3[3 * h], pos3[3 * h + 1], pos3[3 * h + 2], type_bits((int)type[h]));
       if (vel3) hv[s] = make_dbl4(vel3[3 * h], vel3[3 * h + 1], vel3[3 * h + 2], 0.0);
       ht[s] = (int)type[h];
       hid[s] = (uint32_t)ii;
       rep_of[s] = r;
-      msum[r] += c->p.mass[type[h]];
+      ++ntype[(size_t)r * CAVGPU_MAX_TYPES + type[h]];
     }
     for (int k = 0; k < rb.ncell; ++k) cell_rep[rb.cell_off + k] = r;
   }
@@ -666,39 +682,50 @@ int upload_common(cavgpu_ctx *c, const int64_t *counts, const double *pos3, cons
   const size_t nblk_d = (size_t)std::max((NS + 255) / 256, 1);
   d.partials_blocks = (int)nblk;
   int rc = CAVGPU_OK;
-  dbl4 **d4[] = {&d.pos, &d.vel, &d.acc, &d.pos_ref, &d.t_pos, &d.t_vel, &d.t_acc};
-  for (auto pp : d4) if (!rc) rc = dalloc(c, pp, NS);
-  if (!rc) rc = dalloc(c, &d.rel, NS);
-  if (!rc) rc = dalloc(c, &d.rel_ref, NS);
-  // the second buffer of the coordinates a pair kernel gathers (it drifts into it)
-  if (c->p.precision == CAVGPU_MIXED) {
-    if (!rc) rc = dalloc(c, &d.rel_alt, NS);
-  } else {
-    if (!rc) rc = dalloc(c, &d.pos_alt, NS);
+  // the per-slot and per-cell arrays, carved out of one allocation (one cudaMalloc
+  // rather than thirty: part of the set-up cost a short run pays)
+  {
+    size_t total_bytes = 0;
+    std::vector<std::pair<void **, size_t>> parts;
+    auto take = [&](auto **p, size_t count) {
+      using E = typename std::remove_pointer<typename std::remove_reference<decltype(*p)>::type>::type;
+      parts.push_back({reinterpret_cast<void **>(p), total_bytes});
+      total_bytes += (std::max<size_t>(count, 1) * sizeof(E) + 255) & ~(size_t)255;
+    };
+    for (dbl4 **pp : {&d.pos, &d.vel, &d.acc, &d.pos_ref, &d.t_pos, &d.t_vel, &d.t_acc}) take(pp, NS);
+    take(&d.rel, NS);
+    take(&d.rel_ref, NS);
+    // the second buffer of the coordinates a pair kernel gathers (it drifts into it)
+    if (c->p.precision == CAVGPU_MIXED) take(&d.rel_alt, NS);
+    else take(&d.pos_alt, NS);
+    for (int **pp : {&d.type, &d.cell_of, &d.t_type, &d.atom_cell, &d.perm, &d.perm_tmp, &d.nnbr}) take(pp, NS);
+    take(&d.id, NS);
+    take(&d.t_id, NS);
+    take(&d.skey, NS);
+    take(&d.cell_count, ncell_all);
+    take(&d.cell_cursor, ncell_all);
+    take(&d.cell_start, (size_t)ncell_all + 1);
+    take(&d.partials_ke, 4 * std::max(nblk, nblk_d));
+    take(&d.partials_ke_end, 4 * nblk);
+    take(&d.partials_ev, 2 * nblk);
+    take(&d.h3, 3 * (size_t)N);
+    take(&d.hi3, 3 * (size_t)N);
+    if (c->p.msd_process) {  // Atom_data::msd_process: boundary crossings per atom
+      take(&d.img, NS);
+      take(&d.t_img, NS);
+    }
+    if (c->p.ignore_intra_molecule) {
+      take(&d.mol, NS);
+      take(&d.t_mol, NS);
+    }
+    char *arena = nullptr;
+    rc = dalloc(c, &arena, total_bytes);
+    if (rc) return rc;
+    for (auto &pt : parts) *pt.first = arena + pt.second;
   }
-  int **di[] = {&d.type, &d.cell_of, &d.t_type, &d.atom_cell, &d.perm, &d.perm_tmp, &d.nnbr};
-  for (auto pp : di) if (!rc) rc = dalloc(c, pp, NS);
-  if (!rc) rc = dalloc(c, &d.id, NS);
-  if (!rc) rc = dalloc(c, &d.t_id, NS);
-  if (!rc) rc = dalloc(c, &d.skey, NS);
-  if (!rc) rc = dalloc(c, &d.cell_count, ncell_all);
-  if (!rc) rc = dalloc(c, &d.cell_cursor, ncell_all);
-  if (!rc) rc = dalloc(c, &d.cell_start, (size_t)ncell_all + 1);
-  if (!rc) rc = dalloc(c, &d.partials_ke, 4 * std::max(nblk, nblk_d));
-  if (!rc) rc = dalloc(c, &d.partials_ke_end, 4 * nblk);
-  if (!rc) rc = dalloc(c, &d.partials_ev, 2 * nblk);
-  if (!rc) rc = dalloc(c, &d.h3, 3 * (size_t)N);
-  if (!rc) rc = dalloc(c, &d.hi3, 3 * (size_t)N);
-  if (c->p.msd_process) {  // Atom_data::msd_process: boundary crossings per atom, zero at upload
-    if (!rc) rc = dalloc(c, &d.img, NS);
-    if (!rc) rc = dalloc(c, &d.t_img, NS);
-    if (!rc) rc = cuda_rc(cudaMemsetAsync(d.img, 0, NS * sizeof(int4), c->st));
-  }
-  if (c->p.ignore_intra_molecule) {  // molecule index -1 for every atom (Atom_data::add_atom) until set
-    if (!rc) rc = dalloc(c, &d.mol, NS);
-    if (!rc) rc = dalloc(c, &d.t_mol, NS);
-    if (!rc) rc = cuda_rc(cudaMemsetAsync(d.mol, 0xff, NS * sizeof(int), c->st));
-  }
+  if (c->p.msd_process) rc = cuda_rc(cudaMemsetAsync(d.img, 0, NS * sizeof(int4), c->st));  // zero at upload
+  // molecule index -1 for every atom (Atom_data::add_atom) until set
+  if (!rc && c->p.ignore_intra_molecule) rc = cuda_rc(cudaMemsetAsync(d.mol, 0xff, NS * sizeof(int), c->st));
   if (c->nve.step > 0) {
     if (R > 1) return CAVGPU_E_ARG;  // constraint::Nve acts on one system's kinetic energy
     if (!rc) rc = dalloc(c, &d.nve_partials, 4 * (size_t)NVE_BLOCKS);
@@ -733,17 +760,41 @@ int upload_common(cavgpu_ctx *c, const int64_t *counts, const double *pos3, cons
   const double ce = c->cutoff_extra;
   const int cap = c->p.nbr_capacity > 0 ? c->p.nbr_capacity : (int)(1.4 * rho * 4.18879020479 * ce * ce * ce) + 48;
   RK(alloc_nbr(c, cap));
-  CK(cudaMemcpyAsync(d.pos, hp.data(), NS * sizeof(dbl4), cudaMemcpyHostToDevice, c->st));
-  CK(cudaMemcpyAsync(d.vel, hv.data(), NS * sizeof(dbl4), cudaMemcpyHostToDevice, c->st));
+  if (on_device) {
+    // the caller's arrays, raw, into the rebuild scratch (32 B per slot each: positions
+    // and velocities 24 B, types and ids 8 B + 8 B), then converted and checked
+    double *raw_pos = reinterpret_cast<double *>(d.t_pos), *raw_vel = reinterpret_cast<double *>(d.t_vel);
+    uint64_t *raw_type = reinterpret_cast<uint64_t *>(d.t_acc), *raw_id = raw_type + N;
+    int *type_count = d.scan_part;  // SCAN_SLICES >= CAVGPU_MAX_TYPES ints
+    CK(cudaMemcpyAsync(raw_pos, pos3, 3 * sizeof(double) * (size_t)N, cudaMemcpyHostToDevice, c->st));
+    if (vel3) CK(cudaMemcpyAsync(raw_vel, vel3, 3 * sizeof(double) * (size_t)N, cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(raw_type, type, sizeof(uint64_t) * (size_t)N, cudaMemcpyHostToDevice, c->st));
+    if (id) CK(cudaMemcpyAsync(raw_id, id, sizeof(uint64_t) * (size_t)N, cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemsetAsync(d.perm, 0, NS * sizeof(int), c->st));
+    CK(cudaMemsetAsync(type_count, 0, CAVGPU_MAX_TYPES * sizeof(int), c->st));
+    RK(launch_upload_single(d, b, N, c->p.ntypes, vel3 != nullptr, id != nullptr, raw_pos, raw_vel, raw_type,
+                            raw_id, d.perm, type_count, c->st));
+    int f[F_NWORDS];
+    int counts_h[CAVGPU_MAX_TYPES];
+    CK(cudaMemcpyAsync(counts_h, type_count, sizeof(counts_h), cudaMemcpyDeviceToHost, c->st));
+    RK(read_flags(c, f));
+    if (f[F_UPLOAD_BAD]) return CAVGPU_E_ARG;
+    for (int t = 0; t < CAVGPU_MAX_TYPES; ++t) ntype[t] = counts_h[t];
+  } else {
+    CK(cudaMemcpyAsync(d.pos, hp.data(), NS * sizeof(dbl4), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.vel, hv.data(), NS * sizeof(dbl4), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.type, ht.data(), NS * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.id, hid.data(), NS * sizeof(uint32_t), cudaMemcpyHostToDevice, c->st));
+  }
   CK(cudaMemsetAsync(d.acc, 0, NS * sizeof(dbl4), c->st));
   CK(cudaMemsetAsync(d.nnbr, 0, NS * sizeof(int), c->st));
-  CK(cudaMemcpyAsync(d.type, ht.data(), NS * sizeof(int), cudaMemcpyHostToDevice, c->st));
-  CK(cudaMemcpyAsync(d.id, hid.data(), NS * sizeof(uint32_t), cudaMemcpyHostToDevice, c->st));
   CK(cudaMemsetAsync(d.cell_count, 0, ncell_all * sizeof(int), c->st));
   CK(cudaMemsetAsync(d.cell_cursor, 0, ncell_all * sizeof(int), c->st));
   const int end_slot = NS;  // the start after the last cell (the per-replica scans never write it)
   CK(cudaMemcpyAsync(d.cell_start + ncell_all, &end_slot, sizeof(int), cudaMemcpyHostToDevice, c->st));
-  double th[8] = {0, 0, 0, 0, 0, msum[0], 0, 0};
+  double msum0 = 0.0;
+  for (int t = 0; t < CAVGPU_MAX_TYPES; ++t) msum0 += c->p.mass[t] * (double)ntype[t];
+  double th[8] = {0, 0, 0, 0, 0, msum0, 0, 0};
   CK(cudaMemcpyAsync(d.thermo, th, sizeof(th), cudaMemcpyHostToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
   c->uploaded = true;

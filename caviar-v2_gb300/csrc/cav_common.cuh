@@ -22,6 +22,22 @@ __host__ __device__ inline dbl4 make_dbl4(double x, double y, double z, double w
   r.x = x; r.y = y; r.z = z; r.w = w;
   return r;
 }
+// The atom type rides in the w component of its position as the integer's bit
+// pattern (not as a double value): reading it back is integer work, off the FP64
+// pipe the FP64 pair loop is bound by.
+__host__ __device__ inline double type_bits(int t) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)t);
+#else
+  double r;
+  const long long v = t;
+  static_assert(sizeof(r) == sizeof(v), "64-bit double");
+  __builtin_memcpy(&r, &v, sizeof(r));
+  return r;
+#endif
+}
+__device__ inline int type_of(const double w) { return (int)__double_as_longlong(w); }
+
 // read-only (non-coherent) 256-bit load of a neighbour's position
 __device__ inline dbl4 ldg_dbl4(const dbl4 *p) {
   dbl4 r;
@@ -54,6 +70,7 @@ enum Flag : int {
   F_HALT = 7,
   F_STEPS_OK = 8,   // steps of the current chunk whose pair kernel ran (the step counter adds them)
   F_HALT_STEP = 9,  // steps of the halted chunk that completed before the halt
+  F_UPLOAD_BAD = 10,  // an uploaded atom outside the box, of an unknown type or with a bad id
   F_NWORDS = 12
 };
 
@@ -419,6 +436,14 @@ int launch_export_pairs(const Dev &d, const Box &b, int mode, int32_t *rows, uns
                         int64_t cap, cudaStream_t st);
 int launch_ref_bins(const Dev &d, int n, double cutoff_inv, const int nb[3], const double lo_local[3],
                     cudaStream_t st);
+// Single system: the host arrays as the caller passed them (pos3, vel3 doubles; type,
+// id uint64), copied raw into the rebuild scratch, become the slot arrays; every atom
+// is checked as Atom_data::add_atom(tools::Atom &) checks it (inside [lo, hi)), its
+// type and id too; F_UPLOAD_BAD is raised for a bad atom.  type_count[t] counts the
+// atoms of each type (exact integers: the total mass follows in a fixed order).
+int launch_upload_single(const Dev &d, const Box &b, int n, int ntypes, bool has_vel, bool has_id,
+                         const double *raw_pos, const double *raw_vel, const uint64_t *raw_type,
+                         const uint64_t *raw_id, int *seen, int *type_count, cudaStream_t st);
 int launch_ghosts(const Dev &d, const Box &b, int n, double gc, int *counts, int *starts, int32_t *src,
                   int32_t *shift3, double *pos3, int32_t *bins3, int64_t cap, double cutoff_inv, const int nb[3],
                   const double lo_local[3], cudaStream_t st);

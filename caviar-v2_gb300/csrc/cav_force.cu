@@ -485,8 +485,14 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 1) k_force(Dev d, Box b, Step
         fx = ax; fy = ay; fz = az; vir = vr; pe = pp;
       } else {
         const dbl4 xi = d.pos[i];
-        ti = (int)xi.w;
+        ti = type_of(xi.w);
         const bool jump = sc.jump_tol > 0.0;
+        // single type: the pair constants in registers, no table lookups; the cutoff
+        // test r^2 <= rc^2 compares the bit patterns as integers (the same order for
+        // doubles >= +0, and rc^2 < 0, an eps == 0 pair, admits none), off the FP64 pipe
+        const int t1 = ti * nt;
+        const long long rc2b1 = __double_as_longlong(tab.rc2[t1]);
+        const double sig21 = tab.sig2[t1], e61 = tab.e6[t1], e121 = tab.e12[t1], gc1 = tab.gc[t1];
         for (int q = 0, k0 = 4 * t; k0 < nn; ++q, k0 += 4 * TPA) {
           const uint4 w4 = __ldg(row4 + (size_t)q * 32);
           const uint32_t e[4] = {w4.x, w4.y, w4.z, w4.w};
@@ -507,17 +513,19 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 1) k_force(Dev d, Box b, Step
             }
             const double dx = jx - xi.x, dy = jy - xi.y, dz = jz - xi.z;
             const double r2d = dx * dx + dy * dy + dz * dz;
-            const int tt = ti * nt + (int)xj[u].w;
-            if (r2d <= tab.rc2[tt]) {
+            const int tt = ONE ? t1 : t1 + type_of(xj[u].w);
+            const long long rc2b = ONE ? rc2b1 : __double_as_longlong(tab.rc2[tt]);
+            if (__double_as_longlong(r2d) <= rc2b) {
               // Lj jump_fix (src/force/lj.cpp:459-468): r^2 floored at jump_tol after the
               // cutoff test (jump_tol = 0 when off); the direction stays dx, dy, dz
               double r2 = r2d;
               if (jump) r2 = r2d < sc.jump_tol ? sc.jump_tol : r2d;
               const double r2i = rcp_nr(r2);
-              const double s2 = tab.sig2[tt] * r2i;
+              const double s2 = (ONE ? sig21 : tab.sig2[tt]) * r2i;
               const double s6 = s2 * s2 * s2;
               // eps4 s6 (6 - 12 s6) / r^2 - g(rc) as (s6 (e6 - e12 s6)) r2i - gc
-              const double coef = fma(s6 * fma(-tab.e12[tt], s6, tab.e6[tt]), r2i, -tab.gc[tt]);
+              const double coef = ONE ? fma(s6 * fma(-e121, s6, e61), r2i, -gc1)
+                                      : fma(s6 * fma(-tab.e12[tt], s6, tab.e6[tt]), r2i, -tab.gc[tt]);
               fx = fma(coef, dx, fx); fy = fma(coef, dy, fy); fz = fma(coef, dz, fz);
               if (EV) {
                 vir -= coef * r2;
@@ -687,9 +695,9 @@ __global__ void __launch_bounds__(256) k_force_seg(Dev d, Box b, StepConsts sc, 
 template <int TPA, bool MIXED, int KICK>
 static void launch_ev(bool ev, bool one, int grid, int block, const Dev &d, const Box &b, const StepConsts &sc,
                       const ForceArgs &fa, cudaStream_t st) {
-  if (MIXED && one) {  // single-type systems: constants in registers (mixed form)
-    if (ev) k_force<TPA, MIXED, KICK, true, MIXED><<<grid, block, 0, st>>>(d, b, sc, fa);
-    else k_force<TPA, MIXED, KICK, false, MIXED><<<grid, block, 0, st>>>(d, b, sc, fa);
+  if (one) {  // single-type systems: pair constants in registers
+    if (ev) k_force<TPA, MIXED, KICK, true, true><<<grid, block, 0, st>>>(d, b, sc, fa);
+    else k_force<TPA, MIXED, KICK, false, true><<<grid, block, 0, st>>>(d, b, sc, fa);
     return;
   }
   if (ev) k_force<TPA, MIXED, KICK, true, false><<<grid, block, 0, st>>>(d, b, sc, fa);

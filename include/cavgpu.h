@@ -154,8 +154,12 @@ int cavgpu_step(cavgpu_ctx *ctx, int64_t nsteps);
 
 /* Same as cavgpu_step, recording thermo every `every` steps into
  * out5[k*5 + {0..4}] = {KE, T, P, virialForce, PE} for k < nsteps/every.
- * Both calls return once the steps and the copies into out5 have completed
- * (they end by reading the device status word: NaN, list overflow). */
+ * Both calls return once the steps and the copies into out5 have completed.
+ * The device status (NaN, list overflow) is read after every CUDA graph of steps:
+ * a NaN acceleration returns CAVGPU_E_NAN with the steps before it done (the rest
+ * of that graph does nothing; the context steps no further); a list that needs
+ * more slots than it has is grown and the step completed from the same positions,
+ * and the run goes on. */
 int cavgpu_run(cavgpu_ctx *ctx, int64_t nsteps, int64_t every, double *out5);
 
 /* Recompute the force at the current positions (list rebuilt if the half-skin
@@ -229,8 +233,10 @@ const char *cavgpu_last_cuda_error(void);
  * Scratch: a fixed 320 KiB __device__ array (per-block partial sums) that every
  * device loading this library keeps until exit; n > 16,777,216 returns
  * CAVGPU_E_RANGE.  The first call on a device looks up that array's device
- * address once; make that first call before any stream capture.  Calls share
- * the array: two calls that overlap on the GPU race. */
+ * address once; make that first call before any stream capture.  The address is
+ * kept for the life of the process: after cudaDeviceReset it is stale, so do not
+ * call this on a device that was reset.  Calls share the array: two calls that
+ * overlap on the GPU race. */
 int cavgpu_kinetic_energy_noalloc(int64_t n, const double *vel3, const uint64_t *type, const double *mass,
                                   int32_t ntypes, int32_t n_r_df, double k_b, double *out2, void *stream);
 

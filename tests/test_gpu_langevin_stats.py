@@ -1,8 +1,9 @@
 """Langevin runs with noise on, checked by statistics (the noise is Philox, not the
 reference's unseeded mt19937, so trajectories cannot match the reference).
 
-A 2048-atom LJ fluid (ρ 0.8442, target T 1.0, γ 1, dt 0.005, n_r_df 0, the
-Langevin benchmark's parameters at small N) is equilibrated and then sampled:
+A 2048-atom LJ fluid with every parameter of the 4,194,304-atom Langevin
+benchmark (ρ 0.8442, target T 1.0, γ 1, dt 0.005, r_c 2.5, skin 0.4, n_r_df 0)
+is equilibrated and then sampled:
 the mean kinetic temperature must sit at the target within the statistical
 error (instantaneous T fluctuates by sqrt(2/3N) = 1.8%, ~100 independent
 samples in 20,000 steps at a correlation time of ~1/γ = 200 steps, so the mean

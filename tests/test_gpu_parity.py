@@ -262,3 +262,29 @@ def test_larger_system_against_oracle(gpu, oracle_lib):
     assert np.abs(dp).max() <= TRAJ_ATOL
     assert np.abs(vg - vo).max() <= TRAJ_ATOL
     s.close()
+
+
+@pytest.mark.parametrize("n_r_df", [1, 3])
+def test_kinetic_energy_with_fast_centre_of_mass(gpu, oracle_lib, n_r_df):
+    """Atom_data::kinetic_energy with n_r_df 1..3 removes the centre-of-mass motion
+    (src/atom_data/kinetic_energy.cpp:56-65, the reference subtracting v_cm from each
+    atom).  The device folds sum m v^2 and P = sum m v and takes sum m v^2 - |P|^2 / M,
+    which cancels when the whole system drifts fast: here every velocity carries a
+    uniform offset of 10 x the thermal speed.  KE and T at set-up and after 20 steps
+    must still agree with the oracle to 1e-12."""
+    import workloads as W
+
+    pos, vel, typ, p = W.lj_fluid((5, 5, 5), seed=17, n_r_df=n_r_df)
+    vel = vel + 10.0 * np.sqrt(1.44) * np.array([1.0, -0.6, 0.3])
+    p = dict(p, n_r_df=n_r_df)
+    s = gpu.System(pos, vel, typ, p, precision=gpu.FP64)
+    s.setup()
+    o = oracle_lib.System(pos, vel, typ, p, noise_mode=0)
+    o.setup()
+    for _ in range(2):
+        tg, to = s.thermo(), o.thermo()
+        assert rel(tg["ke"], to["ke"]) <= FORCE_RTOL, (tg["ke"], to["ke"])
+        assert rel(tg["temperature"], to["temperature"]) <= FORCE_RTOL
+        s.step(20)
+        o.step(20)
+    s.close()
