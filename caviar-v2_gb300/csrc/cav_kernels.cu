@@ -458,7 +458,7 @@ struct BuildLane {
   int mol;            // molecule index (ignore_intra_molecule)
   unsigned long long rxx, ryy, rzz;  // the atom's coordinates in the group frame, packed twice
   float hi;           // upper end of the FP32 band (-1 for non-members: they never hit)
-  uint32_t *wp;       // where the atom's list row takes its next word
+  uint32_t *row;      // the atom's list row
   int cnt;            // list words the atom has so far
   const int *selfpos; // shared: per lane, where its own atom sits in the current stage (-1: not in it)
 };
@@ -467,15 +467,9 @@ struct BuildLane {
 // Staged words carry j and a code: the image code (mode 0), or (mode 1) the cell's
 // x index in the group's window of cells plus 3 x its row, from which a member
 // subtracts its own x index to get the stencil index of j's cell relative to its own.
-// Phase 1 tests the candidates 32 at a time and keeps each lane's hit masks in shared
-// memory; phase 2 then has every lane walk its own hits of the whole pass, so the
-// warp loops as often as its busiest lane has hits in the pass -- not, chunk after
-// chunk, as often as its busiest lane has hits in each chunk (neighbouring candidates
-// sit close together, so one lane often takes most of a chunk's hits).  Rows keep the
-// candidate order either way.
 __device__ __forceinline__ void build_sweep(const Dev &d, const Box &b, const RepBox &rb, int mode, int nst,
-                                            const float4 *sxy, const float4 *szw, const uint8_t *su,
-                                            uint32_t *hmask, BuildLane &L, int cshift) {
+                                            const float4 *sxy, const float4 *szw, const uint8_t *su, BuildLane &L,
+                                            int cshift) {
   const int lane = threadIdx.x & 31;
   const float *fzw = reinterpret_cast<const float *>(szw);
   float *pxy = const_cast<float *>(reinterpret_cast<const float *>(sxy));
@@ -490,7 +484,9 @@ __device__ __forceinline__ void build_sweep(const Dev &d, const Box &b, const Re
   }
   __syncwarp();
   const float lo = b.ce2_lo;
+  const int cap = d.cap;
   const int self = L.selfpos[lane];
+  const uint32_t ci_code = (uint32_t)L.ci << CODE_SHIFT;
   for (int t0 = 0; t0 < npad32; t0 += 32) {
     // phase 1: bits of the sure hits (q < ce2_lo) and of everything up to ce2_hi
     uint32_t hm = 0u, am = 0u;
@@ -527,31 +523,18 @@ __device__ __forceinline__ void build_sweep(const Dev &d, const Box &b, const Re
         if (exact_pair(d, rb, b.ce2, L.i, j, img)) hm |= 1u << u;
       }
     }
-    hmask[t0 + lane] = hm;
-  }
-  // phase 2: the lane's hits of the pass, in candidate order (with
-  // ignore_intra_molecule none of the atom's own molecule, as
-  // Lj::calculate_acceleration skips them, src/force/lj.cpp:446)
-  const int cap = d.cap;
-  const uint32_t ci_code = (uint32_t)L.ci << CODE_SHIFT;
-  const int stride3 = (1 << cshift) - 3;  // from a chunk's 4th word to the next chunk's 1st
-  int t0 = 0;
-  uint32_t hm = hmask[lane];
-  for (;;) {
-    while (hm == 0u && t0 + 32 < npad32) {
-      t0 += 32;
-      hm = hmask[t0 + lane];
+    // phase 2: the hits, in candidate order (with ignore_intra_molecule none of the
+    // atom's own molecule, as Lj::calculate_acceleration skips them, src/force/lj.cpp:446)
+    while (hm) {
+      const int u = __ffs(hm) - 1;
+      hm &= hm - 1u;
+      const int t = t0 + u;
+      uint32_t w = __float_as_uint(fzw[(t >> 1) * 4 + 2 + (t & 1)]);
+      if (d.mol && d.mol[w & IDX_MASK] == L.mol) continue;
+      if (mode != 0) w -= ci_code;  // stencil index of j's cell relative to the atom's
+      if (L.cnt < cap) L.row[((L.cnt >> 2) << cshift) + (L.cnt & 3)] = w;
+      ++L.cnt;
     }
-    if (hm == 0u) break;
-    const int u = __ffs(hm) - 1;
-    hm &= hm - 1u;
-    const int t = t0 + u;
-    uint32_t w = __float_as_uint(fzw[(t >> 1) * 4 + 2 + (t & 1)]);
-    if (d.mol && d.mol[w & IDX_MASK] == L.mol) continue;
-    if (mode != 0) w -= ci_code;  // stencil index of j's cell relative to the atom's
-    if (L.cnt < cap) *L.wp = w;
-    L.wp += (L.cnt & 3) == 3 ? stride3 : 1;
-    ++L.cnt;
   }
   __syncwarp();  // the stage is refilled next
 }
@@ -571,7 +554,6 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_group(Dev d, Box 
   __shared__ float4 stage_all[BUILD_WARPS][BUILD_STAGE];
   __shared__ uint8_t su_all[BUILD_WARPS][BUILD_STAGE];
   __shared__ int selfpos_all[BUILD_WARPS][32];
-  __shared__ uint32_t hmask_all[BUILD_WARPS][BUILD_STAGE];  // phase-1 hit masks of a pass, per lane
   const int lane = threadIdx.x & 31;
   // pair p = candidates 2p, 2p+1: sxy[p] = {x, x', y, y'}, szw[p] = {z, z', word, word'}
   float4 *sxy = stage_all[threadIdx.x >> 5], *szw = sxy + BUILD_STAGE / 2;
@@ -601,6 +583,7 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_group(Dev d, Box 
       ri = d.rel[L.i];
       if (d.mol) L.mol = d.mol[L.i];
     }
+    L.row = d.nbr + nbr_block_base(act ? L.i : 0, d.cap, d.tpa);
     int *selfpos = selfpos_all[threadIdx.x >> 5];
     L.selfpos = selfpos;
     const int win0 = win << 5;
@@ -627,7 +610,6 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_group(Dev d, Box 
       L.rzz = pack2(gz);
       L.hi = L.me ? b.ce2_hi : -1.0f;
       L.cnt = 0;
-      L.wp = d.nbr + nbr_block_base(L.me ? L.i : 0, d.cap, d.tpa);
       // candidate cells q = r * nu + u: row r = (dy+1) + 3 (dz+1), x cell cx0 - 1 + u
       const int nu = span + 3, ncand = 9 * nu;
       int nst = 0;
@@ -698,7 +680,7 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_group(Dev d, Box 
             nst += __popc(km);
             if (nst > BUILD_STAGE - 32) {
               __syncwarp();
-              build_sweep(d, b, rb, mode, nst, sxy, szw, su, hmask_all[threadIdx.x >> 5], L, cshift);
+              build_sweep(d, b, rb, mode, nst, sxy, szw, su, L, cshift);
               selfpos[lane] = -1;
               __syncwarp();
               nst = 0;
@@ -708,7 +690,7 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_group(Dev d, Box 
       }
       if (nst > 0) {
         __syncwarp();
-        build_sweep(d, b, rb, mode, nst, sxy, szw, su, hmask_all[threadIdx.x >> 5], L, cshift);
+        build_sweep(d, b, rb, mode, nst, sxy, szw, su, L, cshift);
       }
       if (L.me) {
         d.nnbr[L.i] = min(L.cnt, d.cap);
@@ -1124,27 +1106,36 @@ __global__ void __launch_bounds__(256) k_upload_single(Dev d, Box b, int n, int 
                                                        const double *raw_pos, const double *raw_vel,
                                                        const uint64_t *raw_type, const uint64_t *raw_id, int *seen,
                                                        int *type_count) {
+  // per-type counts of the block in shared memory, one global atomic per type and
+  // block (one per atom on a single address serialised the whole upload)
+  __shared__ int s_count[CAVGPU_MAX_TYPES];
+  if (threadIdx.x < CAVGPU_MAX_TYPES) s_count[threadIdx.x] = 0;
+  __syncthreads();
   const int h = blockIdx.x * blockDim.x + threadIdx.x;
-  if (h >= n) return;
-  const RepBox &rb = b.r0;
-  const double x = raw_pos[3 * (size_t)h], y = raw_pos[3 * (size_t)h + 1], z = raw_pos[3 * (size_t)h + 2];
-  // Atom_data::position_inside_global_domain (src/atom_data.cpp:548-559)
-  bool bad = !(x >= rb.lo[0] && x < rb.hi[0] && y >= rb.lo[1] && y < rb.hi[1] && z >= rb.lo[2] && z < rb.hi[2]);
-  const uint64_t t = raw_type[h];
-  bad |= t >= (uint64_t)ntypes;
-  const uint64_t id = has_id ? raw_id[h] : (uint64_t)h;
-  if (id >= (uint64_t)n) bad = true;
-  else if (atomicExch(&seen[id], 1) != 0) bad = true;  // ids: a permutation of 0..n-1
-  if (bad) {
-    d.flags[F_UPLOAD_BAD] = 1;
-    return;
+  if (h < n) {
+    const RepBox &rb = b.r0;
+    const double x = raw_pos[3 * (size_t)h], y = raw_pos[3 * (size_t)h + 1], z = raw_pos[3 * (size_t)h + 2];
+    // Atom_data::position_inside_global_domain (src/atom_data.cpp:548-559)
+    bool bad = !(x >= rb.lo[0] && x < rb.hi[0] && y >= rb.lo[1] && y < rb.hi[1] && z >= rb.lo[2] && z < rb.hi[2]);
+    const uint64_t t = raw_type[h];
+    bad |= t >= (uint64_t)ntypes;
+    const uint64_t id = has_id ? raw_id[h] : (uint64_t)h;
+    if (id >= (uint64_t)n) bad = true;
+    else if (atomicExch(&seen[id], 1) != 0) bad = true;  // ids: a permutation of 0..n-1
+    if (bad) {
+      d.flags[F_UPLOAD_BAD] = 1;
+    } else {
+      atomicAdd_block(&s_count[t], 1);
+      d.pos[h] = make_dbl4(x, y, z, type_bits((int)t));
+      d.vel[h] = has_vel ? make_dbl4(raw_vel[3 * (size_t)h], raw_vel[3 * (size_t)h + 1], raw_vel[3 * (size_t)h + 2],
+                                     0.0)
+                         : make_dbl4(0.0, 0.0, 0.0, 0.0);
+      d.type[h] = (int)t;
+      d.id[h] = (uint32_t)id;
+    }
   }
-  atomicAdd(&type_count[t], 1);
-  d.pos[h] = make_dbl4(x, y, z, type_bits((int)t));
-  d.vel[h] = has_vel ? make_dbl4(raw_vel[3 * (size_t)h], raw_vel[3 * (size_t)h + 1], raw_vel[3 * (size_t)h + 2], 0.0)
-                     : make_dbl4(0.0, 0.0, 0.0, 0.0);
-  d.type[h] = (int)t;
-  d.id[h] = (uint32_t)id;
+  __syncthreads();
+  if (threadIdx.x < CAVGPU_MAX_TYPES && s_count[threadIdx.x]) atomicAdd(&type_count[threadIdx.x], s_count[threadIdx.x]);
 }
 
 // ---------------------------------------------------------------------------
