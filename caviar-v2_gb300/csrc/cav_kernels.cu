@@ -793,12 +793,17 @@ __global__ void __launch_bounds__(256) k_thermo_final(Dev d, ThermoCfg tc, int n
   }
   __syncthreads();
   if (!last) return;
-  // level 2, in the last block: the blocks' sums in block order
+  // level 2, in the last block: the blocks' sums in block order.  All loads first
+  // (L2-coherent, independent of one another), then the adds in block order: a
+  // volatile load per add waited a full L2 round trip 32 times in a row
   if (threadIdx.x < 10) {
     __threadfence();
-    const volatile double *f = d.fold;
+    double v[THERMO_FOLD_BLOCKS];
+#pragma unroll
+    for (int g = 0; g < THERMO_FOLD_BLOCKS; ++g) v[g] = __ldcg(&d.fold[g * 10 + threadIdx.x]);
     double s = 0.0;
-    for (int g = 0; g < (int)gridDim.x; ++g) s += f[g * 10 + threadIdx.x];
+#pragma unroll
+    for (int g = 0; g < THERMO_FOLD_BLOCKS; ++g) s += v[g];
     out[threadIdx.x] = s;
   }
   __syncthreads();
