@@ -288,10 +288,8 @@ def time_device(cavgpu, torch, pos, vel, typ, params, precision, steps, warmup, 
     nlaunch, force_ms = s.read_profile()
     s.set_profiling(False)
     nbar = s._check(cavgpu.lib().cavgpu_export_pairs(s._h, None, 0), "pairs") / len(pos)
-    ls = s.list_stats()
     out = dict(ms=ms, force_ms=force_ms, force_launches=nlaunch, rebuilds=st1["rebuilds"] - st0["rebuilds"],
                kernel_launches=st1["kernel_launches"] - st0["kernel_launches"], nbar=nbar,
-               tbar=ls["table_entries"] / max(ls["windows"], 1), lists=ls,
                clocks=cs.summary(), tpa=st1["threads_per_atom"], block=st1["block_size"],
                capacity=st1["capacity"], autotune=choice)
     return s, out
@@ -581,8 +579,8 @@ def main():
     drift_64, dE_64 = nve_drift(cavgpu, p_eq, v_eq, typ, params, cavgpu.FP64, d64)
 
     tuned = rm["autotune"] or {}
-    kern = {"staged": cavgpu.FORCE_STAGED, "strided": cavgpu.FORCE_STRIDED}.get(tuned.get("force_kernel"),
-                                                                                  cavgpu.FORCE_AUTO)
+    kern = {"segments": cavgpu.FORCE_SEGMENTS, "strided": cavgpu.FORCE_STRIDED}.get(tuned.get("force_kernel"),
+                                                                                      cavgpu.FORCE_AUTO)
     spg = LAUNCH.get("steps_per_graph", tuned.get("steps_per_graph", 0))
     e2e_rate, h2d, d2h, phases = time_e2e(cavgpu, torch, pos, vel, typ, params, cavgpu.MIXED, args.steps,
                                           tpa=rm["tpa"], block=rm["block"], steps_per_graph=spg, force_kernel=kern)
@@ -593,17 +591,15 @@ def main():
                                            tpa=rm["tpa"], block=rm["block"], steps_per_graph=spg, force_kernel=kern)
 
     # roofline of the dominant kernel (mixed force kernel): algorithmic bytes per launch
-    #   per atom: 2 * nbar list entries + 4 * tbar / 32 window-table words (tbar entries per
-    #   window of 32 atoms) + rel_i 16 + nnbr 4 + vel r/w 64 + acc r 32 (a_old) + acc w 32,
+    #   per atom: 4 * nbar list words + rel_i 16 + nnbr 4 + vel r/w 64 + acc r 32 (a_old) + acc w 32,
     #   and on the launches that also drift the next step: pos r/w 64 + pos_ref 32 + rel_ref 16
-    #   + the next rel 16 = 128 more.  The neighbour coordinates (rel, 16 B per atom) are
-    #   read from DRAM once; their reuse across windows is served by L2.
+    #   + the next rel 16 = 128 more
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs")
     peak_note = "measured" if hbm else "fallback"
     hbm = hbm or 6800.0
     fused = fused_fraction(args.steps, rm["autotune"])
-    bytes_per_atom = 2.0 * rm["nbar"] + 4.0 * rm["tbar"] / 32.0 + 148.0 + 128.0 * fused
+    bytes_per_atom = 4.0 * rm["nbar"] + 148.0 + 128.0 * fused
     launch_ms = rm["force_ms"] / max(rm["force_launches"], 1)
     achieved = bytes_per_atom * n / (launch_ms * 1e-3) / 1e9
     traffic = read_profile_traffic("lj_force_mixed_1M.md")
@@ -631,7 +627,6 @@ def main():
     config.update({"fp64_value": value64, "mixed_over_fp64": value / value64, "fp64_steps": k64,
                    "rebuilds_in_timed_region": rm["rebuilds"], "mean_neighbours": rm["nbar"],
                    "threads_per_atom": rm["tpa"], "block": rm["block"], "capacity": rm["capacity"],
-                   "mean_window_table": rm["tbar"], "lists": rm["lists"],
                    "autotune": rm["autotune"], "parallelism": f"replicas x{ws}"})
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,

@@ -18,8 +18,7 @@ MAXT = 8
 
 OK, E_ARG, E_CUDA, E_NAN, E_NLIST_OVERFLOW, E_STATE, E_NOMEM, E_RANGE = 0, -1, -2, -3, -4, -5, -6, -7
 FP64, MIXED = 0, 1
-FORCE_AUTO, FORCE_STRIDED, FORCE_STAGED = 0, 1, 2
-FORCE_SEGMENTS = FORCE_STAGED  # the former name of the staged kernel
+FORCE_AUTO, FORCE_STRIDED, FORCE_SEGMENTS = 0, 1, 2
 NVE_ENERGY_PER_DOF, NVE_ENERGY_TOT, NVE_KBT, NVE_KB_TEMPERATURE = 0, 1, 2, 3
 VELOCITY_VERLET, VELOCITY_VERLET_LANGEVIN, LEAP_FROG = 0, 1, 2
 
@@ -39,7 +38,7 @@ class Params(C.Structure):
         ("steps_per_graph", C.c_int32), ("force_kernel", C.c_int32), ("jump_tol", C.c_double),
         ("initial_step", C.c_int64), ("nve_step", C.c_int64), ("nve_mode", C.c_int32), ("nve_pad", C.c_int32),
         ("nve_value", C.c_double), ("nve_kb", C.c_double), ("msd_process", C.c_int32),
-        ("ignore_intra_molecule", C.c_int32), ("table_capacity", C.c_int32),
+        ("ignore_intra_molecule", C.c_int32),
     ]
 
 
@@ -71,7 +70,6 @@ _SIGS = {
     "cavgpu_export_ghosts": (C.c_int64, [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                          C.c_int64]),
     "cavgpu_stats": (C.c_int, [C.c_void_p, C.c_void_p]),
-    "cavgpu_list_stats": (C.c_int, [C.c_void_p, C.c_void_p]),
     "cavgpu_stream": (C.c_void_p, [C.c_void_p]),
     "cavgpu_set_profiling": (C.c_int, [C.c_void_p, C.c_int32]),
     "cavgpu_read_profile": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -119,7 +117,7 @@ def _ptr(a):
 
 
 def make_params(p, precision=FP64, noise_off=False, tpa=0, block=0, nbr_capacity=0, steps_per_graph=0,
-                force_kernel=FORCE_AUTO, table_capacity=0):
+                force_kernel=FORCE_AUTO):
     """cavgpu_params from a parameter dict in the CAVIAR2 setter vocabulary (see workloads.lj_params)."""
     o = Params()
     lib().cavgpu_default_params(C.byref(o))
@@ -150,7 +148,6 @@ def make_params(p, precision=FP64, noise_off=False, tpa=0, block=0, nbr_capacity
     o.threads_per_atom, o.block_size = int(tpa), int(block)
     o.nbr_capacity, o.steps_per_graph = int(nbr_capacity), int(steps_per_graph)
     o.force_kernel = int(force_kernel)
-    o.table_capacity = int(table_capacity)
     o.jump_tol = float(p.get("jump_tol", 0.0))
     o.initial_step = int(p.get("initial_step", 0))
     nve = p.get("nve")  # {"step": k, "mode": CAVGPU_NVE_*, "value": x, "kb": y}
@@ -252,14 +249,6 @@ class System:
                 "graph_launches", "kernel_launches")
         return dict(zip(keys, (int(x) for x in o)))
 
-    def list_stats(self):
-        """Neighbour-list storage: row and window-table capacities, their largest use."""
-        o = np.zeros(8, np.int64)
-        self._check(lib().cavgpu_list_stats(self._h, _ptr(o)), "list_stats")
-        keys = ("capacity", "max_neighbours", "table_capacity", "max_table", "stage_entries", "bytes",
-                "table_entries", "windows")
-        return dict(zip(keys, (int(x) for x in o)))
-
     def stream(self):
         return lib().cavgpu_stream(self._h)
 
@@ -268,7 +257,7 @@ class System:
         o = np.zeros(6, np.int64)
         self._check(lib().cavgpu_autotune(self._h, int(trial_steps), int(bool(force)), _ptr(o)), "autotune")
         return dict(threads_per_atom=int(o[0]), block_size=int(o[1]), steps_per_graph=int(o[2]), trials=int(o[3]),
-                    force_kernel="staged" if int(o[4]) == FORCE_STAGED else "strided")
+                    force_kernel="segments" if int(o[4]) == FORCE_SEGMENTS else "strided")
 
     def set_profiling(self, on):
         self._check(lib().cavgpu_set_profiling(self._h, int(on)), "set_profiling")

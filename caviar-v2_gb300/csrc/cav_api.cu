@@ -56,7 +56,7 @@ struct TuneKey {
   }
 };
 struct TuneChoice {
-  int tpa, block, spg, stage;
+  int tpa, block, spg, seg;
 };
 std::mutex g_tune_mu;
 std::vector<std::pair<TuneKey, TuneChoice>> g_tune_cache;
@@ -95,7 +95,7 @@ struct cavgpu_ctx {
   long long prof_launches = 0;
   // allocations
   std::vector<void *> allocs;
-  size_t nbr_bytes = 0;         // neighbour rows and window tables
+  size_t nbr_bytes = 0;
 };
 
 namespace {
@@ -343,54 +343,29 @@ int check_status(cavgpu_ctx *c) {
   RK(read_flags(c, f));
   c->max_nb = std::max(c->max_nb, f[F_MAXNB]);
   if (f[F_NAN]) return CAVGPU_E_NAN;
-  if (f[F_OVERFLOW] || f[F_TAB_OVERFLOW]) return CAVGPU_E_NLIST_OVERFLOW;
+  if (f[F_OVERFLOW]) return CAVGPU_E_NLIST_OVERFLOW;
   return CAVGPU_OK;
 }
 
-// (re)allocate the neighbour rows for `cap` entries per atom and the window tables
-// for `tcap` entries per window (a size <= 0 keeps the current one)
-int alloc_lists(cavgpu_ctx *c, int cap, int tcap) {
-  if (cap <= 0) cap = c->d.cap;
-  if (tcap <= 0) tcap = c->d.tcap;
-  cap = (cap + 63) / 64 * 64;  // nbr_index needs cap % 8 == 0
-  tcap = (tcap + 31) / 32 * 32;
-  if (tcap > TAB_MAX) return CAVGPU_E_NLIST_OVERFLOW;  // a window's neighbours past 16-bit entries
+// (re)allocate the neighbour list for `cap` slots per atom
+int alloc_nbr(cavgpu_ctx *c, int cap) {
+  cap = (cap + 63) / 64 * 64;  // nbr_index needs cap % (4 * tpa) == 0, tpa <= 16
   const int A = 32 / c->d.tpa;  // whole blocks of A slots (nbr_index)
-  const size_t nwin = (size_t)(c->b.nslot + 31) / 32;
-  const size_t rows = (size_t)((c->b.nslot + A - 1) / A) * A * (size_t)cap * sizeof(uint16_t);
-  const size_t tabs = nwin * (size_t)tcap * sizeof(uint32_t);
-  for (void *old : {(void *)c->d.nbr, (void *)c->d.wtab}) {
-    if (!old) continue;
-    auto it = std::find(c->allocs.begin(), c->allocs.end(), old);
+  const size_t bytes = (size_t)((c->b.nslot + A - 1) / A) * A * (size_t)cap * sizeof(uint32_t);
+  if (c->d.nbr) {
+    auto it = std::find(c->allocs.begin(), c->allocs.end(), (void *)c->d.nbr);
     if (it != c->allocs.end()) c->allocs.erase(it);
-    cudaFree(old);
+    cudaFree(c->d.nbr);
+    c->d.nbr = nullptr;
   }
-  c->d.nbr = nullptr;
-  c->d.wtab = nullptr;
-  void *q = nullptr, *w = nullptr;
-  if (cudaMalloc(&q, rows) != cudaSuccess || cudaMalloc(&w, tabs) != cudaSuccess) {
-    cudaGetLastError();
-    cudaFree(q);
-    return CAVGPU_E_NOMEM;
-  }
+  void *q = nullptr;
+  if (cudaMalloc(&q, bytes) != cudaSuccess) { cudaGetLastError(); return CAVGPU_E_NOMEM; }
   c->allocs.push_back(q);
-  c->allocs.push_back(w);
-  c->d.nbr = static_cast<uint16_t *>(q);
-  c->d.wtab = static_cast<uint32_t *>(w);
+  c->d.nbr = static_cast<uint32_t *>(q);
   c->d.cap = cap;
-  c->d.tcap = tcap;
-  c->lc.tcap = tcap;
-  c->nbr_bytes = rows + tabs;
+  c->nbr_bytes = bytes;
   free_graphs(c);  // graphs hold the old Dev by value
   return CAVGPU_OK;
-}
-
-// capacities after a build that overflowed: 25% over what it wanted
-int grow_lists(cavgpu_ctx *c, const int *f) {
-  const int cap = f[F_OVERFLOW] ? (int)(f[F_OVERFLOW] * 1.25) + 32 : 0;
-  const int tcap = f[F_TAB_OVERFLOW] ? std::min((int)(f[F_TAB_OVERFLOW] * 1.25) + 32, TAB_MAX) : 0;
-  if (f[F_TAB_OVERFLOW] > TAB_MAX) return CAVGPU_E_NLIST_OVERFLOW;
-  return alloc_lists(c, cap, tcap);
 }
 
 // forced list build of every replica; grows the capacity until the build fits.
@@ -411,7 +386,7 @@ int forced_build(cavgpu_ctx *c, bool count = true) {
     c->kernel_launches += rebuild_kernels(c->b);
     RK(read_flags(c, f));
     c->max_nb = f[F_MAXNB];
-    if (!f[F_OVERFLOW] && !f[F_TAB_OVERFLOW]) {
+    if (!f[F_OVERFLOW]) {
       if (!count) {
         f[F_REBUILDS] = f0[F_REBUILDS];
         f[F_PASSES] = f0[F_PASSES];
@@ -420,7 +395,7 @@ int forced_build(cavgpu_ctx *c, bool count = true) {
       }
       return CAVGPU_OK;
     }
-    RK(grow_lists(c, f));
+    RK(alloc_nbr(c, (int)(f[F_OVERFLOW] * 1.25) + 32));
   }
   return CAVGPU_E_NLIST_OVERFLOW;
 }
@@ -537,10 +512,8 @@ int create_common(const cavgpu_params *p, int nrep, const double *lo3, const dou
   c->lc.block = p->block_size ? p->block_size : 128;
   if (c->lc.tpa != 1 && c->lc.tpa != 2 && c->lc.tpa != 4 && c->lc.tpa != 8 && c->lc.tpa != 16) { delete c; return CAVGPU_E_ARG; }
   if (c->lc.block < 32 || c->lc.block > 256 || c->lc.block % 32) { delete c; return CAVGPU_E_ARG; }
-  if (p->table_capacity < 0 || p->table_capacity > TAB_MAX || p->nbr_capacity < 0) { delete c; return CAVGPU_E_ARG; }
-  if (p->force_kernel < CAVGPU_FORCE_AUTO || p->force_kernel > CAVGPU_FORCE_STAGED) { delete c; return CAVGPU_E_ARG; }
-  c->lc.stage = p->precision == CAVGPU_MIXED && p->force_kernel != CAVGPU_FORCE_STRIDED;
-  if (prepare_force() != CAVGPU_OK) { delete c; return CAVGPU_E_CUDA; }
+  if (p->force_kernel < CAVGPU_FORCE_AUTO || p->force_kernel > CAVGPU_FORCE_SEGMENTS) { delete c; return CAVGPU_E_ARG; }
+  c->lc.use_seg = p->precision == CAVGPU_MIXED && p->force_kernel == CAVGPU_FORCE_SEGMENTS;
   c->lc.ntypes = p->ntypes;
   c->d.tpa = c->lc.tpa;
   if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) { delete c; return CAVGPU_E_CUDA; }
@@ -569,6 +542,43 @@ int create_common(const cavgpu_params *p, int nrep, const double *lo3, const dou
   if (rc) { cavgpu_destroy(c); return rc; }
   *out = c;
   return CAVGPU_OK;
+}
+
+// Row segments of the mixed force kernel.  Replica r's x-rows are cut into
+// segments of S cells, S chosen so that the 9 x (S + 2) staged cells hold about
+// STAGE_TARGET atoms at the replica's mean cell occupancy; the stage is sized
+// for the largest estimate with 35% headroom (a segment that still overflows it
+// falls back to global gathers).
+int build_segments(cavgpu_ctx *c) {
+  constexpr double STAGE_TARGET = 4096.0;
+  constexpr int SEG_MAX = 62;  // cells per segment
+  std::vector<int4> segs;
+  int umax = 3;
+  double need = 0.0;
+  for (int r = 0; r < c->b.nrep; ++r) {
+    const RepBox &rb = c->reps[r];
+    if (rb.nc[1] > 0xffff || rb.nc[2] > 0x7fff) return CAVGPU_E_RANGE;
+    const double navg = (double)rb.natoms / rb.ncell;
+    const int smax = std::max(1, std::min(SEG_MAX, (int)(STAGE_TARGET / (9.0 * navg * 1.3)) - 2));
+    const int ncx = rb.nc[0], nsx = (ncx + smax - 1) / smax, S = (ncx + nsx - 1) / nsx;
+    for (int cz = 0; cz < rb.nc[2]; ++cz)
+      for (int cy = 0; cy < rb.nc[1]; ++cy)
+        for (int x0 = 0; x0 < ncx; x0 += S) segs.push_back(make_int4(r, cy | (cz << 16), x0, std::min(S, ncx - x0)));
+    umax = std::max(umax, S + 2);
+    need = std::max(need, 9.0 * (S + 2) * navg * 1.35);
+  }
+  // dynamic shared memory within the 227 KiB a block may hold, beside ~4 KiB of static
+  const size_t limit = 227 * 1024 - 4096 - (size_t)2 * 9 * umax * sizeof(int);
+  c->d.stage_cap = (int)std::min<double>(need + 128.0, (double)(limit / 16));
+  int4 *dseg = nullptr;
+  RK(dalloc(c, &dseg, segs.size()));
+  CK(cudaMemcpyAsync(dseg, segs.data(), segs.size() * sizeof(int4), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->d.seg = dseg;
+  c->d.nseg = (int)segs.size();
+  c->d.seg_umax = umax;
+  c->lc.nseg = c->d.nseg;
+  return prepare_force_seg(seg_smem_bytes(c->d.stage_cap, umax));
 }
 
 // Lay the replicas out (32-aligned slot ranges, consecutive cell ranges with one
@@ -656,16 +666,19 @@ int upload_common(cavgpu_ctx *c, const int64_t *counts, const double *pos3, cons
   c->tc.volume = vol;
   c->tc.langevin = is_lang(c);
   Dev &d = c->d;
-  // partial sums for the largest force grid of any launch shape (the autotuner
-  // changes it later) and for the drift grid
+  if (c->p.precision == CAVGPU_MIXED) RK(build_segments(c));
+  // partial sums for the largest force grid of any launch shape and kernel (the
+  // autotuner changes them later) and for the drift grid
   size_t nblk = 1;
-  for (int tpa = 1; tpa <= 16; tpa *= 2)
-    for (int blk = 32; blk <= 256; blk += 32) {
-      LaunchCfg t = c->lc;
-      t.tpa = tpa;
-      t.block = blk;
-      nblk = std::max(nblk, (size_t)force_grid_blocks(t));
-    }
+  for (int seg = 0; seg < 2; ++seg)
+    for (int tpa = 1; tpa <= 16; tpa *= 2)
+      for (int blk = 32; blk <= 256; blk += 32) {
+        LaunchCfg t = c->lc;
+        t.tpa = tpa;
+        t.block = blk;
+        t.use_seg = seg;
+        nblk = std::max(nblk, (size_t)force_grid_blocks(t));
+      }
   const size_t nblk_d = (size_t)std::max((NS + 255) / 256, 1);
   d.partials_blocks = (int)nblk;
   int rc = CAVGPU_OK;
@@ -689,7 +702,6 @@ int upload_common(cavgpu_ctx *c, const int64_t *counts, const double *pos3, cons
     take(&d.id, NS);
     take(&d.t_id, NS);
     take(&d.skey, NS);
-    take(&d.wtab_len, ((size_t)NS + 31) / 32);
     take(&d.cell_count, ncell_all);
     take(&d.cell_cursor, ncell_all);
     take(&d.cell_start, (size_t)ncell_all + 1);
@@ -747,15 +759,7 @@ int upload_common(cavgpu_ctx *c, const int64_t *counts, const double *pos3, cons
   for (const RepBox &rb : c->reps) rho = std::max(rho, rb.natoms / (rb.L[0] * rb.L[1] * rb.L[2]));
   const double ce = c->cutoff_extra;
   const int cap = c->p.nbr_capacity > 0 ? c->p.nbr_capacity : (int)(1.4 * rho * 4.18879020479 * ce * ce * ce) + 48;
-  // window tables: the atoms within ce of a group of 32 atoms (a w x w x a box, w >= ce
-  // the cell width, a = 32 / (rho w^2)), Minkowski volume of the box and the ball;
-  // 2.2 x that for windows of two groups (a row's end) and fluctuations
-  const double w = ce, ax = std::max(w, 32.0 / (rho * w * w));
-  const double vol_u = ax * w * w + 2.0 * ce * (2.0 * ax * w + w * w) + 3.14159265358979 * ce * ce * (ax + 2.0 * w) +
-                       4.18879020479 * ce * ce * ce;
-  const int tcap = c->p.table_capacity > 0 ? c->p.table_capacity
-                                          : (int)std::min<double>(2.2 * rho * vol_u + 64.0, (double)TAB_MAX);
-  RK(alloc_lists(c, cap, tcap));
+  RK(alloc_nbr(c, cap));
   if (on_device) {
     // the caller's arrays, raw, into the rebuild scratch (32 B per slot each: positions
     // and velocities 24 B, types and ids 8 B + 8 B), then converted and checked
@@ -797,27 +801,9 @@ int upload_common(cavgpu_ctx *c, const int64_t *counts, const double *pos3, cons
   return CAVGPU_OK;
 }
 
-// The mixed pair kernel's stage per warp: the table length that 97% of the windows
-// do not exceed (the rest gather from global memory) -- a stage sized for the
-// longest table, a window across a row's end, would halve the warps an SM holds.
-int fit_stage(cavgpu_ctx *c) {
-  c->lc.scap = 0;
-  if (c->p.precision != CAVGPU_MIXED) return CAVGPU_OK;
-  const size_t nwin = ((size_t)c->b.nslot + 31) / 32;
-  std::vector<int> len(nwin);
-  CK(cudaMemcpyAsync(len.data(), c->d.wtab_len, nwin * sizeof(int), cudaMemcpyDeviceToHost, c->st));
-  CK(cudaStreamSynchronize(c->st));
-  const size_t k = std::min(nwin - 1, (size_t)(0.97 * (double)nwin));
-  std::nth_element(len.begin(), len.begin() + k, len.end());
-  c->lc.scap = std::min(c->d.tcap, std::max(32, (len[k] + 31) / 32 * 32));
-  free_graphs(c);  // graphs hold the launch arguments by value
-  return CAVGPU_OK;
-}
-
 int setup_common(cavgpu_ctx *c) {
   if (!c->uploaded) return CAVGPU_E_STATE;
   RK(forced_build(c));
-  RK(fit_stage(c));
   RK(launch_force(c->d, c->b, c->sc, c->lc, 0, 1, 0, FUSE_NONE, 0, 0, c->st));
   c->kernel_launches += 1;
   if (c->b.nrep == 1) {
@@ -848,14 +834,14 @@ int ensure_status(cavgpu_ctx *c) {
 // its pair kernel with the closing update, its thermo record, constraint::Nve.
 // `g` = the step's index in the call (for the thermo record).
 int complete_overflowed_step(cavgpu_ctx *c, const ChunkPlan &pl, int k, int64_t g, int64_t nsteps, int64_t every,
-                             double *out5, const int *need) {
+                             double *out5, int need) {
   if (pl.fused_before(k) & 1) {
     if (c->p.precision == CAVGPU_MIXED)
       CK(cudaMemcpyAsync(c->d.rel, c->d.rel_alt, (size_t)c->b.nslot * sizeof(float4), cudaMemcpyDeviceToDevice, c->st));
     else
       CK(cudaMemcpyAsync(c->d.pos, c->d.pos_alt, (size_t)c->b.nslot * sizeof(dbl4), cudaMemcpyDeviceToDevice, c->st));
   }
-  RK(grow_lists(c, need));
+  RK(alloc_nbr(c, (int)(need * 1.25) + 32));
   RK(forced_build(c, false));
   const bool th = (every > 0 && (g + 1) % every == 0) || (every == 0 && g == nsteps - 1);
   const int ring_slot = (th && every > 0) ? 0 : -1;
@@ -963,9 +949,9 @@ int run_steps(cavgpu_ctx *c, int64_t nsteps, int64_t every, double *out5) {
     const int k = f[F_HALT_STEP];
     done = p.start + k;
     c->steps_done += k;
-    if (f[F_NAN] || !(f[F_OVERFLOW] || f[F_TAB_OVERFLOW])) return CAVGPU_E_NAN;
+    if (f[F_NAN] || !f[F_OVERFLOW]) return CAVGPU_E_NAN;
     const ChunkPlan plan = *p.plan;  // growing the list frees the graphs that hold it
-    RK(complete_overflowed_step(c, plan, k, done, nsteps, every, out5, f));
+    RK(complete_overflowed_step(c, plan, k, done, nsteps, every, out5, f[F_OVERFLOW]));
     RK(read_flags(c, f));
     if (f[F_HALT]) return f[F_NAN] ? CAVGPU_E_NAN : CAVGPU_E_NLIST_OVERFLOW;
     done += 1;
@@ -1142,12 +1128,12 @@ int cavgpu_autotune(cavgpu_ctx *c, int32_t trial_steps, int32_t flags, int64_t *
   };
   // back to the snapshot with launch shape (tpa, block, kernel): list storage for the
   // shape, state copied back, forced rebuild
-  auto restore = [&](int tpa, int block, int stage) -> int {
+  auto restore = [&](int tpa, int block, int seg) -> int {
     c->lc.tpa = tpa;
     c->lc.block = block;
-    c->lc.stage = stage;
+    c->lc.use_seg = seg;
     c->d.tpa = tpa;
-    RK(alloc_lists(c, 0, 0));
+    RK(alloc_nbr(c, c->d.cap));
     for (int k = 0; k < 3; ++k)
       CK(cudaMemcpyAsync(src4[k], snap + k * NS, NS * sizeof(dbl4), cudaMemcpyDeviceToDevice, c->st));
     CK(cudaMemcpyAsync(c->d.type, snap_i, NS * sizeof(int), cudaMemcpyDeviceToDevice, c->st));
@@ -1178,8 +1164,8 @@ int cavgpu_autotune(cavgpu_ctx *c, int32_t trial_steps, int32_t flags, int64_t *
   int trials = 0;
   // one trial: a warm-up graph (capture, first replay) then T steps timed on the stream
   // (an eager context, steps_per_graph < 0, stays eager: spg is then -1)
-  auto trial = [&](int tpa, int block, int stage, int spg, float *ms) -> int {
-    RK(restore(tpa, block, stage));
+  auto trial = [&](int tpa, int block, int seg, int spg, float *ms) -> int {
+    RK(restore(tpa, block, seg));
     c->p.steps_per_graph = spg;
     RK(cavgpu_run(c, spg > 0 ? std::min(T, spg) : 2, 0, nullptr));
     CK(cudaEventRecord(e0, c->st));
@@ -1193,29 +1179,29 @@ int cavgpu_autotune(cavgpu_ctx *c, int32_t trial_steps, int32_t flags, int64_t *
   const int spg0 = c->p.steps_per_graph > 0 ? c->p.steps_per_graph : (c->p.steps_per_graph < 0 ? -1 : 50);
   if (!rc && !cached) {
     float best_ms = 1e30f;
-    best = {c->lc.tpa, c->lc.block, spg0, c->lc.stage};
+    best = {c->lc.tpa, c->lc.block, spg0, c->lc.use_seg};
     const int tpas[] = {1, 2, 4, 8};
     const int blocks[] = {64, 128, 256};
-    // kernels: the mixed form tries the staged and the global-gather kernel unless the
+    // kernels: the mixed form tries the segment and the grid-strided kernel unless the
     // caller fixed one
-    int kernels[2] = {c->lc.stage, -1};
+    int kernels[2] = {c->lc.use_seg, -1};
     if (c->p.precision == CAVGPU_MIXED && c->p.force_kernel == CAVGPU_FORCE_AUTO) kernels[0] = 1, kernels[1] = 0;
-    for (int stage : kernels) {
-      if (stage < 0) break;
+    for (int seg : kernels) {
+      if (seg < 0) break;
       for (int tpa : tpas)
         for (int block : blocks) {
           if (rc) break;
           float ms = 0.f;
-          const int trc = trial(tpa, block, stage, spg0, &ms);
+          const int trc = trial(tpa, block, seg, spg0, &ms);
           if (trc == CAVGPU_E_CUDA || trc == CAVGPU_E_NOMEM) { rc = trc; break; }
-          if (trc == CAVGPU_OK && ms < best_ms) { best_ms = ms; best = {tpa, block, spg0, stage}; }
+          if (trc == CAVGPU_OK && ms < best_ms) { best_ms = ms; best = {tpa, block, spg0, seg}; }
         }
     }
     // graph length: the host reads status once per chunk group; longer graphs cost memory
     for (int spg : {25, 100}) {
       if (rc || spg0 < 0) break;
       float ms = 0.f;
-      const int trc = trial(best.tpa, best.block, best.stage, spg, &ms);
+      const int trc = trial(best.tpa, best.block, best.seg, spg, &ms);
       if (trc == CAVGPU_E_CUDA || trc == CAVGPU_E_NOMEM) { rc = trc; break; }
       if (trc == CAVGPU_OK && ms < 0.98f * best_ms) { best_ms = ms; best.spg = spg; }
     }
@@ -1228,7 +1214,7 @@ int cavgpu_autotune(cavgpu_ctx *c, int32_t trial_steps, int32_t flags, int64_t *
   if (e1) cudaEventDestroy(e1);
   if (!rc) {
     c->p.steps_per_graph = best.spg;
-    rc = restore(best.tpa, best.block, best.stage);
+    rc = restore(best.tpa, best.block, best.seg);
   }
   cudaFree(snap);
   cudaFree(snap_i);
@@ -1244,7 +1230,7 @@ int cavgpu_autotune(cavgpu_ctx *c, int32_t trial_steps, int32_t flags, int64_t *
     out6[1] = best.block;
     out6[2] = best.spg;
     out6[3] = trials;
-    out6[4] = best.stage ? CAVGPU_FORCE_STAGED : CAVGPU_FORCE_STRIDED;
+    out6[4] = best.seg ? CAVGPU_FORCE_SEGMENTS : CAVGPU_FORCE_STRIDED;
     out6[5] = 0;
   }
   return CAVGPU_OK;
@@ -1413,29 +1399,6 @@ int cavgpu_stats(cavgpu_ctx *c, int64_t *o) {
   o[5] = c->lc.block;
   o[6] = c->graph_launches;
   o[7] = c->kernel_launches;
-  return CAVGPU_OK;
-}
-
-int cavgpu_list_stats(cavgpu_ctx *c, int64_t *o) {
-  if (!c || !o) return CAVGPU_E_ARG;
-  int f[F_NWORDS] = {0};
-  if (c->uploaded) RK(read_flags(c, f));
-  o[0] = c->d.cap;
-  o[1] = std::max(c->max_nb, f[F_MAXNB]);
-  o[2] = c->d.tcap;
-  o[3] = f[F_TABLEN];
-  o[4] = force_staged(c->lc) ? c->lc.scap : 0;
-  o[5] = (int64_t)c->nbr_bytes;
-  o[6] = 0;
-  o[7] = 0;
-  if (c->set_up) {
-    const size_t nwin = ((size_t)c->b.nslot + 31) / 32;
-    std::vector<int> len(nwin);
-    CK(cudaMemcpyAsync(len.data(), c->d.wtab_len, nwin * sizeof(int), cudaMemcpyDeviceToHost, c->st));
-    CK(cudaStreamSynchronize(c->st));
-    for (int v : len) o[6] += v;
-    o[7] = (int64_t)nwin;
-  }
   return CAVGPU_OK;
 }
 

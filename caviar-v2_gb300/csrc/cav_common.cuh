@@ -71,9 +71,7 @@ enum Flag : int {
   F_STEPS_OK = 8,   // steps of the current chunk whose pair kernel ran (the step counter adds them)
   F_HALT_STEP = 9,  // steps of the halted chunk that completed before the halt
   F_UPLOAD_BAD = 10,  // an uploaded atom outside the box, of an unknown type or with a bad id
-  F_TAB_OVERFLOW = 11,  // a build wanted more than `tcap` entries in a window's table (the most wanted)
-  F_TABLEN = 12,    // largest window table of the builds since the last forced build
-  F_NWORDS = 14
+  F_NWORDS = 12
 };
 
 // what the pair kernel does after the closing update of its step: nothing, or the
@@ -157,16 +155,11 @@ struct Dev {
   int *t_mol;
   int *atom_cell, *cell_count, *cell_start, *cell_cursor, *perm, *perm_tmp;
   uint64_t *skey;             // order inside a cell: Morton index of the 4x4x4 sub-cell, then id
-  // neighbour list: per window of 32 slots a table of the distinct neighbours of its
-  // atoms (slots, in the order the build met them), per atom 16-bit entries that
-  // index that table (see the layout below)
-  uint16_t *nbr;
+  // neighbour list
+  uint32_t *nbr;
   int *nnbr;
-  int cap;                    // entries per atom (multiple of 64)
+  int cap;                    // slots per atom (multiple of 64)
   int tpa;                    // force-kernel lanes per atom (fixes the list layout)
-  uint32_t *wtab;             // [window][tcap]: neighbour words (slot | code << CODE_SHIFT)
-  int *wtab_len;              // [window]: entries of the window's table
-  int tcap;                   // table entries per window (multiple of 32, at most TAB_MAX)
   // status, reductions
   int *flags;
   double *partials_ke;        // per-block {sum m v^2, sum m v} (4 per block)
@@ -187,28 +180,26 @@ struct Dev {
   // host-order staging for downloads
   double *h3;
   int32_t *hi3;
+  // row segments of the mixed force kernel: {replica, cy | cz << 16, first cell x, cells}
+  const int4 *seg;
+  int nseg;
+  int seg_umax;               // most cells a segment stages per row (segment length + 2)
+  int stage_cap;              // staged atoms the shared memory holds (float4 each)
 };
 
+// Dynamic shared memory of the segment force kernel: the staged coordinates, then
+// two int tables of 9 rows x seg_umax cells (slot offset, count).
+inline size_t seg_smem_bytes(int stage_cap, int umax) {
+  return (size_t)stage_cap * 16 + (size_t)2 * 9 * umax * sizeof(int);
+}
+
 // ---- neighbour-list layout -------------------------------------------------
-// Windows: slots [32 w, 32 w + 32) (replica slot ranges start on multiples of 32).
-// Window w's table holds, from wtab[w * tcap], the neighbours of its atoms, each
-// once per (slot, cell offset), in the order the build met them (cell by cell):
-// words j | code << CODE_SHIFT, code the image code (FP64 form) or, for the mixed
-// form, the row of j's cell relative to the atom group's, (dy+1) + 3 (dz+1).  An
-// atom's list entry is (kx << TAB_BITS) | index into its window's table, kx = dx+1
-// of j's cell relative to the atom's (mixed form; 0 in the FP64 form).  The pair
-// kernel reads a window's table once per step with coalesced loads (the mixed form
-// stages the coordinates into shared memory) and gathers from it.
-//
 // A warp of the force kernel serves A = 32/tpa atoms (a block of A consecutive
-// slots).  Within a block, entries come in chunks of eight: chunk g of atom i
-// holds entries 8g..8g+7 at block_base + g*8A + (i % A)*8.  Force-kernel lane
+// slots).  Within a block, entries come in chunks of four: chunk g of atom i
+// holds entries 4g..4g+3 at block_base + g*4A + (i % A)*4.  Force-kernel lane
 // (t, a) reads chunks g = t + tpa*q with one 128-bit load, so a warp reads 512
 // consecutive bytes per step of q.  A and tpa are powers of two: shifts only.
-// `cap` is a multiple of 8 (64 in practice).
-constexpr int TAB_BITS = 14;
-constexpr int TAB_MAX = 1 << TAB_BITS;           // table entries a window may hold (16384)
-constexpr uint32_t TAB_IDX_MASK = TAB_MAX - 1u;
+// `cap` is a multiple of 4*tpa (64 covers every tpa up to 16).
 __host__ __device__ inline int log2_pow2(int v) {
 #ifdef __CUDA_ARCH__
   return __ffs(v) - 1;
@@ -218,13 +209,12 @@ __host__ __device__ inline int log2_pow2(int v) {
 }
 __host__ __device__ inline size_t nbr_block_base(int i, int cap, int tpa) {
   const int as = 5 - log2_pow2(tpa);  // log2(A)
-  return ((size_t)(i >> as) * (size_t)cap << as) + ((size_t)(i & ((1 << as) - 1)) << 3);
+  return ((size_t)(i >> as) * (size_t)cap << as) + ((size_t)(i & ((1 << as) - 1)) << 2);
 }
 __host__ __device__ inline size_t nbr_index(int i, int k, int cap, int tpa) {
   const int as = 5 - log2_pow2(tpa);
-  return nbr_block_base(i, cap, tpa) + ((size_t)(k >> 3) << (as + 3)) + (k & 7);
+  return nbr_block_base(i, cap, tpa) + ((size_t)(k >> 2) << (as + 2)) + (k & 3);
 }
-__host__ __device__ inline uint16_t nbr_entry(int kx, int idx) { return (uint16_t)((kx << TAB_BITS) | idx); }
 
 __host__ __device__ inline int image_code(int sx, int sy, int sz) { return (sx + 1) + 3 * (sy + 1) + 9 * (sz + 1); }
 
@@ -376,10 +366,9 @@ struct LaunchCfg {
   int integrator;  // CAVGPU_VELOCITY_VERLET / ..._LANGEVIN
   int tpa, block;
   int n;           // slots
-  int ntypes;      // 1: the kernels keep the pair constants in registers
-  int tcap;        // table entries per window (the tables' stride)
-  int stage;       // mixed form: stage window tables in shared memory
-  int scap;        // window-table entries a warp's stage holds (longer tables: global gathers)
+  int nseg;        // row segments (mixed form; 0 = none)
+  int use_seg;     // mixed form: run the segment kernel (shared-memory stage)
+  int ntypes;      // 1: the mixed kernels keep the pair constants in registers
 };
 
 struct ThermoCfg {
@@ -394,18 +383,8 @@ struct ThermoCfg {
 // whose half-skin test did not fire.
 int drift_grid_blocks(const LaunchCfg &lc);
 int force_grid_blocks(const LaunchCfg &lc);
-// Dynamic shared memory of the mixed pair kernel: one table stage (float4 per entry)
-// per warp, scap entries each.  The stage is used when it fits FORCE_SMEM_MAX; a
-// window whose table is longer than scap is gathered from global memory instead.
-// prepare_force raises every staged variant's dynamic shared-memory limit to
-// FORCE_SMEM_MAX (once per process, outside stream capture).
-constexpr size_t FORCE_SMEM_MAX = 192 * 1024;
-inline size_t force_smem_bytes(int block, int tcap) { return (size_t)(block / 32) * tcap * 16; }
-inline bool force_staged(const LaunchCfg &lc) {
-  return lc.precision == CAVGPU_MIXED && lc.stage && lc.scap > 0 &&
-         force_smem_bytes(lc.block, lc.scap) <= FORCE_SMEM_MAX;
-}
-int prepare_force();
+// sets the dynamic shared-memory limit of every segment-kernel variant (call outside capture)
+int prepare_force_seg(size_t smem_bytes);
 // thermo < 0 (Langevin): the velocity half only; launch_lang_pos then moves the atoms
 int launch_drift(const Dev &d, const Box &b, const StepConsts &sc, const LaunchCfg &lc, int k_in_chunk,
                  int thermo, cudaStream_t st);

@@ -2,15 +2,12 @@
 // src/force/lj.cpp:393-517), fused with the closing integrator update of the step.
 //
 // Full neighbour list, gather only (no atomics, deterministic): TPA lanes work on one
-// atom, a warp on A = 32/TPA atoms.  The 32 slots of a window share a table of their
-// distinct neighbours, and an atom's list entries are 16-bit indices into it; the
-// list layout (nbr_index) makes every iteration one coalesced 512-byte read of eight
-// entries per lane.  Two precisions:
+// atom, a warp on A = 32/TPA atoms, and the list layout (nbr_index) makes every
+// iteration one coalesced 128-byte read of neighbour words.  Two precisions:
 //   FP64  : image = x_j + s*L, all pair arithmetic in double;
 //   MIXED : FP32 pair arithmetic on coordinates relative to each atom's build cell
-//           (float4 x,y,z,type; cell offsets from the entry and the table word), FP64
+//           (float4 x,y,z,type; cell offsets decoded from the stencil index), FP64
 //           accumulation across lanes, FP64 acceleration/velocity/reductions.
-#include <mutex>
 #include <type_traits>
 
 #include "cav_common.cuh"
@@ -160,109 +157,94 @@ __device__ __forceinline__ uint4 ld_list(const uint4 *p) {
   return v;
 }
 
-// Bits a mixed-form neighbour coordinate carries in .w besides its type (< 256):
-// ky << 8 | kz << 10, ky = dy+1 and kz = dz+1 of its cell relative to the atom's,
-// from the table word's row r = ky + 3 kz ((11 r) >> 5 = r / 3 for r <= 8).
-__device__ __forceinline__ int row_bits(uint32_t word) {
-  const int r = (int)(word >> CODE_SHIFT), kz = (r * 11) >> 5;
-  return ((r - 3 * kz) << 8) | (kz << 10);
-}
-
-// Mixed-form pair loop of one lane: list chunks t, t+TPA, ... of atom i (eight 16-bit
-// entries per 128-bit load, the next chunk's load in flight), taken four entries at
-// a time (four neighbour coordinates in flight); `gather(entry)` returns the
-// neighbour's float4 with its row bits (a shared-memory stage of the window's table,
-// or global memory through the table).  Two pairs go through each packed FP32x2
-// evaluation (even and odd list entries, with their own accumulators, folded at the
-// end); a pair beyond its cutoff gets coef = 0.  ONE: single-type system, pair
-// constants in registers; otherwise from the shared-memory table.
+// Mixed-form pair loop of one lane: list chunks t, t+TPA, ... of atom i (four words
+// per 128-bit load; the next chunk's load and four neighbour coordinates in
+// flight); `gather(word)` returns the neighbour's float4 (global memory or a
+// shared-memory stage).  Two pairs go through each packed FP32x2 evaluation (even
+// and odd list entries, with their own accumulators, folded at the end); a pair
+// beyond its cutoff gets coef = 0.  ONE: single-type system, pair constants in
+// registers; otherwise from the shared-memory table.
 //
 // ((r_j - r_i) + d wf) + d wlo, each sum rounded once (d wf and d wlo are exact
 // products): rounding is symmetric under negation and i seen from j has offset -d,
 // so d_ji = -d_ij bit for bit and the FP32 pair forces obey Newton's third law
-// exactly (each half of a packed operation rounds as the scalar one).  d = k - 1 per
-// axis, kx from the entry, ky and kz from the coordinate's row bits.
+// exactly (each half of a packed operation rounds as the scalar one).  d comes from
+// the stencil index k = (dx+1) + 3 (dy+1) + 9 (dz+1) by integer arithmetic (a table
+// in shared memory would load the L1 pipe that the neighbour gathers saturate).
 template <int TPA, bool EV, bool ONE, class Gather>
 __device__ __forceinline__ void mixed_pairs(const uint4 *row4, int nn, int t, const float4 ri, int ti, int nt,
                                             const SmemTabF &tab, const OneType c1, const float4 wf,
                                             const float4 wl, const float jtol, Gather gather, float &ax,
                                             float &ay, float &az, float &vr, float &pp) {
   F2 ax2 = f2(0.f, 0.f), ay2 = ax2, az2 = ax2, vr2 = ax2, pp2 = ax2;  // vr2: sum of +coef r^2
-  uint4 nxt = 8 * t < nn ? ld_list(row4) : make_uint4(0, 0, 0, 0);
-  for (int q = 0, k0 = 8 * t; k0 < nn; ++q, k0 += 8 * TPA) {
+  uint4 nxt = 4 * t < nn ? ld_list(row4) : make_uint4(0, 0, 0, 0);
+  for (int q = 0, k0 = 4 * t; k0 < nn; ++q, k0 += 4 * TPA) {
     const uint4 w4 = nxt;
-    if (k0 + 8 * TPA < nn) nxt = ld_list(row4 + (size_t)(q + 1) * 32);  // the next list chunk in flight
-    const uint32_t ew[4] = {w4.x, w4.y, w4.z, w4.w};
+    if (k0 + 4 * TPA < nn) nxt = ld_list(row4 + (size_t)(q + 1) * 32);  // the next list chunk in flight
+    const uint32_t e[4] = {w4.x, w4.y, w4.z, w4.w};
+    float4 rj[4];
 #pragma unroll
-    for (int hq = 0; hq < 2; ++hq) {
-      const int kb = k0 + 4 * hq;
-      if (kb >= nn) break;
-      const uint32_t e[4] = {ew[2 * hq] & 0xffffu, ew[2 * hq] >> 16, ew[2 * hq + 1] & 0xffffu, ew[2 * hq + 1] >> 16};
-      float4 rj[4];
+    for (int u = 0; u < 4; ++u)  // four independent gathers in flight
+      if (k0 + u < nn) rj[u] = gather(e[u]);
+      else rj[u] = make_float4(1e18f, 1e18f, 1e18f, __int_as_float(ti));  // beyond every cutoff
 #pragma unroll
-      for (int u = 0; u < 4; ++u)  // four independent gathers in flight
-        if (kb + u < nn) rj[u] = gather(e[u]);
-        else rj[u] = make_float4(1e18f, 1e18f, 1e18f, __int_as_float(ti));  // beyond every cutoff
+    for (int a = 0; a < 4; a += 2) {
+      if (k0 + a >= nn) break;
+      // d = k - 1 for k in {0, 1, 2} without an int-to-float conversion: the float
+      // with bits 0x4B400000 | k is 12582912 + k exactly, and 12582913 is subtracted
+      float dd[6];
 #pragma unroll
-      for (int a = 0; a < 4; a += 2) {
-        if (kb + a >= nn) break;
-        // d = k - 1 for k in {0, 1, 2} without an int-to-float conversion: the float
-        // with bits 0x4B400000 | k is 12582912 + k exactly, and 12582913 is subtracted
-        float dd[6];
-        int tj[2];
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const int wb = __float_as_int(rj[a + h].w);
-          dd[h] = __int_as_float(0x4B400000 | (int)(e[a + h] >> TAB_BITS));
-          dd[2 + h] = __int_as_float(0x4B400000 | ((wb >> 8) & 3));
-          dd[4 + h] = __int_as_float(0x4B400000 | ((wb >> 10) & 3));
-          tj[h] = wb & 0xff;
-        }
-        const F2 magic = f2(12582913.0f, 12582913.0f);
-        const F2 ddx = sub2(f2(dd[0], dd[1]), magic), ddy = sub2(f2(dd[2], dd[3]), magic),
-                 ddz = sub2(f2(dd[4], dd[5]), magic);
-        const F2 dx = fma2(ddx, f2(wl.x, wl.x), fma2(ddx, f2(wf.x, wf.x), sub2(f2(rj[a].x, rj[a + 1].x), f2(ri.x, ri.x))));
-        const F2 dy = fma2(ddy, f2(wl.y, wl.y), fma2(ddy, f2(wf.y, wf.y), sub2(f2(rj[a].y, rj[a + 1].y), f2(ri.y, ri.y))));
-        const F2 dz = fma2(ddz, f2(wl.z, wl.z), fma2(ddz, f2(wf.z, wf.z), sub2(f2(rj[a].z, rj[a + 1].z), f2(ri.z, ri.z))));
-        const F2 r2d = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
-        float r2a, r2b;
-        unf2(r2d, r2a, r2b);
-        float rc2a, rc2b, sg2a, sg2b, e4a, e4b, gca, gcb, pka, pkb;
-        if (ONE) {
-          rc2a = rc2b = c1.rc2; sg2a = sg2b = c1.sig2; e4a = e4b = c1.eps4; gca = gcb = c1.gc; pka = pkb = c1.pk;
-        } else {
-          const int ta = ti * nt + tj[0], tb = ti * nt + tj[1];
-          const float4 pa = tab.c4[ta], pb = tab.c4[tb];
-          rc2a = pa.x; sg2a = pa.y; e4a = pa.z; gca = pa.w;
-          rc2b = pb.x; sg2b = pb.y; e4b = pb.z; gcb = pb.w;
-          pka = EV ? tab.pk[ta] : 0.0f;
-          pkb = EV ? tab.pk[tb] : 0.0f;
-        }
-        const bool ina = r2a <= rc2a, inb = r2b <= rc2b;
-        if (!(ina || inb)) continue;
-        const float r2ca = fmaxf(r2a, jtol), r2cb = fmaxf(r2b, jtol);  // Lj jump_fix floor (0 when off)
-        const F2 r2 = f2(r2ca, r2cb), r2i = f2(rcp_approx(r2ca), rcp_approx(r2cb));
-        const F2 eps4 = f2(e4a, e4b);
-        const F2 s2 = mul2(f2(sg2a, sg2b), r2i);
-        const F2 s6 = mul2(mul2(s2, s2), s2);
-        const F2 w = mul2(mul2(eps4, r2i), s6);
-        F2 coef = fma2(w, fma2(f2(-12.0f, -12.0f), s6, f2(6.0f, 6.0f)), f2(-gca, -gcb));
-        float ca, cb;
-        unf2(coef, ca, cb);
-        ca = ina ? ca : 0.0f;
-        cb = inb ? cb : 0.0f;
-        coef = f2(ca, cb);
-        ax2 = fma2(coef, dx, ax2);
-        ay2 = fma2(coef, dy, ay2);
-        az2 = fma2(coef, dz, az2);
-        if (EV) {
-          vr2 = fma2(coef, r2, vr2);
-          const F2 pe = fma2(mul2(eps4, s6), sub2(s6, f2(1.0f, 1.0f)),
-                             fma2(f2(-0.5f * gca, -0.5f * gcb), r2, f2(pka, pkb)));
-          float pa, pb;
-          unf2(pe, pa, pb);
-          pp2 = add2(pp2, f2(ina ? pa : 0.0f, inb ? pb : 0.0f));
-        }
+      for (int h = 0; h < 2; ++h) {
+        const int code = e[a + h] >> CODE_SHIFT;
+        const int kz = (code * 57) >> 9, r9 = code - 9 * kz, ky = (r9 * 11) >> 5, kx = r9 - 3 * ky;  // k/9, k/3
+        dd[h] = __int_as_float(0x4B400000 | kx);
+        dd[2 + h] = __int_as_float(0x4B400000 | ky);
+        dd[4 + h] = __int_as_float(0x4B400000 | kz);
+      }
+      const F2 magic = f2(12582913.0f, 12582913.0f);
+      const F2 ddx = sub2(f2(dd[0], dd[1]), magic), ddy = sub2(f2(dd[2], dd[3]), magic),
+               ddz = sub2(f2(dd[4], dd[5]), magic);
+      const F2 dx = fma2(ddx, f2(wl.x, wl.x), fma2(ddx, f2(wf.x, wf.x), sub2(f2(rj[a].x, rj[a + 1].x), f2(ri.x, ri.x))));
+      const F2 dy = fma2(ddy, f2(wl.y, wl.y), fma2(ddy, f2(wf.y, wf.y), sub2(f2(rj[a].y, rj[a + 1].y), f2(ri.y, ri.y))));
+      const F2 dz = fma2(ddz, f2(wl.z, wl.z), fma2(ddz, f2(wf.z, wf.z), sub2(f2(rj[a].z, rj[a + 1].z), f2(ri.z, ri.z))));
+      const F2 r2d = fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+      float r2a, r2b;
+      unf2(r2d, r2a, r2b);
+      float rc2a, rc2b, sg2a, sg2b, e4a, e4b, gca, gcb, pka, pkb;
+      if (ONE) {
+        rc2a = rc2b = c1.rc2; sg2a = sg2b = c1.sig2; e4a = e4b = c1.eps4; gca = gcb = c1.gc; pka = pkb = c1.pk;
+      } else {
+        const int ta = ti * nt + __float_as_int(rj[a].w), tb = ti * nt + __float_as_int(rj[a + 1].w);
+        const float4 pa = tab.c4[ta], pb = tab.c4[tb];
+        rc2a = pa.x; sg2a = pa.y; e4a = pa.z; gca = pa.w;
+        rc2b = pb.x; sg2b = pb.y; e4b = pb.z; gcb = pb.w;
+        pka = EV ? tab.pk[ta] : 0.0f;
+        pkb = EV ? tab.pk[tb] : 0.0f;
+      }
+      const bool ina = r2a <= rc2a, inb = r2b <= rc2b;
+      if (!(ina || inb)) continue;
+      const float r2ca = fmaxf(r2a, jtol), r2cb = fmaxf(r2b, jtol);  // Lj jump_fix floor (0 when off)
+      const F2 r2 = f2(r2ca, r2cb), r2i = f2(rcp_approx(r2ca), rcp_approx(r2cb));
+      const F2 eps4 = f2(e4a, e4b);
+      const F2 s2 = mul2(f2(sg2a, sg2b), r2i);
+      const F2 s6 = mul2(mul2(s2, s2), s2);
+      const F2 w = mul2(mul2(eps4, r2i), s6);
+      F2 coef = fma2(w, fma2(f2(-12.0f, -12.0f), s6, f2(6.0f, 6.0f)), f2(-gca, -gcb));
+      float ca, cb;
+      unf2(coef, ca, cb);
+      ca = ina ? ca : 0.0f;
+      cb = inb ? cb : 0.0f;
+      coef = f2(ca, cb);
+      ax2 = fma2(coef, dx, ax2);
+      ay2 = fma2(coef, dy, ay2);
+      az2 = fma2(coef, dz, az2);
+      if (EV) {
+        vr2 = fma2(coef, r2, vr2);
+        const F2 pe = fma2(mul2(eps4, s6), sub2(s6, f2(1.0f, 1.0f)),
+                           fma2(f2(-0.5f * gca, -0.5f * gcb), r2, f2(pka, pkb)));
+        float pa, pb;
+        unf2(pe, pa, pb);
+        pp2 = add2(pp2, f2(ina ? pa : 0.0f, inb ? pb : 0.0f));
       }
     }
   }
@@ -427,7 +409,6 @@ struct ForceArgs {
   int fuse;                         // Fuse: the next step's drift in this launch
   int set_cond;                     // set `cond` at the end (inside a captured graph)
   cudaGraphConditionalHandle cond;  // the next step's rebuild node
-  int scap;                         // MODE 2: window-table entries the stage of a warp holds
 };
 
 template <int KICK, bool EV>
@@ -439,19 +420,12 @@ __device__ inline void store_partials(const Dev &d, double (&ke_p)[4], double (&
   }
 }
 
-// Pair kernel.  Warps take windows of 32 slots (a window's table serves its atoms),
-// each window as TPA tasks of A consecutive slots (the list layout's unit).
-//   MODE 0: FP64, neighbour positions gathered from global memory through the table;
-//   MODE 1: mixed, neighbour coordinates gathered from global memory through the table;
-//   MODE 2: mixed, the window's table staged into shared memory first (fa.scap float4
-//           per warp, dynamic): one coalesced read of the table, one gather per
-//           distinct neighbour, and the pair loop reads shared memory; a window whose
-//           table is longer than the stage gathers as MODE 1 does.
-template <int TPA, int MODE, int KICK, bool EV, bool ONE>
-__global__ void __launch_bounds__(256, MODE != 0 ? 4 : 1) k_force(Dev d, Box b, StepConsts sc, ForceArgs fa) {
-  constexpr bool MIXED = MODE != 0, STAGED = MODE == 2;
+// Grid-strided pair kernel (the FP64 form; the mixed form when it has no segments):
+// warp-sized tasks of A consecutive slots, neighbour coordinates gathered from
+// global memory.
+template <int TPA, bool MIXED, int KICK, bool EV, bool ONE>
+__global__ void __launch_bounds__(256, MIXED ? 4 : 1) k_force(Dev d, Box b, StepConsts sc, ForceArgs fa) {
   constexpr int A = 32 / TPA;
-  extern __shared__ float4 stage_all[];
   __shared__ typename std::conditional<MIXED, SmemTabF, SmemTabD>::type tab;
   __shared__ WarpImages<MIXED> wimg[8];
   __shared__ int s_halt;
@@ -462,9 +436,9 @@ __global__ void __launch_bounds__(256, MODE != 0 ? 4 : 1) k_force(Dev d, Box b, 
   const int nt = d.tab->nt;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int a = lane % A, t = lane / A;
-  const int n = sc.n, cap = d.cap, tcap = d.tcap;
+  const int n = sc.n, cap = d.cap;
   const int warps_total = (gridDim.x * blockDim.x) >> 5;
-  const int nwin = was_halted ? 0 : (n + 31) >> 5;
+  const int ntask = was_halted ? 0 : (n + A - 1) / A;
   // EV: each thread's KE / virial / PE sums live in shared memory between tasks;
   // six doubles held in registers across the pair loop spill at 64 registers
   __shared__ double s_sum[EV ? 6 * 256 : 1];
@@ -474,10 +448,10 @@ __global__ void __launch_bounds__(256, MODE != 0 ? 4 : 1) k_force(Dev d, Box b, 
   long long step = 0;
   if (KICK == 2) step = *d.step_base + fa.k_in_chunk;
   int img_rep = -1;
-  float4 *sm = stage_all + (size_t)wid * fa.scap;
 
-  for (int win = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; win < nwin; win += warps_total) {
-    const int rep = rep_of_slot(b, win << 5);  // a window lies in one replica; its first slot is an atom
+  for (int task = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; task < ntask; task += warps_total) {
+    const int rep = rep_of_slot(b, task * A);
+    if (rep < 0) continue;  // a task of padding slots (uniform over the warp)
     if (rep != img_rep) {
       const RepBox &rb = repbox(b, rep);
       if constexpr (MIXED) {
@@ -492,136 +466,85 @@ __global__ void __launch_bounds__(256, MODE != 0 ? 4 : 1) k_force(Dev d, Box b, 
       __syncwarp();
       img_rep = rep;
     }
-    const uint32_t *wt = d.wtab + (size_t)win * tcap;
-    bool staged = false;
-    if constexpr (STAGED) {
-      // the table's coordinates (current rel, row bits added), eight loads per lane in flight
-      const int len = d.wtab_len[win];
-      staged = len <= fa.scap;
-      for (int k0 = 0; staged && k0 < len; k0 += 256) {
-        uint32_t w[8];
-        float4 r[8];
+    const int i = task * A + a;
+    const bool act = i < n && rep_of_slot(b, i) >= 0;
+    double fx = 0.0, fy = 0.0, fz = 0.0, vir = 0.0, pe = 0.0;
+    int ti = 0;
+    if (act) {
+      const int nn = d.nnbr[i];
+      // this lane's neighbour words: chunk g = t + TPA q (entries 4g..4g+3), one 128-bit
+      // load each; the warp's loads for one q cover 512 consecutive bytes (nbr_index)
+      const uint4 *row4 = reinterpret_cast<const uint4 *>(d.nbr + (size_t)task * cap * A) + (t * A + a);
+      if constexpr (MIXED) {
+        const float4 ri = d.rel[i];
+        ti = __float_as_int(ri.w);
+        float ax = 0.f, ay = 0.f, az = 0.f, vr = 0.f, pp = 0.f;
+        const float4 *rel = d.rel;
+        mixed_pairs<TPA, EV, ONE>(row4, nn, t, ri, ti, nt, tab, one_type(tab), wimg[wid].w, wimg[wid].lo, sc.jump_tolf,
+                             [rel](uint32_t w) { return __ldg(&rel[w & IDX_MASK]); }, ax, ay, az, vr, pp);
+        fx = ax; fy = ay; fz = az; vir = vr; pe = pp;
+      } else {
+        const dbl4 xi = d.pos[i];
+        ti = type_of(xi.w);
+        const bool jump = sc.jump_tol > 0.0;
+        // single type: the pair constants in registers, no table lookups; the cutoff
+        // test r^2 <= rc^2 compares the bit patterns as integers (the same order for
+        // doubles >= +0, and rc^2 < 0, an eps == 0 pair, admits none), off the FP64 pipe
+        const int t1 = ti * nt;
+        const long long rc2b1 = __double_as_longlong(tab.rc2[t1]);
+        const double sig21 = tab.sig2[t1], e61 = tab.e6[t1], e121 = tab.e12[t1], gc1 = tab.gc[t1];
+        for (int q = 0, k0 = 4 * t; k0 < nn; ++q, k0 += 4 * TPA) {
+          const uint4 w4 = __ldg(row4 + (size_t)q * 32);
+          const uint32_t e[4] = {w4.x, w4.y, w4.z, w4.w};
+          dbl4 xj[4];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int k = k0 + 32 * u + lane;
-          w[u] = k < len ? __ldg(wt + k) : 0u;  // slot 0 stands in past the end
-        }
+          for (int u = 0; u < 4; ++u)
+            if (k0 + u < nn) xj[u] = ldg_dbl4(&d.pos[e[u] & IDX_MASK]);
 #pragma unroll
-        for (int u = 0; u < 8; ++u) r[u] = __ldg(&d.rel[w[u] & IDX_MASK]);
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int k = k0 + 32 * u + lane;
-          if (k < len) {
-            r[u].w = __int_as_float(__float_as_int(r[u].w) | row_bits(w[u]));
-            sm[k] = r[u];
-          }
-        }
-      }
-      __syncwarp();
-    }
-    for (int s = 0; s < TPA; ++s) {
-      const int task = win * TPA + s;
-      const int i = task * A + a;
-      const bool act = i < n && rep_of_slot(b, i) >= 0;
-      double fx = 0.0, fy = 0.0, fz = 0.0, vir = 0.0, pe = 0.0;
-      int ti = 0;
-      if (act) {
-        const int nn = d.nnbr[i];
-        // this lane's list entries: chunk g = t + TPA q (entries 8g..8g+7), one 128-bit
-        // load each; the warp's loads for one q cover 512 consecutive bytes (nbr_index)
-        const uint4 *row4 = reinterpret_cast<const uint4 *>(d.nbr + (size_t)task * cap * A) + (t * A + a);
-        if constexpr (MIXED) {
-          const float4 ri = d.rel[i];
-          ti = __float_as_int(ri.w);
-          float ax = 0.f, ay = 0.f, az = 0.f, vr = 0.f, pp = 0.f;
-          if (STAGED && staged) {
-            mixed_pairs<TPA, EV, ONE>(row4, nn, t, ri, ti, nt, tab, one_type(tab), wimg[wid].w, wimg[wid].lo,
-                                      sc.jump_tolf, [sm](uint32_t e) { return sm[e & TAB_IDX_MASK]; }, ax, ay, az,
-                                      vr, pp);
-          } else {
-            const float4 *rel = d.rel;
-            mixed_pairs<TPA, EV, ONE>(row4, nn, t, ri, ti, nt, tab, one_type(tab), wimg[wid].w, wimg[wid].lo,
-                                      sc.jump_tolf,
-                                      [wt, rel](uint32_t e) {
-                                        const uint32_t w = __ldg(wt + (e & TAB_IDX_MASK));
-                                        float4 r = __ldg(&rel[w & IDX_MASK]);
-                                        r.w = __int_as_float(__float_as_int(r.w) | row_bits(w));
-                                        return r;
-                                      },
-                                      ax, ay, az, vr, pp);
-          }
-          fx = ax; fy = ay; fz = az; vir = vr; pe = pp;
-        } else {
-          const dbl4 xi = d.pos[i];
-          ti = type_of(xi.w);
-          const bool jump = sc.jump_tol > 0.0;
-          // single type: the pair constants in registers, no table lookups; the cutoff
-          // test r^2 <= rc^2 compares the bit patterns as integers (the same order for
-          // doubles >= +0, and rc^2 < 0, an eps == 0 pair, admits none), off the FP64 pipe
-          const int t1 = ti * nt;
-          const long long rc2b1 = __double_as_longlong(tab.rc2[t1]);
-          const double sig21 = tab.sig2[t1], e61 = tab.e6[t1], e121 = tab.e12[t1], gc1 = tab.gc[t1];
-          for (int q = 0, k0 = 8 * t; k0 < nn; ++q, k0 += 8 * TPA) {
-            const uint4 w4 = __ldg(row4 + (size_t)q * 32);
-            const uint32_t ew[4] = {w4.x, w4.y, w4.z, w4.w};
-            // the table words, then the positions: eight independent gathers in flight
-            uint32_t wd[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-              const uint32_t e = (ew[u >> 1] >> (16 * (u & 1))) & 0xffffu;
-              wd[u] = k0 + u < nn ? __ldg(wt + (e & TAB_IDX_MASK)) : 0u;
+          for (int u = 0; u < 4; ++u) {
+            if (k0 + u >= nn) break;
+            // image x_j + s L (the reference's ghost coordinate); s = 0 for most
+            // entries, where x_j + 0 is x_j exactly and the three adds are skipped
+            const int code = (int)(e[u] >> CODE_SHIFT);
+            double jx = xj[u].x, jy = xj[u].y, jz = xj[u].z;
+            if (code != CODE_ZERO) {
+              const double3 s = wimg[wid].v[code];
+              jx += s.x; jy += s.y; jz += s.z;
             }
-            dbl4 xj[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u)
-              if (k0 + u < nn) xj[u] = ldg_dbl4(&d.pos[wd[u] & IDX_MASK]);
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-              if (k0 + u >= nn) break;
-              // image x_j + s L (the reference's ghost coordinate); s = 0 for most
-              // entries, where x_j + 0 is x_j exactly and the three adds are skipped
-              const int code = (int)(wd[u] >> CODE_SHIFT);
-              double jx = xj[u].x, jy = xj[u].y, jz = xj[u].z;
-              if (code != CODE_ZERO) {
-                const double3 sh = wimg[wid].v[code];
-                jx += sh.x; jy += sh.y; jz += sh.z;
-              }
-              const double dx = jx - xi.x, dy = jy - xi.y, dz = jz - xi.z;
-              const double r2d = dx * dx + dy * dy + dz * dz;
-              const int tt = ONE ? t1 : t1 + type_of(xj[u].w);
-              const long long rc2b = ONE ? rc2b1 : __double_as_longlong(tab.rc2[tt]);
-              if (__double_as_longlong(r2d) <= rc2b) {
-                // Lj jump_fix (src/force/lj.cpp:459-468): r^2 floored at jump_tol after the
-                // cutoff test (jump_tol = 0 when off); the direction stays dx, dy, dz
-                double r2 = r2d;
-                if (jump) r2 = r2d < sc.jump_tol ? sc.jump_tol : r2d;
-                const double r2i = rcp_nr(r2);
-                const double s2 = (ONE ? sig21 : tab.sig2[tt]) * r2i;
-                const double s6 = s2 * s2 * s2;
-                // eps4 s6 (6 - 12 s6) / r^2 - g(rc) as (s6 (e6 - e12 s6)) r2i - gc
-                const double coef = ONE ? fma(s6 * fma(-e121, s6, e61), r2i, -gc1)
-                                        : fma(s6 * fma(-tab.e12[tt], s6, tab.e6[tt]), r2i, -tab.gc[tt]);
-                fx = fma(coef, dx, fx); fy = fma(coef, dy, fy); fz = fma(coef, dz, fz);
-                if (EV) {
-                  vir -= coef * r2;
-                  pe += tab.eps4[tt] * (s6 * s6 - s6) - tab.uc[tt] - 0.5 * tab.gc[tt] * (r2 - tab.rc2[tt]);
-                }
+            const double dx = jx - xi.x, dy = jy - xi.y, dz = jz - xi.z;
+            const double r2d = dx * dx + dy * dy + dz * dz;
+            const int tt = ONE ? t1 : t1 + type_of(xj[u].w);
+            const long long rc2b = ONE ? rc2b1 : __double_as_longlong(tab.rc2[tt]);
+            if (__double_as_longlong(r2d) <= rc2b) {
+              // Lj jump_fix (src/force/lj.cpp:459-468): r^2 floored at jump_tol after the
+              // cutoff test (jump_tol = 0 when off); the direction stays dx, dy, dz
+              double r2 = r2d;
+              if (jump) r2 = r2d < sc.jump_tol ? sc.jump_tol : r2d;
+              const double r2i = rcp_nr(r2);
+              const double s2 = (ONE ? sig21 : tab.sig2[tt]) * r2i;
+              const double s6 = s2 * s2 * s2;
+              // eps4 s6 (6 - 12 s6) / r^2 - g(rc) as (s6 (e6 - e12 s6)) r2i - gc
+              const double coef = ONE ? fma(s6 * fma(-e121, s6, e61), r2i, -gc1)
+                                      : fma(s6 * fma(-tab.e12[tt], s6, tab.e6[tt]), r2i, -tab.gc[tt]);
+              fx = fma(coef, dx, fx); fy = fma(coef, dy, fy); fz = fma(coef, dz, fz);
+              if (EV) {
+                vir -= coef * r2;
+                pe += tab.eps4[tt] * (s6 * s6 - s6) - tab.uc[tt] - 0.5 * tab.gc[tt] * (r2 - tab.rc2[tt]);
               }
             }
           }
         }
       }
-      double ke_t[4] = {0.0, 0.0, 0.0, 0.0}, ev_t[2] = {0.0, 0.0};
-      finish_atom<A, MIXED, KICK, EV>(d, b, sc, tab, act, t, i, ti, rep, step, fa.fuse, fx, fy, fz, vir, pe, ke_t,
-                                      ev_t);
-      if (EV) {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) s_sum[q * 256 + threadIdx.x] += ke_t[q];
-#pragma unroll
-        for (int q = 0; q < 2; ++q) s_sum[(4 + q) * 256 + threadIdx.x] += ev_t[q];
-      }
     }
-    if constexpr (STAGED) __syncwarp();  // the stage is refilled for the next window
+    double ke_t[4] = {0.0, 0.0, 0.0, 0.0}, ev_t[2] = {0.0, 0.0};
+    finish_atom<A, MIXED, KICK, EV>(d, b, sc, tab, act, t, i, ti, rep, step, fa.fuse, fx, fy, fz, vir, pe, ke_t,
+                                    ev_t);
+    if (EV) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) s_sum[q * 256 + threadIdx.x] += ke_t[q];
+#pragma unroll
+      for (int q = 0; q < 2; ++q) s_sum[(4 + q) * 256 + threadIdx.x] += ev_t[q];
+    }
   }
   double ke_p[4] = {0.0, 0.0, 0.0, 0.0}, ev_p[2] = {0.0, 0.0};
   if (EV) {
@@ -634,54 +557,224 @@ __global__ void __launch_bounds__(256, MODE != 0 ? 4 : 1) k_force(Dev d, Box b, 
   if (KICK != 0) end_of_step(d, was_halted, fa.set_cond, fa.cond);
 }
 
-// Launch (or, with launch = false, raise the dynamic shared-memory limit of) one variant.
-template <int TPA, int MODE, int KICK>
-static int launch_ev(bool launch, bool ev, bool one, int grid, int block, size_t smem, const Dev &d, const Box &b,
-                     const StepConsts &sc, const ForceArgs &fa, cudaStream_t st) {
-  auto k = one ? (ev ? k_force<TPA, MODE, KICK, true, true> : k_force<TPA, MODE, KICK, false, true>)
-               : (ev ? k_force<TPA, MODE, KICK, true, false> : k_force<TPA, MODE, KICK, false, false>);
-  if (!launch)
-    return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FORCE_SMEM_MAX) == cudaSuccess
-               ? CAVGPU_OK
-               : CAVGPU_E_CUDA;
-  k<<<grid, block, smem, st>>>(d, b, sc, fa);
+// Mixed-form pair kernel over row segments.  A block takes a segment -- up to
+// seg_umax - 2 consecutive cells of one x-row of one replica -- and stages into
+// shared memory the FP32 coordinates of the atoms of the 9 neighbouring rows'
+// cells x0-1 .. x0+len (periodic), so that every neighbour gather of the
+// segment's atoms reads shared memory.  A list word (slot j, stencil index k)
+// finds its copy through a table: row r = k / 3 of the stencil, staged cell
+// u = (home cell - x0) + k % 3, index = j + (stage offset - first slot) of (r, u).
+// The arithmetic is that of the grid-strided kernel, so results are the same bit
+// for bit.  A segment whose stencil holds more atoms than the stage falls back to
+// global gathers.  Warps take the segment's A-slot tasks; lanes whose atom lies
+// outside the segment idle (their atoms belong to the adjacent segment).
+template <int TPA, int KICK, bool EV, bool ONE>
+__global__ void __launch_bounds__(256) k_force_seg(Dev d, Box b, StepConsts sc, ForceArgs fa) {
+  constexpr int A = 32 / TPA;
+  constexpr int AS = 5 - (TPA == 1 ? 0 : TPA == 2 ? 1 : TPA == 4 ? 2 : TPA == 8 ? 3 : 4);  // log2(A)
+  __shared__ SmemTabF tab;
+  __shared__ float4 s_wf, s_wl;
+  __shared__ int s_total;
+  extern __shared__ float4 stage[];
+  const int umax = d.seg_umax;
+  int *const toff = reinterpret_cast<int *>(stage + d.stage_cap);  // [9 * umax] stage offset - first slot
+  int *const tcnt = toff + 9 * umax;                                 // [9 * umax] atoms, then exclusive scan
+  __shared__ int s_halt;
+  if (threadIdx.x == 0) s_halt = halted(d);
+  load_tab(d, tab);
+  __syncthreads();
+  const bool was_halted = s_halt != 0;  // a step after a halt does nothing
+  const int nt = d.tab->nt;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  const int a = lane % A, t = lane / A;
+  const int cap = d.cap;
+  double ke_p[4] = {0.0, 0.0, 0.0, 0.0};
+  double ev_p[2] = {0.0, 0.0};
+  long long step = 0;
+  if (KICK == 2) step = *d.step_base + fa.k_in_chunk;
+  int img_rep = -1;
+  const int nseg = was_halted ? 0 : d.nseg;
+
+  for (int sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
+    const int4 sg = d.seg[sgi];
+    const int rep = sg.x, cy = sg.y & 0xffff, cz = sg.y >> 16, x0 = sg.z, len = sg.w;
+    const RepBox &rb = repbox(b, rep);
+    const int U = len + 2, nq = 9 * U;
+    __syncthreads();  // the previous segment's gathers are done with the stage and tables
+    if (rep != img_rep) {
+      if (threadIdx.x == 0) {
+        s_wf = make_float4(rb.wf[0], rb.wf[1], rb.wf[2], 0.f);
+        s_wl = make_float4(rb.wlo[0], rb.wlo[1], rb.wlo[2], 0.f);
+      }
+      img_rep = rep;
+    }
+    // staged cells q = r * U + u: row r = (dy + 1) + 3 (dz + 1), x cell x0 - 1 + u (periodic)
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+      const int r = q / U, u = q - r * U;
+      int ny = cy + r % 3 - 1, nz = cz + r / 3 - 1, nx = (x0 - 1 + u) % rb.nc[0];
+      if (nx < 0) nx += rb.nc[0];
+      if (ny < 0) ny += rb.nc[1]; else if (ny >= rb.nc[1]) ny -= rb.nc[1];
+      if (nz < 0) nz += rb.nc[2]; else if (nz >= rb.nc[2]) nz -= rb.nc[2];
+      const int c = rb.cell_off + nx + rb.nc[0] * (ny + rb.nc[1] * nz);
+      const int st = d.cell_start[c];
+      toff[q] = st;
+      tcnt[q] = d.cell_start[c + 1] - st;
+    }
+    __syncthreads();
+    // exclusive scan of the counts (nq <= 9 * umax) by warp 0, 32 entries at a time
+    if (wid == 0) {
+      int carry = 0;
+      for (int base = 0; base < nq; base += 32) {
+        const int q = base + lane;
+        const int v = q < nq ? tcnt[q] : 0;
+        int inc = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(FULL_MASK, inc, o);
+          if (lane >= o) inc += y;
+        }
+        if (q < nq) tcnt[q] = carry + inc - v;
+        carry += __shfl_sync(FULL_MASK, inc, 31);
+      }
+      if (lane == 0) s_total = carry;
+    }
+    __syncthreads();
+    const bool staged = s_total <= d.stage_cap;
+    if (staged) {
+      // copy: warp w takes staged cells w, w + nwarp, ...; lanes copy the cell's atoms
+      for (int q = wid; q < nq; q += nwarp) {
+        const int st = toff[q], base = tcnt[q];
+        const int cn = (q + 1 < nq ? tcnt[q + 1] : s_total) - base;
+        for (int k = lane; k < cn; k += 32) stage[base + k] = __ldg(&d.rel[st + k]);
+      }
+      __syncthreads();
+      for (int q = threadIdx.x; q < nq; q += blockDim.x) toff[q] = tcnt[q] - toff[q];
+    }
+    __syncthreads();
+    // the segment's atoms: slots of its cells (consecutive cell indices, so one range)
+    const int rowc = rb.cell_off + rb.nc[0] * (cy + rb.nc[1] * cz);
+    const int hs = d.cell_start[rowc + x0], he = d.cell_start[rowc + x0 + len];
+    if (he > hs) {
+      const int t_first = hs >> AS, t_last = (he - 1) >> AS;
+      for (int task = t_first + wid; task <= t_last; task += nwarp) {
+        const int i = task * A + a;
+        const bool act = i >= hs && i < he;
+        double fx = 0.0, fy = 0.0, fz = 0.0, vir = 0.0, pe = 0.0;
+        int ti = 0;
+        if (act) {
+          const int nn = d.nnbr[i];
+          const uint4 *row4 = reinterpret_cast<const uint4 *>(d.nbr + (size_t)task * cap * A) + (t * A + a);
+          const float4 ri = d.rel[i];
+          ti = __float_as_int(ri.w);
+          float ax = 0.f, ay = 0.f, az = 0.f, vr = 0.f, pp = 0.f;
+          if (staged) {
+            const int hx = d.cell_of[i] - rowc - x0;  // home cell within the segment
+            const int *tr = toff + hx;
+            mixed_pairs<TPA, EV, ONE>(row4, nn, t, ri, ti, nt, tab, one_type(tab), s_wf, s_wl, sc.jump_tolf,
+                                 [tr, U](uint32_t w) {  // `stage` is the block's shared array
+                                   const int k = (int)(w >> CODE_SHIFT), r = (k * 11) >> 5;  // k / 3 for k < 27
+                                   return stage[(int)(w & IDX_MASK) + tr[r * U + (k - 3 * r)]];
+                                 },
+                                 ax, ay, az, vr, pp);
+          } else {
+            const float4 *rel = d.rel;
+            mixed_pairs<TPA, EV, ONE>(row4, nn, t, ri, ti, nt, tab, one_type(tab), s_wf, s_wl, sc.jump_tolf,
+                                 [rel](uint32_t w) { return __ldg(&rel[w & IDX_MASK]); }, ax, ay, az, vr, pp);
+          }
+          fx = ax; fy = ay; fz = az; vir = vr; pe = pp;
+        }
+        finish_atom<A, true, KICK, EV>(d, b, sc, tab, act, t, i, ti, rep, step, fa.fuse, fx, fy, fz, vir, pe, ke_p,
+                                       ev_p);
+      }
+    }
+  }
+  if (!was_halted) store_partials<KICK, EV>(d, ke_p, ev_p);
+  if (KICK != 0) end_of_step(d, was_halted, fa.set_cond, fa.cond);
+}
+
+template <int TPA, bool MIXED, int KICK>
+static void launch_ev(bool ev, bool one, int grid, int block, const Dev &d, const Box &b, const StepConsts &sc,
+                      const ForceArgs &fa, cudaStream_t st) {
+  if (one) {  // single-type systems: pair constants in registers
+    if (ev) k_force<TPA, MIXED, KICK, true, true><<<grid, block, 0, st>>>(d, b, sc, fa);
+    else k_force<TPA, MIXED, KICK, false, true><<<grid, block, 0, st>>>(d, b, sc, fa);
+    return;
+  }
+  if (ev) k_force<TPA, MIXED, KICK, true, false><<<grid, block, 0, st>>>(d, b, sc, fa);
+  else k_force<TPA, MIXED, KICK, false, false><<<grid, block, 0, st>>>(d, b, sc, fa);
+}
+
+template <int TPA, bool MIXED>
+static void launch_kick(int kick, bool ev, bool one, int grid, int block, const Dev &d, const Box &b,
+                        const StepConsts &sc, const ForceArgs &fa, cudaStream_t st) {
+  if (kick == 0) launch_ev<TPA, MIXED, 0>(ev, one, grid, block, d, b, sc, fa, st);
+  else if (kick == 1) launch_ev<TPA, MIXED, 1>(ev, one, grid, block, d, b, sc, fa, st);
+  else launch_ev<TPA, MIXED, 2>(ev, one, grid, block, d, b, sc, fa, st);
+}
+
+template <bool MIXED>
+static int launch_tpa(int tpa, int kick, bool ev, bool one, int grid, int block, const Dev &d, const Box &b,
+                      const StepConsts &sc, const ForceArgs &fa, cudaStream_t st) {
+  switch (tpa) {
+    case 1: launch_kick<1, MIXED>(kick, ev, one, grid, block, d, b, sc, fa, st); break;
+    case 2: launch_kick<2, MIXED>(kick, ev, one, grid, block, d, b, sc, fa, st); break;
+    case 4: launch_kick<4, MIXED>(kick, ev, one, grid, block, d, b, sc, fa, st); break;
+    case 8: launch_kick<8, MIXED>(kick, ev, one, grid, block, d, b, sc, fa, st); break;
+    case 16: launch_kick<16, MIXED>(kick, ev, one, grid, block, d, b, sc, fa, st); break;
+    default: return CAVGPU_E_ARG;
+  }
   return CAVGPU_OK;
 }
 
-template <int TPA, int MODE>
-static int launch_kick(bool launch, int kick, bool ev, bool one, int grid, int block, size_t smem, const Dev &d,
-                       const Box &b, const StepConsts &sc, const ForceArgs &fa, cudaStream_t st) {
-  if (kick == 0) return launch_ev<TPA, MODE, 0>(launch, ev, one, grid, block, smem, d, b, sc, fa, st);
-  if (kick == 1) return launch_ev<TPA, MODE, 1>(launch, ev, one, grid, block, smem, d, b, sc, fa, st);
-  return launch_ev<TPA, MODE, 2>(launch, ev, one, grid, block, smem, d, b, sc, fa, st);
+// the segment kernel's variants, for launching and for their shared-memory attribute
+template <int TPA, int KICK, bool EV>
+static int seg_variant(bool launch, bool one, int grid, int block, size_t smem, const Dev &d, const Box &b,
+                       const StepConsts &sc, const ForceArgs &fa, cudaStream_t st) {
+  if (!launch) {
+    if (cudaFuncSetAttribute(k_force_seg<TPA, KICK, EV, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess ||
+        cudaFuncSetAttribute(k_force_seg<TPA, KICK, EV, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess)
+      return CAVGPU_E_CUDA;
+    return CAVGPU_OK;
+  }
+  if (one) k_force_seg<TPA, KICK, EV, true><<<grid, block, smem, st>>>(d, b, sc, fa);
+  else k_force_seg<TPA, KICK, EV, false><<<grid, block, smem, st>>>(d, b, sc, fa);
+  return CAVGPU_OK;
 }
-
-template <int MODE>
-static int launch_tpa(bool launch, int tpa, int kick, bool ev, bool one, int grid, int block, size_t smem,
-                      const Dev &d, const Box &b, const StepConsts &sc, const ForceArgs &fa, cudaStream_t st) {
+template <int TPA>
+static int seg_kick(bool launch, int kick, bool ev, bool one, int grid, int block, size_t smem, const Dev &d,
+                    const Box &b, const StepConsts &sc, const ForceArgs &fa, cudaStream_t st) {
+  if (kick == 0) return ev ? seg_variant<TPA, 0, true>(launch, one, grid, block, smem, d, b, sc, fa, st)
+                           : seg_variant<TPA, 0, false>(launch, one, grid, block, smem, d, b, sc, fa, st);
+  if (kick == 1) return ev ? seg_variant<TPA, 1, true>(launch, one, grid, block, smem, d, b, sc, fa, st)
+                           : seg_variant<TPA, 1, false>(launch, one, grid, block, smem, d, b, sc, fa, st);
+  return ev ? seg_variant<TPA, 2, true>(launch, one, grid, block, smem, d, b, sc, fa, st)
+            : seg_variant<TPA, 2, false>(launch, one, grid, block, smem, d, b, sc, fa, st);
+}
+static int seg_tpa(bool launch, int tpa, int kick, bool ev, bool one, int grid, int block, size_t smem,
+                   const Dev &d, const Box &b, const StepConsts &sc, const ForceArgs &fa, cudaStream_t st) {
   switch (tpa) {
-    case 1: return launch_kick<1, MODE>(launch, kick, ev, one, grid, block, smem, d, b, sc, fa, st);
-    case 2: return launch_kick<2, MODE>(launch, kick, ev, one, grid, block, smem, d, b, sc, fa, st);
-    case 4: return launch_kick<4, MODE>(launch, kick, ev, one, grid, block, smem, d, b, sc, fa, st);
-    case 8: return launch_kick<8, MODE>(launch, kick, ev, one, grid, block, smem, d, b, sc, fa, st);
-    case 16: return launch_kick<16, MODE>(launch, kick, ev, one, grid, block, smem, d, b, sc, fa, st);
+    case 1: return seg_kick<1>(launch, kick, ev, one, grid, block, smem, d, b, sc, fa, st);
+    case 2: return seg_kick<2>(launch, kick, ev, one, grid, block, smem, d, b, sc, fa, st);
+    case 4: return seg_kick<4>(launch, kick, ev, one, grid, block, smem, d, b, sc, fa, st);
+    case 8: return seg_kick<8>(launch, kick, ev, one, grid, block, smem, d, b, sc, fa, st);
+    case 16: return seg_kick<16>(launch, kick, ev, one, grid, block, smem, d, b, sc, fa, st);
     default: return CAVGPU_E_ARG;
   }
 }
 
-int prepare_force() {
-  static std::once_flag once;
-  static int rc = CAVGPU_OK;
-  std::call_once(once, [] {
-    const Dev d{};
-    const Box b{};
-    const StepConsts sc{};
-    for (int tpa = 1; tpa <= 16 && !rc; tpa *= 2)
-      for (int kick = 0; kick < 3 && !rc; ++kick)
-        for (int v = 0; v < 4 && !rc; ++v)
-          rc = launch_tpa<2>(false, tpa, kick, v & 1, v >> 1, 0, 0, 0, d, b, sc, ForceArgs{}, nullptr);
-  });
-  return rc;
+int prepare_force_seg(size_t smem_bytes) {
+  Dev d{};
+  Box b{};
+  StepConsts sc{};
+  for (int tpa = 1; tpa <= 16; tpa *= 2)
+    for (int kick = 0; kick < 3; ++kick)
+      for (int ev = 0; ev < 2; ++ev) {
+        const int rc = seg_tpa(false, tpa, kick, ev != 0, false, 0, 0, smem_bytes, d, b, sc, ForceArgs{}, nullptr);
+        if (rc) return rc;
+      }
+  return CAVGPU_OK;
 }
 
 static int g_num_sms = 0;
@@ -693,9 +786,12 @@ int force_grid_blocks(const LaunchCfg &lc) {
     cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
     if (g_num_sms <= 0) g_num_sms = 148;
   }
-  const long long nwin = (lc.n + 31) / 32;
+  if (lc.precision == CAVGPU_MIXED && lc.use_seg && lc.nseg > 0)  // one segment per block at a time
+    return lc.nseg < g_num_sms * 4 ? lc.nseg : g_num_sms * 4;
+  const int A = 32 / lc.tpa;
+  const long long ntask = (lc.n + A - 1) / A;
   const long long warps_per_block = lc.block / 32;
-  long long need = (nwin + warps_per_block - 1) / warps_per_block;
+  long long need = (ntask + warps_per_block - 1) / warps_per_block;
   // persistent-style cap: enough resident blocks to fill every SM several times
   const long long cap = (long long)g_num_sms * (2048 / lc.block) * 4;
   if (need > cap) need = cap;
@@ -707,18 +803,18 @@ int launch_force(const Dev &d, const Box &b, const StepConsts &sc, const LaunchC
   const int grid = force_grid_blocks(lc);
   if (grid > d.partials_blocks) return CAVGPU_E_ARG;  // each block writes its own partial sums
   if (kick == 0 && (fuse || set_cond)) return CAVGPU_E_ARG;
-  if (lc.tcap != d.tcap) return CAVGPU_E_ARG;
-  const bool staged = force_staged(lc);
-  const ForceArgs fa{k, fuse, set_cond, cond, staged ? lc.scap : 0};
-  const bool one = lc.ntypes == 1, ev = thermo != 0;
+  const ForceArgs fa{k, fuse, set_cond, cond};
   int rc;
-  if (lc.precision != CAVGPU_MIXED)
-    rc = launch_tpa<0>(true, lc.tpa, kick, ev, one, grid, lc.block, 0, d, b, sc, fa, st);
-  else if (staged)
-    rc = launch_tpa<2>(true, lc.tpa, kick, ev, one, grid, lc.block, force_smem_bytes(lc.block, lc.scap), d, b, sc,
-                       fa, st);
-  else
-    rc = launch_tpa<1>(true, lc.tpa, kick, ev, one, grid, lc.block, 0, d, b, sc, fa, st);
+  if (lc.precision == CAVGPU_MIXED && lc.use_seg && lc.nseg > 0) {
+    if (!d.seg || d.nseg != lc.nseg) return CAVGPU_E_ARG;
+    rc = seg_tpa(true, lc.tpa, kick, thermo != 0, lc.ntypes == 1, grid, lc.block,
+                 seg_smem_bytes(d.stage_cap, d.seg_umax), d, b, sc, fa, st);
+  } else {
+    const bool one = lc.ntypes == 1;
+    rc = lc.precision == CAVGPU_MIXED
+             ? launch_tpa<true>(lc.tpa, kick, thermo != 0, one, grid, lc.block, d, b, sc, fa, st)
+             : launch_tpa<false>(lc.tpa, kick, thermo != 0, one, grid, lc.block, d, b, sc, fa, st);
+  }
   if (rc) return rc;
   return cudaPeekAtLastError() == cudaSuccess ? CAVGPU_OK : CAVGPU_E_CUDA;
 }

@@ -458,19 +458,15 @@ struct BuildLane {
   int mol;            // molecule index (ignore_intra_molecule)
   unsigned long long rxx, ryy, rzz;  // the atom's coordinates in the group frame, packed twice
   float hi;           // upper end of the FP32 band (-1 for non-members: they never hit)
-  uint16_t *row;      // the atom's list row
-  int cnt;            // list entries the atom has so far
+  uint32_t *row;      // the atom's list row
+  int cnt;            // list words the atom has so far
   const int *selfpos; // shared: per lane, where its own atom sits in the current stage (-1: not in it)
-  uint32_t *tab;      // the window's table of neighbour slots
-  int tb;             // entries in the window's table so far (the same in every lane)
 };
 
 // Sweep of nst staged candidates against every member of the group (see above).
-// Staged words carry j and a code: the image code (mode 0) or (mode 1) the row of
-// the candidate's cell, (dy+1) + 3 (dz+1) -- the table words of the window.  The
-// candidates some member hits join the window's table; a member's entry holds the
-// table index and (mode 1) dx+1 of j's cell relative to the member's own, its cell's
-// x index in the group's window of cells (the byte `su`) minus the member's.
+// Staged words carry j and a code: the image code (mode 0), or (mode 1) the cell's
+// x index in the group's window of cells plus 3 x its row, from which a member
+// subtracts its own x index to get the stencil index of j's cell relative to its own.
 __device__ __forceinline__ void build_sweep(const Dev &d, const Box &b, const RepBox &rb, int mode, int nst,
                                             const float4 *sxy, const float4 *szw, const uint8_t *su, BuildLane &L,
                                             int cshift) {
@@ -488,9 +484,9 @@ __device__ __forceinline__ void build_sweep(const Dev &d, const Box &b, const Re
   }
   __syncwarp();
   const float lo = b.ce2_lo;
-  const int cap = d.cap, tcap = d.tcap;
+  const int cap = d.cap;
   const int self = L.selfpos[lane];
-  const unsigned lt_mask = (1u << lane) - 1u;
+  const uint32_t ci_code = (uint32_t)L.ci << CODE_SHIFT;
   for (int t0 = 0; t0 < npad32; t0 += 32) {
     // phase 1: bits of the sure hits (q < ce2_lo) and of everything up to ce2_hi
     uint32_t hm = 0u, am = 0u;
@@ -527,30 +523,18 @@ __device__ __forceinline__ void build_sweep(const Dev &d, const Box &b, const Re
         if (exact_pair(d, rb, b.ce2, L.i, j, img)) hm |= 1u << u;
       }
     }
-    // the window's table: the candidates of this chunk that some member hits, in
-    // candidate order
-    const uint32_t um = __reduce_or_sync(FULL_MASK, hm);
-    if ((um >> lane) & 1u) {
-      const int pos = L.tb + __popc(um & lt_mask), t = t0 + lane;
-      if (pos < tcap) L.tab[pos] = __float_as_uint(fzw[(t >> 1) * 4 + 2 + (t & 1)]);  // slot | code
-    }
-    // phase 2: the hits, in candidate order, as (code, table index) entries (with
-    // ignore_intra_molecule none of the atom's own molecule, as
-    // Lj::calculate_acceleration skips them, src/force/lj.cpp:446)
+    // phase 2: the hits, in candidate order (with ignore_intra_molecule none of the
+    // atom's own molecule, as Lj::calculate_acceleration skips them, src/force/lj.cpp:446)
     while (hm) {
       const int u = __ffs(hm) - 1;
       hm &= hm - 1u;
       const int t = t0 + u;
-      if (d.mol) {
-        const uint32_t w = __float_as_uint(fzw[(t >> 1) * 4 + 2 + (t & 1)]);
-        if (d.mol[w & IDX_MASK] == L.mol) continue;
-      }
-      const int kx = mode != 0 ? (su[t] & 7) - L.ci : 0;
-      const int idx = L.tb + __popc(um & ((1u << u) - 1u));
-      if (L.cnt < cap && idx < tcap) L.row[((L.cnt >> 3) << cshift) + (L.cnt & 7)] = nbr_entry(kx, idx);
+      uint32_t w = __float_as_uint(fzw[(t >> 1) * 4 + 2 + (t & 1)]);
+      if (d.mol && d.mol[w & IDX_MASK] == L.mol) continue;
+      if (mode != 0) w -= ci_code;  // stencil index of j's cell relative to the atom's
+      if (L.cnt < cap) L.row[((L.cnt >> 2) << cshift) + (L.cnt & 3)] = w;
       ++L.cnt;
     }
-    L.tb += __popc(um);
   }
   __syncwarp();  // the stage is refilled next
 }
@@ -576,10 +560,10 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_group(Dev d, Box 
   float *fxy = reinterpret_cast<float *>(sxy), *fzw = reinterpret_cast<float *>(szw);
   uint8_t *su = su_all[threadIdx.x >> 5];
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-  const int cshift = 8 - log2_pow2(d.tpa);  // chunk stride 8A entries = 2^(log2 A + 3)
+  const int cshift = 7 - log2_pow2(d.tpa);  // chunk stride 4A words = 2^(log2 A + 2)
   const unsigned lt_mask = (1u << lane) - 1u;
   const int nwin = (b.nslot + 31) >> 5;
-  int wmax = 0, tmax = 0;
+  int wmax = 0;
   for (int win = gw; win < nwin; win += nw) {
     BuildLane L;
     L.i = (win << 5) + lane;
@@ -600,8 +584,6 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_group(Dev d, Box 
       if (d.mol) L.mol = d.mol[L.i];
     }
     L.row = d.nbr + nbr_block_base(act ? L.i : 0, d.cap, d.tpa);
-    L.tab = d.wtab + (size_t)win * d.tcap;
-    L.tb = 0;
     int *selfpos = selfpos_all[threadIdx.x >> 5];
     L.selfpos = selfpos;
     const int win0 = win << 5;
@@ -649,9 +631,10 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_group(Dev d, Box 
           const int c2 = rb.cell_off + nx + rb.nc[0] * (ny + rb.nc[1] * nz);
           kb = d.cell_start[c2];
           kn = d.cell_start[c2 + 1] - kb;
-          // mode 0: the image code; mode 1: the row (the x offset is per member)
+          // mode 0: the image code; mode 1: x index + 3 x row (<= 7 + 24), from which a
+          // member's stencil index follows by subtracting its own x index
           kimg = image_code(sx, sy, sz);
-          kcode = (uint32_t)(mode == 0 ? kimg : r) << CODE_SHIFT;
+          kcode = (uint32_t)(mode == 0 ? kimg : u + 3 * r) << CODE_SHIFT;
           ks = u | (r << 3);
           kox = (float)(u - 1) * rb.wf[0];
           koy = (float)dy * rb.wf[1];
@@ -715,18 +698,11 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_group(Dev d, Box 
         wmax = max(wmax, L.cnt);
       }
     }
-    const unsigned built = __ballot_sync(FULL_MASK, act);
-    if (built != 0u && lane == 0) {  // a window of a replica that rebuilt
-      d.wtab_len[win] = min(L.tb, d.tcap);
-      if (L.tb > d.tcap) atomicMax(&d.flags[F_TAB_OVERFLOW], L.tb);
-      tmax = max(tmax, L.tb);
-    }
   }
   // one atomic per warp for the largest list length (not one per atom)
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(FULL_MASK, wmax, o));
   if (lane == 0 && wmax > 0) atomicMax(&d.flags[F_MAXNB], wmax);
-  if (lane == 0 && tmax > 0) atomicMax(&d.flags[F_TABLEN], tmax);
 }
 
 // after the build: count the rebuilt replicas, clear their flags and the global one;
@@ -752,7 +728,7 @@ __global__ void __launch_bounds__(256) k_finish_rebuild(Dev d, Box b, int forced
       d.flags[F_PASSES] += 1;
     }
     d.flags[F_REBUILD] = 0;
-    if (d.flags[F_OVERFLOW] || d.flags[F_TAB_OVERFLOW]) d.flags[F_HALT] = 1;
+    if (d.flags[F_OVERFLOW]) d.flags[F_HALT] = 1;
   }
 }
 
@@ -1008,18 +984,11 @@ __global__ void __launch_bounds__(256) k_export_pairs(Dev d, Box b, int mode, in
   const int ci = d.cell_of[i] - rb.cell_off;
   const int c3[3] = {ci % rb.nc[0], (ci / rb.nc[0]) % rb.nc[1], ci / (rb.nc[0] * rb.nc[1])};
   const int nn = d.nnbr[i];
-  const uint32_t *wt = d.wtab + (size_t)(i >> 5) * d.tcap;  // the window's table
   for (int k = 0; k < nn; ++k) {
-    const uint16_t e = d.nbr[nbr_index(i, k, d.cap, d.tpa)];
-    const uint32_t w = wt[e & TAB_IDX_MASK];
-    const int j = (int)(w & IDX_MASK), code = (int)(w >> CODE_SHIFT);
+    const uint32_t e = d.nbr[nbr_index(i, k, d.cap, d.tpa)];
+    const int j = (int)(e & IDX_MASK), code = (int)(e >> CODE_SHIFT);
     int s[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
-    if (mode == 1) {  // dx + 1 from the entry, the row from the word: cell offset -> image shift
-      s[0] = (int)(e >> TAB_BITS) - 1;
-      s[1] = code % 3 - 1;
-      s[2] = code / 3 - 1;
-    }
-    if (mode == 1)
+    if (mode == 1)  // cell-offset code -> image shift
       for (int q = 0; q < 3; ++q) {
         const int c = c3[q] + s[q];
         s[q] = c < 0 ? -1 : (c >= rb.nc[q] ? 1 : 0);

@@ -105,9 +105,6 @@ typedef struct cavgpu_params {
    * until then, as Atom_data::add_atom sets it) take no force.  Applied when the
    * list is built, so cavgpu_export_pairs leaves those pairs out. */
   int32_t ignore_intra_molecule;
-  /* table entries per window of 32 slots (the window's distinct neighbours; at most
-   * 16384); 0 = sized at set-up.  A build that wants more grows the tables. */
-  int32_t table_capacity;
 } cavgpu_params;
 
 #define CAVGPU_NVE_ENERGY_PER_DOF 0
@@ -116,12 +113,10 @@ typedef struct cavgpu_params {
 #define CAVGPU_NVE_KB_TEMPERATURE 3
 
 /* pair-kernel variants of the mixed form (the FP64 form has one kernel); both give
- * the same results bit for bit.  The list keeps, per window of 32 slots, a table of
- * the window's distinct neighbours, and per atom 16-bit indices into it. */
-#define CAVGPU_FORCE_AUTO 0       /* staged; the autotuner may switch to global gathers */
-#define CAVGPU_FORCE_STRIDED 1    /* neighbour coordinates gathered from global memory */
-#define CAVGPU_FORCE_STAGED 2     /* each window's table staged in shared memory first */
-#define CAVGPU_FORCE_SEGMENTS CAVGPU_FORCE_STAGED  /* the former name of the staged kernel */
+ * the same results bit for bit */
+#define CAVGPU_FORCE_AUTO 0       /* grid-strided; the autotuner may switch to segments */
+#define CAVGPU_FORCE_STRIDED 1    /* grid-strided tasks, neighbour gathers from global memory */
+#define CAVGPU_FORCE_SEGMENTS 2   /* row segments staged in shared memory */
 
 typedef struct cavgpu_ctx cavgpu_ctx;
 
@@ -211,14 +206,6 @@ int64_t cavgpu_export_ghosts(cavgpu_ctx *ctx, double ghost_cutoff, int32_t *src,
  * threads per atom, block size, graph launches, kernel launches}. */
 int cavgpu_stats(cavgpu_ctx *ctx, int64_t *out8);
 
-/* Neighbour-list storage: out8 = {entries per atom (capacity), largest list,
- * table entries per window (capacity), largest window table since the last forced
- * build, table entries a warp of the mixed pair kernel stages in shared memory
- * (0: none), bytes of rows and tables, table entries over all windows, windows}.
- * No counterpart in the reference, whose lists are vectors of vectors
- * (src/neighborlist.cpp:247-297). */
-int cavgpu_list_stats(cavgpu_ctx *ctx, int64_t *out8);
-
 /* The CUDA stream the context launches on (a cudaStream_t). */
 void *cavgpu_stream(cavgpu_ctx *ctx);
 
@@ -255,7 +242,7 @@ int cavgpu_kinetic_energy_noalloc(int64_t n, const double *vel3, const uint64_t 
 
 /* Autotuner (no counterpart in the reference, whose loop has no launch shape):
  * times short trial runs of every launch shape -- pair kernel (mixed form with
- * CAVGPU_FORCE_AUTO: staged and global gathers) x force-kernel lanes per atom
+ * CAVGPU_FORCE_AUTO: segments and grid-strided) x force-kernel lanes per atom
  * {1,2,4,8} x block size {64,128,256}, then steps per captured graph {25,50,100}
  * -- each started from a snapshot of the current state, and keeps the fastest.
  * The state afterwards is the snapshot's (positions, velocities, accelerations,
@@ -265,7 +252,7 @@ int cavgpu_kinetic_energy_noalloc(int64_t n, const double *vel3, const uint64_t 
  * Results are cached per process by (device, precision, integrator, replica
  * count, atom count, type count, force_kernel); CAVGPU_TUNE_FORCE re-measures.
  * out6 (may be NULL) = {threads per atom, block size, steps per graph, trials,
- * pair kernel (CAVGPU_FORCE_STRIDED or _STAGED), 0}. */
+ * pair kernel (CAVGPU_FORCE_STRIDED or _SEGMENTS), 0}. */
 #define CAVGPU_TUNE_FORCE 1
 int cavgpu_autotune(cavgpu_ctx *ctx, int32_t trial_steps, int32_t flags, int64_t *out6);
 

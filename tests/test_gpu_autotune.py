@@ -29,7 +29,7 @@ def test_autotune_restores_state_and_trajectory(precision):
     # FP64: 12 shapes + 2 graph lengths; mixed: both pair kernels x 12 shapes + 2
     assert choice["steps_per_graph"] in (25, 50, 100)
     assert choice["trials"] == (14 if precision == G.FP64 else 26)
-    assert choice["force_kernel"] in ("staged", "strided")
+    assert choice["force_kernel"] in ("segments", "strided")
     after, st1, th1 = s.state(), s.stats(), s.thermo()
     for a, b in zip(before, after):
         np.testing.assert_array_equal(a, b)

@@ -10,11 +10,6 @@ bit, a run whose list never overflowed.  Here an FCC lattice at rho 0.65 (54
 neighbours per atom within r_c + skin at set-up, under the 64 slots asked for)
 melts at T 1.44 and its largest neighbour count climbs past 64 during the run.
 
-The window tables (per 32 slots, the distinct neighbours of their atoms) have a
-fixed size as well and overflow the same way; a run whose tables start at the
-set-up's largest table grows them when the melt asks for more, with the same
-result bit for bit.
-
 A NaN acceleration ends the run with CAVGPU_E_NAN at the step that met it, as the
 reference ends there; a context that met one does not step again.
 """
@@ -56,31 +51,23 @@ def test_overflow_mid_run_equals_large_list_run(precision):
     np.testing.assert_array_equal(th64, thbig)
 
 
-@pytest.mark.parametrize("precision", [G.FP64, G.MIXED], ids=["fp64", "mixed"])
-def test_table_overflow_mid_run_equals_large_table_run(precision):
+@pytest.mark.parametrize("every", [3, 7])
+def test_overflow_records_stay_on_their_steps(every):
+    """After a completed overflow step the run resumes at a step that need not end a
+    record period; the records must still fall on steps every, 2 every, ... (a
+    chunk that resumes mid-period runs up to the next record first)."""
     pos, vel, typ, p = melting_lattice()
-    probe = G.System(pos, vel, typ, p, precision=precision, nbr_capacity=512)
-    probe.setup()
-    t0 = probe.list_stats()["max_table"]
-    probe.close()
-    tight = (t0 + 31) // 32 * 32
     runs = {}
-    for tcap in (tight, 4096):
-        s = G.System(pos, vel, typ, p, precision=precision, nbr_capacity=512, table_capacity=tcap)
+    for cap in (64, 512):
+        s = G.System(pos, vel, typ, p, precision=G.FP64, nbr_capacity=cap)
         s.setup()
-        assert s.list_stats()["table_capacity"] == tcap  # the set-up build fits
-        th = s.run(600, 10)
-        runs[tcap] = (s.state(), th, s.stats(), s.list_stats())
+        th = s.run(600, every)
+        runs[cap] = (th, s.stats(), s.state())
         s.close()
-    (pa, va, aa), tha, sta, la = runs[tight]
-    (pb, vb, ab), thb, stb, lb = runs[4096]
-    assert lb["max_table"] > tight, (t0, lb)  # the melt wanted longer tables
-    assert la["table_capacity"] > tight
-    assert sta["steps"] == stb["steps"] == 600 and sta["rebuilds"] == stb["rebuilds"]
-    np.testing.assert_array_equal(pa, pb)
-    np.testing.assert_array_equal(va, vb)
-    np.testing.assert_array_equal(aa, ab)
-    np.testing.assert_array_equal(tha, thb)
+    assert runs[64][1]["capacity"] > 64  # the small list overflowed during the run
+    np.testing.assert_array_equal(runs[64][0], runs[512][0])
+    for a, b in zip(runs[64][2], runs[512][2]):
+        np.testing.assert_array_equal(a, b)
 
 
 def test_nan_ends_the_run_at_its_step():
