@@ -418,9 +418,9 @@ __device__ __noinline__ bool exact_pair(const Dev &d, const RepBox &rb, double c
 // lists do not depend on how slots fall into windows.
 //
 // Staging: candidates u and u+1 (u even) interleaved as {x_u, x_u+1, y_u, y_u+1}
-// and {z_u, z_u+1, word_u, word_u+1} in the warp's slice of shared memory
-// (coordinates relative to the origin of the group's first cell, word = j | image
-// code), plus one byte per candidate: its cell's x index in the group's window of
+// and {z_u, z_u+1} in the warp's slice of shared memory (coordinates relative to
+// the origin of the group's first cell), the words (j | code) in an array of their
+// own, plus one byte per candidate: its cell's x index in the group's window of
 // cells and its row (dy, dz).  The sweep takes 32 candidates at a time, two per
 // packed FP32x2 distance evaluation: every pair of candidates is two shared-memory
 // broadcasts tested by all group atoms, the results collect in a hit and a band bit
@@ -464,23 +464,23 @@ struct BuildLane {
 };
 
 // Sweep of nst staged candidates against every member of the group (see above).
-// Staged words carry j and a code: the image code (mode 0), or (mode 1) the cell's
+// Staged words carry j and a code: the image code (MODE 0), or (MODE 1) the cell's
 // x index in the group's window of cells plus 3 x its row, from which a member
 // subtracts its own x index to get the stencil index of j's cell relative to its own.
-__device__ __forceinline__ void build_sweep(const Dev &d, const Box &b, const RepBox &rb, int mode, int nst,
-                                            const float4 *sxy, const float4 *szw, const uint8_t *su, BuildLane &L,
-                                            int cshift) {
+template <int MODE>
+__device__ __forceinline__ void build_sweep(const Dev &d, const Box &b, const RepBox &rb, int nst,
+                                            const float4 *sxy, const float2 *sz, const uint32_t *sw,
+                                            const uint8_t *su, BuildLane &L, int cshift, bool by_mol) {
   const int lane = threadIdx.x & 31;
-  const float *fzw = reinterpret_cast<const float *>(szw);
   float *pxy = const_cast<float *>(reinterpret_cast<const float *>(sxy));
-  float *pzw = const_cast<float *>(fzw);
+  float *pz = const_cast<float *>(reinterpret_cast<const float *>(sz));
   const int npad32 = (nst + 31) & ~31;
   for (int t = nst + lane; t < npad32; t += 32) {  // far-away padding up to a whole 32
     const int e = (t >> 1) * 4 + (t & 1);
     pxy[e] = 1e18f;
     pxy[e + 2] = 1e18f;
-    pzw[e] = 1e18f;
-    pzw[e + 2] = 0.f;
+    pz[t] = 1e18f;
+    const_cast<uint32_t *>(sw)[t] = 0u;
   }
   __syncwarp();
   const float lo = b.ce2_lo;
@@ -493,8 +493,8 @@ __device__ __forceinline__ void build_sweep(const Dev &d, const Box &b, const Re
 #pragma unroll
     for (int u = 0; u < 32; u += 2) {
       const int pr = (t0 + u) >> 1;
-      const float4 xy = sxy[pr];                                     // broadcast
-      const float2 z = *reinterpret_cast<const float2 *>(&szw[pr]);  // broadcast
+      const float4 xy = sxy[pr];  // broadcast
+      const float2 z = sz[pr];    // broadcast
       float q0, q1;
       dist2_pair(xy, z, L.rxx, L.ryy, L.rzz, q0, q1);
       if (q0 < lo) hm |= 1u << u;
@@ -506,15 +506,16 @@ __device__ __forceinline__ void build_sweep(const Dev &d, const Box &b, const Re
     if (ts >= 0 && ts < 32) am &= ~(1u << ts);
     hm &= am;
     uint32_t bm = am & ~hm;  // the band
+    const uint32_t *swc = sw + t0;
     if (__any_sync(FULL_MASK, bm != 0u)) {  // rare: the exact FP64 predicate
       while (bm) {
         const int u = __ffs(bm) - 1;
         bm &= bm - 1u;
         const int t = t0 + u;
-        const uint32_t w = __float_as_uint(fzw[(t >> 1) * 4 + 2 + (t & 1)]);
+        const uint32_t w = swc[u];
         const int j = (int)(w & IDX_MASK);
         int img = (int)(w >> CODE_SHIFT);
-        if (mode != 0) {  // the image from the candidate cell's unwrapped index
+        if (MODE != 0) {  // the image from the candidate cell's unwrapped index
           const int s = su[t], r = s >> 3;
           const int nx = L.cx + (s & 7) - 1 - L.ci, ny = L.cy + r % 3 - 1, nz = L.cz + r / 3 - 1;
           img = image_code(nx < 0 ? -1 : (nx >= rb.nc[0] ? 1 : 0), ny < 0 ? -1 : (ny >= rb.nc[1] ? 1 : 0),
@@ -528,10 +529,9 @@ __device__ __forceinline__ void build_sweep(const Dev &d, const Box &b, const Re
     while (hm) {
       const int u = __ffs(hm) - 1;
       hm &= hm - 1u;
-      const int t = t0 + u;
-      uint32_t w = __float_as_uint(fzw[(t >> 1) * 4 + 2 + (t & 1)]);
-      if (d.mol && d.mol[w & IDX_MASK] == L.mol) continue;
-      if (mode != 0) w -= ci_code;  // stencil index of j's cell relative to the atom's
+      uint32_t w = swc[u];
+      if (by_mol && d.mol[w & IDX_MASK] == L.mol) continue;
+      if (MODE != 0) w -= ci_code;  // stencil index of j's cell relative to the atom's
       if (L.cnt < cap) L.row[((L.cnt >> 2) << cshift) + (L.cnt & 3)] = w;
       ++L.cnt;
     }
@@ -550,15 +550,21 @@ __device__ inline float warp_maxf(float v) {
   return v;
 }
 
-__global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_group(Dev d, Box b, int mode, int forced) {
-  __shared__ float4 stage_all[BUILD_WARPS][BUILD_STAGE];
+template <int MODE>
+__global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_group(Dev d, Box b, int forced) {
+  __shared__ float4 sxy_all[BUILD_WARPS][BUILD_STAGE / 2];
+  __shared__ float2 sz_all[BUILD_WARPS][BUILD_STAGE / 2];
+  __shared__ uint32_t sw_all[BUILD_WARPS][BUILD_STAGE];
   __shared__ uint8_t su_all[BUILD_WARPS][BUILD_STAGE];
   __shared__ int selfpos_all[BUILD_WARPS][32];
   const int lane = threadIdx.x & 31;
-  // pair p = candidates 2p, 2p+1: sxy[p] = {x, x', y, y'}, szw[p] = {z, z', word, word'}
-  float4 *sxy = stage_all[threadIdx.x >> 5], *szw = sxy + BUILD_STAGE / 2;
-  float *fxy = reinterpret_cast<float *>(sxy), *fzw = reinterpret_cast<float *>(szw);
+  // pair p = candidates 2p, 2p+1: sxy[p] = {x, x', y, y'}, sz[p] = {z, z'}; sw[t] = word of t
+  float4 *sxy = sxy_all[threadIdx.x >> 5];
+  float2 *sz = sz_all[threadIdx.x >> 5];
+  uint32_t *sw = sw_all[threadIdx.x >> 5];
+  float *fxy = reinterpret_cast<float *>(sxy), *fz = reinterpret_cast<float *>(sz);
   uint8_t *su = su_all[threadIdx.x >> 5];
+  const bool by_mol = d.mol != nullptr;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
   const int cshift = 7 - log2_pow2(d.tpa);  // chunk stride 4A words = 2^(log2 A + 2)
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -634,7 +640,7 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_group(Dev d, Box 
           // mode 0: the image code; mode 1: x index + 3 x row (<= 7 + 24), from which a
           // member's stencil index follows by subtracting its own x index
           kimg = image_code(sx, sy, sz);
-          kcode = (uint32_t)(mode == 0 ? kimg : u + 3 * r) << CODE_SHIFT;
+          kcode = (uint32_t)(MODE == 0 ? kimg : u + 3 * r) << CODE_SHIFT;
           ks = u | (r << 3);
           kox = (float)(u - 1) * rb.wf[0];
           koy = (float)dy * rb.wf[1];
@@ -670,8 +676,8 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_group(Dev d, Box 
               const int e = (s >> 1) * 4 + (s & 1);
               fxy[e] = X;
               fxy[e + 2] = Y;
-              fzw[e] = Z;
-              fzw[e + 2] = __uint_as_float((uint32_t)(jb + t) | code);
+              fz[s] = Z;
+              sw[s] = (uint32_t)(jb + t) | code;
               su[s] = sbyte;
               // a window atom at its own cell and zero image: that lane's self position
               const unsigned l = (unsigned)(jb + t - win0);
@@ -680,7 +686,7 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_group(Dev d, Box 
             nst += __popc(km);
             if (nst > BUILD_STAGE - 32) {
               __syncwarp();
-              build_sweep(d, b, rb, mode, nst, sxy, szw, su, L, cshift);
+              build_sweep<MODE>(d, b, rb, nst, sxy, sz, sw, su, L, cshift, by_mol);
               selfpos[lane] = -1;
               __syncwarp();
               nst = 0;
@@ -690,7 +696,7 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, 4) k_build_group(Dev d, Box 
       }
       if (nst > 0) {
         __syncwarp();
-        build_sweep(d, b, rb, mode, nst, sxy, szw, su, L, cshift);
+        build_sweep<MODE>(d, b, rb, nst, sxy, sz, sw, su, L, cshift, by_mol);
       }
       if (L.me) {
         d.nnbr[L.i] = min(L.cnt, d.cap);
@@ -1198,9 +1204,9 @@ int launch_rebuild(const Dev &d, const Box &b, const LaunchCfg &lc, int forced, 
   k_cell_sort<<<ceil_div((long long)b.ncell_all * 32, 256), 256, 0, st>>>(d, b, forced);
   k_copy_state<<<g, 256, 0, st>>>(d, b, forced);
   k_gather<<<g, 256, 0, st>>>(d, b, forced);
-  const int mode = lc.precision == CAVGPU_MIXED ? 1 : 0;
   const int build_grid = std::min(ceil_div(ceil_div(b.nslot, 32), BUILD_WARPS), num_sms() * 8);
-  k_build_group<<<build_grid, BUILD_WARPS * 32, 0, st>>>(d, b, mode, forced);
+  if (lc.precision == CAVGPU_MIXED) k_build_group<1><<<build_grid, BUILD_WARPS * 32, 0, st>>>(d, b, forced);
+  else k_build_group<0><<<build_grid, BUILD_WARPS * 32, 0, st>>>(d, b, forced);
   k_finish_rebuild<<<1, 256, 0, st>>>(d, b, forced);
   return chk();
 }
