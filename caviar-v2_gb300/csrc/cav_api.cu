@@ -378,7 +378,8 @@ int forced_build(cavgpu_ctx *c, bool count = true) {
   for (int attempt = 0; attempt < 4; ++attempt) {
     int zero[F_NWORDS] = {0};
     int f[F_NWORDS];
-    RK(read_flags(c, f));
+    if (attempt == 0) std::memcpy(f, f0, sizeof(f));  // nothing ran since f0 was read
+    else RK(read_flags(c, f));
     zero[F_REBUILDS] = f[F_REBUILDS];
     zero[F_PASSES] = f[F_PASSES];
     CK(cudaMemcpyAsync(c->d.flags, zero, sizeof(zero), cudaMemcpyHostToDevice, c->st));
