@@ -1,9 +1,9 @@
 /*
  * cav_oracle.h -- CPU restatement of CAVIAR2's molecular-dynamics step.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the GPU path:
- * only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may
- * load it.  The product (libcavgpu.so) never links or calls it.
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle the GPU path is tested
+ * against: only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
+ * may load it.  The product (libcavgpu.so) never links or calls it.
  *
  * It restates, in plain C, the single-rank CPU path of caviar-md/caviar-v2:
  *   Domain::fix_position               src/domain.cpp:443-493
