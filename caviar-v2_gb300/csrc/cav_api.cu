@@ -204,8 +204,9 @@ ChunkPlan make_plan(const cavgpu_ctx *c, int S, int ev) {
 // The steps of a chunk, captured into the graph being recorded on c->st (capture)
 // or launched directly.  A step: [drift kernel] -> rebuild kernels, behind a
 // conditional node in a graph (they return at once without a half-skin trigger when
-// launched directly) -> pair kernel with the closing update [and the next drift] ->
-// [thermo fold] -> [constraint::Nve].  The conditional value comes from the
+// launched directly) -> pair kernel with the closing update [and the next drift]
+// [and, single systems, the thermo fold in its last block] -> [thermo fold kernel:
+// batches, constraint::Nve] -> [constraint::Nve].  The conditional value comes from the
 // condition kernel after a drift kernel, else from the previous pair kernel.
 int enqueue_chunk(cavgpu_ctx *c, const ChunkPlan &pl, bool capture, long long *launches) {
   Dev view = c->d;
@@ -268,7 +269,12 @@ int enqueue_chunk(cavgpu_ctx *c, const ChunkPlan &pl, bool capture, long long *l
     }
     if (c->prof && k < (int)c->ev0.size())
       CK(capture ? cudaEventRecordWithFlags(c->ev0[k], c->st, cudaEventRecordExternal) : cudaEventRecord(c->ev0[k], c->st));
-    RK(launch_force(view, c->b, c->sc, c->lc, is_lang(c) ? 2 : 1, th, k, fuse, set_cond, hnext, c->st));
+    // a recorded step of a single system: the pair kernel's last block folds the record
+    const bool fold = th && c->b.nrep == 1 && c->nve.step == 0;
+    FoldArgs fa{c->tc, is_lang(c) ? drift_grid_blocks(c->lc) : force_grid_blocks(c->lc),
+                is_lang(c) ? force_grid_blocks(c->lc) : 0, ring_slot};
+    RK(launch_force(view, c->b, c->sc, c->lc, is_lang(c) ? 2 : 1, th, k, fuse, set_cond, hnext, c->st,
+                    fold ? &fa : nullptr));
     if (c->prof && k < (int)c->ev1.size())
       CK(capture ? cudaEventRecordWithFlags(c->ev1[k], c->st, cudaEventRecordExternal) : cudaEventRecord(c->ev1[k], c->st));
     nl += 1;
@@ -276,7 +282,7 @@ int enqueue_chunk(cavgpu_ctx *c, const ChunkPlan &pl, bool capture, long long *l
       if (mixed) std::swap(view.rel, view.rel_alt);
       else std::swap(view.pos, view.pos_alt);
     }
-    if (th) RK(enqueue_thermo_after_force(c, ring_slot, &nl));
+    if (th && !fold) RK(enqueue_thermo_after_force(c, ring_slot, &nl));
     if (c->nve.step > 0 && !is_lang(c)) {  // constraint::Nve after the temperature (src/md_simulator.cpp:681-694)
       RK(launch_nve(view, c->b, c->tc, c->nve, k, th, ring_slot, c->st));
       nl += 3;

@@ -378,6 +378,23 @@ struct ThermoCfg {
   int langevin;    // pressure without the force virial (the reference computes it before the force)
 };
 
+// KE, T, P, virial, PE from the folded sums (Atom_data::kinetic_energy_mpi_domain /
+// finalize_temperature / finalize_pressure, src/atom_data/kinetic_energy.cpp:26-134,
+// 189-198, 238-303)
+__device__ inline void thermo_finish(double ke2, const double P3[3], double msum, double vir2, double pe2, int natoms,
+                                     int n_r_df, double k_b, double volume, int langevin, double *out) {
+  if (n_r_df >= 1 && n_r_df <= 3 && msum > 0) ke2 -= (P3[0] * P3[0] + P3[1] * P3[1] + P3[2] * P3[2]) / msum;
+  const double ke = 0.5 * ke2;
+  const int dof = 3 * natoms - n_r_df;
+  const double T = 2.0 * ke / (k_b * dof);
+  const double vir = 0.5 * vir2;  // each pair was visited from both sides
+  out[0] = ke;
+  out[1] = T;
+  out[2] = ((double)natoms * k_b * T) / volume + (langevin ? 0.0 : vir) / (3.0 * volume);
+  out[3] = vir;
+  out[4] = 0.5 * pe2;
+}
+
 // Kernel launchers (cav_kernels.cu, cav_force.cu).  `forced` rebuilds every
 // replica regardless of the flags; otherwise the rebuild kernels skip replicas
 // whose half-skin test did not fire.
@@ -406,8 +423,18 @@ inline int rebuild_kernels(const Box &b) { return 8 + (scan_slices(b) > 1 ? 1 : 
 // cond: when set_cond, the last block sets the conditional node of the next step's
 // rebuild to the half-skin flag (unless halted).  The last block also counts the
 // step (F_STEPS_OK) and raises the halt on a NaN.
+// The thermo fold of a recorded step done by the pair kernel's last block (single
+// systems): the fixed-order sums of the KE partials (nb_ke blocks; Langevin: the
+// drift kernel's) and of the launch's own virial/PE partials (and, Langevin, of its
+// end-of-step KE partials, nb_ke_end), then the record -- what launch_thermo_final
+// does after the launch, without its launch.
+struct FoldArgs {
+  ThermoCfg tc;
+  int nb_ke, nb_ke_end, ring_slot;
+};
 int launch_force(const Dev &d, const Box &b, const StepConsts &sc, const LaunchCfg &lc, int kick, int thermo,
-                 int k_in_chunk, int fuse, int set_cond, cudaGraphConditionalHandle cond, cudaStream_t st);
+                 int k_in_chunk, int fuse, int set_cond, cudaGraphConditionalHandle cond, cudaStream_t st,
+                 const FoldArgs *fold = nullptr);
 // nb_ke_end > 0 (Langevin): KE from partials_ke_end, the temperature from partials_ke.
 // Two levels in a fixed order: THERMO_FOLD_BLOCKS blocks fold strided subsets of the
 // partials, the last block to finish folds their sums (deterministic).

@@ -382,34 +382,104 @@ __device__ __forceinline__ void finish_atom(const Dev &d, const Box &b, const St
   }
 }
 
-// End of a pair-kernel launch, every block: the last block to finish counts the
-// step, turns a NaN seen by the fused drift into a halt, and -- inside a graph --
-// sets the conditional node of the next step's rebuild.  The flag stores of this
-// launch are ordered before the ticket by the fence.
-__device__ __forceinline__ void end_of_step(const Dev &d, bool was_halted, int set_cond,
-                                            cudaGraphConditionalHandle cond) {
-  __syncthreads();
-  if (threadIdx.x != 0) return;
-  __threadfence();
-  const unsigned int t = atomicAdd(d.force_ticket, 1u);
-  if (t != gridDim.x - 1) return;
-  __threadfence();
-  volatile int *f = d.flags;
-  if (!was_halted) {
-    f[F_STEPS_OK] = f[F_STEPS_OK] + 1;
-    if (f[F_NAN]) f[F_HALT] = 1;
-  }
-  if (set_cond) cudaGraphSetConditional(cond, (f[F_REBUILD] != 0 && f[F_HALT] == 0) ? 1u : 0u);
-  *d.force_ticket = 0u;
-}
-
 // per-launch arguments of the pair kernels
 struct ForceArgs {
   int k_in_chunk;                   // step index inside the chunk (Langevin noise counter)
   int fuse;                         // Fuse: the next step's drift in this launch
   int set_cond;                     // set `cond` at the end (inside a captured graph)
   cudaGraphConditionalHandle cond;  // the next step's rebuild node
+  int fold;                         // the last block folds the thermo record (EV launches)
+  FoldArgs fa;
 };
+
+// The thermo fold in the last block: every thread sums a strided subset of the
+// partials (L2 loads: other blocks wrote them), the block folds the threads' sums
+// in a fixed order, thread 0 finishes the record.  The sums do not depend on which
+// block finished last.
+// sums of n blocks' partials of W doubles (W = 2 or 4) into v[0..W): thread t takes
+// blocks t, t + B, t + 2B, ... in that order, four blocks' loads in flight at a time
+template <int W>
+__device__ __forceinline__ void fold_strided(const double *p, int n, double *v) {
+  const int B = blockDim.x;
+  for (int k0 = threadIdx.x; k0 < n; k0 += 4 * B) {
+    double2 x[4][W / 2];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int h = 0; h < W / 2; ++h)
+        x[u][h] = k0 + u * B < n ? __ldcg(reinterpret_cast<const double2 *>(p + (size_t)(k0 + u * B) * W) + h)
+                                 : make_double2(0.0, 0.0);
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (k0 + u * B < n)
+#pragma unroll
+        for (int h = 0; h < W / 2; ++h) {
+          v[2 * h] += x[u][h].x;
+          v[2 * h + 1] += x[u][h].y;
+        }
+  }
+}
+
+__device__ __noinline__ void fold_thermo(const Dev &d, const FoldArgs &fa, int nb_ev) {
+  double v[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  fold_strided<4>(d.partials_ke, fa.nb_ke, v);
+  fold_strided<2>(d.partials_ev, nb_ev, v + 4);
+  fold_strided<4>(d.partials_ke_end, fa.nb_ke_end, v + 6);
+  __shared__ double out[10];
+  block_sum_store_f<10>(v, out);
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  const ThermoCfg &tc = fa.tc;
+  double res[5];
+  const double P3[3] = {out[1], out[2], out[3]};
+  thermo_finish(out[0], P3, d.thermo[5], out[4], out[5], tc.n, tc.n_r_df, tc.k_b, tc.volume, tc.langevin, res);
+  if (fa.nb_ke_end > 0) {  // KE as Atom_data::kinetic_energy() reads it after the step
+    double e[5];
+    const double Q3[3] = {out[7], out[8], out[9]};
+    thermo_finish(out[6], Q3, d.thermo[5], 0.0, 0.0, tc.n, tc.n_r_df, tc.k_b, tc.volume, tc.langevin, e);
+    res[0] = e[0];
+  }
+#pragma unroll
+  for (int q = 0; q < 5; ++q) d.thermo[q] = res[q];
+  if (fa.ring_slot >= 0) {
+    double *r = d.thermo_ring + (size_t)fa.ring_slot * THERMO_REC;
+#pragma unroll
+    for (int q = 0; q < THERMO_REC; ++q) r[q] = res[q];
+  }
+}
+
+// End of a pair-kernel launch, every block: the last block to finish counts the
+// step, turns a NaN seen by the fused drift into a halt, -- inside a graph -- sets
+// the conditional node of the next step's rebuild, and (EV, fold) folds the thermo
+// record unless the chunk halted.  The flag and partial stores of this launch are
+// ordered before the ticket by the fence.
+template <bool EV>
+__device__ __forceinline__ void end_of_step(const Dev &d, bool was_halted, const ForceArgs &fa) {
+  __shared__ int s_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(d.force_ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __shared__ int s_fold;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    volatile int *f = d.flags;
+    if (!was_halted) {
+      f[F_STEPS_OK] = f[F_STEPS_OK] + 1;
+      if (f[F_NAN]) f[F_HALT] = 1;
+    }
+    if (fa.set_cond) cudaGraphSetConditional(fa.cond, (f[F_REBUILD] != 0 && f[F_HALT] == 0) ? 1u : 0u);
+    *d.force_ticket = 0u;
+    s_fold = EV && fa.fold && f[F_HALT] == 0;
+  }
+  __syncthreads();
+  if constexpr (EV) {
+    if (s_fold) fold_thermo(d, fa.fa, gridDim.x);
+  }
+}
 
 template <int KICK, bool EV>
 __device__ inline void store_partials(const Dev &d, double (&ke_p)[4], double (&ev_p)[2]) {
@@ -554,7 +624,7 @@ __global__ void __launch_bounds__(256, MIXED ? 4 : 1) k_force(Dev d, Box b, Step
     for (int q = 0; q < 2; ++q) ev_p[q] = s_sum[(4 + q) * 256 + threadIdx.x];
   }
   if (!was_halted) store_partials<KICK, EV>(d, ke_p, ev_p);
-  if (KICK != 0) end_of_step(d, was_halted, fa.set_cond, fa.cond);
+  if (KICK != 0) end_of_step<EV>(d, was_halted, fa);
 }
 
 // Mixed-form pair kernel over row segments.  A block takes a segment -- up to
@@ -689,7 +759,7 @@ __global__ void __launch_bounds__(256) k_force_seg(Dev d, Box b, StepConsts sc, 
     }
   }
   if (!was_halted) store_partials<KICK, EV>(d, ke_p, ev_p);
-  if (KICK != 0) end_of_step(d, was_halted, fa.set_cond, fa.cond);
+  if (KICK != 0) end_of_step<EV>(d, was_halted, fa);
 }
 
 template <int TPA, bool MIXED, int KICK>
@@ -803,11 +873,14 @@ int force_grid_blocks(const LaunchCfg &lc) {
 }
 
 int launch_force(const Dev &d, const Box &b, const StepConsts &sc, const LaunchCfg &lc, int kick, int thermo,
-                 int k, int fuse, int set_cond, cudaGraphConditionalHandle cond, cudaStream_t st) {
+                 int k, int fuse, int set_cond, cudaGraphConditionalHandle cond, cudaStream_t st,
+                 const FoldArgs *fold) {
   const int grid = force_grid_blocks(lc);
   if (grid > d.partials_blocks) return CAVGPU_E_ARG;  // each block writes its own partial sums
   if (kick == 0 && (fuse || set_cond)) return CAVGPU_E_ARG;
-  const ForceArgs fa{k, fuse, set_cond, cond};
+  if (fold && (kick == 0 || !thermo)) return CAVGPU_E_ARG;  // the fold needs this launch's EV partials
+  ForceArgs fa{k, fuse, set_cond, cond, fold ? 1 : 0, {}};
+  if (fold) fa.fa = *fold;
   int rc;
   if (lc.precision == CAVGPU_MIXED && lc.use_seg && lc.nseg > 0) {
     if (!d.seg || d.nseg != lc.nseg) return CAVGPU_E_ARG;

@@ -758,19 +758,6 @@ __global__ void k_halt_check(Dev d) {
 //  src/atom_data/kinetic_energy.cpp:26-134, 189-198, 238-303)
 // thermo[] = {KE, T, P, virial, PE, sum m, -, -}
 // ---------------------------------------------------------------------------
-__device__ inline void thermo_finish(double ke2, const double P3[3], double msum, double vir2, double pe2, int natoms,
-                                     int n_r_df, double k_b, double volume, int langevin, double *out) {
-  if (n_r_df >= 1 && n_r_df <= 3 && msum > 0) ke2 -= (P3[0] * P3[0] + P3[1] * P3[1] + P3[2] * P3[2]) / msum;
-  const double ke = 0.5 * ke2;
-  const int dof = 3 * natoms - n_r_df;
-  const double T = 2.0 * ke / (k_b * dof);
-  const double vir = 0.5 * vir2;  // each pair was visited from both sides
-  out[0] = ke;
-  out[1] = T;
-  out[2] = ((double)natoms * k_b * T) / volume + (langevin ? 0.0 : vir) / (3.0 * volume);
-  out[3] = vir;
-  out[4] = 0.5 * pe2;
-}
 
 __global__ void __launch_bounds__(256) k_thermo_final(Dev d, ThermoCfg tc, int nb_ke, int nb_ev, int nb_ke_end,
                                                       int ring_slot) {
