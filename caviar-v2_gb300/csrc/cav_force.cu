@@ -392,12 +392,9 @@ struct ForceArgs {
   FoldArgs fa;
 };
 
-// The thermo fold in the last block: every thread sums a strided subset of the
-// partials (L2 loads: other blocks wrote them), the block folds the threads' sums
-// in a fixed order, thread 0 finishes the record.  The sums do not depend on which
-// block finished last.
-// sums of n blocks' partials of W doubles (W = 2 or 4) into v[0..W): thread t takes
+// Sums of n blocks' partials of W doubles (W = 2 or 4) into v[0..W): thread t takes
 // blocks t, t + B, t + 2B, ... in that order, four blocks' loads in flight at a time
+// (L2 loads: other blocks wrote them).
 template <int W>
 __device__ __forceinline__ void fold_strided(const double *p, int n, double *v) {
   const int B = blockDim.x;
@@ -420,6 +417,9 @@ __device__ __forceinline__ void fold_strided(const double *p, int n, double *v) 
   }
 }
 
+// The thermo fold in the last block: every thread sums a strided subset of the
+// partials, the block folds the threads' sums in a fixed order, thread 0 finishes
+// the record.  The sums do not depend on which block finished last.
 __device__ __noinline__ void fold_thermo(const Dev &d, const FoldArgs &fa, int nb_ev) {
   double v[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   fold_strided<4>(d.partials_ke, fa.nb_ke, v);
