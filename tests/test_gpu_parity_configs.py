@@ -1,4 +1,4 @@
-"""GPU parity, FP64 form, at the full per-system sizes of the two Langevin benchmark
+"""GPU parity, FP64 form, at the full sizes of the Langevin and batched benchmark
 configurations, against the oracle.
 
 * Langevin fluid, 4,194,304 atoms (128 x 128 x 64 FCC cells, rho 0.8442, T 1.0,
@@ -10,6 +10,8 @@ configurations, against the oracle.
   per-pair cutoffs 2.5 sigma_ij), run as replica 1 of a two-replica batch: replica
   r draws the noise stream of seed + r, so after 50 steps it equals the oracle's
   single system with seed + 1 within 1e-10.
+* The 4096-replica batch (17.5M atoms, NVE): sampled replicas after 20 steps equal
+  the oracle's single-system runs within 1e-10.
 """
 import numpy as np
 import pytest
@@ -65,3 +67,28 @@ def test_kob_andersen_batch_replica_against_oracle(oracle_lib):
     L = np.asarray(p["hi"], float) - np.asarray(p["lo"], float)
     assert np.abs(wrap_diff(pg, po, L)).max() <= 1e-10
     assert np.abs(vg - vo).max() <= 1e-10
+
+
+def test_replica_batch_4096_sampled_against_oracle(oracle_lib):
+    """The 4096-replica benchmark batch itself (17,480,270 atoms, N_r in [256, 8192],
+    rho_r in [0.6, 1.0], NVE), FP64, 20 steps: replicas 0, 1, 2047, 4095 and the
+    largest one equal the oracle's single-system runs within 1e-10."""
+    sets = W.replica_set(4096)
+    systems = [(q, v, np.zeros(len(q), np.int32), np.zeros(3), box) for q, v, box, _, _ in sets]
+    params = W.lj_params(systems[0][4])
+    b = G.Batch(systems, params, precision=G.FP64)
+    b.setup()
+    b.step(20)
+    pos, vel, _ = b.state()
+    ps, vs = b.split(pos), b.split(vel)
+    b.close()
+    largest = int(np.argmax([len(s[0]) for s in systems]))
+    for r in sorted({0, 1, 2047, 4095, largest}):
+        q, v, t, lo, hi = systems[r]
+        p = dict(params, lo=lo, hi=hi)
+        o = oracle_lib.System(q, v, t, p, noise_mode=0)
+        o.setup()
+        o.step(20)
+        po, vo, _ = o.state()
+        assert np.abs(wrap_diff(ps[r], po, hi - lo)).max() <= 1e-10, r
+        assert np.abs(vs[r] - vo).max() <= 1e-10, r
